@@ -1,0 +1,315 @@
+/*
+ * rpd_gb300.h — C ABI of the GB300 (sm_103a) StatMC / RPD denoise stage.
+ *
+ * The reference (andersonliu1/rpd-statmc-denoiser) runs this stage as free C++ functions
+ * over process globals in path_tracer/main.cpp. This header replaces them with explicit
+ * job handles whose state lives in HBM; every entry point below names the reference
+ * function it stands in for. Plain C types only: no CUDA or C++ types cross the boundary.
+ *
+ * Threading: one host thread per job handle at a time. Jobs of one context may be driven
+ * from different host threads. Every call is asynchronous on the job's CUDA stream unless
+ * it returns host data (rpd_job_read, rpd_compute_adaptive_sample_counts with a host
+ * destination, rpd_job_sync).
+ *
+ * Errors: every function returns an rpd_status. rpd_last_error() gives the message of the
+ * last failure on the calling thread. Configuration errors use the reference's messages
+ * (path_tracer/core/config.h:116-195).
+ */
+#ifndef RPD_GB300_H
+#define RPD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RPD_ABI_VERSION 1
+
+typedef enum rpd_status {
+    RPD_OK = 0,
+    RPD_ERR_INVALID_CONFIG = 1,   /* config.h:116-195 validation failed */
+    RPD_ERR_INVALID_ARGUMENT = 2, /* null handle, bad size, out-of-range pixel span */
+    RPD_ERR_OUT_OF_MEMORY = 3,    /* device or pinned-host allocation failed */
+    RPD_ERR_OVER_BUDGET = 4,      /* job would exceed the context's HBM budget */
+    RPD_ERR_CUDA = 5,             /* CUDA runtime error (message has the CUDA text) */
+    RPD_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up */
+    RPD_ERR_STATE = 7,            /* call out of order (e.g. denoise before any samples) */
+    RPD_ERR_NO_DEVICE = 8         /* no CUDA device, or the device is not sm_103 */
+} rpd_status;
+
+/* Where the pointers handed to a call live. */
+typedef enum rpd_memory {
+    RPD_MEM_HOST = 0,   /* host memory (pinned or pageable); the call copies it to HBM */
+    RPD_MEM_DEVICE = 1  /* device memory of the context's GPU; used in place */
+} rpd_memory;
+
+/*
+ * Denoise-stage knobs. Field names, meanings and defaults are those of RenderConfig
+ * (path_tracer/core/config.h:15-49); only the fields the stage reads are kept.
+ * seed plays the role of g_sampler_base_seed (main.cpp:43), which the adaptive
+ * allocation hashes for its systematic-sampling offset (main.cpp:1427).
+ */
+typedef struct rpd_config {
+    int32_t image_width;
+    int32_t image_height;
+    int32_t rpf_tile_size;                 /* default 8 */
+    float rpf_shrinkage_scale;             /* default 1.0; 0 disables all RPD influence */
+    float rpf_confidence_samples;          /* default 128 */
+    int32_t color_window_radius;           /* default 7 */
+    float color_normal_threshold;          /* default 0.5 */
+    float color_depth_threshold;           /* default 0.25 */
+    float color_compat_alpha;              /* default 0.05 */
+    float color_sigma_max;                 /* default 6 */
+    int32_t var_window_radius;             /* default 1 */
+    float var_normal_threshold;            /* default 0.5 */
+    float var_depth_threshold;             /* default 0.25 */
+    float var_compat_sigma;                /* default 30 */
+    float var_shrinkage_k;                 /* default 1e-3 */
+    int32_t var_iterations;                /* default 2 */
+    int32_t adaptive_base_samples;         /* default 0 */
+    int32_t adaptive_spp;                  /* default 0 */
+    float adaptive_sigma_max;              /* default 3 */
+    int32_t adaptive_passes;               /* default 1 */
+    int32_t adaptive_importance_smoothing_radius; /* default 1 */
+    int32_t debug_statmc_outputs;          /* default 0; accepted, no files are written */
+    uint32_t seed;                         /* g_sampler_base_seed */
+} rpd_config;
+
+/*
+ * Per-sample record, structure of arrays. One entry per traced camera sample, in the
+ * order the tracer produced them: all samples of a pixel are contiguous and pixels are
+ * in increasing index order (the reference's render loops, main.cpp:685-719 and
+ * 1488-1519, consume them in the same order).
+ *
+ * The fields are what the reference's per-sample hooks see:
+ *   radiance        path radiance returned by mis_path_trace (main.cpp:706); a sample whose
+ *                   radiance is not finite is dropped from the statistics and the grid
+ *                   (main.cpp:707) but its primary-hit features still count (572-576).
+ *   normal/depth/albedo   primary-hit features accumulated into FrameBuffers
+ *                   (main.cpp:572-576); ignored when RPD_SAMPLE_HIT is clear.
+ *   pixel_u, lens_u, brdf_u, light_u, env_u, category   the first-valid record
+ *                   rpf::Sample (core/stats.h:331-399).
+ *
+ * A NULL plane means "never valid": the matching valid bit is treated as clear.
+ * albedo may be NULL when pixel_albedo is given: every hit sample of a pixel then
+ * contributes that pixel's albedo (indexed by pixel - first_pixel).
+ */
+#define RPD_SAMPLE_HIT                 0x01u
+#define RPD_SAMPLE_PIXEL_VALID         0x02u
+#define RPD_SAMPLE_LENS_VALID          0x04u
+#define RPD_SAMPLE_BRDF_VALID          0x08u
+#define RPD_SAMPLE_LIGHT_VALID         0x10u /* light_u (light_valid) */
+#define RPD_SAMPLE_LIGHT_SELECT_VALID  0x20u
+#define RPD_SAMPLE_ENV_VALID           0x40u
+#define RPD_SAMPLE_RR_VALID            0x80u
+
+#define RPD_CATEGORY_LIGHT_INDEX_MASK  0x0Fu /* light_index, valid only when < 16 (main.cpp:407) */
+#define RPD_CATEGORY_RR_SURVIVED       0x10u
+
+typedef struct rpd_sample_soa {
+    const float* radiance[3];
+    const float* normal[3];
+    const float* depth;
+    const float* albedo[3];
+    const float* pixel_albedo[3];
+    const float* pixel_u[2];
+    const float* lens_u[2];
+    const float* brdf_u[2];
+    const float* light_u[2];
+    const float* env_u[2];
+    const uint8_t* flags;
+    const uint8_t* category;
+} rpd_sample_soa;
+
+/* Readable per-job fields (rpd_job_read). Per-pixel fields are row-major W*H; RGB fields
+ * are interleaved W*H*3 floats like the reference's Image; node fields are
+ * nodes_x*nodes_y floats; the grid is nodes*13*36 doubles (see RPD_FIELD_GRID). */
+typedef enum rpd_field {
+    RPD_FIELD_DENOISED = 0,          /* buffers.denoised (main.cpp:1125) */
+    RPD_FIELD_UNCERTAINTY,           /* buffers.uncertainty */
+    RPD_FIELD_ALPHA,                 /* buffers.alpha */
+    RPD_FIELD_VAR_TOTAL_DEBUG,       /* buffers.var_total_debug */
+    RPD_FIELD_VAR_EFF_DEBUG,         /* buffers.var_eff_debug */
+    RPD_FIELD_VAR_RATIO_DEBUG,       /* buffers.var_ratio_debug */
+    RPD_FIELD_VARIANCE_DENOISED,     /* buffers.variance_denoised (main.cpp:1264) */
+    RPD_FIELD_ADAPTIVE_IMPORTANCE,   /* buffers.adaptive_importance (main.cpp:1373) */
+    RPD_FIELD_SENSITIVITY_CONFIDENCE,/* buffers.sensitivity_confidence (main.cpp:932) */
+    RPD_FIELD_SENSITIVITY_GRADIENT,  /* buffers.sensitivity_gradient (main.cpp:945) */
+    RPD_FIELD_HIT_COUNT,             /* int32 buffers.hit_count */
+    RPD_FIELD_SAMPLE_COUNT,          /* int32 buffers.sample_count */
+    RPD_FIELD_RADIANCE_SUM,          /* RGB sum of finite samples (buffers.radiance before finalize) */
+    RPD_FIELD_NORMAL_SUM,            /* RGB buffers.normal before finalize */
+    RPD_FIELD_ALBEDO_SUM,            /* RGB buffers.albedo before finalize */
+    RPD_FIELD_DEPTH_SUM,             /* buffers.depth before finalize */
+    RPD_FIELD_STATS_MEAN,            /* PixelStats::mean (core/stats.h:7) */
+    RPD_FIELD_STATS_SQUARE_DIFF,     /* PixelStats::square_diff */
+    RPD_FIELD_STATS_N,               /* int32 PixelStats::n */
+    RPD_FIELD_STATS_COLOR_MEAN,      /* RGB PixelStats::color_mean */
+    RPD_FIELD_STATS_SQRT_MEAN,       /* RGB PixelStats::sqrt_color_mean */
+    RPD_FIELD_STATS_SQRT_SQUARE_DIFF,/* RGB PixelStats::sqrt_color_square_diff */
+    RPD_FIELD_NODE_ALL,              /* sensitivity_tiles.all ... (core/buffers.h:23-40) */
+    RPD_FIELD_NODE_ALL_CONF,
+    RPD_FIELD_NODE_PIXEL,
+    RPD_FIELD_NODE_PIXEL_CONF,
+    RPD_FIELD_NODE_BRDF,
+    RPD_FIELD_NODE_BRDF_CONF,
+    RPD_FIELD_NODE_LENS,
+    RPD_FIELD_NODE_LENS_CONF,
+    RPD_FIELD_NODE_LIGHT,
+    RPD_FIELD_NODE_LIGHT_CONF,
+    RPD_FIELD_NODE_LIGHT_UV,
+    RPD_FIELD_NODE_LIGHT_UV_CONF,
+    RPD_FIELD_NODE_LIGHT_SELECT,
+    RPD_FIELD_NODE_LIGHT_SELECT_CONF,
+    RPD_FIELD_NODE_ENVIRONMENT,
+    RPD_FIELD_NODE_ENVIRONMENT_CONF,
+    RPD_FIELD_NODE_RR,
+    RPD_FIELD_NODE_RR_CONF,
+    /* rpf::Grid (core/stats.h:305-329): per node the 13 Tile dependencies in member order
+     * (pixel, brdf, screen_brdf, lens, screen_lens, light_uv, screen_light_uv,
+     * environment, screen_environment, light_select, screen_light_select, rr, screen_rr),
+     * each as 36 doubles: weight[16], sum_y[16], w_sum, w2_sum, y_sum, y2_sum
+     * (rr uses bins 0-1 of weight and sum_y; the rest are zero). */
+    RPD_FIELD_GRID,
+    /* Per-pixel bilinear expansions written by output_buffers (core/buffers.h:221-229). */
+    RPD_FIELD_EXPANDED_ALL,
+    RPD_FIELD_EXPANDED_PIXEL,
+    RPD_FIELD_EXPANDED_BRDF,
+    RPD_FIELD_EXPANDED_LENS,
+    RPD_FIELD_EXPANDED_LIGHT,
+    RPD_FIELD_EXPANDED_LIGHT_UV,
+    RPD_FIELD_EXPANDED_LIGHT_SELECT,
+    RPD_FIELD_EXPANDED_ENVIRONMENT,
+    RPD_FIELD_EXPANDED_RR,
+    RPD_FIELD_ADAPTIVE_COUNTS,       /* int32 last compute_adaptive_sample_counts result */
+    RPD_FIELD_COUNT_
+} rpd_field;
+
+#define RPD_GRID_DEPENDENCIES 13
+#define RPD_GRID_DEP_STRIDE 36
+
+/* Stage timers (CUDA events on the job stream), like the reference's ms log lines
+ * (main.cpp:952,1161,1267,1444). */
+typedef enum rpd_stage {
+    RPD_STAGE_ACCUMULATE = 0,       /* per-sample statistics + RPD grid (push) */
+    RPD_STAGE_SENSITIVITY,          /* recompute_sensitivity */
+    RPD_STAGE_STATMC,               /* statmc_denoise */
+    RPD_STAGE_VARIANCE,             /* variance_denoise */
+    RPD_STAGE_ADAPTIVE,             /* compute_adaptive_sample_counts */
+    RPD_STAGE_COUNT_
+} rpd_stage;
+
+typedef struct rpd_ctx rpd_ctx;
+typedef struct rpd_job rpd_job;
+
+/* ---- configuration (core/config.h) ------------------------------------------------ */
+
+/* RenderConfig defaults (core/config.h:27-48); image size 0, seed 0. */
+void rpd_config_defaults(rpd_config* cfg);
+/* parse_render_config's checks on the stage's fields (core/config.h:116-195), plus a
+ * positive image size. Writes the reference's message into msg. */
+int rpd_config_validate(const rpd_config* cfg, char* msg, size_t msg_capacity);
+
+/* ---- context and jobs ------------------------------------------------------------- */
+
+/* Opens the CUDA device and sets the HBM budget that jobs are admitted against
+ * (0 = all free memory at creation). */
+int rpd_ctx_create(int device, uint64_t hbm_budget_bytes, rpd_ctx** out);
+void rpd_ctx_destroy(rpd_ctx* ctx);
+/* Bytes of HBM a job with this config would hold. */
+uint64_t rpd_job_footprint(const rpd_config* cfg);
+uint64_t rpd_ctx_bytes_in_use(const rpd_ctx* ctx);
+
+/* buffers.init + pixel_stats.assign + rpf_grid.init/reset (main.cpp:651-655), in HBM. */
+int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out);
+void rpd_job_destroy(rpd_job* job);
+/* Replace the knobs of later calls (the reference passes RenderConfig to every stage).
+ * Image size and rpf_tile_size are fixed at job creation. */
+int rpd_job_set_config(rpd_job* job, const rpd_config* cfg);
+/* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */
+int rpd_job_begin_frame(rpd_job* job);
+
+/*
+ * Accumulate traced samples: per-pixel Welford statistics (accumulate_sample,
+ * core/stats.h:25-41), primary-hit features (main.cpp:572-576) and the RPD grid
+ * (accumulate_rpf_sample_to_grid, main.cpp:329-376) for pixels
+ * [first_pixel, first_pixel + pixel_count). counts == NULL means every pixel has spp
+ * samples; otherwise counts[i] is the number of samples of pixel first_pixel + i.
+ * Pushes of one pass must come in increasing pixel order and cover each pixel once.
+ * The planes of s and counts live in `where` memory.
+ */
+int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first_pixel,
+                         int64_t pixel_count, int32_t spp, const int32_t* counts,
+                         rpd_memory where);
+/* End of a render pass: merge_rpf_grids_into (main.cpp:378-388, 730, 1531) and cache
+ * invalidation (main.cpp:1533). */
+int rpd_job_end_pass(rpd_job* job);
+
+/* The four stage entry points (main.cpp:741, 957, 1166, 1273). */
+int rpd_recompute_sensitivity(rpd_job* job);
+int rpd_statmc_denoise(rpd_job* job);
+int rpd_variance_denoise(rpd_job* job);
+/* Extra sample count per pixel for one adaptive pass; written to counts_out (W*H int32
+ * in `where` memory; may be NULL, the result stays readable as RPD_FIELD_ADAPTIVE_COUNTS). */
+int rpd_compute_adaptive_sample_counts(rpd_job* job, int32_t* counts_out, rpd_memory where);
+/* FrameBuffers::finalize (core/buffers.h:152-167) on the radiance/feature sums. */
+int rpd_finalize(rpd_job* job);
+
+/* Copy a field to `where` memory. bytes must equal the field's size. */
+int rpd_job_read(rpd_job* job, rpd_field field, void* dst, size_t bytes, rpd_memory where);
+uint64_t rpd_field_bytes(const rpd_job* job, rpd_field field);
+int rpd_job_sync(rpd_job* job);
+/* Device milliseconds of the last run of a stage on this job. */
+float rpd_job_stage_ms(const rpd_job* job, rpd_stage stage);
+/* Kernel launches issued by this job since creation (for launch accounting). */
+uint64_t rpd_job_launch_count(const rpd_job* job);
+
+/* ---- standalone filters (denoising/atrous_wavelet.cpp, denoising/joint_bilateral.cpp) ---- */
+
+/* atrous_wavelet filter() core (denoising/atrous_wavelet.cpp:151-197): `iterations`
+ * passes of atrous_filter_pass with step 2^i. raw/normal/albedo/out are interleaved RGB
+ * W*H*3 floats in `where` memory. */
+int rpd_atrous_wavelet(rpd_ctx* ctx, const float* raw, const float* normal, const float* albedo,
+                       int32_t width, int32_t height, float sigma_c, float sigma_n, float sigma_a,
+                       int32_t iterations, float* out, rpd_memory where);
+/* joint_bilateral filter() core (denoising/joint_bilateral.cpp:15-132): writes the
+ * gaussian, colour-bilateral and joint outputs in one pass. */
+int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, const float* albedo,
+                        int32_t width, int32_t height, float sigma_c, float sigma_n,
+                        float sigma_p, float sigma_a, float* gaussian, float* bilateral,
+                        float* joint, rpd_memory where);
+
+/* ---- memory helpers for callers without a CUDA toolchain ---------------------------- */
+
+/* HBM owned by the caller (sample planes for RPD_MEM_DEVICE pushes). Counts against the
+ * context's budget. */
+int rpd_device_alloc(rpd_ctx* ctx, uint64_t bytes, void** out);
+int rpd_device_free(rpd_ctx* ctx, void* ptr);
+/* Page-locked host memory (fast host->HBM pushes). */
+int rpd_host_alloc(uint64_t bytes, void** out);
+int rpd_host_free(void* ptr);
+/* Synchronous copy; kind 0 = host->device, 1 = device->host, 2 = device->device. */
+int rpd_memcpy(rpd_ctx* ctx, void* dst, const void* src, uint64_t bytes, int kind);
+
+/* ---- synthetic samples (include/rpd_synth.h) ---------------------------------------- */
+
+struct rpd_synth_params;
+/* Fill the planes of `out` (radiance, normal, depth, pixel_u, lens_u, brdf_u, light_u,
+ * flags, category; albedo and pixel_albedo when non-NULL) with the seeded synthetic
+ * samples of pixels [first_pixel, first_pixel + pixel_count): spp each, or counts[i],
+ * with sample ordinals starting at start_n[i] (0 when NULL). Host and device fills are
+ * bit-identical. counts/start_n live in `where` memory like the planes. */
+int rpd_synth_fill(rpd_ctx* ctx, const struct rpd_synth_params* params, int64_t first_pixel,
+                   int64_t pixel_count, int32_t spp, const int32_t* counts, const int32_t* start_n,
+                   const rpd_sample_soa* out, rpd_memory where);
+
+const char* rpd_last_error(void);
+const char* rpd_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RPD_GB300_H */

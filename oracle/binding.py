@@ -1,0 +1,286 @@
+"""ctypes binding of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Two CPU implementations of the denoise stage with the same call sequence as the product
+(include/rpd_gb300.h):
+
+  OracleJob  the C restatement in oracle/rpd_oracle.c (built on every machine by
+             `make -C oracle port`, loaded from oracle/_build/librpd_oracle.so)
+  RefJob     the reference's own sources compiled against oracle/ref_shim
+             (`make -C oracle ref`, oracle/_ref/librpdref.so; only where the reference
+             checkout exists). Its state is the reference's process globals, so only one
+             RefJob is live at a time.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+sys.path.insert(0, str(ROOT / "rpd-statmc-denoiser_gb300"))
+import rpd_gb300 as R  # noqa: E402  (structure definitions only; the CUDA library is not loaded)
+
+PORT_LIB = HERE / "_build" / "librpd_oracle.so"
+REF_LIB = HERE / "_ref" / "librpdref.so"
+
+_port = None
+_ref = None
+
+
+def build_port() -> Path:
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "port"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return PORT_LIB
+
+
+def port() -> C.CDLL:
+    global _port
+    if _port is not None:
+        return _port
+    if not PORT_LIB.exists():
+        build_port()
+    L = C.CDLL(str(PORT_LIB))
+    vp, i32, i64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_float
+    sig = {
+        "orc_config_validate": (C.c_int, [C.POINTER(R.Config), C.c_char_p, C.c_size_t]),
+        "orc_job_create": (vp, [C.POINTER(R.Config)]),
+        "orc_job_destroy": (None, [vp]),
+        "orc_set_threads": (None, [vp, C.c_int]),
+        "orc_job_set_config": (C.c_int, [vp, C.POINTER(R.Config)]),
+        "orc_job_begin_frame": (C.c_int, [vp]),
+        "orc_job_push_samples": (C.c_int, [vp, C.POINTER(R.SampleSoA), i64, i64, i32, vp]),
+        "orc_job_end_pass": (C.c_int, [vp]),
+        "orc_recompute_sensitivity": (C.c_int, [vp]),
+        "orc_statmc_denoise": (C.c_int, [vp]),
+        "orc_variance_denoise": (C.c_int, [vp]),
+        "orc_compute_adaptive_sample_counts": (C.c_int, [vp, vp]),
+        "orc_finalize": (C.c_int, [vp]),
+        "orc_job_read": (C.c_int, [vp, C.c_int, vp, C.c_size_t]),
+        "orc_stage_ms": (C.c_double, [vp, C.c_int]),
+        "orc_atrous_wavelet": (C.c_int, [vp, vp, vp, i32, i32, f32, f32, f32, i32, vp, C.c_int]),
+        "orc_joint_bilateral": (C.c_int, [vp, vp, vp, i32, i32, f32, f32, f32, f32, vp, vp, vp, C.c_int]),
+        "orc_synth_fill": (i64, [C.POINTER(R.SynthParams), i64, i64, i32, vp, vp, C.POINTER(R.SampleSoA), C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _port = L
+    return L
+
+
+def have_ref() -> bool:
+    return REF_LIB.exists()
+
+
+def ref() -> C.CDLL:
+    global _ref
+    if _ref is not None:
+        return _ref
+    if not REF_LIB.exists():
+        raise RuntimeError(f"{REF_LIB} is not built (needs the reference checkout; make -C oracle ref)")
+    L = C.CDLL(str(REF_LIB))
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    sig = {
+        "ref_max_threads": (C.c_int, []),
+        "ref_parse_yaml": (C.c_int, [C.c_char_p, C.POINTER(R.Config), C.c_char_p, C.c_size_t]),
+        "ref_trace_cornell": (i64, [C.c_char_p, i32, i32, i32, C.c_uint32, vp, vp, C.POINTER(R.SampleSoA), i64]),
+        "ref_begin_frame": (C.c_int, [C.POINTER(R.Config)]),
+        "ref_set_config": (C.c_int, [C.POINTER(R.Config)]),
+        "ref_push_samples": (C.c_int, [C.POINTER(R.SampleSoA), i64, i64, i32, vp, C.c_int]),
+        "ref_end_pass": (C.c_int, [C.c_int]),
+        "ref_recompute_sensitivity": (C.c_int, [C.c_int]),
+        "ref_statmc_denoise": (C.c_int, [C.c_int]),
+        "ref_variance_denoise": (C.c_int, [C.c_int]),
+        "ref_compute_adaptive_sample_counts": (C.c_int, [vp, C.c_int]),
+        "ref_finalize": (C.c_int, [C.c_int]),
+        "ref_stage_ms": (C.c_double, [C.c_int]),
+        "ref_read": (C.c_int, [C.c_int, vp, C.c_size_t]),
+        "ref_render_cornell": (C.c_int, [C.c_char_p, C.POINTER(R.Config), i32, C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _ref = L
+    return L
+
+
+def _counts_ptr(counts):
+    if counts is None:
+        return None, None
+    c = np.ascontiguousarray(counts, dtype=np.int32)
+    return c, c.ctypes.data
+
+
+def synth_fill(params: R.SynthParams, first: int, count: int, spp: int, counts=None, start_n=None,
+               threads: int = 0, planes=None) -> R.HostSamples:
+    """Synthetic samples on the host (include/rpd_synth.h through oracle/synth_host.c)."""
+    c, cp = _counts_ptr(counts)
+    s0, sp = _counts_ptr(start_n)
+    total = int(c.sum()) if c is not None else count * spp
+    hs = R.HostSamples(total, count, planes)
+    soa = hs.soa()
+    n = port().orc_synth_fill(C.byref(params), first, count, spp, cp, sp, C.byref(soa), threads)
+    assert n == total
+    return hs
+
+
+class OracleJob:
+    """The C restatement (oracle/rpd_oracle.c) behind the product's call sequence."""
+
+    def __init__(self, cfg: R.Config, threads: int = 0):
+        self.cfg = cfg
+        self.handle = port().orc_job_create(C.byref(cfg))
+        if not self.handle:
+            raise ValueError("invalid config")
+        port().orc_set_threads(self.handle, threads)
+
+    def close(self):
+        if self.handle:
+            port().orc_job_destroy(self.handle)
+            self.handle = None
+
+    def set_threads(self, threads: int):
+        port().orc_set_threads(self.handle, threads)
+
+    def set_config(self, cfg: R.Config):
+        assert port().orc_job_set_config(self.handle, C.byref(cfg)) == 0
+        self.cfg = cfg.replace(image_width=self.cfg.image_width, image_height=self.cfg.image_height,
+                               rpf_tile_size=self.cfg.rpf_tile_size)
+
+    def begin_frame(self):
+        port().orc_job_begin_frame(self.handle)
+
+    def push(self, samples: R.HostSamples, first: int, count: int, spp: int = 0, counts=None):
+        c, cp = _counts_ptr(counts)
+        soa = samples.soa()
+        assert port().orc_job_push_samples(self.handle, C.byref(soa), first, count, spp, cp) == 0
+
+    def end_pass(self):
+        port().orc_job_end_pass(self.handle)
+
+    def recompute_sensitivity(self):
+        port().orc_recompute_sensitivity(self.handle)
+
+    def statmc_denoise(self):
+        port().orc_statmc_denoise(self.handle)
+
+    def variance_denoise(self):
+        port().orc_variance_denoise(self.handle)
+
+    def compute_adaptive_sample_counts(self) -> np.ndarray:
+        out = np.empty(self.cfg.image_width * self.cfg.image_height, dtype=np.int32)
+        port().orc_compute_adaptive_sample_counts(self.handle, out.ctypes.data)
+        return out
+
+    def finalize(self):
+        port().orc_finalize(self.handle)
+
+    def read(self, name: str) -> np.ndarray:
+        shape, dt = R.field_shape(self.cfg, name)
+        out = np.empty(shape, dtype=dt)
+        assert port().orc_job_read(self.handle, R.FIELD[name], out.ctypes.data, out.nbytes) == 0, name
+        return out
+
+    def stage_ms(self, stage: str) -> float:
+        return float(port().orc_stage_ms(self.handle, R.STAGE[stage]))
+
+
+class RefJob:
+    """The reference's own code (compiled in oracle/_ref) behind the same call sequence."""
+
+    def __init__(self, cfg: R.Config, threads: int = 1):
+        self.cfg = cfg
+        self.threads = threads
+        ref().ref_begin_frame(C.byref(cfg))
+
+    def close(self):
+        pass
+
+    def set_config(self, cfg: R.Config):
+        ref().ref_set_config(C.byref(cfg))
+        self.cfg = cfg.replace(image_width=self.cfg.image_width, image_height=self.cfg.image_height,
+                               rpf_tile_size=self.cfg.rpf_tile_size)
+
+    def begin_frame(self):
+        ref().ref_begin_frame(C.byref(self.cfg))
+
+    def push(self, samples: R.HostSamples, first: int, count: int, spp: int = 0, counts=None):
+        c, cp = _counts_ptr(counts)
+        soa = samples.soa()
+        assert ref().ref_push_samples(C.byref(soa), first, count, spp, cp, self.threads) == 0
+
+    def end_pass(self):
+        ref().ref_end_pass(self.threads)
+
+    def recompute_sensitivity(self):
+        ref().ref_recompute_sensitivity(self.threads)
+
+    def statmc_denoise(self):
+        ref().ref_statmc_denoise(self.threads)
+
+    def variance_denoise(self):
+        ref().ref_variance_denoise(self.threads)
+
+    def compute_adaptive_sample_counts(self) -> np.ndarray:
+        out = np.empty(self.cfg.image_width * self.cfg.image_height, dtype=np.int32)
+        ref().ref_compute_adaptive_sample_counts(out.ctypes.data, self.threads)
+        return out
+
+    def finalize(self):
+        ref().ref_finalize(self.threads)
+
+    def read(self, name: str) -> np.ndarray:
+        shape, dt = R.field_shape(self.cfg, name)
+        out = np.empty(shape, dtype=dt)
+        assert ref().ref_read(R.FIELD[name], out.ctypes.data, out.nbytes) == 0, name
+        return out
+
+    def stage_ms(self, stage: str) -> float:
+        return float(ref().ref_stage_ms(R.STAGE[stage]))
+
+
+CORNELL_PLANES = ("radiance", "normal", "depth", "albedo", "pixel_u", "lens_u", "brdf_u", "light_u", "env_u",
+                  "flags", "category")
+
+
+def trace_cornell(yaml_path: str, w: int, h: int, spp: int, seed: int, start_n=None, counts=None) -> R.HostSamples:
+    """Camera samples of the reference's cornell_box scene, traced by the reference."""
+    s0, sp = _counts_ptr(start_n)
+    c, cp = _counts_ptr(counts)
+    total = int(c.sum()) if c is not None else w * h * spp
+    hs = R.HostSamples(total, w * h, CORNELL_PLANES)
+    soa = hs.soa()
+    n = ref().ref_trace_cornell(yaml_path.encode(), w, h, spp, seed, sp, cp, C.byref(soa), total)
+    assert n == total, (n, total)
+    return hs
+
+
+def ref_parse_yaml(path: str) -> R.Config:
+    cfg = R.Config()
+    msg = C.create_string_buffer(256)
+    if ref().ref_parse_yaml(path.encode(), C.byref(cfg), msg, 256) != 0:
+        raise ValueError(msg.value.decode())
+    return cfg
+
+
+def run_pipeline(job, samples: R.HostSamples, spp: int, statmc: bool = True, variance: bool = True) -> None:
+    """The non-adaptive StatMC sequence of render() (main.cpp:1543-1557) minus finalize:
+    one pass of samples, recompute_sensitivity, statmc_denoise, variance_denoise."""
+    w, h = job.cfg.image_width, job.cfg.image_height
+    job.begin_frame()
+    job.push(samples, 0, w * h, spp)
+    job.end_pass()
+    job.recompute_sensitivity()
+    if statmc:
+        job.statmc_denoise()
+    if variance:
+        job.variance_denoise()

@@ -1,0 +1,1017 @@
+// C ABI of the GB300 denoise stage (include/rpd_gb300.h): contexts, jobs, HBM layout,
+// admission against the HBM budget, the stage entry points and field reads.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <new>
+
+#include "rpd_internal.h"
+#include "device_math.cuh"
+#include "rpd_synth.h"
+
+namespace rpd {
+
+cudaError_t launch_synth(const rpd_synth_params& prm, const rpd_synth_region* d_table, int64_t first, int64_t count,
+                         const int64_t* d_offsets, int64_t total, const int32_t* d_start_n, int32_t* d_region_of,
+                         const rpd_sample_soa& out, cudaStream_t stream);
+
+namespace {
+thread_local std::string t_last_error;
+
+// Deterministic placement of every plane in one arena, 256-byte aligned.
+struct Layout {
+    uint64_t bytes = 0;
+    template <typename T>
+    void add(T*& ptr, int64_t count) {
+        bytes = (bytes + 255) & ~uint64_t(255);
+        ptr = reinterpret_cast<T*>(static_cast<uintptr_t>(bytes));
+        bytes += uint64_t(count) * sizeof(T);
+    }
+};
+
+template <typename T>
+void rebase(T*& ptr, char* base) {
+    ptr = reinterpret_cast<T*>(base + reinterpret_cast<uintptr_t>(ptr));
+}
+
+Geometry make_geometry(const rpd_config& c) {
+    Geometry g{};
+    g.w = c.image_width;
+    g.h = c.image_height;
+    g.support = c.rpf_tile_size;
+    g.step = std::max(1, g.support / 2);                          // core/stats.h:314
+    g.nodes_x = std::max(2, (g.w + g.step - 1) / g.step + 1);     // core/stats.h:315
+    g.nodes_y = std::max(2, (g.h + g.step - 1) / g.step + 1);
+    g.np = int64_t(g.w) * g.h;
+    g.nn = int64_t(g.nodes_x) * g.nodes_y;
+    return g;
+}
+
+// Assigns (offset-encoded) plane pointers; returns the arena size.
+uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n) {
+    Layout L;
+    const int64_t np = g.np, nn = g.nn;
+    L.add(p.mean, np);
+    L.add(p.square_diff, np);
+    L.add(p.n, np);
+    for (int c = 0; c < 3; ++c) L.add(p.color_mean[c], np);
+    for (int c = 0; c < 3; ++c) L.add(p.sqrt_mean[c], np);
+    for (int c = 0; c < 3; ++c) L.add(p.sqrt_sq[c], np);
+    L.add(p.hit_count, np);
+    L.add(p.sample_count, np);
+    for (int c = 0; c < 3; ++c) L.add(p.radiance[c], np);
+    for (int c = 0; c < 3; ++c) L.add(p.normal[c], np);
+    for (int c = 0; c < 3; ++c) L.add(p.albedo[c], np);
+    L.add(p.depth, np);
+    for (int c = 0; c < 3; ++c) L.add(p.f_normal[c], np);
+    L.add(p.f_depth, np);
+    for (int c = 0; c < 3; ++c) L.add(p.f_albedo[c], np);
+    L.add(p.sens_confidence, np);
+    L.add(p.sens_gradient, np);
+    for (int c = 0; c < 6; ++c) L.add(p.rpd[c], np);
+    for (int c = 0; c < 3; ++c) L.add(p.denoised[c], np);
+    L.add(p.uncertainty, np);
+    L.add(p.alpha, np);
+    L.add(p.var_total, np);
+    L.add(p.var_eff, np);
+    L.add(p.var_ratio, np);
+    for (int c = 0; c < 3; ++c) L.add(p.sqrt_var_mean[c], np);
+    for (int c = 0; c < 3; ++c) L.add(p.sqrt_var_stable[c], np);
+    L.add(p.variance_denoised, np);
+    L.add(p.var_ping, np);
+    L.add(p.var_pong, np);
+    L.add(p.importance, np);
+    L.add(p.importance_tmp, np);
+    L.add(p.desired_add, np);
+    L.add(p.residual, np);
+    L.add(p.counts, np);
+    L.add(p.active_a, np);
+    L.add(p.active_b, np);
+    L.add(n.grid, nn * kDeps * kDepStride);
+    L.add(n.pass_grid, nn * kDeps * kDepStride);
+    for (int f = 0; f < N_FIELDS; ++f) L.add(n.field[f], nn);
+    for (int f = 0; f < R_FIELDS; ++f) L.add(n.raw[f], nn);
+    for (int f = 0; f < R_FIELDS; ++f) L.add(n.conf[f], nn);
+    for (int f = 0; f < R_FIELDS; ++f) L.add(n.prior[f], nn);
+    for (int c = 0; c < 3; ++c) L.add(n.n_normal[c], nn);
+    L.add(n.n_depth, nn);
+    for (int c = 0; c < 3; ++c) L.add(n.n_albedo[c], nn);
+    return (L.bytes + 255) & ~uint64_t(255);
+}
+
+void rebase_all(PixelPlanes& p, NodePlanes& n, char* base) {
+    rebase(p.mean, base);
+    rebase(p.square_diff, base);
+    rebase(p.n, base);
+    for (int c = 0; c < 3; ++c) {
+        rebase(p.color_mean[c], base);
+        rebase(p.sqrt_mean[c], base);
+        rebase(p.sqrt_sq[c], base);
+        rebase(p.radiance[c], base);
+        rebase(p.normal[c], base);
+        rebase(p.albedo[c], base);
+        rebase(p.f_normal[c], base);
+        rebase(p.f_albedo[c], base);
+        rebase(p.denoised[c], base);
+        rebase(p.sqrt_var_mean[c], base);
+        rebase(p.sqrt_var_stable[c], base);
+        rebase(n.n_normal[c], base);
+        rebase(n.n_albedo[c], base);
+    }
+    rebase(p.hit_count, base);
+    rebase(p.sample_count, base);
+    rebase(p.depth, base);
+    rebase(p.f_depth, base);
+    rebase(p.sens_confidence, base);
+    rebase(p.sens_gradient, base);
+    for (int c = 0; c < 6; ++c) rebase(p.rpd[c], base);
+    rebase(p.uncertainty, base);
+    rebase(p.alpha, base);
+    rebase(p.var_total, base);
+    rebase(p.var_eff, base);
+    rebase(p.var_ratio, base);
+    rebase(p.variance_denoised, base);
+    rebase(p.var_ping, base);
+    rebase(p.var_pong, base);
+    rebase(p.importance, base);
+    rebase(p.importance_tmp, base);
+    rebase(p.desired_add, base);
+    rebase(p.residual, base);
+    rebase(p.counts, base);
+    rebase(p.active_a, base);
+    rebase(p.active_b, base);
+    rebase(n.grid, base);
+    rebase(n.pass_grid, base);
+    for (int f = 0; f < N_FIELDS; ++f) rebase(n.field[f], base);
+    for (int f = 0; f < R_FIELDS; ++f) {
+        rebase(n.raw[f], base);
+        rebase(n.conf[f], base);
+        rebase(n.prior[f], base);
+    }
+    rebase(n.n_depth, base);
+}
+
+struct StageTimer {
+    Job& j;
+    rpd_stage s;
+    StageTimer(Job& job, rpd_stage stage) : j(job), s(stage) {
+        cudaEventRecord(j.ev_start[s], j.stream);
+    }
+    ~StageTimer() {
+        cudaEventRecord(j.ev_stop[s], j.stream);
+        j.ev_used[s] = true;
+    }
+};
+
+__global__ void k_pack3(const float* a, const float* b, const float* c, float* out, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[3 * i] = a[i];
+    out[3 * i + 1] = b[i];
+    out[3 * i + 2] = c[i];
+}
+
+bool device_ok(int device, std::string* why) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) {
+        *why = "no CUDA device " + std::to_string(device);
+        return false;
+    }
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        *why = "cannot query CUDA device";
+        return false;
+    }
+    if (prop.major != 10 || prop.minor != 3) {
+        *why = "device " + std::string(prop.name) + " is sm_" + std::to_string(prop.major) +
+               std::to_string(prop.minor) + "; this build targets sm_103a (GB300)";
+        return false;
+    }
+    return true;
+}
+
+int grow_device(Job& j, void** buf, uint64_t* cap, uint64_t need) {
+    if (*cap >= need) return RPD_OK;
+    if (*buf) {
+        cudaStreamSynchronize(j.stream);
+        cudaFree(*buf);
+        j.ctx->in_use -= *cap;
+        *buf = nullptr;
+        *cap = 0;
+    }
+    const uint64_t want = need + need / 8;
+    if (j.ctx->in_use.load() + want > j.ctx->budget)
+        return fail(RPD_ERR_OVER_BUDGET, "staging buffer of " + std::to_string(want) + " bytes exceeds the HBM budget");
+    cudaError_t e = cudaMalloc(buf, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMalloc staging: ") + cudaGetErrorString(e));
+    }
+    j.ctx->in_use += want;
+    *cap = want;
+    return RPD_OK;
+}
+
+int ensure_offsets(Job& j, int64_t count) {
+    // count+1 offsets plus room for the scan's block sums
+    const int64_t need = count + 1 + (count + 1023) / 1024 + 2;
+    if (j.offsets_cap >= need) return RPD_OK;
+    if (j.offsets) {
+        cudaStreamSynchronize(j.stream);
+        cudaFree(j.offsets);
+        j.ctx->in_use -= uint64_t(j.offsets_cap) * 8;
+        j.offsets = nullptr;
+        j.offsets_cap = 0;
+    }
+    const int64_t want = need + need / 8 + 64;
+    cudaError_t e = cudaMalloc(&j.offsets, uint64_t(want) * 8);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMalloc offsets: ") + cudaGetErrorString(e));
+    }
+    j.ctx->in_use += uint64_t(want) * 8;
+    j.offsets_cap = want;
+    return RPD_OK;
+}
+
+int ensure_features(Job& j) {
+    if (j.features_valid) return RPD_OK;
+    RPD_CUDA(launch_feature_cache(j));
+    j.features_valid = true;
+    return RPD_OK;
+}
+
+int ensure_cache(Job& j) {
+    if (j.cache_valid) return RPD_OK;
+    RPD_CUDA(launch_rpd_cache(j));
+    j.cache_valid = true;
+    return RPD_OK;
+}
+
+#define CHECK_JOB(j) \
+    if (!(j)) return fail(RPD_ERR_INVALID_ARGUMENT, "null job handle")
+
+}  // namespace
+
+void set_error(const std::string& msg) { t_last_error = msg; }
+int fail(int status, const std::string& msg) {
+    t_last_error = msg;
+    return status;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    cudaGetLastError();
+    t_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return RPD_ERR_CUDA;
+}
+
+}  // namespace rpd
+
+using namespace rpd;
+
+extern "C" {
+
+const char* rpd_last_error(void) { return t_last_error.c_str(); }
+
+const char* rpd_status_string(int s) {
+    switch (s) {
+    case RPD_OK: return "ok";
+    case RPD_ERR_INVALID_CONFIG: return "invalid config";
+    case RPD_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case RPD_ERR_OUT_OF_MEMORY: return "out of memory";
+    case RPD_ERR_OVER_BUDGET: return "over HBM budget";
+    case RPD_ERR_CUDA: return "CUDA error";
+    case RPD_ERR_TIMEOUT: return "device wait timed out";
+    case RPD_ERR_STATE: return "call out of order";
+    case RPD_ERR_NO_DEVICE: return "no sm_103 device";
+    default: return "unknown status";
+    }
+}
+
+void rpd_config_defaults(rpd_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    // RenderConfig defaults (core/config.h:28-47)
+    c->rpf_tile_size = 8;
+    c->rpf_shrinkage_scale = 1.0f;
+    c->rpf_confidence_samples = 128.0f;
+    c->color_window_radius = 7;
+    c->color_normal_threshold = 0.5f;
+    c->color_depth_threshold = 0.25f;
+    c->color_compat_alpha = 0.05f;
+    c->color_sigma_max = 6.0f;
+    c->var_window_radius = 1;
+    c->var_normal_threshold = 0.5f;
+    c->var_depth_threshold = 0.25f;
+    c->var_compat_sigma = 30.0f;
+    c->var_shrinkage_k = 1e-3f;
+    c->var_iterations = 2;
+    c->adaptive_base_samples = 0;
+    c->adaptive_spp = 0;
+    c->adaptive_sigma_max = 3.0f;
+    c->adaptive_passes = 1;
+    c->adaptive_importance_smoothing_radius = 1;
+    c->debug_statmc_outputs = 0;
+}
+
+int rpd_config_validate(const rpd_config* c, char* msg, size_t cap) {
+    auto bad = [&](const char* text) {
+        if (msg && cap) {
+            std::strncpy(msg, text, cap - 1);
+            msg[cap - 1] = 0;
+        }
+        set_error(text);
+        return int(RPD_ERR_INVALID_CONFIG);
+    };
+    if (!c) return bad("null config");
+    // parse_render_config's checks (core/config.h:116-195) on the stage's fields
+    if (c->image_width <= 0 || c->image_height <= 0) return bad("image_width and image_height must be positive");
+    if (c->rpf_tile_size <= 0) return bad("rpf_tile_size must be positive");
+    if (c->color_window_radius <= 0) return bad("color_window_radius must be positive");
+    if (!std::isfinite(c->color_normal_threshold) || c->color_normal_threshold <= 0.0f || c->color_normal_threshold > 1.0f)
+        return bad("color_normal_threshold must be finite and in (0,1]");
+    if (!std::isfinite(c->color_depth_threshold) || c->color_depth_threshold < 0.0f)
+        return bad("color_depth_threshold must be finite and non-negative");
+    if (!std::isfinite(c->color_compat_alpha) || c->color_compat_alpha <= 0.0f || c->color_compat_alpha >= 1.0f)
+        return bad("color_compat_alpha must be finite and in (0,1)");
+    if (!std::isfinite(c->color_sigma_max) || c->color_sigma_max <= 0.0f)
+        return bad("color_sigma_max must be finite and positive");
+    if (c->var_window_radius <= 0) return bad("var_window_radius must be positive");
+    if (!std::isfinite(c->var_normal_threshold) || c->var_normal_threshold <= 0.0f || c->var_normal_threshold > 1.0f)
+        return bad("var_normal_threshold must be finite and in (0,1]");
+    if (!std::isfinite(c->var_depth_threshold) || c->var_depth_threshold < 0.0f)
+        return bad("var_depth_threshold must be finite and non-negative");
+    if (!std::isfinite(c->var_compat_sigma) || c->var_compat_sigma <= 0.0f)
+        return bad("var_compat_sigma must be finite and positive");
+    if (!std::isfinite(c->var_shrinkage_k) || c->var_shrinkage_k <= 0.0f)
+        return bad("var_shrinkage_k must be finite and positive");
+    if (c->adaptive_base_samples < 0) return bad("adaptive_base_samples must be non-negative");
+    if (c->adaptive_spp < 0) return bad("adaptive_spp must be non-negative");
+    if (c->adaptive_base_samples > c->adaptive_spp) return bad("adaptive_base_samples cannot exceed adaptive_spp");
+    if (!std::isfinite(c->adaptive_sigma_max) || c->adaptive_sigma_max <= 0.0f)
+        return bad("adaptive_sigma_max must be finite and positive");
+    if (c->adaptive_passes < 0) return bad("adaptive_passes must be non-negative");
+    if (c->adaptive_importance_smoothing_radius < 0) return bad("adaptive_importance_smoothing_radius must be non-negative");
+    if (c->var_iterations <= 0) return bad("var_iterations must be positive");
+    if (!std::isfinite(c->rpf_shrinkage_scale) || c->rpf_shrinkage_scale < 0.0f)
+        return bad("rpf_shrinkage_scale must be finite and non-negative");
+    if (!std::isfinite(c->rpf_confidence_samples) || c->rpf_confidence_samples <= 0.0f)
+        return bad("rpf_confidence_samples must be finite and positive");
+    if (int64_t(c->image_width) * c->image_height > (int64_t(1) << 31) / 8)
+        return bad("image is too large for 32-bit sample budgets");
+    if (msg && cap) msg[0] = 0;
+    return RPD_OK;
+}
+
+int rpd_ctx_create(int device, uint64_t budget, rpd_ctx** out) {
+    if (!out) return fail(RPD_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    std::string why;
+    if (!device_ok(device, &why)) return fail(RPD_ERR_NO_DEVICE, why);
+    RPD_CUDA(cudaSetDevice(device));
+    size_t free_b = 0, total_b = 0;
+    RPD_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    Ctx* c = new (std::nothrow) Ctx();
+    if (!c) return fail(RPD_ERR_OUT_OF_MEMORY, "context allocation failed");
+    c->device = device;
+    c->budget = budget ? budget : uint64_t(free_b);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->util_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    *out = reinterpret_cast<rpd_ctx*>(c);
+    return RPD_OK;
+}
+
+void rpd_ctx_destroy(rpd_ctx* ctx) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->util_stream) cudaStreamDestroy(c->util_stream);
+    delete c;
+}
+
+uint64_t rpd_ctx_bytes_in_use(const rpd_ctx* ctx) {
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c ? c->in_use.load() : 0;
+}
+
+uint64_t rpd_job_footprint(const rpd_config* cfg) {
+    if (!cfg || cfg->image_width <= 0 || cfg->image_height <= 0 || cfg->rpf_tile_size <= 0) return 0;
+    PixelPlanes p{};
+    NodePlanes n{};
+    return plan(make_geometry(*cfg), p, n);
+}
+
+int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !cfg || !out) return fail(RPD_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    char msg[256];
+    if (rpd_config_validate(cfg, msg, sizeof(msg)) != RPD_OK) return fail(RPD_ERR_INVALID_CONFIG, msg);
+    RPD_CUDA(cudaSetDevice(c->device));
+    Job* j = new (std::nothrow) Job();
+    if (!j) return fail(RPD_ERR_OUT_OF_MEMORY, "job allocation failed");
+    j->ctx = c;
+    j->cfg = *cfg;
+    j->g = make_geometry(*cfg);
+    j->arena_bytes = plan(j->g, j->p, j->n);
+    {
+        std::lock_guard<std::mutex> lock(c->mu);
+        if (c->in_use.load() + j->arena_bytes > c->budget) {
+            const uint64_t need = j->arena_bytes;
+            delete j;
+            return fail(RPD_ERR_OVER_BUDGET, "job needs " + std::to_string(need) + " bytes of HBM; " +
+                                                 std::to_string(c->budget - std::min(c->budget, c->in_use.load())) +
+                                                 " left in the budget");
+        }
+        cudaError_t e = cudaMalloc(&j->arena, j->arena_bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            delete j;
+            return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMalloc job arena: ") + cudaGetErrorString(e));
+        }
+        c->in_use += j->arena_bytes;
+    }
+    rebase_all(j->p, j->n, static_cast<char*>(j->arena));
+    cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
+    for (int s = 0; s < RPD_STAGE_COUNT_ && e == cudaSuccess; ++s) {
+        e = cudaEventCreate(&j->ev_start[s]);
+        if (e == cudaSuccess) e = cudaEventCreate(&j->ev_stop[s]);
+    }
+    if (e == cudaSuccess) e = cudaMallocHost(&j->scalars, 64);
+    if (e == cudaSuccess) e = cudaMemsetAsync(j->arena, 0, j->arena_bytes, j->stream);
+    if (e != cudaSuccess) {
+        rpd_job_destroy(reinterpret_cast<rpd_job*>(j));
+        return cuda_fail(e, "job set-up");
+    }
+    *out = reinterpret_cast<rpd_job*>(j);
+    return RPD_OK;
+}
+
+void rpd_job_destroy(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    if (!j) return;
+    cudaSetDevice(j->ctx->device);
+    if (j->stream) cudaStreamSynchronize(j->stream);
+    if (j->arena) {
+        cudaFree(j->arena);
+        j->ctx->in_use -= j->arena_bytes;
+    }
+    if (j->staging) {
+        cudaFree(j->staging);
+        j->ctx->in_use -= j->staging_bytes;
+    }
+    if (j->offsets) {
+        cudaFree(j->offsets);
+        j->ctx->in_use -= uint64_t(j->offsets_cap) * 8;
+    }
+    if (j->scalars) cudaFreeHost(j->scalars);
+    for (int s = 0; s < RPD_STAGE_COUNT_; ++s) {
+        if (j->ev_start[s]) cudaEventDestroy(j->ev_start[s]);
+        if (j->ev_stop[s]) cudaEventDestroy(j->ev_stop[s]);
+    }
+    if (j->stream) cudaStreamDestroy(j->stream);
+    delete j;
+}
+
+int rpd_job_set_config(rpd_job* job, const rpd_config* cfg) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!cfg) return fail(RPD_ERR_INVALID_ARGUMENT, "null config");
+    rpd_config c = *cfg;
+    c.image_width = j->cfg.image_width;
+    c.image_height = j->cfg.image_height;
+    c.rpf_tile_size = j->cfg.rpf_tile_size;
+    char msg[256];
+    if (rpd_config_validate(&c, msg, sizeof(msg)) != RPD_OK) return fail(RPD_ERR_INVALID_CONFIG, msg);
+    j->cfg = c;
+    return RPD_OK;
+}
+
+int rpd_job_begin_frame(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    RPD_CUDA(cudaMemsetAsync(j->arena, 0, j->arena_bytes, j->stream));
+    j->pass_open = false;
+    j->features_valid = false;
+    j->cache_valid = false;
+    j->have_samples = false;
+    return RPD_OK;
+}
+
+int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first, int64_t count, int32_t spp,
+                         const int32_t* counts, rpd_memory where) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!s) return fail(RPD_ERR_INVALID_ARGUMENT, "null sample planes");
+    if (first < 0 || count < 0 || first + count > j->g.np)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "pixel span [" + std::to_string(first) + ", " +
+                                                  std::to_string(first + count) + ") is outside the image");
+    if (!counts && spp < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "negative spp");
+    if (count == 0) return RPD_OK;
+    if (!s->radiance[0] || !s->radiance[1] || !s->radiance[2])
+        return fail(RPD_ERR_INVALID_ARGUMENT, "radiance planes are required");
+    if (!s->flags) return fail(RPD_ERR_INVALID_ARGUMENT, "flags plane is required");
+    {
+        // a multi-component plane is either fully present or fully absent
+        auto pair_ok = [](const float* const* v, int n) {
+            int present = 0;
+            for (int c = 0; c < n; ++c) present += v[c] != nullptr;
+            return present == 0 || present == n;
+        };
+        if (!pair_ok(s->normal, 3) || !pair_ok(s->albedo, 3) || !pair_ok(s->pixel_albedo, 3) ||
+            !pair_ok(s->pixel_u, 2) || !pair_ok(s->lens_u, 2) || !pair_ok(s->brdf_u, 2) || !pair_ok(s->light_u, 2) ||
+            !pair_ok(s->env_u, 2))
+            return fail(RPD_ERR_INVALID_ARGUMENT, "a multi-component sample plane is only partly given");
+    }
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    int st = ensure_offsets(*j, count);
+    if (st != RPD_OK) return st;
+
+    StageTimer timer(*j, RPD_STAGE_ACCUMULATE);
+    int64_t total = 0;
+    if (counts) {
+        if (where == RPD_MEM_HOST) {
+            for (int64_t i = 0; i < count; ++i) {
+                if (counts[i] < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "negative per-pixel sample count");
+                total += counts[i];
+            }
+        }
+    } else {
+        total = int64_t(count) * spp;
+    }
+
+    DeviceSamples d{};
+    if (where == RPD_MEM_HOST) {
+        // one staging arena: the planes that are present, then the counts
+        struct Plane { const void* src; uint64_t bytes; const void** dst; };
+        std::vector<Plane> planes;
+        auto fplane = [&](const float* src, const float** dst, int64_t n) {
+            if (src) planes.push_back({src, uint64_t(n) * 4, reinterpret_cast<const void**>(dst)});
+        };
+        for (int c = 0; c < 3; ++c) {
+            fplane(s->radiance[c], &d.radiance[c], total);
+            fplane(s->normal[c], &d.normal[c], total);
+            fplane(s->albedo[c], &d.albedo[c], total);
+            fplane(s->pixel_albedo[c], &d.pixel_albedo[c], count);
+        }
+        fplane(s->depth, &d.depth, total);
+        for (int c = 0; c < 2; ++c) {
+            fplane(s->pixel_u[c], &d.pixel_u[c], total);
+            fplane(s->lens_u[c], &d.lens_u[c], total);
+            fplane(s->brdf_u[c], &d.brdf_u[c], total);
+            fplane(s->light_u[c], &d.light_u[c], total);
+            fplane(s->env_u[c], &d.env_u[c], total);
+        }
+        planes.push_back({s->flags, uint64_t(total), reinterpret_cast<const void**>(&d.flags)});
+        if (s->category) planes.push_back({s->category, uint64_t(total), reinterpret_cast<const void**>(&d.category)});
+        const int32_t* d_counts = nullptr;
+        if (counts) planes.push_back({counts, uint64_t(count) * 4, reinterpret_cast<const void**>(&d_counts)});
+        uint64_t need = 0;
+        for (auto& p : planes) need = ((need + 255) & ~uint64_t(255)) + p.bytes;
+        st = grow_device(*j, &j->staging, &j->staging_bytes, need + 256);
+        if (st != RPD_OK) return st;
+        uint64_t off = 0;
+        for (auto& p : planes) {
+            off = (off + 255) & ~uint64_t(255);
+            char* dst = static_cast<char*>(j->staging) + off;
+            if (p.bytes) RPD_CUDA(cudaMemcpyAsync(dst, p.src, p.bytes, cudaMemcpyHostToDevice, j->stream));
+            *p.dst = dst;
+            off += p.bytes;
+        }
+        if (counts) RPD_CUDA(launch_offsets_scan(*j, d_counts, count));
+        else RPD_CUDA(launch_offsets_uniform(*j, count, spp));
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            d.radiance[c] = s->radiance[c];
+            d.normal[c] = s->normal[c];
+            d.albedo[c] = s->albedo[c];
+            d.pixel_albedo[c] = s->pixel_albedo[c];
+        }
+        d.depth = s->depth;
+        for (int c = 0; c < 2; ++c) {
+            d.pixel_u[c] = s->pixel_u[c];
+            d.lens_u[c] = s->lens_u[c];
+            d.brdf_u[c] = s->brdf_u[c];
+            d.light_u[c] = s->light_u[c];
+            d.env_u[c] = s->env_u[c];
+        }
+        d.flags = s->flags;
+        d.category = s->category;
+        if (counts) RPD_CUDA(launch_offsets_scan(*j, counts, count));
+        else RPD_CUDA(launch_offsets_uniform(*j, count, spp));
+    }
+    if (!d.normal[0] || !d.normal[1] || !d.normal[2] || !d.depth ||
+        (!d.albedo[0] && !d.pixel_albedo[0]))
+        return fail(RPD_ERR_INVALID_ARGUMENT, "normal, depth and albedo (per sample or per pixel) are required");
+    RPD_CUDA(launch_accumulate_pixels(*j, d, first, count));
+    if (j->cfg.rpf_shrinkage_scale > 0.0f) {
+        if (!d.category) return fail(RPD_ERR_INVALID_ARGUMENT, "category plane is required when RPD is enabled");
+        RPD_CUDA(launch_accumulate_grid(*j, d, first, count));
+    }
+    j->pass_open = true;
+    j->have_samples = true;
+    j->features_valid = false;
+    j->cache_valid = false;
+    return RPD_OK;
+}
+
+int rpd_job_end_pass(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    if (j->pass_open && j->cfg.rpf_shrinkage_scale > 0.0f) RPD_CUDA(launch_merge_grid(*j));
+    j->pass_open = false;
+    j->features_valid = false;
+    j->cache_valid = false;
+    return RPD_OK;
+}
+
+int rpd_recompute_sensitivity(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    if (j->pass_open) {
+        int st = rpd_job_end_pass(job);
+        if (st != RPD_OK) return st;
+    }
+    StageTimer timer(*j, RPD_STAGE_SENSITIVITY);
+    j->cache_valid = false;
+    if (j->cfg.rpf_shrinkage_scale <= 0.0f) {
+        RPD_CUDA(launch_sensitivity_zero(*j));
+    } else {
+        int st = ensure_features(*j);
+        if (st != RPD_OK) return st;
+        RPD_CUDA(launch_sensitivity(*j));
+    }
+    return ensure_cache(*j);
+}
+
+int rpd_statmc_denoise(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    StageTimer timer(*j, RPD_STAGE_STATMC);
+    int st = ensure_features(*j);
+    if (st != RPD_OK) return st;
+    st = ensure_cache(*j);
+    if (st != RPD_OK) return st;
+    RPD_CUDA(launch_statmc(*j));
+    return RPD_OK;
+}
+
+int rpd_variance_denoise(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    StageTimer timer(*j, RPD_STAGE_VARIANCE);
+    int st = ensure_features(*j);
+    if (st != RPD_OK) return st;
+    RPD_CUDA(launch_variance(*j));
+    return RPD_OK;
+}
+
+int rpd_compute_adaptive_sample_counts(rpd_job* job, int32_t* out, rpd_memory where) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    {
+        StageTimer timer(*j, RPD_STAGE_ADAPTIVE);
+        int st = ensure_features(*j);
+        if (st != RPD_OK) return st;
+        RPD_CUDA(launch_adaptive(*j));
+    }
+    if (out) {
+        const uint64_t bytes = uint64_t(j->g.np) * 4;
+        RPD_CUDA(cudaMemcpyAsync(out, j->p.counts, bytes,
+                                 where == RPD_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, j->stream));
+        if (where == RPD_MEM_HOST) RPD_CUDA(cudaStreamSynchronize(j->stream));
+    }
+    return RPD_OK;
+}
+
+int rpd_finalize(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    RPD_CUDA(launch_finalize(*j));
+    j->features_valid = false;
+    return RPD_OK;
+}
+
+uint64_t rpd_field_bytes(const rpd_job* job, rpd_field f) {
+    const Job* j = reinterpret_cast<const Job*>(job);
+    if (!j) return 0;
+    const uint64_t np = uint64_t(j->g.np), nn = uint64_t(j->g.nn);
+    switch (f) {
+    case RPD_FIELD_DENOISED: case RPD_FIELD_RADIANCE_SUM: case RPD_FIELD_NORMAL_SUM: case RPD_FIELD_ALBEDO_SUM:
+    case RPD_FIELD_STATS_COLOR_MEAN: case RPD_FIELD_STATS_SQRT_MEAN: case RPD_FIELD_STATS_SQRT_SQUARE_DIFF:
+        return np * 12;
+    case RPD_FIELD_GRID: return nn * kDeps * kDepStride * 8;
+    default:
+        if (f >= RPD_FIELD_NODE_ALL && f <= RPD_FIELD_NODE_RR_CONF) return nn * 4;
+        if (f >= 0 && f < RPD_FIELD_COUNT_) return np * 4;
+        return 0;
+    }
+}
+
+int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory where) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    const uint64_t need = rpd_field_bytes(job, f);
+    if (need == 0 || bytes != need || !dst)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "field " + std::to_string(int(f)) + " needs " + std::to_string(need) +
+                                                  " bytes, got " + std::to_string(bytes));
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    const int64_t np = j->g.np;
+    const cudaMemcpyKind kind = where == RPD_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    const void* src = nullptr;
+    float* const* rgb = nullptr;
+    switch (f) {
+    case RPD_FIELD_DENOISED: rgb = j->p.denoised; break;
+    case RPD_FIELD_RADIANCE_SUM: rgb = j->p.radiance; break;
+    case RPD_FIELD_NORMAL_SUM: rgb = j->p.normal; break;
+    case RPD_FIELD_ALBEDO_SUM: rgb = j->p.albedo; break;
+    case RPD_FIELD_STATS_COLOR_MEAN: rgb = j->p.color_mean; break;
+    case RPD_FIELD_STATS_SQRT_MEAN: rgb = j->p.sqrt_mean; break;
+    case RPD_FIELD_STATS_SQRT_SQUARE_DIFF: rgb = j->p.sqrt_sq; break;
+    case RPD_FIELD_UNCERTAINTY: src = j->p.uncertainty; break;
+    case RPD_FIELD_ALPHA: src = j->p.alpha; break;
+    case RPD_FIELD_VAR_TOTAL_DEBUG: src = j->p.var_total; break;
+    case RPD_FIELD_VAR_EFF_DEBUG: src = j->p.var_eff; break;
+    case RPD_FIELD_VAR_RATIO_DEBUG: src = j->p.var_ratio; break;
+    case RPD_FIELD_VARIANCE_DENOISED: src = j->p.variance_denoised; break;
+    case RPD_FIELD_ADAPTIVE_IMPORTANCE: src = j->p.importance; break;
+    case RPD_FIELD_SENSITIVITY_CONFIDENCE: src = j->p.sens_confidence; break;
+    case RPD_FIELD_SENSITIVITY_GRADIENT: src = j->p.sens_gradient; break;
+    case RPD_FIELD_HIT_COUNT: src = j->p.hit_count; break;
+    case RPD_FIELD_SAMPLE_COUNT: src = j->p.sample_count; break;
+    case RPD_FIELD_DEPTH_SUM: src = j->p.depth; break;
+    case RPD_FIELD_STATS_MEAN: src = j->p.mean; break;
+    case RPD_FIELD_STATS_SQUARE_DIFF: src = j->p.square_diff; break;
+    case RPD_FIELD_STATS_N: src = j->p.n; break;
+    case RPD_FIELD_GRID: src = j->n.grid; break;
+    case RPD_FIELD_ADAPTIVE_COUNTS: src = j->p.counts; break;
+    default: break;
+    }
+    if (f >= RPD_FIELD_NODE_ALL && f <= RPD_FIELD_NODE_RR_CONF) src = j->n.field[f - RPD_FIELD_NODE_ALL];
+    if (src) {
+        RPD_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, j->stream));
+        RPD_CUDA(cudaStreamSynchronize(j->stream));
+        return RPD_OK;
+    }
+    // fields computed on read go through the staging buffer
+    int st = grow_device(*j, &j->staging, &j->staging_bytes, need);
+    if (st != RPD_OK) return st;
+    float* tmp = static_cast<float*>(j->staging);
+    if (rgb) {
+        k_pack3<<<grid_for(np, 256), 256, 0, j->stream>>>(rgb[0], rgb[1], rgb[2], tmp, np);
+        j->launches += 1;
+        RPD_CUDA(cudaGetLastError());
+    } else if (f >= RPD_FIELD_EXPANDED_ALL && f <= RPD_FIELD_EXPANDED_RR) {
+        static const int map[9] = {N_ALL, N_PIXEL, N_BRDF, N_LENS, N_LIGHT, N_LIGHT_UV, N_LIGHT_SELECT, N_ENV, N_RR};
+        RPD_CUDA(launch_expand(*j, j->n.field[map[f - RPD_FIELD_EXPANDED_ALL]], tmp));
+    } else {
+        return fail(RPD_ERR_INVALID_ARGUMENT, "unknown field");
+    }
+    RPD_CUDA(cudaMemcpyAsync(dst, tmp, bytes, kind, j->stream));
+    RPD_CUDA(cudaStreamSynchronize(j->stream));
+    return RPD_OK;
+}
+
+int rpd_job_sync(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    RPD_CUDA(cudaStreamSynchronize(j->stream));
+    return RPD_OK;
+}
+
+float rpd_job_stage_ms(const rpd_job* job, rpd_stage s) {
+    const Job* j = reinterpret_cast<const Job*>(job);
+    if (!j || s < 0 || s >= RPD_STAGE_COUNT_ || !j->ev_used[s]) return -1.0f;
+    float ms = -1.0f;
+    if (cudaEventSynchronize(j->ev_stop[s]) != cudaSuccess) return -1.0f;
+    if (cudaEventElapsedTime(&ms, j->ev_start[s], j->ev_stop[s]) != cudaSuccess) return -1.0f;
+    return ms;
+}
+
+uint64_t rpd_job_launch_count(const rpd_job* job) {
+    const Job* j = reinterpret_cast<const Job*>(job);
+    return j ? j->launches.load() : 0;
+}
+
+int rpd_device_alloc(rpd_ctx* ctx, uint64_t bytes, void** out) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !out) return fail(RPD_ERR_INVALID_ARGUMENT, "null argument");
+    if (c->in_use.load() + bytes > c->budget) return fail(RPD_ERR_OVER_BUDGET, "allocation exceeds the HBM budget");
+    RPD_CUDA(cudaSetDevice(c->device));
+    cudaError_t e = cudaMalloc(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    c->in_use += bytes;
+    std::lock_guard<std::mutex> lock(c->mu);
+    c->user_allocs[*out] = bytes;
+    return RPD_OK;
+}
+
+int rpd_device_free(rpd_ctx* ctx, void* ptr) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c) return fail(RPD_ERR_INVALID_ARGUMENT, "null context");
+    if (!ptr) return RPD_OK;
+    uint64_t bytes = 0;
+    {
+        std::lock_guard<std::mutex> lock(c->mu);
+        auto it = c->user_allocs.find(ptr);
+        if (it == c->user_allocs.end()) return fail(RPD_ERR_INVALID_ARGUMENT, "pointer was not allocated by rpd_device_alloc");
+        bytes = it->second;
+        c->user_allocs.erase(it);
+    }
+    RPD_CUDA(cudaSetDevice(c->device));
+    RPD_CUDA(cudaFree(ptr));
+    c->in_use -= bytes;
+    return RPD_OK;
+}
+
+int rpd_host_alloc(uint64_t bytes, void** out) {
+    if (!out) return fail(RPD_ERR_INVALID_ARGUMENT, "null argument");
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    return RPD_OK;
+}
+
+int rpd_host_free(void* ptr) {
+    if (ptr) RPD_CUDA(cudaFreeHost(ptr));
+    return RPD_OK;
+}
+
+int rpd_memcpy(rpd_ctx* ctx, void* dst, const void* src, uint64_t bytes, int kind) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c) return fail(RPD_ERR_INVALID_ARGUMENT, "null context");
+    RPD_CUDA(cudaSetDevice(c->device));
+    const cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost
+                                                                             : cudaMemcpyDeviceToDevice;
+    RPD_CUDA(cudaMemcpyAsync(dst, src, bytes, k, c->util_stream));
+    RPD_CUDA(cudaStreamSynchronize(c->util_stream));
+    return RPD_OK;
+}
+
+int rpd_synth_fill(rpd_ctx* ctx, const rpd_synth_params* prm, int64_t first, int64_t count, int32_t spp,
+                   const int32_t* counts, const int32_t* start_n, const rpd_sample_soa* out, rpd_memory where) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!prm || !out) return fail(RPD_ERR_INVALID_ARGUMENT, "null argument");
+    if (prm->regions <= 0 || prm->regions > RPD_SYNTH_MAX_REGIONS || prm->lights <= 0 || prm->lights > 15)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "synthetic regions must be in 1..256 and lights in 1..15");
+    if (first < 0 || count < 0 || first + count > int64_t(prm->width) * prm->height)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "pixel span outside the synthetic image");
+    std::vector<rpd_synth_region> table(size_t(prm->regions));
+    for (int r = 0; r < prm->regions; ++r) rpd_synth_region_make(prm, r, &table[size_t(r)]);
+    if (where == RPD_MEM_HOST) {
+        int64_t k = 0;
+        for (int64_t i = 0; i < count; ++i) {
+            const int64_t pix = first + i;
+            const int x = int(pix % prm->width), y = int(pix / prm->width);
+            const rpd_synth_region& reg = table[size_t(rpd_synth_pixel_region(prm, table.data(), x, y))];
+            if (out->pixel_albedo[0])
+                for (int ch = 0; ch < 3; ++ch) const_cast<float*>(out->pixel_albedo[ch])[i] = reg.albedo[ch];
+            const int32_t n = counts ? counts[i] : spp;
+            const uint32_t n0 = start_n ? uint32_t(start_n[i]) : 0u;
+            for (int32_t q = 0; q < n; ++q, ++k) {
+                rpd_synth_sample sm;
+                rpd_synth_sample_make(prm, &reg, x, y, n0 + uint32_t(q), &sm);
+                for (int ch = 0; ch < 3; ++ch) {
+                    const_cast<float*>(out->radiance[ch])[k] = sm.radiance[ch];
+                    const_cast<float*>(out->normal[ch])[k] = sm.normal[ch];
+                    if (out->albedo[0]) const_cast<float*>(out->albedo[ch])[k] = reg.albedo[ch];
+                }
+                const_cast<float*>(out->depth)[k] = sm.depth;
+                for (int ch = 0; ch < 2; ++ch) {
+                    const_cast<float*>(out->pixel_u[ch])[k] = sm.pixel_u[ch];
+                    const_cast<float*>(out->lens_u[ch])[k] = sm.lens_u[ch];
+                    const_cast<float*>(out->brdf_u[ch])[k] = sm.brdf_u[ch];
+                    const_cast<float*>(out->light_u[ch])[k] = sm.light_u[ch];
+                }
+                const_cast<uint8_t*>(out->flags)[k] = sm.flags;
+                const_cast<uint8_t*>(out->category)[k] = sm.category;
+            }
+        }
+        return RPD_OK;
+    }
+    if (!c) return fail(RPD_ERR_INVALID_ARGUMENT, "a context is needed for a device fill");
+    RPD_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->util_stream;
+    rpd_synth_region* d_table = nullptr;
+    int64_t* d_offsets = nullptr;
+    int32_t* d_region = nullptr;
+    const int64_t nblocks = (count + 1023) / 1024;
+    RPD_CUDA(cudaMallocAsync(&d_table, table.size() * sizeof(rpd_synth_region), st));
+    RPD_CUDA(cudaMallocAsync(&d_offsets, uint64_t(count + 1) * 8, st));
+    RPD_CUDA(cudaMallocAsync(&d_region, uint64_t(std::max<int64_t>(count, 1)) * 4, st));
+    RPD_CUDA(cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(rpd_synth_region), cudaMemcpyHostToDevice, st));
+    int64_t total = 0;
+    {
+        // offsets through a temporary job-less scan
+        Job tmp;
+        tmp.ctx = c;
+        tmp.stream = st;
+        tmp.offsets = d_offsets;
+        if (counts) {
+            // launch_offsets_scan writes its block sums after offsets[count]; use a
+            // dedicated buffer large enough for both
+            int64_t* both = nullptr;
+            RPD_CUDA(cudaMallocAsync(&both, uint64_t(count + 1 + nblocks + 2) * 8, st));
+            tmp.offsets = both;
+            RPD_CUDA(launch_offsets_scan(tmp, counts, count));
+            RPD_CUDA(cudaMemcpyAsync(d_offsets, both, uint64_t(count + 1) * 8, cudaMemcpyDeviceToDevice, st));
+            RPD_CUDA(cudaMemcpyAsync(&total, both + count, 8, cudaMemcpyDeviceToHost, st));
+            RPD_CUDA(cudaStreamSynchronize(st));
+            RPD_CUDA(cudaFreeAsync(both, st));
+            tmp.offsets = d_offsets;
+        } else {
+            RPD_CUDA(launch_offsets_uniform(tmp, count, spp));
+            total = count * int64_t(spp);
+        }
+    }
+    RPD_CUDA(launch_synth(*prm, d_table, first, count, d_offsets, total, start_n, d_region, *out, st));
+    RPD_CUDA(cudaFreeAsync(d_table, st));
+    RPD_CUDA(cudaFreeAsync(d_offsets, st));
+    RPD_CUDA(cudaFreeAsync(d_region, st));
+    RPD_CUDA(cudaStreamSynchronize(st));
+    return RPD_OK;
+}
+
+int rpd_atrous_wavelet(rpd_ctx* ctx, const float* raw, const float* normal, const float* albedo, int32_t w, int32_t h,
+                       float sigma_c, float sigma_n, float sigma_a, int32_t iterations, float* out, rpd_memory where) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !raw || !normal || !albedo || !out || w <= 0 || h <= 0 || iterations < 0)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "bad a-trous arguments");
+    RPD_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->util_stream;
+    const uint64_t bytes = uint64_t(w) * h * 12;
+    float *d_raw = nullptr, *d_n = nullptr, *d_a = nullptr, *b0 = nullptr, *b1 = nullptr;
+    RPD_CUDA(cudaMallocAsync(&b0, bytes, st));
+    RPD_CUDA(cudaMallocAsync(&b1, bytes, st));
+    if (where == RPD_MEM_HOST) {
+        RPD_CUDA(cudaMallocAsync(&d_raw, bytes, st));
+        RPD_CUDA(cudaMallocAsync(&d_n, bytes, st));
+        RPD_CUDA(cudaMallocAsync(&d_a, bytes, st));
+        RPD_CUDA(cudaMemcpyAsync(d_raw, raw, bytes, cudaMemcpyHostToDevice, st));
+        RPD_CUDA(cudaMemcpyAsync(d_n, normal, bytes, cudaMemcpyHostToDevice, st));
+        RPD_CUDA(cudaMemcpyAsync(d_a, albedo, bytes, cudaMemcpyHostToDevice, st));
+    }
+    const float* r_in = where == RPD_MEM_HOST ? d_raw : raw;
+    const float* n_in = where == RPD_MEM_HOST ? d_n : normal;
+    const float* a_in = where == RPD_MEM_HOST ? d_a : albedo;
+    float* result = nullptr;
+    uint64_t launches = 0;
+    RPD_CUDA(launch_atrous(r_in, n_in, a_in, w, h, sigma_c, sigma_n, sigma_a, iterations, b0, b1, &result, st, &launches));
+    RPD_CUDA(cudaMemcpyAsync(out, result, bytes, where == RPD_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    RPD_CUDA(cudaFreeAsync(b0, st));
+    RPD_CUDA(cudaFreeAsync(b1, st));
+    if (d_raw) RPD_CUDA(cudaFreeAsync(d_raw, st));
+    if (d_n) RPD_CUDA(cudaFreeAsync(d_n, st));
+    if (d_a) RPD_CUDA(cudaFreeAsync(d_a, st));
+    RPD_CUDA(cudaStreamSynchronize(st));
+    return RPD_OK;
+}
+
+int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, const float* albedo, int32_t w, int32_t h,
+                        float sigma_c, float sigma_n, float sigma_p, float sigma_a, float* gaussian, float* bilateral,
+                        float* joint, rpd_memory where) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !raw || !normal || !albedo || !gaussian || !bilateral || !joint || w <= 0 || h <= 0)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "bad joint-bilateral arguments");
+    RPD_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->util_stream;
+    const uint64_t bytes = uint64_t(w) * h * 12;
+    if (where == RPD_MEM_DEVICE) {
+        uint64_t launches = 0;
+        RPD_CUDA(launch_joint_bilateral(raw, normal, albedo, w, h, sigma_c, sigma_n, sigma_p, sigma_a, gaussian,
+                                        bilateral, joint, st, &launches));
+        RPD_CUDA(cudaStreamSynchronize(st));
+        return RPD_OK;
+    }
+    float* d[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    for (auto& p : d) RPD_CUDA(cudaMallocAsync(&p, bytes, st));
+    RPD_CUDA(cudaMemcpyAsync(d[0], raw, bytes, cudaMemcpyHostToDevice, st));
+    RPD_CUDA(cudaMemcpyAsync(d[1], normal, bytes, cudaMemcpyHostToDevice, st));
+    RPD_CUDA(cudaMemcpyAsync(d[2], albedo, bytes, cudaMemcpyHostToDevice, st));
+    uint64_t launches = 0;
+    RPD_CUDA(launch_joint_bilateral(d[0], d[1], d[2], w, h, sigma_c, sigma_n, sigma_p, sigma_a, d[3], d[4], d[5], st,
+                                    &launches));
+    RPD_CUDA(cudaMemcpyAsync(gaussian, d[3], bytes, cudaMemcpyDeviceToHost, st));
+    RPD_CUDA(cudaMemcpyAsync(bilateral, d[4], bytes, cudaMemcpyDeviceToHost, st));
+    RPD_CUDA(cudaMemcpyAsync(joint, d[5], bytes, cudaMemcpyDeviceToHost, st));
+    for (auto& p : d) RPD_CUDA(cudaFreeAsync(p, st));
+    RPD_CUDA(cudaStreamSynchronize(st));
+    return RPD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,400 @@
+// Per-sample accumulation: pixel statistics, primary-hit features and the RPD grid.
+//
+//   k_accumulate_pixels  accumulate_sample (core/stats.h:25-41) and the feature / radiance
+//                        sums of the render loops (main.cpp:572-576, 706-717), one thread
+//                        per pixel walking its samples in order — bit-identical to the
+//                        reference, whose pixel is also owned by a single thread.
+//   k_grid_ordered       accumulate_rpf_sample_to_grid (main.cpp:329-376) regrouped by
+//                        owner: one thread per (node, dependency) visits the node's support
+//                        pixels in row-major order and their samples in order, which is the
+//                        reference's summation order with one OpenMP thread, so the grid is
+//                        bit-identical to that run. No atomics; deterministic.
+//   k_merge_grid         merge_rpf_grids_into (main.cpp:378-388).
+//   k_feature_cache      ensure_feature_cache (main.cpp:94-122).
+//   k_finalize           FrameBuffers::finalize (core/buffers.h:152-167).
+#include "rpd_internal.h"
+#include "device_math.cuh"
+
+namespace rpd {
+
+namespace {
+
+constexpr int kScanBlock = 1024;
+
+__global__ void k_offsets_uniform(int64_t* offsets, int64_t count, int32_t spp) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i <= count) offsets[i] = i * int64_t(spp);
+}
+
+// Three-phase exclusive scan of int32 counts into int64 offsets[0..count].
+__global__ void k_scan_block_sums(const int32_t* counts, int64_t count, int64_t* block_sums) {
+    __shared__ int64_t s[kScanBlock];
+    const int64_t i = int64_t(blockIdx.x) * kScanBlock + threadIdx.x;
+    s[threadIdx.x] = (i < count) ? int64_t(counts[i]) : 0;
+    __syncthreads();
+    for (int stride = kScanBlock / 2; stride > 0; stride >>= 1) {
+        if (threadIdx.x < stride) s[threadIdx.x] += s[threadIdx.x + stride];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = s[0];
+}
+
+__global__ void k_scan_block_offsets(int64_t* block_sums, int64_t nblocks) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int64_t run = 0;
+    for (int64_t b = 0; b < nblocks; ++b) {
+        const int64_t v = block_sums[b];
+        block_sums[b] = run;
+        run += v;
+    }
+    block_sums[nblocks] = run;
+}
+
+__global__ void k_scan_finish(const int32_t* counts, int64_t count, const int64_t* block_sums, int64_t* offsets) {
+    __shared__ int64_t s[kScanBlock];
+    const int64_t i = int64_t(blockIdx.x) * kScanBlock + threadIdx.x;
+    const int64_t v = (i < count) ? int64_t(counts[i]) : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    // Hillis-Steele inclusive scan
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        int64_t t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
+        __syncthreads();
+        s[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < count) offsets[i] = block_sums[blockIdx.x] + s[threadIdx.x] - v;
+    if (i == count - 1) offsets[count] = block_sums[blockIdx.x] + s[threadIdx.x];
+}
+
+__global__ void k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets, int32_t spp,
+                                    int64_t first, int64_t count) {
+    const int64_t local = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (local >= count) return;
+    const int64_t idx = first + local;
+    const int64_t k0 = offsets ? offsets[local] : local * spp;
+    const int64_t k1 = offsets ? offsets[local + 1] : (local + 1) * spp;
+    if (k0 == k1) return;
+
+    float mean = p.mean[idx], m2 = p.square_diff[idx];
+    int n = p.n[idx];
+    float cm[3], sm[3], sq[3], rad[3], nor[3], alb[3];
+    for (int c = 0; c < 3; ++c) {
+        cm[c] = p.color_mean[c][idx];
+        sm[c] = p.sqrt_mean[c][idx];
+        sq[c] = p.sqrt_sq[c][idx];
+        rad[c] = p.radiance[c][idx];
+        nor[c] = p.normal[c][idx];
+        alb[c] = p.albedo[c][idx];
+    }
+    float dep = p.depth[idx];
+    int hits = p.hit_count[idx];
+    int nsamples = p.sample_count[idx];
+    const bool per_sample_albedo = s.albedo[0] != nullptr;
+    float palb[3] = {0.0f, 0.0f, 0.0f};
+    if (!per_sample_albedo && s.pixel_albedo[0]) {
+        for (int c = 0; c < 3; ++c) palb[c] = s.pixel_albedo[c][local];
+    }
+
+    for (int64_t k = k0; k < k1; ++k) {
+        const uint8_t f = s.flags ? s.flags[k] : 0;
+        if (f & RPD_SAMPLE_HIT) {
+            ++hits;
+            for (int c = 0; c < 3; ++c) nor[c] += s.normal[c][k];
+            for (int c = 0; c < 3; ++c) alb[c] += per_sample_albedo ? s.albedo[c][k] : palb[c];
+            dep += s.depth[k];
+        }
+        const float L[3] = {s.radiance[0][k], s.radiance[1][k], s.radiance[2][k]};
+        if (!finite3(L[0], L[1], L[2])) continue;
+        // accumulate_sample (core/stats.h:25-41)
+        const float lum = luminance(L[0], L[1], L[2]);
+        const float delta = lum - mean;
+        ++n;
+        mean += delta / float(n);
+        const float delta2 = lum - mean;
+        m2 += delta * delta2;
+        for (int c = 0; c < 3; ++c) {
+            const float cd = L[c] - cm[c];
+            cm[c] += cd / float(n);
+        }
+        for (int c = 0; c < 3; ++c) {
+            const float sc = sqrtf(fmaxs(0.0f, L[c]));
+            const float sd = sc - sm[c];
+            sm[c] += sd / float(n);
+            sq[c] += sd * (sc - sm[c]);
+        }
+        for (int c = 0; c < 3; ++c) rad[c] += L[c];
+        ++nsamples;
+    }
+
+    p.mean[idx] = mean;
+    p.square_diff[idx] = m2;
+    p.n[idx] = n;
+    for (int c = 0; c < 3; ++c) {
+        p.color_mean[c][idx] = cm[c];
+        p.sqrt_mean[c][idx] = sm[c];
+        p.sqrt_sq[c][idx] = sq[c];
+        p.radiance[c][idx] = rad[c];
+        p.normal[c][idx] = nor[c];
+        p.albedo[c][idx] = alb[c];
+    }
+    p.depth[idx] = dep;
+    p.hit_count[idx] = hits;
+    p.sample_count[idx] = nsamples;
+}
+
+// Valid-flag bit each dependency needs, and whether it bins the screen position.
+__device__ __forceinline__ uint8_t dep_flag(int d) {
+    switch (d) {
+    case D_PIXEL: return 0;
+    case D_BRDF: case D_SCREEN_BRDF: return RPD_SAMPLE_BRDF_VALID;
+    case D_LENS: case D_SCREEN_LENS: return RPD_SAMPLE_LENS_VALID;
+    case D_LIGHT_UV: case D_SCREEN_LIGHT_UV: return RPD_SAMPLE_LIGHT_VALID;
+    case D_ENV: case D_SCREEN_ENV: return RPD_SAMPLE_ENV_VALID;
+    case D_LIGHT_SELECT: case D_SCREEN_LIGHT_SELECT: return RPD_SAMPLE_LIGHT_SELECT_VALID;
+    default: return RPD_SAMPLE_RR_VALID;
+    }
+}
+__device__ __forceinline__ bool dep_is_screen(int d) {
+    return d == D_PIXEL || d == D_SCREEN_BRDF || d == D_SCREEN_LENS || d == D_SCREEN_LIGHT_UV ||
+           d == D_SCREEN_ENV || d == D_SCREEN_LIGHT_SELECT || d == D_SCREEN_RR;
+}
+
+// Dependency2D::add bin (core/stats.h:166-168)
+__device__ __forceinline__ int bin2d(float u, float v) {
+    const int x = iclamps(int(u * 4.0f), 0, 3);
+    const int z = iclamps(int(v * 4.0f), 0, 3);
+    return z * 4 + x;
+}
+
+__global__ void __launch_bounds__(128) k_grid_ordered(Geometry g, double* pass_grid, DeviceSamples s,
+                                                      const int64_t* offsets, int32_t spp, int64_t first,
+                                                      int64_t count) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= g.nn * kDeps) return;
+    const int node = int(t / kDeps);
+    const int d = int(t % kDeps);
+    const int nx = node % g.nodes_x, ny = node / g.nodes_x;
+    const uint8_t need = dep_flag(d);
+    const bool screen = dep_is_screen(d);
+    const int bins = (d == D_RR) ? 2 : 16;
+    // a NULL plane never validates its dependency
+    const float* const* dims = nullptr;
+    switch (d) {
+    case D_BRDF: dims = s.brdf_u; break;
+    case D_LENS: dims = s.lens_u; break;
+    case D_LIGHT_UV: dims = s.light_u; break;
+    case D_ENV: dims = s.env_u; break;
+    default: break;
+    }
+    if (screen && !s.pixel_u[0]) return;
+    if (dims && !dims[0]) return;
+    if ((d == D_SCREEN_BRDF && !s.brdf_u[0]) || (d == D_SCREEN_LENS && !s.lens_u[0]) ||
+        (d == D_SCREEN_LIGHT_UV && !s.light_u[0]) || (d == D_SCREEN_ENV && !s.env_u[0]))
+        return;
+
+    double* acc = pass_grid + int64_t(node) * kDeps * kDepStride + d * kDepStride;
+    double wbin[16], ybin[16];
+    for (int b = 0; b < 16; ++b) {
+        wbin[b] = acc[b];
+        ybin[b] = acc[16 + b];
+    }
+    double w_sum = acc[32], w2_sum = acc[33], y_sum = acc[34], y2_sum = acc[35];
+
+    const float half_support = 0.5f * float(g.support);
+    const float inv_dummy = 0.0f;
+    (void)inv_dummy;
+    // pixels whose bilinear footprint can reach this node
+    const int xlo = imaxs(0, (nx - 1) * g.step - 1), xhi = imins(g.w - 1, (nx + 1) * g.step + 1);
+    const int ylo = imaxs(0, (ny - 1) * g.step - 1), yhi = imins(g.h - 1, (ny + 1) * g.step + 1);
+    for (int y = ylo; y <= yhi; ++y) {
+        const float gy = float(y) / float(g.step);
+        const int y0 = iclamps(int(floorf(gy)), 0, g.nodes_y - 1);
+        const int y1 = imins(y0 + 1, g.nodes_y - 1);
+        if (y0 != ny && y1 != ny) continue;
+        const float ty = fclamps(gy - float(y0), 0.0f, 1.0f);
+        for (int x = xlo; x <= xhi; ++x) {
+            const int64_t idx = int64_t(y) * g.w + x;
+            if (idx < first || idx >= first + count) continue;
+            const float gx = float(x) / float(g.step);
+            const int x0 = iclamps(int(floorf(gx)), 0, g.nodes_x - 1);
+            const int x1 = imins(x0 + 1, g.nodes_x - 1);
+            if (x0 != nx && x1 != nx) continue;
+            const float tx = fclamps(gx - float(x0), 0.0f, 1.0f);
+            // the four entries of main.cpp:341-346, in order; keep those naming this node
+            float we[4];
+            int ne = 0;
+            if (x0 == nx && y0 == ny) we[ne++] = (1.0f - tx) * (1.0f - ty);
+            if (x1 == nx && y0 == ny) we[ne++] = tx * (1.0f - ty);
+            if (x0 == nx && y1 == ny) we[ne++] = (1.0f - tx) * ty;
+            if (x1 == nx && y1 == ny) we[ne++] = tx * ty;
+            bool any = false;
+            for (int e = 0; e < ne; ++e) any |= we[e] > 1e-8f;
+            if (!any) continue;
+            const int64_t local = idx - first;
+            const int64_t k0 = offsets ? offsets[local] : local * spp;
+            const int64_t k1 = offsets ? offsets[local + 1] : (local + 1) * spp;
+            const float support_left = float(nx * g.step) - half_support;
+            const float support_top = float(ny * g.step) - half_support;
+            for (int64_t k = k0; k < k1; ++k) {
+                uint8_t f = s.flags ? s.flags[k] : 0;
+                if (!s.pixel_u[0]) f &= uint8_t(~RPD_SAMPLE_PIXEL_VALID);
+                if (!s.lens_u[0]) f &= uint8_t(~RPD_SAMPLE_LENS_VALID);
+                if (!s.brdf_u[0]) f &= uint8_t(~RPD_SAMPLE_BRDF_VALID);
+                if (!s.light_u[0]) f &= uint8_t(~RPD_SAMPLE_LIGHT_VALID);
+                if (!s.env_u[0]) f &= uint8_t(~RPD_SAMPLE_ENV_VALID);
+                const bool pixel_valid = (f & RPD_SAMPLE_PIXEL_VALID) != 0;
+                if (screen && !pixel_valid) continue;
+                if (need && !(f & need)) continue;
+                // main.cpp:330 — samples without any captured dimension are skipped
+                if (!(f & (RPD_SAMPLE_PIXEL_VALID | RPD_SAMPLE_LENS_VALID | RPD_SAMPLE_LIGHT_SELECT_VALID |
+                           RPD_SAMPLE_BRDF_VALID | RPD_SAMPLE_LIGHT_VALID | RPD_SAMPLE_ENV_VALID |
+                           RPD_SAMPLE_RR_VALID)))
+                    continue;
+                const float r = s.radiance[0][k], gch = s.radiance[1][k], b = s.radiance[2][k];
+                if (!finite3(r, gch, b)) continue;
+                const float lum = luminance(r, gch, b);
+                int bin;
+                if (screen) {
+                    const float su = fclamps((float(x) + s.pixel_u[0][k] - support_left) / float(g.support), 0.0f, 1.0f);
+                    const float sv = fclamps((float(y) + s.pixel_u[1][k] - support_top) / float(g.support), 0.0f, 1.0f);
+                    bin = bin2d(su, sv);
+                } else if (d == D_LIGHT_SELECT) {
+                    bin = int(s.category[k] & RPD_CATEGORY_LIGHT_INDEX_MASK);
+                } else if (d == D_RR) {
+                    bin = (s.category[k] & RPD_CATEGORY_RR_SURVIVED) ? 1 : 0;
+                } else {
+                    bin = bin2d(dims[0][k], dims[1][k]);
+                }
+                bin = iclamps(bin, 0, bins - 1);
+                const double yd = double(lum);
+                for (int e = 0; e < ne; ++e) {
+                    // BinnedDependency::add (core/stats.h:102-113)
+                    if (we[e] <= 1e-8f) continue;
+                    const double wd = double(we[e]);
+                    wbin[bin] += wd;
+                    ybin[bin] += wd * yd;
+                    w_sum += wd;
+                    w2_sum += wd * wd;
+                    y_sum += wd * yd;
+                    y2_sum += wd * yd * yd;
+                }
+            }
+        }
+    }
+    for (int b = 0; b < 16; ++b) {
+        acc[b] = wbin[b];
+        acc[16 + b] = ybin[b];
+    }
+    acc[32] = w_sum;
+    acc[33] = w2_sum;
+    acc[34] = y_sum;
+    acc[35] = y2_sum;
+}
+
+__global__ void k_merge_grid(double* grid, double* pass_grid, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    grid[i] += pass_grid[i];
+    pass_grid[i] = 0.0;
+}
+
+__global__ void k_feature_cache(PixelPlanes p, int64_t np) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const int hc = p.hit_count[i];
+    if (hc > 0) {
+        const float h = float(hc);
+        float n0 = p.normal[0][i] / h, n1 = p.normal[1][i] / h, n2 = p.normal[2][i] / h;
+        const float z = dot3(n0, n1, n2, n0, n1, n2);
+        if (z > 1e-8f) {
+            // Eigen normalize(): divide by sqrt(squaredNorm) when positive
+            const float sn = sqrtf(z);
+            n0 = n0 / sn;
+            n1 = n1 / sn;
+            n2 = n2 / sn;
+        }
+        p.f_normal[0][i] = n0;
+        p.f_normal[1][i] = n1;
+        p.f_normal[2][i] = n2;
+        p.f_depth[i] = p.depth[i] / h;
+        for (int c = 0; c < 3; ++c) p.f_albedo[c][i] = p.albedo[c][i] / h;
+    } else {
+        for (int c = 0; c < 3; ++c) p.f_normal[c][i] = p.normal[c][i];
+        p.f_depth[i] = p.depth[i];
+        for (int c = 0; c < 3; ++c) p.f_albedo[c][i] = p.albedo[c][i];
+    }
+}
+
+__global__ void k_finalize(PixelPlanes p, int64_t np) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const float samples = float(imaxs(1, p.sample_count[i]));
+    const float hits = float(imaxs(1, p.hit_count[i]));
+    for (int c = 0; c < 3; ++c) p.radiance[c][i] /= samples;
+    for (int c = 0; c < 3; ++c) p.albedo[c][i] /= hits;
+    float n0 = p.normal[0][i] / hits, n1 = p.normal[1][i] / hits, n2 = p.normal[2][i] / hits;
+    const float z = dot3(n0, n1, n2, n0, n1, n2);
+    if (z > 1e-8f) {
+        const float sn = sqrtf(z);
+        n0 = n0 / sn;
+        n1 = n1 / sn;
+        n2 = n2 / sn;
+    }
+    p.normal[0][i] = n0;
+    p.normal[1][i] = n1;
+    p.normal[2][i] = n2;
+    p.depth[i] /= hits;
+}
+
+}  // namespace
+
+cudaError_t launch_offsets_uniform(Job& j, int64_t count, int32_t spp) {
+    k_offsets_uniform<<<grid_for(count + 1, 256), 256, 0, j.stream>>>(j.offsets, count, spp);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count) {
+    const int64_t nblocks = (count + kScanBlock - 1) / kScanBlock;
+    int64_t* block_sums = j.offsets + (count + 1);  // the offsets buffer reserves room for these
+    k_scan_block_sums<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums);
+    k_scan_block_offsets<<<1, 1, 0, j.stream>>>(block_sums, nblocks);
+    k_scan_finish<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums, j.offsets);
+    j.launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count) {
+    k_accumulate_pixels<<<grid_for(count, 128), 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first, int64_t count) {
+    const int64_t threads = j.g.nn * kDeps;
+    k_grid_ordered<<<grid_for(threads, 128), 128, 0, j.stream>>>(j.g, j.n.pass_grid, s, j.offsets, 0, first, count);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge_grid(Job& j) {
+    const int64_t n = j.g.nn * kDeps * kDepStride;
+    k_merge_grid<<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_feature_cache(Job& j) {
+    k_feature_cache<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.p, j.g.np);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(Job& j) {
+    k_finalize<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.p, j.g.np);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace rpd

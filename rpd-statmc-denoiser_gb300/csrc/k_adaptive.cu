@@ -1,0 +1,188 @@
+// compute_adaptive_sample_counts (main.cpp:1273-1446).
+//
+//   k_importance       variance source and importance = sqrt (1303-1327)
+//   k_smooth_importance edge-aware smoothing (1331-1368)
+//   k_allocate_serial  the budget-preserving allocation (1329-1438). Its integers depend on
+//                      sequential double-precision sums (std::accumulate, the running
+//                      remaining_importance of the water-filling and the cursor of the
+//                      systematic residual sampling), so it runs as one device thread in
+//                      the reference's order: the counts are bit-identical for identical
+//                      importance values.
+#include <algorithm>
+
+#include "rpd_internal.h"
+#include "device_math.cuh"
+
+namespace rpd {
+
+namespace {
+
+__device__ __forceinline__ float pixel_variance(float m2, int n) { return (n > 1) ? m2 / float(n - 1) : 0.0f; }
+
+__global__ void k_importance(PixelPlanes p, int64_t np, float sigma_max) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    float raw = pixel_variance(p.square_diff[i], p.n[i]);
+    if (!isfinite(raw)) raw = 1e-8f;
+    raw = fmaxs(1e-8f, raw);
+    float dsv = p.variance_denoised[i];
+    if (!isfinite(dsv) || dsv <= 0.0f) dsv = raw;
+    const float vs = fclamps(fmaxs(raw, dsv), 1e-8f, sigma_max * sigma_max);
+    p.importance[i] = sqrtf(vs);
+}
+
+__global__ void k_smooth_importance(PixelPlanes p, int w, int h, int radius, const float* in, float* out) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= int64_t(w) * h) return;
+    if (p.hit_count[idx] == 0) {
+        out[idx] = in[idx];
+        return;
+    }
+    const int y = int(idx / w), x = int(idx % w);
+    const float ni0 = p.f_normal[0][idx], ni1 = p.f_normal[1][idx], ni2 = p.f_normal[2][idx];
+    const float di = p.f_depth[idx];
+    double accum = 0.0, weight_sum = 0.0;
+    for (int dy = -radius; dy <= radius; ++dy) {
+        const int yy = y + dy;
+        if (yy < 0 || yy >= h) continue;
+        for (int dx = -radius; dx <= radius; ++dx) {
+            const int xx = x + dx;
+            if (xx < 0 || xx >= w) continue;
+            const int64_t nidx = int64_t(yy) * w + xx;
+            if (p.hit_count[nidx] == 0) continue;
+            const float spatial_w = 1.0f / (1.0f + float(dx * dx + dy * dy));
+            const float normal_w = fclamps(
+                (dot3(ni0, ni1, ni2, p.f_normal[0][nidx], p.f_normal[1][nidx], p.f_normal[2][nidx]) + 1.0f) * 0.5f,
+                0.0f, 1.0f);
+            const float depth_w = expf(-4.0f * relative_depth_delta(di, p.f_depth[nidx]));
+            const double w_neighbor = double(spatial_w) * double(normal_w) * double(depth_w);
+            accum += w_neighbor * double(in[nidx]);
+            weight_sum += w_neighbor;
+        }
+    }
+    out[idx] = (weight_sum > double(1e-8f)) ? float(accum / weight_sum) : in[idx];
+}
+
+// hash_u32 / hash_to_unit_float (main.cpp:270-281)
+__device__ __forceinline__ uint32_t hash_u32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+struct AllocParams {
+    int64_t np;
+    int extra_sample_total;
+    int reserved_samples;
+    int max_extra_per_pixel;
+    uint32_t seed;
+};
+
+__global__ void k_allocate_serial(PixelPlanes p, AllocParams a, const float* importance) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int64_t np = a.np;
+    double sum_importance = 0.0;
+    for (int64_t i = 0; i < np; ++i) sum_importance = sum_importance + double(importance[i]);
+    int remaining_samples = imaxs(0, a.extra_sample_total - a.reserved_samples);
+    if (sum_importance <= 0.0 || remaining_samples <= 0) return;
+    float* desired_add = p.desired_add;
+    for (int64_t i = 0; i < np; ++i) desired_add[i] = 0.0f;
+    int32_t* active = p.active_a;
+    int32_t* next_active = p.active_b;
+    int64_t n_active = np;
+    for (int64_t i = 0; i < np; ++i) active[i] = int32_t(i);
+    double remaining_importance = sum_importance;
+    while (n_active > 0 && remaining_samples > 0 && remaining_importance > double(1e-8f)) {
+        bool clipped = false;
+        int64_t n_next = 0;
+        for (int64_t k = 0; k < n_active; ++k) {
+            const int32_t idx = active[k];
+            const double share = double(importance[idx]) / remaining_importance;
+            const double desired = share * double(remaining_samples);
+            if (desired > double(a.max_extra_per_pixel)) {
+                desired_add[idx] = float(a.max_extra_per_pixel);
+                remaining_samples -= a.max_extra_per_pixel;
+                remaining_importance -= double(importance[idx]);
+                clipped = true;
+            } else {
+                next_active[n_next++] = idx;
+            }
+        }
+        if (!clipped) {
+            for (int64_t k = 0; k < n_next; ++k) {
+                const int32_t idx = next_active[k];
+                desired_add[idx] = float(double(importance[idx]) / remaining_importance * double(remaining_samples));
+            }
+            break;
+        }
+        int32_t* t = active;
+        active = next_active;
+        next_active = t;
+        n_active = n_next;
+    }
+    int assigned = 0;
+    double residual_sum = 0.0;
+    for (int64_t i = 0; i < np; ++i) {
+        const int add = int(floorf(desired_add[i]));
+        p.counts[i] += add;
+        assigned += add;
+        p.residual[i] = fmaxs(0.0f, desired_add[i] - float(add));
+        residual_sum += double(p.residual[i]);
+    }
+    const int remaining = imaxs(0, a.extra_sample_total - a.reserved_samples - assigned);
+    if (remaining > 0 && residual_sum > double(1e-8f)) {
+        const double offset = double(float(hash_u32(a.seed ^ 0x4d595df4u) & 0x00ffffffu) / float(0x01000000u));
+        double cumulative = 0.0;
+        int64_t cursor = 0;
+        for (int k = 0; k < remaining; ++k) {
+            const double target = ((double(k) + offset) / double(remaining)) * residual_sum;
+            while (cursor < np && cumulative + double(p.residual[cursor]) < target) {
+                cumulative += double(p.residual[cursor]);
+                ++cursor;
+            }
+            if (cursor < np) p.counts[cursor]++;
+        }
+    }
+}
+
+__global__ void k_fill_counts(int32_t* counts, int64_t np, int value) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < np) counts[i] = value;
+}
+
+__global__ void k_copy(const float* src, float* dst, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+}  // namespace
+
+cudaError_t launch_adaptive(Job& j) {
+    const int64_t np = j.g.np;
+    const int w = j.g.w, h = j.g.h;
+    const int extra_sample_total = j.cfg.adaptive_spp * w * h;
+    const int floor_per_pixel = std::clamp(j.cfg.adaptive_base_samples, 0, j.cfg.adaptive_spp);
+    k_fill_counts<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p.counts, np, floor_per_pixel);
+    j.launches += 1;
+    if (extra_sample_total <= 0) return cudaGetLastError();
+    k_importance<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np, j.cfg.adaptive_sigma_max);
+    j.launches += 1;
+    const float* importance = j.p.importance;
+    const int radius = j.cfg.adaptive_importance_smoothing_radius;
+    if (radius > 0) {
+        k_smooth_importance<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, w, h, radius, j.p.importance,
+                                                                     j.p.importance_tmp);
+        k_copy<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p.importance_tmp, j.p.importance, np);
+        j.launches += 2;
+    }
+    AllocParams a{np, extra_sample_total, floor_per_pixel * w * h,
+                  std::max(4, 8 * std::max(1, j.cfg.adaptive_spp)), j.cfg.seed};
+    k_allocate_serial<<<1, 1, 0, j.stream>>>(j.p, a, importance);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace rpd

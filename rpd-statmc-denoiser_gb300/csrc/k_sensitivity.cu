@@ -1,0 +1,284 @@
+// recompute_sensitivity (main.cpp:741-953) on the node grid.
+//
+//   k_node_stats    per node: the 13 bias-adjusted explained-variance sensitivities and
+//                   confidences (core/stats.h:115-141, 264-302; main.cpp:776-806) and the
+//                   3x3 pixel-feature averages at the node centre (main.cpp:808-813).
+//   k_node_combine  per node: the 3x3 feature-aware prior smoothing of all 13 fields
+//                   (main.cpp:817-863) and the confidence-lerp / relative-sensitivity /
+//                   dominant-component combine (main.cpp:865-928). The depth and albedo
+//                   edge weights are identical for every field, so each neighbour's weight
+//                   is evaluated once and reused for the 13 fields.
+//   k_sens_pixels   bilinear expansion of all / all_conf to pixels and the central-
+//                   difference gradient (main.cpp:930-947, core/buffers.h:68-101).
+//   k_rpd_cache     the per-pixel view statmc_denoise takes of the sensitivity cache:
+//                   components_denoise() of sample_sensitivity() (main.cpp:297-327).
+#include "rpd_internal.h"
+#include "device_math.cuh"
+
+namespace rpd {
+
+namespace {
+
+__device__ __forceinline__ double sample_mass(const double* d) {
+    return d[33] > 0.0 ? d[32] * d[32] / d[33] : 0.0;
+}
+
+// BinnedDependency::compute_sensitivity (core/stats.h:115-137)
+__device__ float compute_sensitivity(const double* d, int bins) {
+    const double kEps = 1e-18;
+    const double effective_n = sample_mass(d);
+    if (effective_n <= 2.0) return 0.0f;
+    const double mean = d[34] / d[32];
+    const double total = d[35] - d[32] * mean * mean;
+    if (total <= kEps) return 0.0f;
+    int active = 0;
+    double between = 0.0;
+    for (int b = 0; b < bins; ++b) {
+        if (d[b] <= kEps) continue;
+        ++active;
+        const double delta = d[16 + b] / d[b] - mean;
+        between += d[b] * delta * delta;
+    }
+    if (active < 2 || effective_n <= double(active)) return 0.0f;
+    const double eta2 = dclamps(between / total, 0.0, 1.0);
+    const double adjusted = dmaxs(0.0, 1.0 - (1.0 - eta2) * (effective_n - 1.0) / (effective_n - active));
+    return float(sqrt(adjusted));
+}
+
+__constant__ int c_raw_dep[R_FIELDS] = {D_PIXEL, D_BRDF, D_LENS, D_LIGHT_UV, D_LIGHT_SELECT, D_ENV, D_RR,
+                                        D_SCREEN_BRDF, D_SCREEN_LENS, D_SCREEN_LIGHT_UV,
+                                        D_SCREEN_LIGHT_SELECT, D_SCREEN_ENV, D_SCREEN_RR};
+
+// sample_scalar_local_average / sample_vec3_local_average with radius 1 (main.cpp:156-185)
+__device__ float local_avg1(const float* v, int w, int h, int cx, int cy) {
+    double accum = 0.0, weight_sum = 0.0;
+    for (int dy = -1; dy <= 1; ++dy) {
+        const int y = iclamps(cy + dy, 0, h - 1);
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int x = iclamps(cx + dx, 0, w - 1);
+            const double weight = 1.0 / (1.0 + double(dx * dx + dy * dy));
+            accum += weight * double(v[int64_t(y) * w + x]);
+            weight_sum += weight;
+        }
+    }
+    return (weight_sum > 0.0) ? float(accum / weight_sum) : 0.0f;
+}
+
+__device__ void local_avg3(float* const* v, int w, int h, int cx, int cy, float out[3]) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, weight_sum = 0.0;
+    for (int dy = -1; dy <= 1; ++dy) {
+        const int y = iclamps(cy + dy, 0, h - 1);
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int x = iclamps(cx + dx, 0, w - 1);
+            const double weight = 1.0 / (1.0 + double(dx * dx + dy * dy));
+            const int64_t i = int64_t(y) * w + x;
+            a0 += double(v[0][i]) * weight;
+            a1 += double(v[1][i]) * weight;
+            a2 += double(v[2][i]) * weight;
+            weight_sum += weight;
+        }
+    }
+    if (weight_sum <= 0.0) {
+        out[0] = out[1] = out[2] = 0.0f;
+        return;
+    }
+    out[0] = float(a0 / weight_sum);
+    out[1] = float(a1 / weight_sum);
+    out[2] = float(a2 / weight_sum);
+}
+
+__global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= g.nn) return;
+    const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
+    const double* tile = n.grid + idx * kDeps * kDepStride;
+    const double n0d = double(n0);
+    for (int f = 0; f < R_FIELDS; ++f) {
+        const int d = c_raw_dep[f];
+        const double* dep = tile + d * kDepStride;
+        n.raw[f][idx] = compute_sensitivity(dep, d == D_RR ? 2 : 16);
+        const double mass = sample_mass(dep);
+        n.conf[f][idx] = float(mass / (mass + n0d));
+    }
+    const int px = iclamps(ix * g.step, 0, g.w - 1);
+    const int py = iclamps(iy * g.step, 0, g.h - 1);
+    float nn3[3], na3[3];
+    local_avg3(p.f_normal, g.w, g.h, px, py, nn3);
+    const float z = dot3(nn3[0], nn3[1], nn3[2], nn3[0], nn3[1], nn3[2]);
+    if (z > 1e-8f) {
+        const float sn = sqrtf(z);
+        nn3[0] = nn3[0] / sn;
+        nn3[1] = nn3[1] / sn;
+        nn3[2] = nn3[2] / sn;
+    }
+    for (int c = 0; c < 3; ++c) n.n_normal[c][idx] = nn3[c];
+    n.n_depth[idx] = local_avg1(p.f_depth, g.w, g.h, px, py);
+    local_avg3(p.f_albedo, g.w, g.h, px, py, na3);
+    for (int c = 0; c < 3; ++c) n.n_albedo[c][idx] = na3[c];
+}
+
+__global__ void k_node_combine(Geometry g, NodePlanes n) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= g.nn) return;
+    const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
+    const float ni0 = n.n_normal[0][idx], ni1 = n.n_normal[1][idx], ni2 = n.n_normal[2][idx];
+    const float di = n.n_depth[idx];
+    const float ai0 = n.n_albedo[0][idx], ai1 = n.n_albedo[1][idx], ai2 = n.n_albedo[2][idx];
+    double accum[R_FIELDS], wsum[R_FIELDS];
+    for (int f = 0; f < R_FIELDS; ++f) accum[f] = wsum[f] = 0.0;
+    for (int dy = -1; dy <= 1; ++dy) {
+        const int sy = iy + dy;
+        if (sy < 0 || sy >= g.nodes_y) continue;
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int sx = ix + dx;
+            if (sx < 0 || sx >= g.nodes_x) continue;
+            const int64_t sidx = int64_t(sy) * g.nodes_x + sx;
+            const float spatial_w = 1.0f / (1.0f + float(dx * dx + dy * dy));
+            const float normal_w = fclamps(
+                (dot3(ni0, ni1, ni2, n.n_normal[0][sidx], n.n_normal[1][sidx], n.n_normal[2][sidx]) + 1.0f) * 0.5f,
+                0.0f, 1.0f);
+            const float depth_w = expf(-4.0f * relative_depth_delta(di, n.n_depth[sidx]));
+            const float albedo_w = expf(-2.5f * norm3(ai0 - n.n_albedo[0][sidx], ai1 - n.n_albedo[1][sidx],
+                                                      ai2 - n.n_albedo[2][sidx]));
+            const double base = double(spatial_w) * double(normal_w) * double(depth_w) * double(albedo_w);
+            for (int f = 0; f < R_FIELDS; ++f) {
+                const double w_neighbor = base * double(fmaxs(0.05f, n.conf[f][sidx]));
+                accum[f] += w_neighbor * double(n.raw[f][sidx]);
+                wsum[f] += w_neighbor;
+            }
+        }
+    }
+    float prior[R_FIELDS], raw[R_FIELDS], conf[R_FIELDS];
+    for (int f = 0; f < R_FIELDS; ++f) {
+        raw[f] = n.raw[f][idx];
+        conf[f] = n.conf[f][idx];
+        prior[f] = (wsum[f] > double(1e-8f)) ? float(accum[f] / wsum[f]) : raw[f];
+        n.prior[f][idx] = prior[f];
+    }
+    float fin[7];
+    for (int f = 0; f < 7; ++f) fin[f] = lerpf(prior[f], raw[f], conf[f]);
+    float screen[6];
+    for (int c = 0; c < 6; ++c) screen[c] = lerpf(prior[7 + c], raw[7 + c], conf[7 + c]);
+    float** T = n.field;
+    T[N_PIXEL][idx] = fclamps(fin[R_PIXEL], 0.0f, 1.0f);
+    const float rnd[6] = {fclamps(fin[R_BRDF], 0.0f, 1.0f), fclamps(fin[R_LENS], 0.0f, 1.0f),
+                          fclamps(fin[R_LIGHT_UV], 0.0f, 1.0f), fclamps(fin[R_LIGHT_SELECT], 0.0f, 1.0f),
+                          fclamps(fin[R_ENV], 0.0f, 1.0f), fclamps(fin[R_RR], 0.0f, 1.0f)};
+    const float rc[6] = {fclamps(conf[R_BRDF], 0.0f, 1.0f), fclamps(conf[R_LENS], 0.0f, 1.0f),
+                         fclamps(conf[R_LIGHT_UV], 0.0f, 1.0f), fclamps(conf[R_LIGHT_SELECT], 0.0f, 1.0f),
+                         fclamps(conf[R_ENV], 0.0f, 1.0f), fclamps(conf[R_RR], 0.0f, 1.0f)};
+    T[N_PIXEL_CONF][idx] = fclamps(conf[R_PIXEL], 0.0f, 1.0f);
+    T[N_BRDF_CONF][idx] = rc[0];
+    T[N_LENS_CONF][idx] = rc[1];
+    T[N_LIGHT_UV_CONF][idx] = rc[2];
+    T[N_LIGHT_SELECT_CONF][idx] = rc[3];
+    T[N_ENV_CONF][idx] = rc[4];
+    T[N_RR_CONF][idx] = rc[5];
+    float rel[6];
+    for (int c = 0; c < 6; ++c) {
+        const float relative = rnd[c] / fmaxs(1e-8f, rnd[c] + screen[c]);  // core/stats.h:48-50
+        rel[c] = relative * fmins(rc[c], conf[7 + c]);
+    }
+    int dominant = 0;
+    for (int c = 1; c < 6; ++c)
+        if (rel[dominant] < rel[c]) dominant = c;
+    T[N_BRDF][idx] = rel[0];
+    T[N_LENS][idx] = rel[1];
+    T[N_LIGHT_UV][idx] = rel[2];
+    T[N_LIGHT_SELECT][idx] = rel[3];
+    T[N_LIGHT][idx] = fmaxs(rel[2], rel[3]);
+    T[N_ENV][idx] = rel[4];
+    T[N_RR][idx] = rel[5];
+    T[N_LIGHT_CONF][idx] = rel[2] >= rel[3] ? rc[2] : rc[3];
+    T[N_ALL][idx] = rel[dominant];
+    T[N_ALL_CONF][idx] = fmins(rc[dominant], conf[7 + dominant]);
+}
+
+// SensitivityTiles::lookup (core/buffers.h:68-87)
+__device__ __forceinline__ float tiles_lookup(const Geometry& g, const float* tiles, int x, int y) {
+    const float gx = float(x) / float(g.step);
+    const float gy = float(y) / float(g.step);
+    const int x0 = iclamps(int(floorf(gx)), 0, g.nodes_x - 1);
+    const int y0 = iclamps(int(floorf(gy)), 0, g.nodes_y - 1);
+    const int x1 = imins(x0 + 1, g.nodes_x - 1);
+    const int y1 = imins(y0 + 1, g.nodes_y - 1);
+    const float tx = fclamps(gx - float(x0), 0.0f, 1.0f);
+    const float ty = fclamps(gy - float(y0), 0.0f, 1.0f);
+    const float v00 = tiles[int64_t(y0) * g.nodes_x + x0];
+    const float v10 = tiles[int64_t(y0) * g.nodes_x + x1];
+    const float v01 = tiles[int64_t(y1) * g.nodes_x + x0];
+    const float v11 = tiles[int64_t(y1) * g.nodes_x + x1];
+    const float top = lerpf(v00, v10, tx);
+    const float bottom = lerpf(v01, v11, tx);
+    return lerpf(top, bottom, ty);
+}
+
+__global__ void k_sens_pixels(Geometry g, NodePlanes n, PixelPlanes p) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= g.np) return;
+    const int y = int(i / g.w), x = int(i % g.w);
+    p.sens_confidence[i] = tiles_lookup(g, n.field[N_ALL_CONF], x, y);
+    const float left = tiles_lookup(g, n.field[N_ALL], imaxs(0, x - 1), y);
+    const float right = tiles_lookup(g, n.field[N_ALL], imins(g.w - 1, x + 1), y);
+    const float up = tiles_lookup(g, n.field[N_ALL], x, imaxs(0, y - 1));
+    const float down = tiles_lookup(g, n.field[N_ALL], x, imins(g.h - 1, y + 1));
+    const float grad = sqrtf((right - left) * (right - left) + (down - up) * (down - up));
+    p.sens_gradient[i] = fclamps(0.5f * grad, 0.0f, 1.0f);
+}
+
+__global__ void k_sens_zero(PixelPlanes p, int64_t np) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    p.sens_confidence[i] = 0.0f;
+    p.sens_gradient[i] = 0.0f;
+}
+
+__constant__ int c_rpd_field[6] = {N_BRDF, N_LENS, N_LIGHT_UV, N_LIGHT_SELECT, N_ENV, N_RR};
+
+__global__ void k_rpd_cache(Geometry g, NodePlanes n, PixelPlanes p) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= g.np) return;
+    const int y = int(i / g.w), x = int(i % g.w);
+    const float gradient = fclamps(p.sens_gradient[i], 0.0f, 1.0f);
+    const float attenuation = 1.0f - gradient;
+    for (int c = 0; c < 6; ++c) {
+        const float v = fclamps(tiles_lookup(g, n.field[c_rpd_field[c]], x, y), 0.0f, 1.0f);
+        p.rpd[c][i] = fclamps(v * attenuation, 0.0f, 1.0f);
+    }
+}
+
+__global__ void k_expand(Geometry g, const float* tiles, float* out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= g.np) return;
+    out[i] = tiles_lookup(g, tiles, int(i % g.w), int(i / g.w));
+}
+
+}  // namespace
+
+cudaError_t launch_sensitivity(Job& j) {
+    k_node_stats<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n, j.p, j.cfg.rpf_confidence_samples);
+    k_node_combine<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n);
+    k_sens_pixels<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.g, j.n, j.p);
+    j.launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sensitivity_zero(Job& j) {
+    k_sens_zero<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.p, j.g.np);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rpd_cache(Job& j) {
+    k_rpd_cache<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.g, j.n, j.p);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expand(Job& j, const float* node_field, float* out) {
+    k_expand<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.g, node_field, out);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace rpd

@@ -1,0 +1,195 @@
+// Internal state of the GB300 denoise stage: job layout in HBM, kernel launch wrappers
+// and the helpers every translation unit shares. Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "rpd_gb300.h"
+
+namespace rpd {
+
+constexpr float kEpsSmall = 1e-8f;        // shared/global.h:4
+constexpr int kDeps = RPD_GRID_DEPENDENCIES;
+constexpr int kDepStride = RPD_GRID_DEP_STRIDE;
+
+// rpf::Tile member order (core/stats.h:185-198).
+enum Dep {
+    D_PIXEL = 0, D_BRDF, D_SCREEN_BRDF, D_LENS, D_SCREEN_LENS, D_LIGHT_UV, D_SCREEN_LIGHT_UV,
+    D_ENV, D_SCREEN_ENV, D_LIGHT_SELECT, D_SCREEN_LIGHT_SELECT, D_RR, D_SCREEN_RR
+};
+
+// Node fields of FrameBuffers::SensitivityTiles (core/buffers.h:23-40), in rpd_field order.
+enum NodeField {
+    N_ALL = 0, N_ALL_CONF, N_PIXEL, N_PIXEL_CONF, N_BRDF, N_BRDF_CONF, N_LENS, N_LENS_CONF,
+    N_LIGHT, N_LIGHT_CONF, N_LIGHT_UV, N_LIGHT_UV_CONF, N_LIGHT_SELECT, N_LIGHT_SELECT_CONF,
+    N_ENV, N_ENV_CONF, N_RR, N_RR_CONF, N_FIELDS
+};
+
+// Raw per-node sensitivity / confidence fields in the order main.cpp:781-806 fills them.
+enum RawField {
+    R_PIXEL = 0, R_BRDF, R_LENS, R_LIGHT_UV, R_LIGHT_SELECT, R_ENV, R_RR,
+    R_S_BRDF, R_S_LENS, R_S_LIGHT_UV, R_S_LIGHT_SELECT, R_S_ENV, R_S_RR, R_FIELDS
+};
+
+// Per-pixel planes (float unless noted). Every plane holds W*H values.
+struct PixelPlanes {
+    // PixelStats (core/stats.h:6-23)
+    float* mean;
+    float* square_diff;
+    int32_t* n;
+    float* color_mean[3];
+    float* sqrt_mean[3];
+    float* sqrt_sq[3];
+    // FrameBuffers sums (core/buffers.h:13-16, 114, 118-119)
+    int32_t* hit_count;
+    int32_t* sample_count;
+    float* radiance[3];
+    float* normal[3];
+    float* albedo[3];
+    float* depth;
+    // DerivedFeatureCache (main.cpp:45-52)
+    float* f_normal[3];
+    float* f_depth;
+    float* f_albedo[3];
+    // sensitivity outputs (main.cpp:932-946) and the denoise view of the sensitivity cache:
+    // rpd[c] = clamp(clamp(expanded component c) * (1 - clamp(gradient)))  (main.cpp:305-327)
+    float* sens_confidence;
+    float* sens_gradient;
+    float* rpd[6];
+    // statmc_denoise outputs (main.cpp:1021-1126)
+    float* denoised[3];
+    float* uncertainty;
+    float* alpha;
+    float* var_total;
+    float* var_eff;
+    float* var_ratio;
+    // statmc scratch: stabilised sqrt variance of the mean (main.cpp:972-990)
+    float* sqrt_var_mean[3];
+    float* sqrt_var_stable[3];
+    // variance_denoise (main.cpp:1178-1264)
+    float* variance_denoised;
+    float* var_ping;
+    float* var_pong;
+    // compute_adaptive_sample_counts (main.cpp:1300-1438)
+    float* importance;
+    float* importance_tmp;
+    float* desired_add;
+    float* residual;
+    int32_t* counts;
+    int32_t* active_a;
+    int32_t* active_b;
+};
+
+struct NodePlanes {
+    double* grid;        // nodes * 13 * 36 doubles, merged grid (rpf_grid)
+    double* pass_grid;   // grid of the open pass (the reference's thread-local grids)
+    float* field[N_FIELDS];
+    float* raw[R_FIELDS];
+    float* conf[R_FIELDS];
+    float* prior[R_FIELDS];
+    float* n_normal[3];
+    float* n_depth;
+    float* n_albedo[3];
+};
+
+struct Geometry {
+    int w, h;
+    int support, step, nodes_x, nodes_y;
+    int64_t np, nn;
+};
+
+struct Ctx {
+    int device = 0;
+    uint64_t budget = 0;
+    std::atomic<uint64_t> in_use{0};
+    std::mutex mu;
+    cudaStream_t util_stream = nullptr;
+    std::unordered_map<void*, uint64_t> user_allocs;  // rpd_device_alloc bookkeeping
+};
+
+struct Job {
+    Ctx* ctx = nullptr;
+    rpd_config cfg{};
+    Geometry g{};
+    cudaStream_t stream = nullptr;
+    void* arena = nullptr;       // one allocation holding every plane
+    uint64_t arena_bytes = 0;
+    PixelPlanes p{};
+    NodePlanes n{};
+    // scalars the serial allocation kernel leaves for the host (int32 + doubles)
+    void* scalars = nullptr;
+    // staging for host-side pushes (grown on demand)
+    void* staging = nullptr;
+    uint64_t staging_bytes = 0;
+    int64_t* offsets = nullptr;  // per-pixel sample offsets of the current push
+    int64_t offsets_cap = 0;
+    bool pass_open = false;
+    bool features_valid = false;
+    bool cache_valid = false;
+    bool have_samples = false;
+    cudaEvent_t ev_start[RPD_STAGE_COUNT_]{};
+    cudaEvent_t ev_stop[RPD_STAGE_COUNT_]{};
+    bool ev_used[RPD_STAGE_COUNT_]{};
+    std::atomic<uint64_t> launches{0};
+};
+
+// ---- error plumbing -------------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+#define RPD_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return ::rpd::cuda_fail(e_, #call); \
+    } while (0)
+
+// ---- kernels (launch wrappers; each returns cudaError_t of the launch) -------------------
+struct DeviceSamples {           // rpd_sample_soa with pointers in HBM
+    const float* radiance[3];
+    const float* normal[3];
+    const float* depth;
+    const float* albedo[3];
+    const float* pixel_albedo[3];
+    const float* pixel_u[2];
+    const float* lens_u[2];
+    const float* brdf_u[2];
+    const float* light_u[2];
+    const float* env_u[2];
+    const uint8_t* flags;
+    const uint8_t* category;
+};
+
+cudaError_t launch_offsets_uniform(Job& j, int64_t count, int32_t spp);
+cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count);
+cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count);
+cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first, int64_t count);
+cudaError_t launch_merge_grid(Job& j);
+cudaError_t launch_feature_cache(Job& j);
+cudaError_t launch_sensitivity(Job& j);
+cudaError_t launch_sensitivity_zero(Job& j);
+cudaError_t launch_rpd_cache(Job& j);
+cudaError_t launch_statmc(Job& j);
+cudaError_t launch_variance(Job& j);
+cudaError_t launch_adaptive(Job& j);
+cudaError_t launch_finalize(Job& j);
+cudaError_t launch_expand(Job& j, const float* node_field, float* out);
+cudaError_t launch_atrous(const float* raw, const float* normal, const float* albedo, int w, int h,
+                          float sigma_c, float sigma_n, float sigma_a, int iterations, float* buf_a,
+                          float* buf_b, float** result, cudaStream_t stream, uint64_t* launches);
+cudaError_t launch_joint_bilateral(const float* raw, const float* normal, const float* albedo, int w, int h,
+                                   float sigma_c, float sigma_n, float sigma_p, float sigma_a, float* gaussian,
+                                   float* bilateral, float* joint, cudaStream_t stream, uint64_t* launches);
+
+inline unsigned grid_for(int64_t n, int block) {
+    return static_cast<unsigned>((n + block - 1) / block);
+}
+
+}  // namespace rpd

@@ -1,0 +1,484 @@
+"""ctypes binding of the GB300 denoise-stage C ABI (include/rpd_gb300.h).
+
+The product is the shared library librpd_gb300.so; this module is the thin Python view
+the tests and bench.py use. Loading fails loudly when the library has not been built:
+there is no Python or CPU fallback for any stage.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "librpd_gb300.so"
+
+# ---- enums (include/rpd_gb300.h) ---------------------------------------------------------
+
+OK = 0
+STATUS = {0: "ok", 1: "invalid config", 2: "invalid argument", 3: "out of memory", 4: "over budget",
+          5: "cuda error", 6: "timeout", 7: "state", 8: "no device"}
+MEM_HOST, MEM_DEVICE = 0, 1
+
+FIELDS = [
+    "DENOISED", "UNCERTAINTY", "ALPHA", "VAR_TOTAL_DEBUG", "VAR_EFF_DEBUG", "VAR_RATIO_DEBUG",
+    "VARIANCE_DENOISED", "ADAPTIVE_IMPORTANCE", "SENSITIVITY_CONFIDENCE", "SENSITIVITY_GRADIENT",
+    "HIT_COUNT", "SAMPLE_COUNT", "RADIANCE_SUM", "NORMAL_SUM", "ALBEDO_SUM", "DEPTH_SUM",
+    "STATS_MEAN", "STATS_SQUARE_DIFF", "STATS_N", "STATS_COLOR_MEAN", "STATS_SQRT_MEAN",
+    "STATS_SQRT_SQUARE_DIFF",
+    "NODE_ALL", "NODE_ALL_CONF", "NODE_PIXEL", "NODE_PIXEL_CONF", "NODE_BRDF", "NODE_BRDF_CONF",
+    "NODE_LENS", "NODE_LENS_CONF", "NODE_LIGHT", "NODE_LIGHT_CONF", "NODE_LIGHT_UV", "NODE_LIGHT_UV_CONF",
+    "NODE_LIGHT_SELECT", "NODE_LIGHT_SELECT_CONF", "NODE_ENVIRONMENT", "NODE_ENVIRONMENT_CONF",
+    "NODE_RR", "NODE_RR_CONF",
+    "GRID",
+    "EXPANDED_ALL", "EXPANDED_PIXEL", "EXPANDED_BRDF", "EXPANDED_LENS", "EXPANDED_LIGHT",
+    "EXPANDED_LIGHT_UV", "EXPANDED_LIGHT_SELECT", "EXPANDED_ENVIRONMENT", "EXPANDED_RR",
+    "ADAPTIVE_COUNTS",
+]
+FIELD = {name: i for i, name in enumerate(FIELDS)}
+RGB_FIELDS = {"DENOISED", "RADIANCE_SUM", "NORMAL_SUM", "ALBEDO_SUM", "STATS_COLOR_MEAN", "STATS_SQRT_MEAN",
+              "STATS_SQRT_SQUARE_DIFF"}
+INT_FIELDS = {"HIT_COUNT", "SAMPLE_COUNT", "STATS_N", "ADAPTIVE_COUNTS"}
+STAGES = ["ACCUMULATE", "SENSITIVITY", "STATMC", "VARIANCE", "ADAPTIVE"]
+STAGE = {name: i for i, name in enumerate(STAGES)}
+
+HIT, PIXEL_VALID, LENS_VALID, BRDF_VALID, LIGHT_VALID, LIGHT_SELECT_VALID, ENV_VALID, RR_VALID = (
+    0x01, 0x02, 0x04, 0x08, 0x10, 0x20, 0x40, 0x80)
+LIGHT_INDEX_MASK, RR_SURVIVED = 0x0F, 0x10
+GRID_DEPS, GRID_STRIDE = 13, 36
+DEP_NAMES = ["pixel", "brdf", "screen_brdf", "lens", "screen_lens", "light_uv", "screen_light_uv",
+             "environment", "screen_environment", "light_select", "screen_light_select", "rr", "screen_rr"]
+
+
+class Config(C.Structure):
+    """rpd_config: the RenderConfig fields the stage reads (path_tracer/core/config.h:15-49)."""
+    _fields_ = [
+        ("image_width", C.c_int32), ("image_height", C.c_int32), ("rpf_tile_size", C.c_int32),
+        ("rpf_shrinkage_scale", C.c_float), ("rpf_confidence_samples", C.c_float),
+        ("color_window_radius", C.c_int32), ("color_normal_threshold", C.c_float),
+        ("color_depth_threshold", C.c_float), ("color_compat_alpha", C.c_float), ("color_sigma_max", C.c_float),
+        ("var_window_radius", C.c_int32), ("var_normal_threshold", C.c_float), ("var_depth_threshold", C.c_float),
+        ("var_compat_sigma", C.c_float), ("var_shrinkage_k", C.c_float), ("var_iterations", C.c_int32),
+        ("adaptive_base_samples", C.c_int32), ("adaptive_spp", C.c_int32), ("adaptive_sigma_max", C.c_float),
+        ("adaptive_passes", C.c_int32), ("adaptive_importance_smoothing_radius", C.c_int32),
+        ("debug_statmc_outputs", C.c_int32), ("seed", C.c_uint32),
+    ]
+
+    def replace(self, **kw) -> "Config":
+        c = Config()
+        C.memmove(C.byref(c), C.byref(self), C.sizeof(Config))
+        for k, v in kw.items():
+            if not hasattr(c, k):
+                raise KeyError(k)
+            setattr(c, k, v)
+        return c
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+def default_config(**kw) -> Config:
+    """RenderConfig defaults (core/config.h:27-48) with overrides."""
+    c = Config()
+    c.rpf_tile_size = 8
+    c.rpf_shrinkage_scale = 1.0
+    c.rpf_confidence_samples = 128.0
+    c.color_window_radius = 7
+    c.color_normal_threshold = 0.5
+    c.color_depth_threshold = 0.25
+    c.color_compat_alpha = 0.05
+    c.color_sigma_max = 6.0
+    c.var_window_radius = 1
+    c.var_normal_threshold = 0.5
+    c.var_depth_threshold = 0.25
+    c.var_compat_sigma = 30.0
+    c.var_shrinkage_k = 1e-3
+    c.var_iterations = 2
+    c.adaptive_base_samples = 0
+    c.adaptive_spp = 0
+    c.adaptive_sigma_max = 3.0
+    c.adaptive_passes = 1
+    c.adaptive_importance_smoothing_radius = 1
+    c.debug_statmc_outputs = 0
+    c.seed = 0
+    return c.replace(**kw) if kw else c
+
+
+class SampleSoA(C.Structure):
+    """rpd_sample_soa (all planes as raw pointers)."""
+    _fields_ = [
+        ("radiance", C.c_void_p * 3), ("normal", C.c_void_p * 3), ("depth", C.c_void_p),
+        ("albedo", C.c_void_p * 3), ("pixel_albedo", C.c_void_p * 3), ("pixel_u", C.c_void_p * 2),
+        ("lens_u", C.c_void_p * 2), ("brdf_u", C.c_void_p * 2), ("light_u", C.c_void_p * 2),
+        ("env_u", C.c_void_p * 2), ("flags", C.c_void_p), ("category", C.c_void_p),
+    ]
+
+
+class SynthParams(C.Structure):
+    """rpd_synth_params (include/rpd_synth.h)."""
+    _fields_ = [
+        ("width", C.c_int32), ("height", C.c_int32), ("seed", C.c_uint32), ("regions", C.c_int32),
+        ("dependent_regions", C.c_int32), ("mu_min", C.c_float), ("mu_max", C.c_float), ("sigma", C.c_float),
+        ("slope", C.c_float), ("firefly_rate", C.c_float), ("firefly_scale", C.c_float), ("lights", C.c_int32),
+        ("miss_regions", C.c_int32), ("nan_rate", C.c_float),
+    ]
+
+
+def synth_params(width: int, height: int, seed: int, **kw) -> SynthParams:
+    """Defaults of the full-size synthetic workload (rpd_synth_defaults)."""
+    p = SynthParams(width=width, height=height, seed=seed, regions=48, dependent_regions=24, mu_min=-2.0,
+                    mu_max=1.0, sigma=0.8, slope=0.5, firefly_rate=0.001, firefly_scale=100.0, lights=4,
+                    miss_regions=0, nan_rate=0.0)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+# Sample planes: name -> (components, dtype, per) where per is "sample" or "pixel".
+PLANES = {
+    "radiance": (3, np.float32, "sample"), "normal": (3, np.float32, "sample"), "depth": (1, np.float32, "sample"),
+    "albedo": (3, np.float32, "sample"), "pixel_albedo": (3, np.float32, "pixel"),
+    "pixel_u": (2, np.float32, "sample"), "lens_u": (2, np.float32, "sample"), "brdf_u": (2, np.float32, "sample"),
+    "light_u": (2, np.float32, "sample"), "env_u": (2, np.float32, "sample"), "flags": (1, np.uint8, "sample"),
+    "category": (1, np.uint8, "sample"),
+}
+
+
+class HostSamples:
+    """Per-sample planes in host memory (numpy), for pixels [first, first+count)."""
+
+    def __init__(self, n_samples: int, n_pixels: int, planes: tuple[str, ...] | None = None):
+        self.n_samples = int(n_samples)
+        self.n_pixels = int(n_pixels)
+        planes = planes or ("radiance", "normal", "depth", "pixel_albedo", "pixel_u", "lens_u", "brdf_u",
+                            "light_u", "flags", "category")
+        self.planes: dict[str, np.ndarray] = {}
+        for name in planes:
+            comps, dt, per = PLANES[name]
+            n = self.n_samples if per == "sample" else self.n_pixels
+            self.planes[name] = np.zeros((comps, n) if comps > 1 else (n,), dtype=dt)
+
+    def soa(self) -> SampleSoA:
+        s = SampleSoA()
+        for name, arr in self.planes.items():
+            comps = PLANES[name][0]
+            if comps == 1:
+                setattr(s, name, arr.ctypes.data)
+            else:
+                field = getattr(s, name)
+                for c in range(comps):
+                    field[c] = arr[c].ctypes.data
+        return s
+
+    def slice_pixels(self, offsets: np.ndarray, p0: int, p1: int) -> "HostSamples":
+        """Samples of pixels [p0, p1) given per-pixel offsets (len n_pixels+1)."""
+        k0, k1 = int(offsets[p0]), int(offsets[p1])
+        out = HostSamples.__new__(HostSamples)
+        out.n_samples, out.n_pixels = k1 - k0, p1 - p0
+        out.planes = {}
+        for name, arr in self.planes.items():
+            per = PLANES[name][2]
+            a, b = (k0, k1) if per == "sample" else (p0, p1)
+            out.planes[name] = np.ascontiguousarray(arr[..., a:b])
+        return out
+
+    def concat(self, other: "HostSamples") -> "HostSamples":
+        out = HostSamples.__new__(HostSamples)
+        out.n_samples = self.n_samples + other.n_samples
+        out.n_pixels = self.n_pixels + other.n_pixels
+        out.planes = {k: np.concatenate([v, other.planes[k]], axis=-1) for k, v in self.planes.items()}
+        return out
+
+    @property
+    def nbytes(self) -> int:
+        return sum(a.nbytes for a in self.planes.values())
+
+
+class RpdError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load librpd_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RpdError(8, f"{LIB_PATH} is missing; run __graft_entry__.build() first")
+    L = C.CDLL(str(LIB_PATH))
+    vp, i32, i64, u64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_float
+    sig = {
+        "rpd_config_defaults": (None, [C.POINTER(Config)]),
+        "rpd_config_validate": (C.c_int, [C.POINTER(Config), C.c_char_p, C.c_size_t]),
+        "rpd_ctx_create": (C.c_int, [C.c_int, u64, C.POINTER(vp)]),
+        "rpd_ctx_destroy": (None, [vp]),
+        "rpd_job_footprint": (u64, [C.POINTER(Config)]),
+        "rpd_ctx_bytes_in_use": (u64, [vp]),
+        "rpd_job_create": (C.c_int, [vp, C.POINTER(Config), C.POINTER(vp)]),
+        "rpd_job_destroy": (None, [vp]),
+        "rpd_job_set_config": (C.c_int, [vp, C.POINTER(Config)]),
+        "rpd_job_begin_frame": (C.c_int, [vp]),
+        "rpd_job_push_samples": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp, C.c_int]),
+        "rpd_job_end_pass": (C.c_int, [vp]),
+        "rpd_recompute_sensitivity": (C.c_int, [vp]),
+        "rpd_statmc_denoise": (C.c_int, [vp]),
+        "rpd_variance_denoise": (C.c_int, [vp]),
+        "rpd_compute_adaptive_sample_counts": (C.c_int, [vp, vp, C.c_int]),
+        "rpd_finalize": (C.c_int, [vp]),
+        "rpd_job_read": (C.c_int, [vp, C.c_int, vp, C.c_size_t, C.c_int]),
+        "rpd_field_bytes": (u64, [vp, C.c_int]),
+        "rpd_job_sync": (C.c_int, [vp]),
+        "rpd_job_stage_ms": (f32, [vp, C.c_int]),
+        "rpd_job_launch_count": (u64, [vp]),
+        "rpd_atrous_wavelet": (C.c_int, [vp, vp, vp, vp, i32, i32, f32, f32, f32, i32, vp, C.c_int]),
+        "rpd_joint_bilateral": (C.c_int, [vp, vp, vp, vp, i32, i32, f32, f32, f32, f32, vp, vp, vp, C.c_int]),
+        "rpd_device_alloc": (C.c_int, [vp, u64, C.POINTER(vp)]),
+        "rpd_device_free": (C.c_int, [vp, vp]),
+        "rpd_host_alloc": (C.c_int, [u64, C.POINTER(vp)]),
+        "rpd_host_free": (C.c_int, [vp]),
+        "rpd_memcpy": (C.c_int, [vp, vp, vp, u64, C.c_int]),
+        "rpd_synth_fill": (C.c_int, [vp, C.POINTER(SynthParams), i64, i64, i32, vp, vp, C.POINTER(SampleSoA),
+                                     C.c_int]),
+        "rpd_last_error": (C.c_char_p, []),
+        "rpd_status_string": (C.c_char_p, [C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def exported_symbols() -> list[str]:
+    """Names declared in include/rpd_gb300.h that the library must export."""
+    return ["rpd_config_defaults", "rpd_config_validate", "rpd_ctx_create", "rpd_ctx_destroy", "rpd_job_footprint",
+            "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config",
+            "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_end_pass", "rpd_recompute_sensitivity",
+            "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
+            "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
+            "rpd_atrous_wavelet", "rpd_joint_bilateral", "rpd_device_alloc", "rpd_device_free", "rpd_host_alloc",
+            "rpd_host_free", "rpd_memcpy", "rpd_synth_fill", "rpd_last_error", "rpd_status_string"]
+
+
+def check(status: int) -> None:
+    if status != OK:
+        raise RpdError(status, lib().rpd_last_error().decode(errors="replace"))
+
+
+def validate(cfg: Config) -> tuple[int, str]:
+    buf = C.create_string_buffer(256)
+    st = lib().rpd_config_validate(C.byref(cfg), buf, 256)
+    return st, buf.value.decode()
+
+
+def node_dims(cfg: Config) -> tuple[int, int]:
+    step = max(1, cfg.rpf_tile_size // 2)
+    nx = max(2, (cfg.image_width + step - 1) // step + 1)
+    ny = max(2, (cfg.image_height + step - 1) // step + 1)
+    return nx, ny
+
+
+def field_shape(cfg: Config, name: str) -> tuple[tuple[int, ...], type]:
+    w, h = cfg.image_width, cfg.image_height
+    nx, ny = node_dims(cfg)
+    if name == "GRID":
+        return (ny * nx, GRID_DEPS, GRID_STRIDE), np.float64
+    if name.startswith("NODE_"):
+        return (ny, nx), np.float32
+    dt = np.int32 if name in INT_FIELDS else np.float32
+    if name in RGB_FIELDS:
+        return (h, w, 3), dt
+    return (h, w), dt
+
+
+class DeviceBuffer:
+    def __init__(self, ctx: "Context", nbytes: int):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        p = C.c_void_p()
+        check(lib().rpd_device_alloc(ctx.handle, self.nbytes, C.byref(p)))
+        self.ptr = p.value
+
+    def free(self) -> None:
+        if self.ptr:
+            check(lib().rpd_device_free(self.ctx.handle, self.ptr))
+            self.ptr = None
+
+    def upload(self, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr)
+        assert a.nbytes <= self.nbytes
+        check(lib().rpd_memcpy(self.ctx.handle, self.ptr, a.ctypes.data, a.nbytes, 0))
+
+    def download(self, arr: np.ndarray) -> np.ndarray:
+        assert arr.flags.c_contiguous and arr.nbytes <= self.nbytes
+        check(lib().rpd_memcpy(self.ctx.handle, arr.ctypes.data, self.ptr, arr.nbytes, 1))
+        return arr
+
+
+class DeviceSamples:
+    """Per-sample planes in HBM (one device buffer per plane component)."""
+
+    def __init__(self, ctx: "Context", n_samples: int, n_pixels: int, planes: tuple[str, ...] | None = None):
+        self.ctx = ctx
+        self.n_samples, self.n_pixels = int(n_samples), int(n_pixels)
+        planes = planes or ("radiance", "normal", "depth", "pixel_albedo", "pixel_u", "lens_u", "brdf_u", "light_u",
+                            "flags", "category")
+        self.bufs: dict[str, list[DeviceBuffer]] = {}
+        for name in planes:
+            comps, dt, per = PLANES[name]
+            n = self.n_samples if per == "sample" else self.n_pixels
+            self.bufs[name] = [DeviceBuffer(ctx, max(1, n) * np.dtype(dt).itemsize) for _ in range(comps)]
+
+    @classmethod
+    def from_host(cls, ctx: "Context", host: HostSamples) -> "DeviceSamples":
+        d = cls(ctx, host.n_samples, host.n_pixels, tuple(host.planes))
+        for name, arr in host.planes.items():
+            comps = PLANES[name][0]
+            for c in range(comps):
+                d.bufs[name][c].upload(arr[c] if comps > 1 else arr)
+        return d
+
+    def soa(self) -> SampleSoA:
+        s = SampleSoA()
+        for name, bl in self.bufs.items():
+            if len(bl) == 1 and PLANES[name][0] == 1:
+                setattr(s, name, bl[0].ptr)
+            else:
+                field = getattr(s, name)
+                for c, b in enumerate(bl):
+                    field[c] = b.ptr
+        return s
+
+    @property
+    def nbytes(self) -> int:
+        total = 0
+        for name in self.bufs:
+            comps, dt, per = PLANES[name]
+            n = self.n_samples if per == "sample" else self.n_pixels
+            total += comps * n * np.dtype(dt).itemsize
+        return total
+
+    def free(self) -> None:
+        for bl in self.bufs.values():
+            for b in bl:
+                b.free()
+        self.bufs = {}
+
+
+class Context:
+    """rpd_ctx: one GPU and the HBM budget jobs are admitted against."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        h = C.c_void_p()
+        check(lib().rpd_ctx_create(device, budget_bytes, C.byref(h)))
+        self.handle = h.value
+
+    def close(self) -> None:
+        if self.handle:
+            lib().rpd_ctx_destroy(self.handle)
+            self.handle = None
+
+    def bytes_in_use(self) -> int:
+        return int(lib().rpd_ctx_bytes_in_use(self.handle))
+
+    def synth_fill(self, params: SynthParams, first: int, count: int, spp: int, out, counts=None, start_n=None):
+        """Fill HostSamples or DeviceSamples with synthetic samples."""
+        where = MEM_DEVICE if isinstance(out, DeviceSamples) else MEM_HOST
+        s = out.soa()
+        cp = counts.ctypes.data if isinstance(counts, np.ndarray) else (counts.ptr if counts is not None else None)
+        sp = start_n.ctypes.data if isinstance(start_n, np.ndarray) else (start_n.ptr if start_n is not None else None)
+        check(lib().rpd_synth_fill(self.handle, C.byref(params), first, count, spp, cp, sp, C.byref(s), where))
+
+    def atrous(self, raw, normal, albedo, sigma_c, sigma_n, sigma_a, iterations):
+        h, w, _ = raw.shape
+        out = np.empty_like(raw, dtype=np.float32)
+        args = [np.ascontiguousarray(a, dtype=np.float32) for a in (raw, normal, albedo)]
+        check(lib().rpd_atrous_wavelet(self.handle, *[a.ctypes.data for a in args], w, h, sigma_c, sigma_n, sigma_a,
+                                       iterations, out.ctypes.data, MEM_HOST))
+        return out
+
+    def joint_bilateral(self, raw, normal, albedo, sigma_c, sigma_n, sigma_p, sigma_a):
+        h, w, _ = raw.shape
+        outs = [np.empty((h, w, 3), dtype=np.float32) for _ in range(3)]
+        args = [np.ascontiguousarray(a, dtype=np.float32) for a in (raw, normal, albedo)]
+        check(lib().rpd_joint_bilateral(self.handle, *[a.ctypes.data for a in args], w, h, sigma_c, sigma_n, sigma_p,
+                                        sigma_a, *[o.ctypes.data for o in outs], MEM_HOST))
+        return tuple(outs)
+
+
+class Job:
+    """rpd_job: one frame's state in HBM and the reference's stage entry points."""
+
+    def __init__(self, ctx: Context, cfg: Config):
+        self.ctx = ctx
+        self.cfg = cfg
+        h = C.c_void_p()
+        check(lib().rpd_job_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+
+    def close(self) -> None:
+        if self.handle:
+            lib().rpd_job_destroy(self.handle)
+            self.handle = None
+
+    def set_config(self, cfg: Config) -> None:
+        check(lib().rpd_job_set_config(self.handle, C.byref(cfg)))
+        self.cfg = cfg.replace(image_width=self.cfg.image_width, image_height=self.cfg.image_height,
+                               rpf_tile_size=self.cfg.rpf_tile_size)
+
+    def begin_frame(self) -> None:
+        check(lib().rpd_job_begin_frame(self.handle))
+
+    def push(self, samples, first: int, count: int, spp: int = 0, counts=None) -> None:
+        where = MEM_DEVICE if isinstance(samples, DeviceSamples) else MEM_HOST
+        s = samples.soa()
+        if counts is None:
+            cp = None
+        elif isinstance(counts, np.ndarray):
+            counts = np.ascontiguousarray(counts, dtype=np.int32)
+            cp = counts.ctypes.data
+        else:
+            cp = counts.ptr
+        check(lib().rpd_job_push_samples(self.handle, C.byref(s), first, count, spp, cp, where))
+
+    def end_pass(self) -> None:
+        check(lib().rpd_job_end_pass(self.handle))
+
+    def recompute_sensitivity(self) -> None:
+        check(lib().rpd_recompute_sensitivity(self.handle))
+
+    def statmc_denoise(self) -> None:
+        check(lib().rpd_statmc_denoise(self.handle))
+
+    def variance_denoise(self) -> None:
+        check(lib().rpd_variance_denoise(self.handle))
+
+    def compute_adaptive_sample_counts(self) -> np.ndarray:
+        out = np.empty(self.cfg.image_width * self.cfg.image_height, dtype=np.int32)
+        check(lib().rpd_compute_adaptive_sample_counts(self.handle, out.ctypes.data, MEM_HOST))
+        return out
+
+    def finalize(self) -> None:
+        check(lib().rpd_finalize(self.handle))
+
+    def sync(self) -> None:
+        check(lib().rpd_job_sync(self.handle))
+
+    def read(self, name: str) -> np.ndarray:
+        shape, dt = field_shape(self.cfg, name)
+        out = np.empty(shape, dtype=dt)
+        check(lib().rpd_job_read(self.handle, FIELD[name], out.ctypes.data, out.nbytes, MEM_HOST))
+        return out
+
+    def stage_ms(self, stage: str) -> float:
+        return float(lib().rpd_job_stage_ms(self.handle, STAGE[stage]))
+
+    def launches(self) -> int:
+        return int(lib().rpd_job_launch_count(self.handle))

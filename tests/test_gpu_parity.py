@@ -1,0 +1,230 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same inputs.
+
+Bars, per stage:
+  * pixel statistics, features, the RPD grid, the raw node statistics, the variance
+    stabilisation and the adaptive integer counts: bit-exact (the kernels perform the
+    reference's IEEE operations in its order; the grid order is the reference's
+    single-thread order, so the oracle runs with one thread for these checks);
+  * stages that call expf / exp (prior smoothing, the StatMC weights, importance
+    smoothing, the filters): the CUDA math library is within 2 ulp of the C library's,
+    so the bar is the plain-form tolerance: max per-pixel relative error <= 1e-4 with a
+    1e-3 floor on |reference| (`max_rel_err`).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import B, R, assert_bitwise, max_rel_err, small_config
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+FLOOR = 1e-3
+
+EXACT_FIELDS = ["STATS_MEAN", "STATS_SQUARE_DIFF", "STATS_N", "STATS_COLOR_MEAN", "STATS_SQRT_MEAN",
+                "STATS_SQRT_SQUARE_DIFF", "HIT_COUNT", "SAMPLE_COUNT", "RADIANCE_SUM", "NORMAL_SUM", "ALBEDO_SUM",
+                "DEPTH_SUM", "GRID"]
+NODE_FIELDS = [f for f in R.FIELDS if f.startswith("NODE_")]
+CLOSE_PIXEL_FIELDS = ["SENSITIVITY_CONFIDENCE", "SENSITIVITY_GRADIENT", "DENOISED", "UNCERTAINTY", "ALPHA",
+                      "VAR_TOTAL_DEBUG", "VAR_EFF_DEBUG", "VAR_RATIO_DEBUG"]
+
+
+def run_both(gpu_ctx, cfg, samples, spp, threads=1):
+    g = R.Job(gpu_ctx, cfg)
+    o = B.OracleJob(cfg, threads=threads)
+    for job in (g, o):
+        B.run_pipeline(job, samples, spp)
+    return g, o
+
+
+def check_pipeline(g, o, exact_grid=True):
+    for f in EXACT_FIELDS:
+        if f == "GRID" and not exact_grid:
+            continue
+        assert_bitwise(g.read(f), o.read(f), f)
+    for f in NODE_FIELDS:
+        x, y = g.read(f), o.read(f)
+        assert np.max(np.abs(x - y)) <= 1e-5, f
+    for f in CLOSE_PIXEL_FIELDS:
+        x, y = g.read(f), o.read(f)
+        err = max_rel_err(x, y, FLOOR) if f != "SENSITIVITY_GRADIENT" else float(np.max(np.abs(x - y)))
+        assert err <= TOL, (f, err)
+    # the variance stabilisation is single precision without exp: bit-exact
+    assert_bitwise(g.read("VARIANCE_DENOISED"), o.read("VARIANCE_DENOISED"), "VARIANCE_DENOISED")
+
+
+@pytest.mark.parametrize("w,h,spp,tile", [(37, 23, 5, 16), (64, 48, 8, 16), (33, 17, 4, 6), (16, 16, 3, 1)])
+def test_synthetic_pipeline(gpu_ctx, w, h, spp, tile):
+    cfg = small_config(w, h, rpf_tile_size=tile)
+    p = R.synth_params(w, h, 11, miss_regions=4, nan_rate=0.005)
+    s = B.synth_fill(p, 0, w * h, spp)
+    g, o = run_both(gpu_ctx, cfg, s, spp)
+    check_pipeline(g, o)
+    g.close()
+    o.close()
+
+
+def test_default_knobs_and_alpha(gpu_ctx):
+    # RenderConfig defaults: tile 8, colour radius 7, alpha 0.05 (t table), variance radius 1
+    w, h, spp = 40, 30, 6
+    cfg = R.default_config(image_width=w, image_height=h, seed=5)
+    s = B.synth_fill(R.synth_params(w, h, 3), 0, w * h, spp)
+    g, o = run_both(gpu_ctx, cfg, s, spp)
+    check_pipeline(g, o)
+    # an alpha outside the two tables takes the normal-quantile branch
+    cfg2 = cfg.replace(color_compat_alpha=0.2)
+    for job in (g, o):
+        job.set_config(cfg2)
+        job.statmc_denoise()
+    assert max_rel_err(g.read("DENOISED"), o.read("DENOISED"), FLOOR) <= TOL
+
+
+def test_rpd_disabled_matches(gpu_ctx):
+    w, h, spp = 32, 24, 4
+    cfg = small_config(w, h, rpf_shrinkage_scale=0.0)
+    s = B.synth_fill(R.synth_params(w, h, 9), 0, w * h, spp)
+    g, o = run_both(gpu_ctx, cfg, s, spp)
+    check_pipeline(g, o)
+    assert not np.any(g.read("SENSITIVITY_GRADIENT"))
+
+
+def test_chunked_pushes_equal_single_push(gpu_ctx):
+    """Pushing a pass in row bands gives the same bits as one push (sequential order)."""
+    w, h, spp = 30, 20, 4
+    cfg = small_config(w, h, rpf_tile_size=8)
+    s = B.synth_fill(R.synth_params(w, h, 21), 0, w * h, spp)
+    g1 = R.Job(gpu_ctx, cfg)
+    B.run_pipeline(g1, s, spp)
+    g2 = R.Job(gpu_ctx, cfg)
+    g2.begin_frame()
+    offsets = np.arange(w * h + 1) * spp
+    for p0, p1 in [(0, 7), (7, 133), (133, 400), (400, w * h)]:
+        g2.push(s.slice_pixels(offsets, p0, p1), p0, p1 - p0, spp)
+    g2.end_pass()
+    g2.recompute_sensitivity()
+    g2.statmc_denoise()
+    g2.variance_denoise()
+    for f in ["GRID", "STATS_MEAN", "DENOISED", "VARIANCE_DENOISED", "NODE_ALL"]:
+        assert_bitwise(g1.read(f), g2.read(f), f)
+
+
+def test_ragged_counts_and_empty_pixels(gpu_ctx):
+    w, h = 25, 19
+    rng = np.random.default_rng(4)
+    counts = rng.integers(0, 9, size=w * h).astype(np.int32)
+    counts[::7] = 0
+    cfg = small_config(w, h)
+    s = B.synth_fill(R.synth_params(w, h, 8, miss_regions=2), 0, w * h, 0, counts=counts)
+    g = R.Job(gpu_ctx, cfg)
+    o = B.OracleJob(cfg, threads=1)
+    for job in (g, o):
+        job.begin_frame()
+        job.push(s, 0, w * h, 0, counts=counts)
+        job.end_pass()
+        job.recompute_sensitivity()
+        job.statmc_denoise()
+        job.variance_denoise()
+    check_pipeline(g, o)
+
+
+def test_single_pixel_and_thin_images(gpu_ctx):
+    for w, h in [(1, 1), (1, 9), (7, 1), (2, 3)]:
+        cfg = small_config(w, h, color_window_radius=2, var_window_radius=1)
+        s = B.synth_fill(R.synth_params(w, h, 2), 0, w * h, 3)
+        g, o = run_both(gpu_ctx, cfg, s, 3)
+        check_pipeline(g, o)
+        g.close()
+
+
+def test_adaptive_counts_bit_exact(gpu_ctx):
+    w, h, spp = 48, 36, 4
+    for radius in (0, 1, 2):
+        cfg = small_config(w, h, adaptive_spp=4, adaptive_base_samples=1, adaptive_importance_smoothing_radius=radius,
+                           seed=77)
+        s = B.synth_fill(R.synth_params(w, h, 13), 0, w * h, spp)
+        g, o = run_both(gpu_ctx, cfg, s, spp)
+        cg = g.compute_adaptive_sample_counts()
+        co = o.compute_adaptive_sample_counts()
+        imp_g, imp_o = g.read("ADAPTIVE_IMPORTANCE"), o.read("ADAPTIVE_IMPORTANCE")
+        if radius == 0:
+            assert_bitwise(imp_g, imp_o, "importance")
+        if np.array_equal(imp_g.view(np.uint32), imp_o.view(np.uint32)):
+            assert np.array_equal(cg, co)
+        else:
+            # importance differs only through expf rounding in the smoothing weights
+            assert max_rel_err(imp_g, imp_o, 1e-6) <= 1e-5
+            assert int(np.abs(cg - co).sum()) <= 4
+        assert cg.sum() == co.sum() == cfg.adaptive_spp * w * h
+        assert cg.min() >= cfg.adaptive_base_samples
+        assert cg.max() <= cfg.adaptive_base_samples + max(4, 8 * cfg.adaptive_spp) + 1
+
+
+def test_adaptive_passes_sequence(gpu_ctx):
+    """render()'s adaptive loop (main.cpp:1547-1552) with synthetic extra samples."""
+    w, h, spp = 32, 24, 2
+    cfg = small_config(w, h, adaptive_spp=4, adaptive_base_samples=1, adaptive_passes=2,
+                       adaptive_importance_smoothing_radius=0)
+    p = R.synth_params(w, h, 31)
+    g = R.Job(gpu_ctx, cfg)
+    o = B.OracleJob(cfg, threads=1)
+    s0 = B.synth_fill(p, 0, w * h, spp)
+    for job in (g, o):
+        job.begin_frame()
+        job.push(s0, 0, w * h, spp)
+        job.end_pass()
+        job.recompute_sensitivity()
+    for _ in range(cfg.adaptive_passes):
+        cs = []
+        for job in (g, o):
+            job.statmc_denoise()
+            job.variance_denoise()
+            cs.append(job.compute_adaptive_sample_counts())
+        assert np.array_equal(cs[0], cs[1])
+        n = o.read("STATS_N").ravel()
+        extra = B.synth_fill(p, 0, w * h, 0, counts=cs[1], start_n=n)
+        for job in (g, o):
+            job.push(extra, 0, w * h, 0, counts=cs[1])
+            job.end_pass()
+            job.recompute_sensitivity()
+    for job in (g, o):
+        job.recompute_sensitivity()
+        job.statmc_denoise()
+        job.variance_denoise()
+        job.finalize()
+    check_pipeline(g, o)
+
+
+def test_filters(gpu_ctx):
+    rng = np.random.default_rng(1)
+    h, w = 37, 53
+    raw = rng.lognormal(-1.0, 0.8, size=(h, w, 3)).astype(np.float32)
+    normal = rng.uniform(0, 1, size=(h, w, 3)).astype(np.float32)
+    albedo = rng.uniform(0, 1, size=(h, w, 3)).astype(np.float32)
+    out_g = gpu_ctx.atrous(raw, normal, albedo, 0.3, 0.2, 0.1, 5)
+    out_o = np.empty_like(raw)
+    B.port().orc_atrous_wavelet(raw.ctypes.data, normal.ctypes.data, albedo.ctypes.data, w, h, 0.3, 0.2, 0.1, 5,
+                                out_o.ctypes.data, 1)
+    assert max_rel_err(out_g, out_o, FLOOR) <= TOL
+    gs = gpu_ctx.joint_bilateral(raw, normal, albedo, 0.3, 0.2, 2.0, 0.1)
+    os_ = [np.empty_like(raw) for _ in range(3)]
+    B.port().orc_joint_bilateral(raw.ctypes.data, normal.ctypes.data, albedo.ctypes.data, w, h, 0.3, 0.2, 2.0, 0.1,
+                                 *[o.ctypes.data for o in os_], 1)
+    for a, b in zip(gs, os_):
+        assert max_rel_err(a, b, FLOOR) <= TOL
+
+
+def test_device_resident_push_matches_host_push(gpu_ctx):
+    w, h, spp = 40, 24, 4
+    cfg = small_config(w, h)
+    p = R.synth_params(w, h, 17)
+    host = B.synth_fill(p, 0, w * h, spp)
+    dev = R.DeviceSamples(gpu_ctx, w * h * spp, w * h)
+    gpu_ctx.synth_fill(p, 0, w * h, spp, dev)
+    g1 = R.Job(gpu_ctx, cfg)
+    g2 = R.Job(gpu_ctx, cfg)
+    B.run_pipeline(g1, host, spp)
+    B.run_pipeline(g2, dev, spp)
+    for f in ["GRID", "STATS_MEAN", "DENOISED", "VARIANCE_DENOISED"]:
+        assert_bitwise(g1.read(f), g2.read(f), f)
+    dev.free()
