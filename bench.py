@@ -1,0 +1,370 @@
+"""Benchmark of the GB300 StatMC / RPD denoise stage.
+
+Workload (one step = one frame of the plain method): 1920x1080, 16 samples per pixel of
+seeded synthetic per-sample buffers (include/rpd_synth.h: 48 Voronoi regions, log-normal
+radiance, 24 regions dependent on two random dims, 0.1% fireflies x100), denoise knobs of
+the reference's cornell_box configuration (path_tracer/config/cornell.yaml) with rpf tile
+16, colour window radius 5, variance radius 3, 2 variance iterations and no adaptive pass.
+A step runs the stage as render() does for a frame: accumulate the samples (statistics,
+features, RPD grid), recompute_sensitivity, statmc_denoise, variance_denoise.
+
+  value  Msamples/s with the samples already resident in HBM (2.06 GB of FP32 planes per
+         frame, larger than the 129 MB L2, so no flush is needed between steps).
+  e2e    the same through the C ABI from pinned host buffers: every step copies the frame's
+         sample planes host->HBM and reads the denoised image back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+`--impl reference` times the reference CPU implementation of the stage on this host's cores
+(the C restatement in oracle/, since the reference checkout does not exist on the GPU host)
+on a 1920x270 band of the same workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "rpd-statmc-denoiser_gb300"))
+
+W, H, SPP, SEED = 1920, 1080, 16, 1234
+METRIC = "denoised Msamples/s at 1080p 16spp (plain)"
+UNIT = "Msamples/s"
+
+
+def workload_config(R, w=W, h=H):
+    # path_tracer/config/cornell.yaml stage knobs + the plain-method overrides
+    return R.default_config(
+        image_width=w, image_height=h, rpf_tile_size=16, color_window_radius=5, color_normal_threshold=0.6,
+        color_depth_threshold=0.2, color_compat_alpha=0.01, color_sigma_max=4.0, var_window_radius=3,
+        var_normal_threshold=0.6, var_compat_sigma=3.0, var_shrinkage_k=0.7, var_iterations=2, adaptive_spp=4,
+        adaptive_base_samples=2, adaptive_sigma_max=4.0, adaptive_passes=0, seed=SEED)
+
+
+def config_json(R, cfg, extra=None):
+    d = {"workload": "plain method, 1920x1080, 16 spp, synthetic per-sample FP32 buffers (seed 1234)",
+         "width": cfg.image_width, "height": cfg.image_height, "spp": SPP, "rpf_tile_size": cfg.rpf_tile_size,
+         "color_window_radius": cfg.color_window_radius, "var_window_radius": cfg.var_window_radius,
+         "var_iterations": cfg.var_iterations, "adaptive_passes": 0,
+         "l2": "inputs larger than L2 (2.06 GB of sample planes per step vs 129 MB L2)",
+         "parallelism": "replicas"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+# Algorithmic bytes each kernel family must move for one frame (per launch of that family
+# in a frame), from the plane sizes: per sample 29 B for the statistics pass (radiance 12,
+# normal 12, depth 4, flags 1), 46 B for the grid pass (radiance 12, pixel/lens/brdf/light
+# uv 32, flags 1, category 1); per pixel 12 B of albedo plus 96 B of state read and written
+# by the statistics pass; per node 3744 B of grid read and written by the grid pass; per
+# pixel 100 B read and 32 B written by the StatMC window.
+def algorithmic_bytes(kernel: str, np_: int, nn: int, n: int) -> float:
+    if kernel == "accumulate_pixels":
+        return 29.0 * n + (12.0 + 192.0) * np_
+    if kernel == "grid":
+        return 46.0 * n + 2.0 * 3744.0 * nn
+    if kernel == "statmc_window":
+        return 132.0 * np_
+    if kernel == "merge":
+        return 3.0 * 3744.0 * nn
+    if kernel == "variance":
+        return np_ * (4 * 2 + 2 * (4 + 4 + 12 + 4 + 4 + 4) + 4 * 3)
+    if kernel == "node_stats":
+        return 3744.0 * nn + 4.0 * 34 * nn
+    return 0.0
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def max_over_ranks(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_gpu(args):
+    import rpd_gb300 as R
+
+    world, rank, local, dist = dist_setup()
+    cfg = workload_config(R)
+    np_ = W * H
+    n = np_ * SPP
+    nx, ny = R.node_dims(cfg)
+    nn = nx * ny
+    ctx = R.Context(local, 0)
+    params = R.synth_params(W, H, SEED + rank)
+    dev = R.DeviceSamples(ctx, n, np_)
+    ctx.synth_fill(params, 0, np_, SPP, dev)
+    job = R.Job(ctx, cfg)
+
+    def step(samples):
+        job.begin_frame()
+        job.push(samples, 0, np_, SPP)
+        job.end_pass()
+        job.recompute_sensitivity()
+        job.statmc_denoise()
+        job.variance_denoise()
+
+    for _ in range(args.warmup):
+        step(dev)
+    job.sync()
+    # device-resident timed region
+    job.set_profiling(True)
+    job.reset_kernel_times()
+    launches0 = job.launches()
+    barrier(dist)
+    job.sync()
+    with ClockSampler(local) as clocks:
+        job.mark(0)
+        for _ in range(args.steps):
+            step(dev)
+        job.mark(1)
+        elapsed = job.elapsed_ms(0, 1)
+    launches = job.launches() - launches0
+    ktimes = job.kernel_times()
+    job.set_profiling(False)
+    elapsed_max = max_over_ranks(dist, elapsed)
+    ms_per_step = elapsed_max / args.steps
+    value = world * n / (ms_per_step * 1e-3) / 1e6
+
+    # end-to-end through the C ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = pinned_host_copy(R, ctx, dev)
+        denoised = np.empty((H, W, 3), dtype=np.float32)
+        for _ in range(max(1, args.warmup)):
+            step(host)
+            job.read("DENOISED")
+        job.sync()
+        barrier(dist)
+        t0 = time.perf_counter()
+        job.mark(2)
+        for _ in range(args.steps):
+            step(host)
+            R.check(R.lib().rpd_job_read(job.handle, R.FIELD["DENOISED"], denoised.ctypes.data, denoised.nbytes,
+                                         R.MEM_HOST))
+        job.mark(3)
+        e2e_ms = job.elapsed_ms(2, 3)
+        wall_ms = (time.perf_counter() - t0) * 1e3
+        e2e_ms = max_over_ranks(dist, max(e2e_ms, wall_ms))
+        e2e = {"value": round(world * n / (e2e_ms / args.steps * 1e-3) / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(denoised.nbytes),
+               "ms_per_step": round(e2e_ms / args.steps, 3)}
+        host.free()
+
+    # roofline of the dominant kernel
+    dominant = max(ktimes, key=lambda k: ktimes[k][0])
+    dom_ms, dom_launches = ktimes[dominant]
+    per_launch_ms = dom_ms / max(1, dom_launches)
+    launches_per_frame = max(1, dom_launches // args.steps)
+    alg = algorithmic_bytes(dominant, np_, nn, n) / launches_per_frame
+    peaks = measured_peaks()
+    achieved = alg / (per_launch_ms * 1e-3) / 1e9 if alg else None
+    roofline = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / peaks["hbm_gbs"], 4) if achieved else None,
+                "traffic": None, "peak_source": peaks["source"], "ms_per_launch": round(per_launch_ms, 4),
+                "algorithmic_bytes_per_launch": alg}
+    kernels_ms = {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]}
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": config_json(R, cfg),
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks.summary(), "roofline": roofline,
+        "kernels_ms_per_step": kernels_ms,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, steps=1)
+    job.close()
+    dev.free()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def pinned_host_copy(R, ctx, dev):
+    """Copy device sample planes into page-locked host planes (for the end-to-end leg)."""
+    import ctypes as C
+
+    class PinnedSamples:
+        def __init__(self):
+            self.ptrs = []
+            self.planes = {}
+            self.nbytes = 0
+            for name, bl in dev.bufs.items():
+                arrs = []
+                for b in bl:
+                    p = C.c_void_p()
+                    R.check(R.lib().rpd_host_alloc(b.nbytes, C.byref(p)))
+                    self.ptrs.append(p.value)
+                    R.check(R.lib().rpd_memcpy(ctx.handle, p.value, b.ptr, b.nbytes, 1))
+                    arrs.append(p.value)
+                    self.nbytes += b.nbytes
+                self.planes[name] = arrs
+
+        def soa(self):
+            s = R.SampleSoA()
+            for name, arrs in self.planes.items():
+                if len(arrs) == 1 and R.PLANES[name][0] == 1:
+                    setattr(s, name, arrs[0])
+                else:
+                    f = getattr(s, name)
+                    for c, p in enumerate(arrs):
+                        f[c] = p
+            return s
+
+        def free(self):
+            for p in self.ptrs:
+                R.lib().rpd_host_free(p)
+            self.ptrs = []
+
+    return PinnedSamples()
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured (MEASURED_PEAKS.json)"}
+    return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
+
+
+def cpu_baseline(args, steps=1, warmup=0):
+    """The reference CPU path (the C restatement in oracle/) on this host's cores, on a
+    1920x270 band (a quarter of the frame) of the same workload."""
+    import rpd_gb300 as R
+    from oracle import binding as B
+
+    threads = os.cpu_count() or 1
+    band_h = H // 4
+    cfg = workload_config(R, W, band_h)
+    params = R.synth_params(W, band_h, SEED)
+    samples = B.synth_fill(params, 0, W * band_h, SPP, threads=threads)
+    job = B.OracleJob(cfg, threads=threads)
+    for _ in range(warmup):
+        B.run_pipeline(job, samples, SPP)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        B.run_pipeline(job, samples, SPP)
+        times.append(time.perf_counter() - t0)
+    job.close()
+    sec = sum(times) / len(times)
+    return {"value": round(W * band_h * SPP / sec / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"1920x{band_h} band, 16 spp ({W * band_h * SPP} samples) per step, {len(times)} step(s), "
+                      f"{sec:.2f} s per step"}
+
+
+def run_reference(args):
+    world, rank, _, dist = dist_setup()
+    if rank != 0:
+        return
+    import rpd_gb300 as R
+
+    cb = cpu_baseline(args, steps=args.steps, warmup=min(args.warmup, 1))
+    cfg = workload_config(R)
+    out = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": min(args.warmup, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32+f64", "data": "synthetic", "impl": "reference",
+           "config": config_json(R, cfg, {"sample": cb["sample"]}), "cpu_baseline": cb,
+           "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

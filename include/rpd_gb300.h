@@ -201,6 +201,25 @@ typedef enum rpd_stage {
     RPD_STAGE_COUNT_
 } rpd_stage;
 
+/* Kernel families, for per-kernel device timing (rpd_job_kernel_time). */
+typedef enum rpd_kernel {
+    RPD_KERNEL_OFFSETS = 0,         /* per-pixel sample offsets of a push */
+    RPD_KERNEL_ACCUMULATE_PIXELS,   /* Welford statistics + features */
+    RPD_KERNEL_GRID,                /* RPD grid accumulation */
+    RPD_KERNEL_MERGE,               /* pass grid merge */
+    RPD_KERNEL_FEATURES,            /* feature cache */
+    RPD_KERNEL_NODE_STATS,          /* per-node sensitivities, confidences, features */
+    RPD_KERNEL_NODE_COMBINE,        /* prior smoothing + combine */
+    RPD_KERNEL_SENS_PIXELS,         /* per-pixel confidence + gradient */
+    RPD_KERNEL_RPD_CACHE,           /* per-pixel RPD components */
+    RPD_KERNEL_SQRT_VARIANCE,       /* sqrt-domain variance of the mean + stabilisation */
+    RPD_KERNEL_STATMC_WINDOW,       /* the StatMC Welch window */
+    RPD_KERNEL_VARIANCE,            /* variance stabilisation iterations */
+    RPD_KERNEL_ADAPTIVE,            /* importance + allocation */
+    RPD_KERNEL_OTHER,               /* finalize, reads, fills */
+    RPD_KERNEL_COUNT_
+} rpd_kernel;
+
 typedef struct rpd_ctx rpd_ctx;
 typedef struct rpd_job rpd_job;
 
@@ -265,6 +284,17 @@ int rpd_job_sync(rpd_job* job);
 float rpd_job_stage_ms(const rpd_job* job, rpd_stage stage);
 /* Kernel launches issued by this job since creation (for launch accounting). */
 uint64_t rpd_job_launch_count(const rpd_job* job);
+/* Per-kernel device timing: with profiling on, every launch of the job is bracketed by
+ * CUDA events on the job's stream. rpd_job_kernel_time synchronises the job and returns
+ * the summed milliseconds and launch count of one kernel family since the last reset. */
+int rpd_job_set_profiling(rpd_job* job, int enable);
+int rpd_job_kernel_time(rpd_job* job, rpd_kernel kernel, double* total_ms, uint64_t* launches);
+int rpd_job_reset_kernel_times(rpd_job* job);
+const char* rpd_kernel_name(rpd_kernel kernel);
+/* Device-time markers on the job's stream (slots 0..7): record, then read the elapsed
+ * milliseconds between two recorded slots (synchronises on the later one). */
+int rpd_job_mark(rpd_job* job, int slot);
+int rpd_job_mark_elapsed(rpd_job* job, int from_slot, int to_slot, float* ms);
 
 /* ---- standalone filters (denoising/atrous_wavelet.cpp, denoising/joint_bilateral.cpp) ---- */
 

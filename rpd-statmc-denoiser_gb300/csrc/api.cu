@@ -472,6 +472,13 @@ void rpd_job_destroy(rpd_job* job) {
         if (j->ev_start[s]) cudaEventDestroy(j->ev_start[s]);
         if (j->ev_stop[s]) cudaEventDestroy(j->ev_stop[s]);
     }
+    for (auto& t : j->ktimes) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    for (auto e : j->event_pool) cudaEventDestroy(e);
+    for (auto e : j->marks)
+        if (e) cudaEventDestroy(e);
     if (j->stream) cudaStreamDestroy(j->stream);
     delete j;
 }
@@ -801,6 +808,76 @@ float rpd_job_stage_ms(const rpd_job* job, rpd_stage s) {
 uint64_t rpd_job_launch_count(const rpd_job* job) {
     const Job* j = reinterpret_cast<const Job*>(job);
     return j ? j->launches.load() : 0;
+}
+
+int rpd_job_set_profiling(rpd_job* job, int enable) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    j->profile = enable != 0;
+    return RPD_OK;
+}
+
+static int fold_kernel_times(Job* j) {
+    RPD_CUDA(cudaStreamSynchronize(j->stream));
+    for (auto& t : j->ktimes) {
+        float ms = 0.0f;
+        RPD_CUDA(cudaEventElapsedTime(&ms, t.a, t.b));
+        j->ktotal[t.kernel] += double(ms);
+        j->kcount[t.kernel] += 1;
+        j->event_pool.push_back(t.a);
+        j->event_pool.push_back(t.b);
+    }
+    j->ktimes.clear();
+    return RPD_OK;
+}
+
+int rpd_job_kernel_time(rpd_job* job, rpd_kernel k, double* total_ms, uint64_t* launches) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (k < 0 || k >= RPD_KERNEL_COUNT_) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown kernel family");
+    int st = fold_kernel_times(j);
+    if (st != RPD_OK) return st;
+    if (total_ms) *total_ms = j->ktotal[k];
+    if (launches) *launches = j->kcount[k];
+    return RPD_OK;
+}
+
+int rpd_job_reset_kernel_times(rpd_job* job) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    int st = fold_kernel_times(j);
+    if (st != RPD_OK) return st;
+    for (int k = 0; k < RPD_KERNEL_COUNT_; ++k) {
+        j->ktotal[k] = 0.0;
+        j->kcount[k] = 0;
+    }
+    return RPD_OK;
+}
+
+int rpd_job_mark(rpd_job* job, int slot) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (slot < 0 || slot >= 8) return fail(RPD_ERR_INVALID_ARGUMENT, "marker slot must be 0..7");
+    if (!j->marks[slot]) RPD_CUDA(cudaEventCreate(&j->marks[slot]));
+    RPD_CUDA(cudaEventRecord(j->marks[slot], j->stream));
+    return RPD_OK;
+}
+
+int rpd_job_mark_elapsed(rpd_job* job, int a, int b, float* ms) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (a < 0 || a >= 8 || b < 0 || b >= 8 || !j->marks[a] || !j->marks[b] || !ms)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "marker slots were not recorded");
+    RPD_CUDA(cudaEventSynchronize(j->marks[b]));
+    RPD_CUDA(cudaEventElapsedTime(ms, j->marks[a], j->marks[b]));
+    return RPD_OK;
+}
+
+const char* rpd_kernel_name(rpd_kernel k) {
+    static const char* names[RPD_KERNEL_COUNT_] = {
+        "offsets", "accumulate_pixels", "grid", "merge", "features", "node_stats", "node_combine",
+        "sens_pixels", "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other"};
+    return (k >= 0 && k < RPD_KERNEL_COUNT_) ? names[k] : "unknown";
 }
 
 int rpd_device_alloc(rpd_ctx* ctx, uint64_t bytes, void** out) {

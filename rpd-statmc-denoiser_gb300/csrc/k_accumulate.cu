@@ -350,12 +350,14 @@ __global__ void k_finalize(PixelPlanes p, int64_t np) {
 }  // namespace
 
 cudaError_t launch_offsets_uniform(Job& j, int64_t count, int32_t spp) {
+    KernelScope ks(j, RPD_KERNEL_OFFSETS);
     k_offsets_uniform<<<grid_for(count + 1, 256), 256, 0, j.stream>>>(j.offsets, count, spp);
     j.launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count) {
+    KernelScope ks(j, RPD_KERNEL_OFFSETS);
     const int64_t nblocks = (count + kScanBlock - 1) / kScanBlock;
     int64_t* block_sums = j.offsets + (count + 1);  // the offsets buffer reserves room for these
     k_scan_block_sums<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums);
@@ -366,12 +368,14 @@ cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count) 
 }
 
 cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count) {
+    KernelScope ks(j, RPD_KERNEL_ACCUMULATE_PIXELS);
     k_accumulate_pixels<<<grid_for(count, 128), 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count);
     j.launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first, int64_t count) {
+    KernelScope ks(j, RPD_KERNEL_GRID);
     const int64_t threads = j.g.nn * kDeps;
     k_grid_ordered<<<grid_for(threads, 128), 128, 0, j.stream>>>(j.g, j.n.pass_grid, s, j.offsets, 0, first, count);
     j.launches += 1;
@@ -379,6 +383,7 @@ cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first
 }
 
 cudaError_t launch_merge_grid(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_MERGE);
     const int64_t n = j.g.nn * kDeps * kDepStride;
     k_merge_grid<<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
     j.launches += 1;
@@ -386,12 +391,14 @@ cudaError_t launch_merge_grid(Job& j) {
 }
 
 cudaError_t launch_feature_cache(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_FEATURES);
     k_feature_cache<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.p, j.g.np);
     j.launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_finalize(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_OTHER);
     k_finalize<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.p, j.g.np);
     j.launches += 1;
     return cudaGetLastError();

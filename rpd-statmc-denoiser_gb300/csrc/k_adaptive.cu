@@ -161,6 +161,7 @@ __global__ void k_copy(const float* src, float* dst, int64_t n) {
 }  // namespace
 
 cudaError_t launch_adaptive(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_ADAPTIVE);
     const int64_t np = j.g.np;
     const int w = j.g.w, h = j.g.h;
     const int extra_sample_total = j.cfg.adaptive_spp * w * h;

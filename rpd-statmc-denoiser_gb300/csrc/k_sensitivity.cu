@@ -256,26 +256,38 @@ __global__ void k_expand(Geometry g, const float* tiles, float* out) {
 }  // namespace
 
 cudaError_t launch_sensitivity(Job& j) {
-    k_node_stats<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n, j.p, j.cfg.rpf_confidence_samples);
-    k_node_combine<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n);
-    k_sens_pixels<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.g, j.n, j.p);
+    {
+        KernelScope ks(j, RPD_KERNEL_NODE_STATS);
+        k_node_stats<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n, j.p, j.cfg.rpf_confidence_samples);
+    }
+    {
+        KernelScope ks(j, RPD_KERNEL_NODE_COMBINE);
+        k_node_combine<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n);
+    }
+    {
+        KernelScope ks(j, RPD_KERNEL_SENS_PIXELS);
+        k_sens_pixels<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.g, j.n, j.p);
+    }
     j.launches += 3;
     return cudaGetLastError();
 }
 
 cudaError_t launch_sensitivity_zero(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_SENS_PIXELS);
     k_sens_zero<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.p, j.g.np);
     j.launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_rpd_cache(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_RPD_CACHE);
     k_rpd_cache<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.g, j.n, j.p);
     j.launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_expand(Job& j, const float* node_field, float* out) {
+    KernelScope ks(j, RPD_KERNEL_OTHER);
     k_expand<<<grid_for(j.g.np, 256), 256, 0, j.stream>>>(j.g, node_field, out);
     j.launches += 1;
     return cudaGetLastError();

@@ -200,8 +200,12 @@ __global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcPara
 
 cudaError_t launch_statmc(Job& j) {
     const int64_t np = j.g.np;
-    k_sqrt_var_mean<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np);
-    k_sqrt_var_stable<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, j.g.w, j.g.h);
+    {
+        KernelScope ks(j, RPD_KERNEL_SQRT_VARIANCE);
+        k_sqrt_var_mean<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np);
+        k_sqrt_var_stable<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, j.g.w, j.g.h);
+    }
+    KernelScope ks(j, RPD_KERNEL_STATMC_WINDOW);
     StatmcParams prm{j.g.w, j.g.h, j.cfg.color_window_radius, j.cfg.color_normal_threshold,
                      j.cfg.color_depth_threshold, j.cfg.rpf_shrinkage_scale, j.cfg.color_compat_alpha,
                      j.cfg.color_sigma_max * j.cfg.color_sigma_max};

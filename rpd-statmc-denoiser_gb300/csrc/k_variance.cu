@@ -78,6 +78,7 @@ __global__ void k_var_final(PixelPlanes p, int64_t np, float max_variance, const
 }  // namespace
 
 cudaError_t launch_variance(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_VARIANCE);
     const int64_t np = j.g.np;
     const float max_variance = j.cfg.adaptive_sigma_max * j.cfg.adaptive_sigma_max;
     float* curr = j.p.var_ping;

@@ -139,6 +139,38 @@ struct Job {
     cudaEvent_t ev_stop[RPD_STAGE_COUNT_]{};
     bool ev_used[RPD_STAGE_COUNT_]{};
     std::atomic<uint64_t> launches{0};
+    // per-kernel event timing (rpd_job_set_profiling)
+    bool profile = false;
+    struct KTiming { int kernel; cudaEvent_t a, b; };
+    std::vector<KTiming> ktimes;
+    std::vector<cudaEvent_t> event_pool;
+    double ktotal[RPD_KERNEL_COUNT_]{};
+    uint64_t kcount[RPD_KERNEL_COUNT_]{};
+    cudaEvent_t marks[8]{};      // rpd_job_mark slots
+};
+
+// Brackets the launches of one kernel family with CUDA events when profiling is on.
+struct KernelScope {
+    Job& j;
+    int kernel;
+    cudaEvent_t a = nullptr, b = nullptr;
+    KernelScope(Job& job, int k) : j(job), kernel(k) {
+        if (!j.profile) return;
+        for (cudaEvent_t* e : {&a, &b}) {
+            if (!j.event_pool.empty()) {
+                *e = j.event_pool.back();
+                j.event_pool.pop_back();
+            } else if (cudaEventCreate(e) != cudaSuccess) {
+                *e = nullptr;
+            }
+        }
+        if (a) cudaEventRecord(a, j.stream);
+    }
+    ~KernelScope() {
+        if (!j.profile || !a || !b) return;
+        cudaEventRecord(b, j.stream);
+        j.ktimes.push_back({kernel, a, b});
+    }
 };
 
 // ---- error plumbing -------------------------------------------------------------------

@@ -41,6 +41,8 @@ RGB_FIELDS = {"DENOISED", "RADIANCE_SUM", "NORMAL_SUM", "ALBEDO_SUM", "STATS_COL
               "STATS_SQRT_SQUARE_DIFF"}
 INT_FIELDS = {"HIT_COUNT", "SAMPLE_COUNT", "STATS_N", "ADAPTIVE_COUNTS"}
 STAGES = ["ACCUMULATE", "SENSITIVITY", "STATMC", "VARIANCE", "ADAPTIVE"]
+KERNELS = ["offsets", "accumulate_pixels", "grid", "merge", "features", "node_stats", "node_combine", "sens_pixels",
+           "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other"]
 STAGE = {name: i for i, name in enumerate(STAGES)}
 
 HIT, PIXEL_VALID, LENS_VALID, BRDF_VALID, LIGHT_VALID, LIGHT_SELECT_VALID, ENV_VALID, RR_VALID = (
@@ -236,6 +238,12 @@ def lib() -> C.CDLL:
         "rpd_job_sync": (C.c_int, [vp]),
         "rpd_job_stage_ms": (f32, [vp, C.c_int]),
         "rpd_job_launch_count": (u64, [vp]),
+        "rpd_job_set_profiling": (C.c_int, [vp, C.c_int]),
+        "rpd_job_kernel_time": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
+        "rpd_job_reset_kernel_times": (C.c_int, [vp]),
+        "rpd_kernel_name": (C.c_char_p, [C.c_int]),
+        "rpd_job_mark": (C.c_int, [vp, C.c_int]),
+        "rpd_job_mark_elapsed": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]),
         "rpd_atrous_wavelet": (C.c_int, [vp, vp, vp, vp, i32, i32, f32, f32, f32, i32, vp, C.c_int]),
         "rpd_joint_bilateral": (C.c_int, [vp, vp, vp, vp, i32, i32, f32, f32, f32, f32, vp, vp, vp, C.c_int]),
         "rpd_device_alloc": (C.c_int, [vp, u64, C.POINTER(vp)]),
@@ -263,6 +271,8 @@ def exported_symbols() -> list[str]:
             "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_end_pass", "rpd_recompute_sensitivity",
             "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
             "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
+            "rpd_job_set_profiling", "rpd_job_kernel_time", "rpd_job_reset_kernel_times", "rpd_kernel_name",
+            "rpd_job_mark", "rpd_job_mark_elapsed",
             "rpd_atrous_wavelet", "rpd_joint_bilateral", "rpd_device_alloc", "rpd_device_free", "rpd_host_alloc",
             "rpd_host_free", "rpd_memcpy", "rpd_synth_fill", "rpd_last_error", "rpd_status_string"]
 
@@ -482,3 +492,26 @@ class Job:
 
     def launches(self) -> int:
         return int(lib().rpd_job_launch_count(self.handle))
+
+    def mark(self, slot: int) -> None:
+        check(lib().rpd_job_mark(self.handle, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        check(lib().rpd_job_mark_elapsed(self.handle, a, b, C.byref(ms)))
+        return float(ms.value)
+
+    def set_profiling(self, on: bool) -> None:
+        check(lib().rpd_job_set_profiling(self.handle, 1 if on else 0))
+
+    def reset_kernel_times(self) -> None:
+        check(lib().rpd_job_reset_kernel_times(self.handle))
+
+    def kernel_times(self) -> dict[str, tuple[float, int]]:
+        """{kernel family: (total ms, launches)} since the last reset."""
+        out = {}
+        for i, name in enumerate(KERNELS):
+            ms, n = C.c_double(), C.c_uint64()
+            check(lib().rpd_job_kernel_time(self.handle, i, C.byref(ms), C.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
