@@ -247,6 +247,18 @@ void rpd_job_destroy(rpd_job* job);
 /* Replace the knobs of later calls (the reference passes RenderConfig to every stage).
  * Image size and rpf_tile_size are fixed at job creation. */
 int rpd_job_set_config(rpd_job* job, const rpd_config* cfg);
+
+/* Exact modes. By default the RPD grid is accumulated in double-float (pairs of floats,
+ * ~2^-44 relative) and the StatMC window is evaluated in single precision with every
+ * threshold decision (q > 25, the accepted-neighbour test, the t-table branch, the
+ * weight-sum test) confirmed in double near its threshold. The exact modes instead run
+ * the reference's double-precision operations in its order: RPD_EXACT_GRID makes the grid
+ * bit-identical to the reference's single-thread run; RPD_EXACT_WINDOW evaluates every
+ * neighbour in double. Both are slower on GB300, whose double-precision rate is 1/55 of
+ * its single-precision rate. */
+#define RPD_EXACT_GRID   0x1
+#define RPD_EXACT_WINDOW 0x2
+int rpd_job_set_exact(rpd_job* job, int flags);
 /* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */
 int rpd_job_begin_frame(rpd_job* job);
 

@@ -1,6 +1,7 @@
 // C ABI of the GB300 denoise stage (include/rpd_gb300.h): contexts, jobs, HBM layout,
 // admission against the HBM budget, the stage entry points and field reads.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -49,7 +50,8 @@ Geometry make_geometry(const rpd_config& c) {
 }
 
 // Assigns (offset-encoded) plane pointers; returns the arena size.
-uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n) {
+uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5] = nullptr,
+              uint8_t** pflags = nullptr) {
     Layout L;
     const int64_t np = g.np, nn = g.nn;
     L.add(p.mean, np);
@@ -97,6 +99,12 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n) {
     for (int c = 0; c < 3; ++c) L.add(n.n_normal[c], nn);
     L.add(n.n_depth, nn);
     for (int c = 0; c < 3; ++c) L.add(n.n_albedo[c], nn);
+    float* cls_tmp[kClasses][5];
+    uint8_t* pflags_tmp = nullptr;
+    float* (*C)[5] = cls ? cls : cls_tmp;
+    for (int c = 0; c < kClasses; ++c)
+        for (int f = 0; f < 5; ++f) L.add(C[c][f], np);
+    L.add(pflags ? *pflags : pflags_tmp, np);
     return (L.bytes + 255) & ~uint64_t(255);
 }
 
@@ -416,7 +424,7 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
     j->ctx = c;
     j->cfg = *cfg;
     j->g = make_geometry(*cfg);
-    j->arena_bytes = plan(j->g, j->p, j->n);
+    j->arena_bytes = plan(j->g, j->p, j->n, j->cls, &j->pflags);
     {
         std::lock_guard<std::mutex> lock(c->mu);
         if (c->in_use.load() + j->arena_bytes > c->budget) {
@@ -435,6 +443,9 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
         c->in_use += j->arena_bytes;
     }
     rebase_all(j->p, j->n, static_cast<char*>(j->arena));
+    for (int c = 0; c < kClasses; ++c)
+        for (int f = 0; f < 5; ++f) rebase(j->cls[c][f], static_cast<char*>(j->arena));
+    rebase(j->pflags, static_cast<char*>(j->arena));
     cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
     for (int s = 0; s < RPD_STAGE_COUNT_ && e == cudaSuccess; ++s) {
         e = cudaEventCreate(&j->ev_start[s]);
@@ -467,6 +478,10 @@ void rpd_job_destroy(rpd_job* job) {
         cudaFree(j->offsets);
         j->ctx->in_use -= uint64_t(j->offsets_cap) * 8;
     }
+    if (j->lum) {
+        cudaFree(j->lum);
+        j->ctx->in_use -= j->lum_cap;
+    }
     if (j->scalars) cudaFreeHost(j->scalars);
     for (int s = 0; s < RPD_STAGE_COUNT_; ++s) {
         if (j->ev_start[s]) cudaEventDestroy(j->ev_start[s]);
@@ -494,6 +509,17 @@ int rpd_job_set_config(rpd_job* job, const rpd_config* cfg) {
     char msg[256];
     if (rpd_config_validate(&c, msg, sizeof(msg)) != RPD_OK) return fail(RPD_ERR_INVALID_CONFIG, msg);
     j->cfg = c;
+    return RPD_OK;
+}
+
+int rpd_job_set_exact(rpd_job* job, int flags) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (flags & ~(RPD_EXACT_GRID | RPD_EXACT_WINDOW)) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown exact-mode flag");
+    if (j->pass_open && bool(flags & RPD_EXACT_GRID) != j->exact_grid)
+        return fail(RPD_ERR_STATE, "the grid mode cannot change while a pass is open");
+    j->exact_grid = (flags & RPD_EXACT_GRID) != 0;
+    j->exact_window = (flags & RPD_EXACT_WINDOW) != 0;
     return RPD_OK;
 }
 
@@ -614,11 +640,42 @@ int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first, i
     if (!d.normal[0] || !d.normal[1] || !d.normal[2] || !d.depth ||
         (!d.albedo[0] && !d.pixel_albedo[0]))
         return fail(RPD_ERR_INVALID_ARGUMENT, "normal, depth and albedo (per sample or per pixel) are required");
-    RPD_CUDA(launch_accumulate_pixels(*j, d, first, count));
-    if (j->cfg.rpf_shrinkage_scale > 0.0f) {
-        if (!d.category) return fail(RPD_ERR_INVALID_ARGUMENT, "category plane is required when RPD is enabled");
-        RPD_CUDA(launch_accumulate_grid(*j, d, first, count));
+    const bool rpd = j->cfg.rpf_shrinkage_scale > 0.0f;
+    if (rpd && !d.category) return fail(RPD_ERR_INVALID_ARGUMENT, "category plane is required when RPD is enabled");
+    GridPrep gp{};
+    gp.width = j->g.w;
+    const bool fast_grid = rpd && !j->exact_grid;
+    if (fast_grid) {
+        // the per-sample total is needed on the host to size the luminance plane
+        int64_t nsamp = total;
+        if (counts && where != RPD_MEM_HOST) {
+            RPD_CUDA(cudaMemcpyAsync(&nsamp, j->offsets + count, 8, cudaMemcpyDeviceToHost, j->stream));
+            RPD_CUDA(cudaStreamSynchronize(j->stream));
+        }
+        // luminance and key planes of the push, one allocation
+        void* lum = j->lum;
+        st = grow_device(*j, &lum, &j->lum_cap, uint64_t(std::max<int64_t>(nsamp, 1)) * 8 + 256);
+        if (st != RPD_OK) return st;
+        j->lum = static_cast<float*>(lum);
+        gp.key = reinterpret_cast<uint32_t*>(j->lum + ((std::max<int64_t>(nsamp, 1) + 63) / 64) * 64);
+        for (int c = 0; c < kClasses; ++c)
+            for (int f = 0; f < 5; ++f) gp.cls[c][f] = j->cls[c][f];
+        gp.pflags = j->pflags;
+        gp.lum = j->lum;
     }
+    RPD_CUDA(launch_accumulate_pixels(*j, d, first, count, gp, counts ? 0 : spp));
+    if (fast_grid) {
+        int32_t max_count = spp;
+        if (counts) {
+            max_count = 0;
+            if (where == RPD_MEM_HOST)
+                for (int64_t i = 0; i < count; ++i) max_count = std::max(max_count, counts[i]);
+            else
+                max_count = INT32_MAX;  // unknown on the host: keep the double-float weights
+        }
+        RPD_CUDA(launch_grid_fast(*j, d, first, count, gp, counts ? 0 : spp, max_count));
+    }
+    else if (rpd) RPD_CUDA(launch_accumulate_grid(*j, d, first, count));
     j->pass_open = true;
     j->have_samples = true;
     j->features_valid = false;

@@ -67,80 +67,283 @@ __global__ void k_scan_finish(const int32_t* counts, int64_t count, const int64_
     if (i == count - 1) offsets[count] = block_sums[blockIdx.x] + s[threadIdx.x];
 }
 
-__global__ void k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets, int32_t spp,
-                                    int64_t first, int64_t count) {
+// Dependency2D::add bin (core/stats.h:166-168)
+__device__ __forceinline__ int bin2d_k(float u, float v) {
+    const int x = iclamps(int(u * 4.0f), 0, 3);
+    const int z = iclamps(int(v * 4.0f), 0, 3);
+    return z * 4 + x;
+}
+
+// TwoSum of x into the double-float (hi, lo).
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bb = s - hi;
+    lo += (hi - (s - bb)) + (x - bb);
+    hi = s;
+}
+
+// One traced sample as the statistics pass sees it.
+struct SampleIn {
+    float L[3], n[3], d, alb[3], pu[2], lu[2], bu[2], liu[2], eu[2];
+    uint8_t f, cat;
+};
+
+// Per-pixel running state of the statistics pass.
+struct PixelAcc {
+    float mean, m2;
+    int n;
+    float cm[3], sm[3], sq[3], rad[3], nor[3], alb[3], dep;
+    int hits, nsamples;
+    // validity-class sums for the grid pass: samples whose class bits equal the pixel's
+    // first pattern share one set of sums; others go to per-class sums
+    uint8_t pat;
+    bool have_pat;
+    float pc, p1h, p1l, p2h, p2l;
+    float cc[kClasses], s1h[kClasses], s1l[kClasses], s2h[kClasses], s2l[kClasses];
+    uint8_t pflags;
+};
+
+__device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, bool per_sample_albedo,
+                                               const float* palb, bool prep, uint8_t plane_mask, float fx,
+                                               float fy, float& lum_out, uint32_t& key_out) {
+    if (in.f & RPD_SAMPLE_HIT) {  // main.cpp:572-576
+        ++a.hits;
+        for (int c = 0; c < 3; ++c) a.nor[c] += in.n[c];
+        for (int c = 0; c < 3; ++c) a.alb[c] += per_sample_albedo ? in.alb[c] : palb[c];
+        a.dep += in.d;
+    }
+    if (!finite3(in.L[0], in.L[1], in.L[2])) {  // main.cpp:707
+        lum_out = __int_as_float(0x7fc00000);  // NaN: dropped by the grid pass
+        key_out = 0;
+        return;
+    }
+    // accumulate_sample (core/stats.h:25-41)
+    const float lum = luminance(in.L[0], in.L[1], in.L[2]);
+    const float delta = lum - a.mean;
+    ++a.n;
+    a.mean += delta / float(a.n);
+    const float delta2 = lum - a.mean;
+    a.m2 += delta * delta2;
+    for (int c = 0; c < 3; ++c) {
+        const float cd = in.L[c] - a.cm[c];
+        a.cm[c] += cd / float(a.n);
+    }
+    for (int c = 0; c < 3; ++c) {
+        const float sc = sqrtf(fmaxs(0.0f, in.L[c]));
+        const float sd = sc - a.sm[c];
+        a.sm[c] += sd / float(a.n);
+        a.sq[c] += sd * (sc - a.sm[c]);
+    }
+    for (int c = 0; c < 3; ++c) a.rad[c] += in.L[c];
+    ++a.nsamples;
+    lum_out = lum;
+    key_out = 0;
+    if (!prep) return;
+    const uint8_t fm = in.f & plane_mask;
+    // packed random-dimension bins (Dependency2D::add, core/stats.h:166-168)
+    uint32_t key = 0;
+    if (fm & RPD_SAMPLE_LENS_VALID) key |= uint32_t(bin2d_k(in.lu[0], in.lu[1]));
+    if (fm & RPD_SAMPLE_BRDF_VALID) key |= uint32_t(bin2d_k(in.bu[0], in.bu[1])) << 4;
+    if (fm & RPD_SAMPLE_LIGHT_VALID) key |= uint32_t(bin2d_k(in.liu[0], in.liu[1])) << 8;
+    if (fm & RPD_SAMPLE_ENV_VALID) key |= uint32_t(bin2d_k(in.eu[0], in.eu[1])) << 12;
+    key |= uint32_t(in.cat & RPD_CATEGORY_LIGHT_INDEX_MASK) << 16;
+    key |= (in.cat & RPD_CATEGORY_RR_SURVIVED) ? (1u << 20) : 0u;
+    key |= uint32_t(fm & 0xfe) << (kKeyValidShift - 1);
+    key_out = key;
+    const uint8_t cls_bits = fm & 0xfe;
+    const float y2 = lum * lum;
+    const float y2e = __fmaf_rn(lum, lum, -y2);
+    if (!a.have_pat) {
+        a.have_pat = true;
+        a.pat = cls_bits;
+    }
+    if (cls_bits == a.pat) {
+        a.pc += 1.0f;
+        df_add(a.p1h, a.p1l, lum);
+        df_add(a.p2h, a.p2l, y2);
+        a.p2l += y2e;
+    } else {
+        #pragma unroll
+        for (int c = 0; c < kClasses; ++c) {
+            if (!(cls_bits & class_bit(c))) continue;
+            a.cc[c] += 1.0f;
+            df_add(a.s1h[c], a.s1l[c], lum);
+            df_add(a.s2h[c], a.s2l[c], y2);
+            a.s2l[c] += y2e;
+        }
+    }
+    if (fm & RPD_SAMPLE_PIXEL_VALID) {
+        // the screen position stays inside the pixel with a margin: fl(x + u) - x in
+        // [0, 1 - 2^-10], so every node's screen coordinate rounds into the same bin
+        const float jx = (fx + in.pu[0]) - fx, jy = (fy + in.pu[1]) - fy;
+        if (!(jx >= 0.0f && jx <= kUniformMax && jy >= 0.0f && jy <= kUniformMax)) a.pflags &= uint8_t(~kPixUniform);
+    } else if (fm & (RPD_SAMPLE_LENS_VALID | RPD_SAMPLE_BRDF_VALID | RPD_SAMPLE_LIGHT_VALID | RPD_SAMPLE_ENV_VALID |
+                     RPD_SAMPLE_LIGHT_SELECT_VALID | RPD_SAMPLE_RR_VALID)) {
+        a.pflags |= kPixMixed;  // a random dimension without the screen position
+    }
+}
+
+__device__ __forceinline__ float4 ld4(const float* p, int64_t k) { return *reinterpret_cast<const float4*>(p + k); }
+__device__ __forceinline__ float lane4(const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+
+// VEC4: every present plane is 16-byte aligned at the pixel's first sample and the pixel's
+// sample count is a multiple of 4, so each plane is read four samples per load.
+template <bool VEC4>
+__global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets,
+                                                           int32_t spp, int64_t first, int64_t count, GridPrep gp) {
     const int64_t local = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (local >= count) return;
     const int64_t idx = first + local;
     const int64_t k0 = offsets ? offsets[local] : local * spp;
     const int64_t k1 = offsets ? offsets[local + 1] : (local + 1) * spp;
-    if (k0 == k1) return;
-
-    float mean = p.mean[idx], m2 = p.square_diff[idx];
-    int n = p.n[idx];
-    float cm[3], sm[3], sq[3], rad[3], nor[3], alb[3];
-    for (int c = 0; c < 3; ++c) {
-        cm[c] = p.color_mean[c][idx];
-        sm[c] = p.sqrt_mean[c][idx];
-        sq[c] = p.sqrt_sq[c][idx];
-        rad[c] = p.radiance[c][idx];
-        nor[c] = p.normal[c][idx];
-        alb[c] = p.albedo[c][idx];
+    const bool prep = gp.lum != nullptr;
+    const uint8_t plane_mask = uint8_t(0xffu & ~((s.pixel_u[0] ? 0 : RPD_SAMPLE_PIXEL_VALID) |
+                                                 (s.lens_u[0] ? 0 : RPD_SAMPLE_LENS_VALID) |
+                                                 (s.brdf_u[0] ? 0 : RPD_SAMPLE_BRDF_VALID) |
+                                                 (s.light_u[0] ? 0 : RPD_SAMPLE_LIGHT_VALID) |
+                                                 (s.env_u[0] ? 0 : RPD_SAMPLE_ENV_VALID)));
+    const float fx = float(idx % gp.width), fy = float(idx / gp.width);
+    PixelAcc a;
+    a.pflags = kPixUniform;
+    a.have_pat = false;
+    a.pat = 0;
+    a.pc = a.p1h = a.p1l = a.p2h = a.p2l = 0.0f;
+    for (int c = 0; c < kClasses; ++c) a.cc[c] = a.s1h[c] = a.s1l[c] = a.s2h[c] = a.s2l[c] = 0.0f;
+    if (k0 == k1) {
+        if (prep) {
+            for (int c = 0; c < kClasses; ++c)
+                for (int f = 0; f < 5; ++f) gp.cls[c][f][idx] = 0.0f;
+            gp.pflags[idx] = a.pflags;
+        }
+        return;
     }
-    float dep = p.depth[idx];
-    int hits = p.hit_count[idx];
-    int nsamples = p.sample_count[idx];
+    a.mean = p.mean[idx];
+    a.m2 = p.square_diff[idx];
+    a.n = p.n[idx];
+    for (int c = 0; c < 3; ++c) {
+        a.cm[c] = p.color_mean[c][idx];
+        a.sm[c] = p.sqrt_mean[c][idx];
+        a.sq[c] = p.sqrt_sq[c][idx];
+        a.rad[c] = p.radiance[c][idx];
+        a.nor[c] = p.normal[c][idx];
+        a.alb[c] = p.albedo[c][idx];
+    }
+    a.dep = p.depth[idx];
+    a.hits = p.hit_count[idx];
+    a.nsamples = p.sample_count[idx];
     const bool per_sample_albedo = s.albedo[0] != nullptr;
     float palb[3] = {0.0f, 0.0f, 0.0f};
     if (!per_sample_albedo && s.pixel_albedo[0]) {
         for (int c = 0; c < 3; ++c) palb[c] = s.pixel_albedo[c][local];
     }
+    const bool dims = prep;  // the random dimensions are only read for the grid pass
 
-    for (int64_t k = k0; k < k1; ++k) {
-        const uint8_t f = s.flags ? s.flags[k] : 0;
-        if (f & RPD_SAMPLE_HIT) {
-            ++hits;
-            for (int c = 0; c < 3; ++c) nor[c] += s.normal[c][k];
-            for (int c = 0; c < 3; ++c) alb[c] += per_sample_albedo ? s.albedo[c][k] : palb[c];
-            dep += s.depth[k];
+    if (VEC4) {
+        for (int64_t k = k0; k < k1; k += 4) {
+            float4 L[3], N[3], A[3], D, PU[2], LU[2], BU[2], LI[2], EU[2];
+            for (int c = 0; c < 3; ++c) {
+                L[c] = ld4(s.radiance[c], k);
+                N[c] = ld4(s.normal[c], k);
+                A[c] = per_sample_albedo ? ld4(s.albedo[c], k) : make_float4(0, 0, 0, 0);
+            }
+            D = ld4(s.depth, k);
+            const float4 z4 = make_float4(0, 0, 0, 0);
+            for (int c = 0; c < 2; ++c) {
+                PU[c] = (dims && s.pixel_u[0]) ? ld4(s.pixel_u[c], k) : z4;
+                LU[c] = (dims && s.lens_u[0]) ? ld4(s.lens_u[c], k) : z4;
+                BU[c] = (dims && s.brdf_u[0]) ? ld4(s.brdf_u[c], k) : z4;
+                LI[c] = (dims && s.light_u[0]) ? ld4(s.light_u[c], k) : z4;
+                EU[c] = (dims && s.env_u[0]) ? ld4(s.env_u[c], k) : z4;
+            }
+            const uint32_t F4 = *reinterpret_cast<const uint32_t*>(s.flags + k);
+            const uint32_t C4 = (dims && s.category) ? *reinterpret_cast<const uint32_t*>(s.category + k) : 0u;
+            float lum4[4];
+            uint32_t key4[4];
+            #pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                SampleIn in;
+                for (int c = 0; c < 3; ++c) {
+                    in.L[c] = lane4(L[c], i);
+                    in.n[c] = lane4(N[c], i);
+                    in.alb[c] = lane4(A[c], i);
+                }
+                in.d = lane4(D, i);
+                for (int c = 0; c < 2; ++c) {
+                    in.pu[c] = lane4(PU[c], i);
+                    in.lu[c] = lane4(LU[c], i);
+                    in.bu[c] = lane4(BU[c], i);
+                    in.liu[c] = lane4(LI[c], i);
+                    in.eu[c] = lane4(EU[c], i);
+                }
+                in.f = uint8_t(F4 >> (8 * i));
+                in.cat = uint8_t(C4 >> (8 * i));
+                process_sample(a, in, per_sample_albedo, palb, prep, plane_mask, fx, fy, lum4[i], key4[i]);
+            }
+            if (prep) {
+                *reinterpret_cast<float4*>(gp.lum + k) = make_float4(lum4[0], lum4[1], lum4[2], lum4[3]);
+                *reinterpret_cast<uint4*>(gp.key + k) = make_uint4(key4[0], key4[1], key4[2], key4[3]);
+            }
         }
-        const float L[3] = {s.radiance[0][k], s.radiance[1][k], s.radiance[2][k]};
-        if (!finite3(L[0], L[1], L[2])) continue;
-        // accumulate_sample (core/stats.h:25-41)
-        const float lum = luminance(L[0], L[1], L[2]);
-        const float delta = lum - mean;
-        ++n;
-        mean += delta / float(n);
-        const float delta2 = lum - mean;
-        m2 += delta * delta2;
-        for (int c = 0; c < 3; ++c) {
-            const float cd = L[c] - cm[c];
-            cm[c] += cd / float(n);
+    } else {
+        for (int64_t k = k0; k < k1; ++k) {
+            SampleIn in;
+            for (int c = 0; c < 3; ++c) {
+                in.L[c] = s.radiance[c][k];
+                in.n[c] = s.normal[c][k];
+                in.alb[c] = per_sample_albedo ? s.albedo[c][k] : 0.0f;
+            }
+            in.d = s.depth[k];
+            for (int c = 0; c < 2; ++c) {
+                in.pu[c] = (dims && s.pixel_u[0]) ? s.pixel_u[c][k] : 0.0f;
+                in.lu[c] = (dims && s.lens_u[0]) ? s.lens_u[c][k] : 0.0f;
+                in.bu[c] = (dims && s.brdf_u[0]) ? s.brdf_u[c][k] : 0.0f;
+                in.liu[c] = (dims && s.light_u[0]) ? s.light_u[c][k] : 0.0f;
+                in.eu[c] = (dims && s.env_u[0]) ? s.env_u[c][k] : 0.0f;
+            }
+            in.f = s.flags[k];
+            in.cat = (dims && s.category) ? s.category[k] : 0;
+            float lum;
+            uint32_t key;
+            process_sample(a, in, per_sample_albedo, palb, prep, plane_mask, fx, fy, lum, key);
+            if (prep) {
+                gp.lum[k] = lum;
+                gp.key[k] = key;
+            }
         }
-        for (int c = 0; c < 3; ++c) {
-            const float sc = sqrtf(fmaxs(0.0f, L[c]));
-            const float sd = sc - sm[c];
-            sm[c] += sd / float(n);
-            sq[c] += sd * (sc - sm[c]);
-        }
-        for (int c = 0; c < 3; ++c) rad[c] += L[c];
-        ++nsamples;
     }
 
-    p.mean[idx] = mean;
-    p.square_diff[idx] = m2;
-    p.n[idx] = n;
+    p.mean[idx] = a.mean;
+    p.square_diff[idx] = a.m2;
+    p.n[idx] = a.n;
     for (int c = 0; c < 3; ++c) {
-        p.color_mean[c][idx] = cm[c];
-        p.sqrt_mean[c][idx] = sm[c];
-        p.sqrt_sq[c][idx] = sq[c];
-        p.radiance[c][idx] = rad[c];
-        p.normal[c][idx] = nor[c];
-        p.albedo[c][idx] = alb[c];
+        p.color_mean[c][idx] = a.cm[c];
+        p.sqrt_mean[c][idx] = a.sm[c];
+        p.sqrt_sq[c][idx] = a.sq[c];
+        p.radiance[c][idx] = a.rad[c];
+        p.normal[c][idx] = a.nor[c];
+        p.albedo[c][idx] = a.alb[c];
     }
-    p.depth[idx] = dep;
-    p.hit_count[idx] = hits;
-    p.sample_count[idx] = nsamples;
+    p.depth[idx] = a.dep;
+    p.hit_count[idx] = a.hits;
+    p.sample_count[idx] = a.nsamples;
+    if (prep) {
+        for (int c = 0; c < kClasses; ++c) {
+            float h1 = a.s1h[c], l1 = a.s1l[c], h2 = a.s2h[c], l2 = a.s2l[c], cnt = a.cc[c];
+            if (a.have_pat && (a.pat & class_bit(c))) {
+                cnt += a.pc;
+                df_add(h1, l1, a.p1h);
+                l1 += a.p1l;
+                df_add(h2, l2, a.p2h);
+                l2 += a.p2l;
+            }
+            gp.cls[c][0][idx] = cnt;
+            gp.cls[c][1][idx] = h1;
+            gp.cls[c][2][idx] = l1;
+            gp.cls[c][3][idx] = h2;
+            gp.cls[c][4][idx] = l2;
+        }
+        gp.pflags[idx] = a.pflags;
+    }
 }
 
 // Valid-flag bit each dependency needs, and whether it bins the screen position.
@@ -367,9 +570,23 @@ cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count) 
     return cudaGetLastError();
 }
 
-cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count) {
+cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,
+                                     const GridPrep& gp, int32_t spp) {
     KernelScope ks(j, RPD_KERNEL_ACCUMULATE_PIXELS);
-    k_accumulate_pixels<<<grid_for(count, 128), 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count);
+    auto aligned = [](const void* ptr) { return (reinterpret_cast<uintptr_t>(ptr) & 15u) == 0; };
+    bool vec4 = spp > 0 && spp % 4 == 0 && aligned(s.depth) && aligned(s.flags) &&
+                (!s.category || aligned(s.category));
+    for (int c = 0; c < 3; ++c)
+        vec4 = vec4 && aligned(s.radiance[c]) && aligned(s.normal[c]) && (!s.albedo[0] || aligned(s.albedo[c]));
+    for (int c = 0; c < 2; ++c)
+        vec4 = vec4 && (!s.pixel_u[0] || aligned(s.pixel_u[c])) && (!s.lens_u[0] || aligned(s.lens_u[c])) &&
+               (!s.brdf_u[0] || aligned(s.brdf_u[c])) && (!s.light_u[0] || aligned(s.light_u[c])) &&
+               (!s.env_u[0] || aligned(s.env_u[c]));
+    vec4 = vec4 && (!gp.lum || (aligned(gp.lum) && aligned(gp.key)));
+    if (vec4)
+        k_accumulate_pixels<true><<<grid_for(count, 128), 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+    else
+        k_accumulate_pixels<false><<<grid_for(count, 128), 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     j.launches += 1;
     return cudaGetLastError();
 }

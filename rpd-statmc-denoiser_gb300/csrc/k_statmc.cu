@@ -3,9 +3,31 @@
 //
 //   k_sqrt_var_mean    sqrt-domain variance of the mean, floored at EPS_SMALL (972-980)
 //   k_sqrt_var_stable  max with its 3x3 inverse-distance average (981-990)
-//   k_statmc_window    the (2r+1)^2 window (998-1127) — one thread per pixel, the
-//                      reference's operations in its order (double where it uses double),
-//                      so every gate and the q > 25 test decide exactly as the reference.
+//   k_statmc_tile      the (2r+1)^2 window (998-1127), fast path. A 32 x BY block stages
+//                      its (32+2r) x (BY+2r) halo tile of per-pixel records in shared memory
+//                      (structure of arrays, so a warp reading 32 neighbours at one offset is
+//                      bank-conflict free) and evaluates every neighbour in single precision:
+//                        * the normal / depth / albedo gates are decided exactly as the
+//                          reference decides them (identical float operations; the depth
+//                          quotient is only rounded exactly when it lies within 2^-20 of the
+//                          threshold; the albedo norm is compared through the exact squared
+//                          threshold of the correctly rounded sqrt);
+//                        * the Welch t^2, Welch-Satterthwaite df, t-table lookup and RPD
+//                          relaxation run in float with approximate division. Their relative
+//                          error is below 3e-6, so whenever q lies within 2^-15 (relative)
+//                          of a decision point — q = 25 (reject), q = 2 ln 20 (the accepted-
+//                          neighbour count), df = 30.5 / 30 (t-table branch) or the 1e-8
+//                          df-denominator test — that neighbour's q is recomputed in double
+//                          exactly as the reference computes it, and the decisions use it.
+//                      Weights are accumulated in float per window row and in double-float
+//                      across rows. The blend's weight_sum >= 1.1 test has its own guard
+//                      band; a pixel inside it is recomputed wholly in double.
+//   k_statmc_window    the whole window in double, the reference's operations in its order
+//                      (the exact mode, the fallback of the fast path, and the path for
+//                      radii whose halo tile would not fit in shared memory).
+#include <algorithm>
+#include <cmath>
+
 #include "rpd_internal.h"
 #include "device_math.cuh"
 
@@ -88,11 +110,35 @@ __global__ void k_sqrt_var_stable(PixelPlanes p, int w, int h) {
 struct StatmcParams {
     int w, h, r;
     float normal_threshold, depth_threshold, rpd_scale, alpha, var2_max;
+    float albedo_sq_threshold;  // smallest float s with fl(sqrt(s)) > 0.12f
+    int table;                  // 0: alpha 0.05 table, 1: alpha 0.01 table, 2: normal quantile
+    float z;                    // normal quantile of the alpha (table == 2)
+    float df_break;             // 30.5 with a table, 30 with the quantile
+    int by;                     // block height of the tiled kernel
 };
 
-__global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcParams prm) {
-    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= int64_t(prm.w) * prm.h) return;
+// The Welch compatibility q of one (i, j) pair in double, the reference's operations in
+// its order (main.cpp:1063-1082).
+__device__ double exact_q(const float* svi, const float* smi, int n_i, const float* svj, const float* smj, int n_j,
+                          float alpha, float adjustment) {
+    double max_t2 = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        const double v_i = double(svi[c]);
+        const double v_j = double(svj[c]);
+        const double variance_sum = v_i + v_j;
+        const double mean_diff = double(smi[c] - smj[c]);
+        const double t2 = mean_diff * mean_diff / dmaxs(double(1e-8f), variance_sum);
+        const double denom_df = (v_i * v_i) / dmaxs(double(n_i - 1), 1.0) + (v_j * v_j) / dmaxs(double(n_j - 1), 1.0);
+        const double df = (denom_df > double(1e-8f)) ? (variance_sum * variance_sum) / denom_df
+                                                     : double(n_i + n_j - 2);
+        const double t_crit = double(lookup_t_critical(float(df), alpha));
+        max_t2 = dmaxs(max_t2, t2 / (t_crit * t_crit));
+    }
+    return max_t2 / (1.0 + double(adjustment));
+}
+
+// One pixel of statmc_denoise entirely in double (main.cpp:999-1127).
+__device__ void exact_pixel(const PixelPlanes& p, const StatmcParams& prm, int64_t idx) {
     const int y = int(idx / prm.w), x = int(idx % prm.w);
     const int n_raw = p.n[idx];
     const float m2_i = p.square_diff[idx];
@@ -140,26 +186,14 @@ __global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcPara
             var_j = fclamps(var_j, 1e-8f, prm.var2_max);
             const int n_j = imaxs(1, n_rawj);
             const float var_mean_j = fmaxs(1e-8f, var_j / float(n_j));
-            double max_t2 = 0.0;
-            for (int c = 0; c < 3; ++c) {
-                const double v_i = double(svi[c]);
-                const double v_j = double(p.sqrt_var_stable[c][jn]);
-                const double variance_sum = v_i + v_j;
-                const double mean_diff = double(smi[c] - p.sqrt_mean[c][jn]);
-                const double t2 = mean_diff * mean_diff / dmaxs(double(1e-8f), variance_sum);
-                const double denom_df = (v_i * v_i) / dmaxs(double(n_i - 1), 1.0) +
-                                        (v_j * v_j) / dmaxs(double(n_j - 1), 1.0);
-                const double df = (denom_df > double(1e-8f)) ? (variance_sum * variance_sum) / denom_df
-                                                             : double(n_i + n_j - 2);
-                const double t_crit = double(lookup_t_critical(float(df), prm.alpha));
-                max_t2 = dmaxs(max_t2, t2 / (t_crit * t_crit));
-            }
+            const float smj[3] = {p.sqrt_mean[0][jn], p.sqrt_mean[1][jn], p.sqrt_mean[2][jn]};
+            const float svj[3] = {p.sqrt_var_stable[0][jn], p.sqrt_var_stable[1][jn], p.sqrt_var_stable[2][jn]};
             // rpf::shared_reliability + relax_compatibility (core/stats.h:56-78)
             float shared = 0.0f;
             for (int c = 0; c < 6; ++c) shared = fmaxs(shared, fmins(rpd_i[c], p.rpd[c][jn]));
             shared = fclamps(shared, 0.0f, 1.0f);
             const float adjustment = fclamps(prm.rpd_scale * shared, 0.0f, 1.0f);
-            const double q = max_t2 / (1.0 + double(adjustment));
+            const double q = exact_q(svi, smi, n_i, svj, smj, n_j, prm.alpha, adjustment);
             if (q > 25.0) continue;
             const double dist2 = double(dx * dx + dy * dy);
             const double spatial_w = 1.0 / (1.0 + dist2);
@@ -188,12 +222,260 @@ __global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcPara
     const float alpha = float(1.0 - blend);
     const float fb = float(blend);
     for (int c = 0; c < 3; ++c) p.denoised[c][idx] = lerpf(cmi[c], mean_nb[c], fb);
-    const float uncertainty = float(double(alpha) * double(alpha) * double(var_mean_i) +
-                                    blend * blend * var_neighbors +
+    const float uncertainty = float(double(alpha) * double(alpha) * double(var_mean_i) + blend * blend * var_neighbors +
                                     2.0 * double(alpha) * blend * (center_weight / dmaxs(weight_sum, double(1e-8f))) *
                                         double(var_mean_i));
     p.alpha[idx] = alpha;
     p.uncertainty[idx] = uncertainty;
+}
+
+__global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcParams prm) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= int64_t(prm.w) * prm.h) return;
+    exact_pixel(p, prm, idx);
+}
+
+// ---- fast tiled path ----------------------------------------------------------------------
+
+enum TileField {
+    F_NX = 0, F_NY, F_NZ, F_D, F_AX, F_AY, F_AZ, F_SM0, F_SM1, F_SM2, F_SV0, F_SV1, F_SV2,
+    F_A0, F_A1, F_A2, F_N, F_CM0, F_CM1, F_CM2, F_VM, F_R0, F_R1, F_R2, F_R3, F_R4, F_R5, F_COUNT
+};
+
+constexpr int kTileX = 32;
+constexpr float kBand = 1.0f / 32768.0f;          // 2^-15 relative guard band
+constexpr float kQAccept = 5.991464547107979f;     // 2 ln 20: exp(-q/2) > 0.05
+constexpr double kWsBand = 1.0 / 65536.0;          // guard band of weight_sum >= 1.1
+
+__device__ __forceinline__ float tile_t_lookup(const float* table, float df, const StatmcParams& prm) {
+    df = fmaxf(df, 1.0f);
+    if (prm.table < 2 && df < 30.5f) {
+        const float lo_f = floorf(df);
+        const int lo = iclamps(int(lo_f), 1, 30);
+        const int hi = iclamps(int(ceilf(df)), 1, 30);
+        const float a = table[lo - 1];
+        if (lo == hi) return a;
+        return __fmaf_rn(table[hi - 1] - a, df - float(lo), a);
+    }
+    float z = prm.z;
+    if (df < 30.0f) z = z * sqrtf(__fdividef(df, fmaxf(1.0f, df - 1.0f)));
+    return z;
+}
+
+__global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcParams prm) {
+    extern __shared__ float smem[];
+    const int r = prm.r;
+    const int tw = kTileX + 2 * r, th = prm.by + 2 * r;
+    const int tn = tw * th;
+    float* T = smem;                       // F_COUNT planes of tn floats
+    float* table = smem + F_COUNT * tn;    // 32 floats of the active t table
+    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * prm.by;
+    const int tid = threadIdx.y * kTileX + threadIdx.x;
+    const int nthreads = kTileX * prm.by;
+
+    if (tid < 32) table[tid] = tid < 30 ? (prm.table == 0 ? c_t05[tid] : c_t01[tid]) : 0.0f;
+    for (int e = tid; e < tn; e += nthreads) {
+        const int gx = x0 - r + e % tw, gy = y0 - r + e / tw;
+        bool inside = gx >= 0 && gx < prm.w && gy >= 0 && gy < prm.h;
+        const int64_t q = inside ? int64_t(gy) * prm.w + gx : 0;
+        const bool hit = inside && p.hit_count[q] > 0;
+        // a neighbour outside the image or without a primary hit fails the normal gate
+        T[F_NX * tn + e] = hit ? p.f_normal[0][q] : 0.0f;
+        T[F_NY * tn + e] = hit ? p.f_normal[1][q] : 0.0f;
+        T[F_NZ * tn + e] = hit ? p.f_normal[2][q] : 0.0f;
+        if (!inside) continue;
+        T[F_D * tn + e] = p.f_depth[q];
+        T[F_AX * tn + e] = p.f_albedo[0][q];
+        T[F_AY * tn + e] = p.f_albedo[1][q];
+        T[F_AZ * tn + e] = p.f_albedo[2][q];
+        const int n_raw = p.n[q];
+        const int nj = imaxs(1, n_raw);
+        float var = pixel_variance(p.square_diff[q], n_raw);
+        if (!isfinite(var)) var = 1e-8f;
+        var = fclamps(var, 1e-8f, prm.var2_max);
+        const float nm1 = fmaxf(float(nj - 1), 1.0f);
+        for (int c = 0; c < 3; ++c) {
+            const float sv = p.sqrt_var_stable[c][q];
+            T[(F_SM0 + c) * tn + e] = p.sqrt_mean[c][q];
+            T[(F_SV0 + c) * tn + e] = sv;
+            T[(F_A0 + c) * tn + e] = __fdividef(sv * sv, nm1);
+            T[(F_CM0 + c) * tn + e] = p.color_mean[c][q];
+        }
+        T[F_N * tn + e] = float(nj);
+        T[F_VM * tn + e] = fmaxs(1e-8f, var / float(nj));
+        for (int c = 0; c < 6; ++c) T[(F_R0 + c) * tn + e] = p.rpd[c][q];
+    }
+    __syncthreads();
+
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= prm.w || y >= prm.h) return;
+    const int64_t idx = int64_t(y) * prm.w + x;
+    if (p.hit_count[idx] == 0) {
+        const int n_raw = p.n[idx];
+        for (int c = 0; c < 3; ++c) p.denoised[c][idx] = p.color_mean[c][idx];
+        p.uncertainty[idx] = pixel_variance(p.square_diff[idx], n_raw) / float(imaxs(1, n_raw));
+        p.alpha[idx] = 1.0f;
+        return;
+    }
+    const int ei = (threadIdx.y + r) * tw + threadIdx.x + r;
+    const float ni0 = T[F_NX * tn + ei], ni1 = T[F_NY * tn + ei], ni2 = T[F_NZ * tn + ei];
+    const float di = T[F_D * tn + ei];
+    const float ai0 = T[F_AX * tn + ei], ai1 = T[F_AY * tn + ei], ai2 = T[F_AZ * tn + ei];
+    float smi[3], svi[3], Ai[3];
+    for (int c = 0; c < 3; ++c) {
+        smi[c] = T[(F_SM0 + c) * tn + ei];
+        svi[c] = T[(F_SV0 + c) * tn + ei];
+        Ai[c] = T[(F_A0 + c) * tn + ei];
+    }
+    const float nif = T[F_N * tn + ei];
+    const int n_i = int(nif);
+    float rpd_i[6];
+    for (int c = 0; c < 6; ++c) rpd_i[c] = T[(F_R0 + c) * tn + ei];
+    {
+        // the debug planes (main.cpp:1021-1023)
+        const int n_raw = p.n[idx];
+        float var_i = pixel_variance(p.square_diff[idx], n_raw);
+        if (!isfinite(var_i)) var_i = 1e-8f;
+        var_i = fclamps(var_i, 1e-8f, prm.var2_max);
+        const float vm = fmaxs(1e-8f, var_i / float(n_i));
+        p.var_total[idx] = var_i;
+        p.var_eff[idx] = vm;
+        p.var_ratio[idx] = (var_i > 1e-8f) ? (vm * float(n_i)) / var_i : 0.0f;
+    }
+    const float dthr = prm.depth_threshold;
+    const float dabs_i = fabsf(di);
+
+    // double-float accumulators across rows: colour (3), weight, weight^2, weight^2*var
+    float acc_hi[6] = {0, 0, 0, 0, 0, 0}, acc_lo[6] = {0, 0, 0, 0, 0, 0};
+    int accepted = 0;
+    for (int dy = -r; dy <= r; ++dy) {
+        float row[6] = {0, 0, 0, 0, 0, 0};
+        const int erow = (threadIdx.y + r + dy) * tw + threadIdx.x + r;
+        for (int dx = -r; dx <= r; ++dx) {
+            const int e = erow + dx;
+            const float nj0 = T[F_NX * tn + e], nj1 = T[F_NY * tn + e], nj2 = T[F_NZ * tn + e];
+            if (dot3(ni0, ni1, ni2, nj0, nj1, nj2) < prm.normal_threshold) continue;
+            // relative_depth_delta(di, dj) > threshold, decided exactly
+            const float dj = T[F_D * tn + e];
+            float m = dabs_i;
+            if (m < fabsf(dj)) m = fabsf(dj);
+            if (m < 1e-8f) m = 1e-8f;
+            const float num = fabsf(di - dj);
+            const float approx = __fdividef(num, m);
+            bool far;
+            if (fabsf(approx - dthr) <= dthr * (1.0f / 1048576.0f) + 1e-30f) far = __fdiv_rn(num, m) > dthr;
+            else far = approx > dthr;
+            if (far) continue;
+            const float da0 = ai0 - T[F_AX * tn + e], da1 = ai1 - T[F_AY * tn + e], da2 = ai2 - T[F_AZ * tn + e];
+            if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) continue;
+
+            const float njf = T[F_N * tn + e];
+            bool exact = false;
+            float qmax = 0.0f;
+            for (int c = 0; c < 3; ++c) {
+                const float vj = T[(F_SV0 + c) * tn + e];
+                const float vs = svi[c] + vj;
+                const float md = smi[c] - T[(F_SM0 + c) * tn + e];
+                const float t2 = __fdividef(md * md, vs);
+                const float den = Ai[c] + T[(F_A0 + c) * tn + e];
+                exact |= fabsf(den - 1e-8f) <= 1e-8f * kBand;
+                const float df = den > 1e-8f ? __fdividef(vs * vs, den) : nif + njf - 2.0f;
+                exact |= fabsf(df - prm.df_break) <= prm.df_break * kBand;
+                const float tc = tile_t_lookup(table, df, prm);
+                qmax = fmaxf(qmax, __fdividef(t2, tc * tc));
+            }
+            float shared = 0.0f;
+            for (int c = 0; c < 6; ++c) shared = fmaxs(shared, fmins(rpd_i[c], T[(F_R0 + c) * tn + e]));
+            shared = fclamps(shared, 0.0f, 1.0f);
+            const float adjustment = fclamps(prm.rpd_scale * shared, 0.0f, 1.0f);
+            const float q = __fdividef(qmax, 1.0f + adjustment);
+            const bool center = dx == 0 && dy == 0;
+            exact |= fabsf(q - 25.0f) <= 25.0f * kBand;
+            exact |= !center && fabsf(q - kQAccept) <= kQAccept * kBand;
+            const float spatial = __frcp_rn(1.0f + float(dx * dx + dy * dy));
+            float wj;
+            if (exact) {
+                float svj[3], smj[3];
+                for (int c = 0; c < 3; ++c) {
+                    svj[c] = T[(F_SV0 + c) * tn + e];
+                    smj[c] = T[(F_SM0 + c) * tn + e];
+                }
+                const double qd = exact_q(svi, smi, n_i, svj, smj, int(njf), prm.alpha, adjustment);
+                if (qd > 25.0) continue;
+                const double sw = 1.0 / (1.0 + double(dx * dx + dy * dy));
+                const double wd = sw * exp(-0.5 * qd);
+                if (!center && wd > 0.05 * sw) ++accepted;
+                wj = float(wd);
+            } else {
+                if (q > 25.0f) continue;
+                if (!center && q < kQAccept) ++accepted;
+                wj = spatial * __expf(-0.5f * q);
+            }
+            const float w2 = wj * wj;
+            row[0] = __fmaf_rn(wj, T[F_CM0 * tn + e], row[0]);
+            row[1] = __fmaf_rn(wj, T[F_CM1 * tn + e], row[1]);
+            row[2] = __fmaf_rn(wj, T[F_CM2 * tn + e], row[2]);
+            row[3] += wj;
+            row[4] += w2;
+            row[5] = __fmaf_rn(w2, T[F_VM * tn + e], row[5]);
+        }
+        for (int k = 0; k < 6; ++k) {  // TwoSum into the double-float accumulators
+            const float s = acc_hi[k] + row[k];
+            const float bb = s - acc_hi[k];
+            const float err = (acc_hi[k] - (s - bb)) + (row[k] - bb);
+            acc_hi[k] = s;
+            acc_lo[k] += err;
+        }
+    }
+    const double cs0 = double(acc_hi[0]) + double(acc_lo[0]);
+    const double cs1 = double(acc_hi[1]) + double(acc_lo[1]);
+    const double cs2 = double(acc_hi[2]) + double(acc_lo[2]);
+    const double weight_sum = double(acc_hi[3]) + double(acc_lo[3]);
+    const double weight_square_sum = double(acc_hi[4]) + double(acc_lo[4]);
+    const double weighted_variance_sum = double(acc_hi[5]) + double(acc_lo[5]);
+    if (accepted >= 2 && fabs(weight_sum - 1.1) <= 1.1 * kWsBand) {
+        exact_pixel(p, prm, idx);
+        return;
+    }
+    const float var_mean_i = T[F_VM * tn + ei];
+    const float cmi[3] = {T[F_CM0 * tn + ei], T[F_CM1 * tn + ei], T[F_CM2 * tn + ei]};
+    float mean_nb[3] = {cmi[0], cmi[1], cmi[2]};
+    double var_neighbors = double(var_mean_i);
+    if (weight_sum > double(1e-8f)) {
+        mean_nb[0] = float(cs0 / weight_sum);
+        mean_nb[1] = float(cs1 / weight_sum);
+        mean_nb[2] = float(cs2 / weight_sum);
+        var_neighbors = weighted_variance_sum / (weight_sum * weight_sum);
+    }
+    const double effective = weight_sum * weight_sum / dmaxs(double(1e-8f), weight_square_sum);
+    const double blend = (accepted >= 2 && weight_sum >= 1.1) ? dclamps(1.0 - 1.0 / sqrt(effective), 0.0, 0.8) : 0.0;
+    const float alpha = float(1.0 - blend);
+    const float fb = float(blend);
+    for (int c = 0; c < 3; ++c) p.denoised[c][idx] = lerpf(cmi[c], mean_nb[c], fb);
+    const float uncertainty = float(double(alpha) * double(alpha) * double(var_mean_i) + blend * blend * var_neighbors +
+                                    2.0 * double(alpha) * blend * (1.0 / dmaxs(weight_sum, double(1e-8f))) *
+                                        double(var_mean_i));
+    p.alpha[idx] = alpha;
+    p.uncertainty[idx] = uncertainty;
+}
+
+// Smallest float s with fl(sqrt(s)) > t: the albedo gate sqrt(s) > 0.12 without a sqrt.
+float sqrt_gate_threshold(float t) {
+    uint32_t lo = 0, hi = 0x7f800000u;  // [0, +inf)
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        float s;
+        std::memcpy(&s, &mid, 4);
+        if (std::sqrt(s) > t) hi = mid;
+        else lo = mid + 1;
+    }
+    float out;
+    std::memcpy(&out, &lo, 4);
+    return out;
+}
+
+size_t tile_bytes(int r, int by) {
+    return (size_t(kTileX + 2 * r) * size_t(by + 2 * r) * F_COUNT + 32) * sizeof(float);
 }
 
 }  // namespace
@@ -206,10 +488,43 @@ cudaError_t launch_statmc(Job& j) {
         k_sqrt_var_stable<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, j.g.w, j.g.h);
     }
     KernelScope ks(j, RPD_KERNEL_STATMC_WINDOW);
-    StatmcParams prm{j.g.w, j.g.h, j.cfg.color_window_radius, j.cfg.color_normal_threshold,
-                     j.cfg.color_depth_threshold, j.cfg.rpf_shrinkage_scale, j.cfg.color_compat_alpha,
-                     j.cfg.color_sigma_max * j.cfg.color_sigma_max};
-    k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
+    StatmcParams prm{};
+    prm.w = j.g.w;
+    prm.h = j.g.h;
+    prm.r = j.cfg.color_window_radius;
+    prm.normal_threshold = j.cfg.color_normal_threshold;
+    prm.depth_threshold = j.cfg.color_depth_threshold;
+    prm.rpd_scale = j.cfg.rpf_shrinkage_scale;
+    prm.alpha = j.cfg.color_compat_alpha;
+    prm.var2_max = j.cfg.color_sigma_max * j.cfg.color_sigma_max;
+    static const float albedo_sq = sqrt_gate_threshold(0.12f);
+    prm.albedo_sq_threshold = albedo_sq;
+    // the branch of lookup_t_critical this alpha takes (main.cpp:189-225)
+    const float a = std::min(std::max(prm.alpha, 1e-8f), 0.999999f);
+    if (std::fabs(a - 0.05f) < 1e-4f) prm.table = 0;
+    else if (std::fabs(a - 0.01f) < 1e-4f) prm.table = 1;
+    else prm.table = 2;
+    prm.z = a <= 0.001f ? 3.29f : a <= 0.005f ? 2.81f : a <= 0.01f ? 2.58f : a <= 0.02f ? 2.33f
+          : a <= 0.05f ? 1.96f : a <= 0.10f ? 1.64f : 1.28f;
+    prm.df_break = prm.table < 2 ? 30.5f : 30.0f;
+    int by = 0;
+    for (int cand : {8, 4, 2}) {
+        if (tile_bytes(prm.r, cand) <= size_t(110) * 1024) {
+            by = cand;
+            break;
+        }
+    }
+    if (j.exact_window || by == 0) {
+        k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
+    } else {
+        prm.by = by;
+        const size_t smem = tile_bytes(prm.r, by);
+        cudaError_t e = cudaFuncSetAttribute(k_statmc_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        const dim3 block(kTileX, by);
+        const dim3 grid((j.g.w + kTileX - 1) / kTileX, (j.g.h + by - 1) / by);
+        k_statmc_tile<<<grid, block, smem, j.stream>>>(j.p, prm);
+    }
     j.launches += 3;
     return cudaGetLastError();
 }

@@ -17,6 +17,7 @@
 namespace rpd {
 
 constexpr float kEpsSmall = 1e-8f;        // shared/global.h:4
+constexpr int kClasses = 7;               // validity classes of the fast grid pass
 constexpr int kDeps = RPD_GRID_DEPENDENCIES;
 constexpr int kDepStride = RPD_GRID_DEP_STRIDE;
 
@@ -129,8 +130,14 @@ struct Job {
     // staging for host-side pushes (grown on demand)
     void* staging = nullptr;
     uint64_t staging_bytes = 0;
+    float* lum = nullptr;        // per-sample luminance of the current push (fast grid pass)
+    uint64_t lum_cap = 0;
+    float* cls[kClasses][5]{};   // per-pixel validity-class sums (arena)
+    uint8_t* pflags = nullptr;   // per-pixel screen-uniform / mixed flags (arena)
     int64_t* offsets = nullptr;  // per-pixel sample offsets of the current push
     int64_t offsets_cap = 0;
+    bool exact_grid = false;     // RPD_EXACT_GRID: double-precision grid in the reference's order
+    bool exact_window = false;   // RPD_EXACT_WINDOW: double-precision StatMC window
     bool pass_open = false;
     bool features_valid = false;
     bool cache_valid = false;
@@ -199,10 +206,45 @@ struct DeviceSamples {           // rpd_sample_soa with pointers in HBM
     const uint8_t* category;
 };
 
+// Per-pixel validity-class sums the statistics pass leaves for the fast grid pass.
+// Class 0: pixel_valid samples; classes 1-6: samples with the brdf, lens, light_uv,
+// environment, light_select and rr dimension valid. Each class holds count, sum y
+// (hi, lo) and sum y^2 (hi, lo) over the pixel's finite samples.
+constexpr uint8_t kPixUniform = 0x1;  // every screen position lies inside its pixel
+constexpr uint8_t kPixMixed = 0x2;    // some sample has a random dimension but no screen position
+constexpr float kUniformMax = 1.0f - 1.0f / 1024.0f;
+__host__ __device__ constexpr uint8_t class_bit(int c) {
+    return c == 0 ? RPD_SAMPLE_PIXEL_VALID : c == 1 ? RPD_SAMPLE_BRDF_VALID : c == 2 ? RPD_SAMPLE_LENS_VALID
+         : c == 3 ? RPD_SAMPLE_LIGHT_VALID : c == 4 ? RPD_SAMPLE_ENV_VALID : c == 5 ? RPD_SAMPLE_LIGHT_SELECT_VALID
+         : RPD_SAMPLE_RR_VALID;
+}
+struct GridPrep {
+    float* cls[kClasses][5];  // W*H planes
+    uint8_t* pflags;          // W*H
+    float* lum;               // per sample of the push (NaN when the radiance is not finite)
+    uint32_t* key;            // per sample of the push: packed random-dimension bins + validity
+    int width;
+};
+// Sample key: bits 0-3 lens bin, 4-7 brdf bin, 8-11 light_uv bin, 12-15 environment bin,
+// 16-19 light index, 20 rr survived; bits 21-27 the valid flags of pixel, lens, brdf,
+// light_uv, light_select, environment, rr (after dropping flags whose plane is absent).
+constexpr int kKeyValidShift = 21;
+__host__ __device__ constexpr uint32_t key_valid_bit(int group) {
+    // group 0 pixel, 1 brdf, 2 lens, 3 light_uv, 4 environment, 5 light_select, 6 rr
+    return group == 0 ? 1u << 21 : group == 1 ? 1u << 23 : group == 2 ? 1u << 22 : group == 3 ? 1u << 24
+         : group == 4 ? 1u << 26 : group == 5 ? 1u << 25 : 1u << 27;
+}
+__host__ __device__ constexpr int key_bin_shift(int group) {
+    return group == 1 ? 4 : group == 2 ? 0 : group == 3 ? 8 : group == 4 ? 12 : 16;
+}
+
 cudaError_t launch_offsets_uniform(Job& j, int64_t count, int32_t spp);
 cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count);
-cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count);
+cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,
+                                     const GridPrep& gp, int32_t spp);
 cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first, int64_t count);
+cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int64_t count, const GridPrep& gp,
+                             int32_t spp, int32_t max_count);
 cudaError_t launch_merge_grid(Job& j);
 cudaError_t launch_feature_cache(Job& j);
 cudaError_t launch_sensitivity(Job& j);

@@ -225,6 +225,7 @@ def lib() -> C.CDLL:
         "rpd_job_create": (C.c_int, [vp, C.POINTER(Config), C.POINTER(vp)]),
         "rpd_job_destroy": (None, [vp]),
         "rpd_job_set_config": (C.c_int, [vp, C.POINTER(Config)]),
+        "rpd_job_set_exact": (C.c_int, [vp, C.c_int]),
         "rpd_job_begin_frame": (C.c_int, [vp]),
         "rpd_job_push_samples": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp, C.c_int]),
         "rpd_job_end_pass": (C.c_int, [vp]),
@@ -267,7 +268,7 @@ def lib() -> C.CDLL:
 def exported_symbols() -> list[str]:
     """Names declared in include/rpd_gb300.h that the library must export."""
     return ["rpd_config_defaults", "rpd_config_validate", "rpd_ctx_create", "rpd_ctx_destroy", "rpd_job_footprint",
-            "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config",
+            "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config", "rpd_job_set_exact",
             "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_end_pass", "rpd_recompute_sensitivity",
             "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
             "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
@@ -442,6 +443,9 @@ class Job:
         check(lib().rpd_job_set_config(self.handle, C.byref(cfg)))
         self.cfg = cfg.replace(image_width=self.cfg.image_width, image_height=self.cfg.image_height,
                                rpf_tile_size=self.cfg.rpf_tile_size)
+
+    def set_exact(self, grid: bool = False, window: bool = False) -> None:
+        check(lib().rpd_job_set_exact(self.handle, (1 if grid else 0) | (2 if window else 0)))
 
     def begin_frame(self) -> None:
         check(lib().rpd_job_begin_frame(self.handle))

@@ -1,14 +1,16 @@
 """GPU parity: the CUDA path (through the C ABI) against the oracle on the same inputs.
 
 Bars, per stage:
-  * pixel statistics, features, the RPD grid, the raw node statistics, the variance
-    stabilisation and the adaptive integer counts: bit-exact (the kernels perform the
-    reference's IEEE operations in its order; the grid order is the reference's
-    single-thread order, so the oracle runs with one thread for these checks);
+  * pixel statistics, features and the variance stabilisation: bit-exact in every mode
+    (the kernels perform the reference's IEEE operations in its order);
+  * the RPD grid: bit-exact in the exact mode (the reference's single-thread order, so the
+    oracle runs with one thread), and within 1e-9 relative of each dependency's largest
+    sum in the default double-float mode;
   * stages that call expf / exp (prior smoothing, the StatMC weights, importance
-    smoothing, the filters): the CUDA math library is within 2 ulp of the C library's,
-    so the bar is the plain-form tolerance: max per-pixel relative error <= 1e-4 with a
-    1e-3 floor on |reference| (`max_rel_err`).
+    smoothing, the filters) and the single-precision StatMC window: the plain-form
+    tolerance, max per-pixel relative error <= 1e-4 with a 1e-3 floor on |reference|
+    (`max_rel_err`);
+  * adaptive sample counts: bit-exact when the importance map is bit-exact.
 """
 from __future__ import annotations
 
@@ -30,17 +32,25 @@ CLOSE_PIXEL_FIELDS = ["SENSITIVITY_CONFIDENCE", "SENSITIVITY_GRADIENT", "DENOISE
                       "VAR_TOTAL_DEBUG", "VAR_EFF_DEBUG", "VAR_RATIO_DEBUG"]
 
 
-def run_both(gpu_ctx, cfg, samples, spp, threads=1):
+def run_both(gpu_ctx, cfg, samples, spp, threads=1, exact=False):
     g = R.Job(gpu_ctx, cfg)
+    g.set_exact(grid=exact, window=exact)
     o = B.OracleJob(cfg, threads=threads)
     for job in (g, o):
         B.run_pipeline(job, samples, spp)
     return g, o
 
 
+def assert_grid_close(x, y, rel=1e-9):
+    scale = np.max(np.abs(y), axis=2, keepdims=True)
+    err = np.abs(x - y) - rel * scale
+    assert np.all(err <= 0.0), f"grid differs by {np.max(np.abs(x - y) / np.maximum(scale, 1e-300)):.3e} relative"
+
+
 def check_pipeline(g, o, exact_grid=True):
     for f in EXACT_FIELDS:
         if f == "GRID" and not exact_grid:
+            assert_grid_close(g.read(f), o.read(f))
             continue
         assert_bitwise(g.read(f), o.read(f), f)
     for f in NODE_FIELDS:
@@ -54,13 +64,15 @@ def check_pipeline(g, o, exact_grid=True):
     assert_bitwise(g.read("VARIANCE_DENOISED"), o.read("VARIANCE_DENOISED"), "VARIANCE_DENOISED")
 
 
-@pytest.mark.parametrize("w,h,spp,tile", [(37, 23, 5, 16), (64, 48, 8, 16), (33, 17, 4, 6), (16, 16, 3, 1)])
-def test_synthetic_pipeline(gpu_ctx, w, h, spp, tile):
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+@pytest.mark.parametrize("w,h,spp,tile", [(37, 23, 5, 16), (64, 48, 8, 16), (33, 17, 4, 6), (16, 16, 3, 1),
+                                          (70, 41, 7, 8), (45, 30, 9, 4)])
+def test_synthetic_pipeline(gpu_ctx, w, h, spp, tile, exact):
     cfg = small_config(w, h, rpf_tile_size=tile)
     p = R.synth_params(w, h, 11, miss_regions=4, nan_rate=0.005)
     s = B.synth_fill(p, 0, w * h, spp)
-    g, o = run_both(gpu_ctx, cfg, s, spp)
-    check_pipeline(g, o)
+    g, o = run_both(gpu_ctx, cfg, s, spp, exact=exact)
+    check_pipeline(g, o, exact_grid=exact)
     g.close()
     o.close()
 
@@ -71,7 +83,7 @@ def test_default_knobs_and_alpha(gpu_ctx):
     cfg = R.default_config(image_width=w, image_height=h, seed=5)
     s = B.synth_fill(R.synth_params(w, h, 3), 0, w * h, spp)
     g, o = run_both(gpu_ctx, cfg, s, spp)
-    check_pipeline(g, o)
+    check_pipeline(g, o, exact_grid=False)
     # an alpha outside the two tables takes the normal-quantile branch
     cfg2 = cfg.replace(color_compat_alpha=0.2)
     for job in (g, o):
@@ -85,18 +97,22 @@ def test_rpd_disabled_matches(gpu_ctx):
     cfg = small_config(w, h, rpf_shrinkage_scale=0.0)
     s = B.synth_fill(R.synth_params(w, h, 9), 0, w * h, spp)
     g, o = run_both(gpu_ctx, cfg, s, spp)
-    check_pipeline(g, o)
+    check_pipeline(g, o, exact_grid=False)
     assert not np.any(g.read("SENSITIVITY_GRADIENT"))
 
 
-def test_chunked_pushes_equal_single_push(gpu_ctx):
-    """Pushing a pass in row bands gives the same bits as one push (sequential order)."""
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_chunked_pushes_equal_single_push(gpu_ctx, exact):
+    """Pushing a pass in row bands gives the same result as one push (in the exact mode the
+    same bits: the grid keeps the reference's sequential order across pushes)."""
     w, h, spp = 30, 20, 4
     cfg = small_config(w, h, rpf_tile_size=8)
     s = B.synth_fill(R.synth_params(w, h, 21), 0, w * h, spp)
     g1 = R.Job(gpu_ctx, cfg)
+    g1.set_exact(grid=exact, window=exact)
     B.run_pipeline(g1, s, spp)
     g2 = R.Job(gpu_ctx, cfg)
+    g2.set_exact(grid=exact, window=exact)
     g2.begin_frame()
     offsets = np.arange(w * h + 1) * spp
     for p0, p1 in [(0, 7), (7, 133), (133, 400), (400, w * h)]:
@@ -105,8 +121,14 @@ def test_chunked_pushes_equal_single_push(gpu_ctx):
     g2.recompute_sensitivity()
     g2.statmc_denoise()
     g2.variance_denoise()
-    for f in ["GRID", "STATS_MEAN", "DENOISED", "VARIANCE_DENOISED", "NODE_ALL"]:
+    for f in ["STATS_MEAN", "VARIANCE_DENOISED"]:
         assert_bitwise(g1.read(f), g2.read(f), f)
+    if exact:
+        for f in ["GRID", "DENOISED", "NODE_ALL"]:
+            assert_bitwise(g1.read(f), g2.read(f), f)
+    else:
+        assert_grid_close(g2.read("GRID"), g1.read("GRID"), rel=1e-12)
+        assert max_rel_err(g2.read("DENOISED"), g1.read("DENOISED"), FLOOR) <= 1e-6
 
 
 def test_ragged_counts_and_empty_pixels(gpu_ctx):
@@ -125,15 +147,16 @@ def test_ragged_counts_and_empty_pixels(gpu_ctx):
         job.recompute_sensitivity()
         job.statmc_denoise()
         job.variance_denoise()
-    check_pipeline(g, o)
+    check_pipeline(g, o, exact_grid=False)
 
 
-def test_single_pixel_and_thin_images(gpu_ctx):
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_single_pixel_and_thin_images(gpu_ctx, exact):
     for w, h in [(1, 1), (1, 9), (7, 1), (2, 3)]:
         cfg = small_config(w, h, color_window_radius=2, var_window_radius=1)
         s = B.synth_fill(R.synth_params(w, h, 2), 0, w * h, 3)
-        g, o = run_both(gpu_ctx, cfg, s, 3)
-        check_pipeline(g, o)
+        g, o = run_both(gpu_ctx, cfg, s, 3, exact=exact)
+        check_pipeline(g, o, exact_grid=exact)
         g.close()
 
 
@@ -143,7 +166,7 @@ def test_adaptive_counts_bit_exact(gpu_ctx):
         cfg = small_config(w, h, adaptive_spp=4, adaptive_base_samples=1, adaptive_importance_smoothing_radius=radius,
                            seed=77)
         s = B.synth_fill(R.synth_params(w, h, 13), 0, w * h, spp)
-        g, o = run_both(gpu_ctx, cfg, s, spp)
+        g, o = run_both(gpu_ctx, cfg, s, spp, exact=True)
         cg = g.compute_adaptive_sample_counts()
         co = o.compute_adaptive_sample_counts()
         imp_g, imp_o = g.read("ADAPTIVE_IMPORTANCE"), o.read("ADAPTIVE_IMPORTANCE")
@@ -167,6 +190,7 @@ def test_adaptive_passes_sequence(gpu_ctx):
                        adaptive_importance_smoothing_radius=0)
     p = R.synth_params(w, h, 31)
     g = R.Job(gpu_ctx, cfg)
+    g.set_exact(grid=True, window=True)
     o = B.OracleJob(cfg, threads=1)
     s0 = B.synth_fill(p, 0, w * h, spp)
     for job in (g, o):
@@ -228,3 +252,13 @@ def test_device_resident_push_matches_host_push(gpu_ctx):
     for f in ["GRID", "STATS_MEAN", "DENOISED", "VARIANCE_DENOISED"]:
         assert_bitwise(g1.read(f), g2.read(f), f)
     dev.free()
+
+
+def test_plain_256x256_4spp(gpu_ctx):
+    """The plain method at the size of the 256x256 / 4 spp cornell_box case, on synthetic
+    samples, default (fast) mode against the oracle."""
+    w, h, spp = 256, 256, 4
+    cfg = small_config(w, h)
+    s = B.synth_fill(R.synth_params(w, h, 1234, miss_regions=3), 0, w * h, spp)
+    g, o = run_both(gpu_ctx, cfg, s, spp, threads=1)
+    check_pipeline(g, o, exact_grid=False)
