@@ -323,6 +323,21 @@ int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, con
                         float sigma_p, float sigma_a, float* gaussian, float* bilateral,
                         float* joint, rpd_memory where);
 
+/* No counterpart in the reference: the a-trous filter above for callers that may not
+ * allocate device memory while they run (all HBM reserved up front, no device-wide
+ * synchronisation from cudaFree allowed, or an allocator that forbids library-internal
+ * allocations). Its ping-pong scratch is a fixed device array of the library holding
+ * RPD_NOALLOC_MAX_PIXELS pixels; larger images fail with RPD_ERR_INVALID_ARGUMENT.
+ * raw/normal/albedo/out are device pointers on the calling thread's current device, out
+ * must not overlap the inputs, and the call is asynchronous on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream). One scratch per device: overlapping calls on a
+ * device race. The first call on a device looks the scratch up and should precede any
+ * stream capture. */
+#define RPD_NOALLOC_MAX_PIXELS 4194304 /* 2048 x 2048; 48 MiB of FP32 RGB scratch */
+int rpd_atrous_wavelet_noalloc(const float* raw, const float* normal, const float* albedo,
+                               int32_t width, int32_t height, float sigma_c, float sigma_n,
+                               float sigma_a, int32_t iterations, float* out, void* stream);
+
 /* ---- memory helpers for callers without a CUDA toolchain ---------------------------- */
 
 /* HBM owned by the caller (sample planes for RPD_MEM_DEVICE pushes). Counts against the

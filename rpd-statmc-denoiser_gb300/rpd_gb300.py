@@ -247,6 +247,7 @@ def lib() -> C.CDLL:
         "rpd_job_mark_elapsed": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]),
         "rpd_atrous_wavelet": (C.c_int, [vp, vp, vp, vp, i32, i32, f32, f32, f32, i32, vp, C.c_int]),
         "rpd_joint_bilateral": (C.c_int, [vp, vp, vp, vp, i32, i32, f32, f32, f32, f32, vp, vp, vp, C.c_int]),
+        "rpd_atrous_wavelet_noalloc": (C.c_int, [vp, vp, vp, i32, i32, f32, f32, f32, i32, vp, vp]),
         "rpd_device_alloc": (C.c_int, [vp, u64, C.POINTER(vp)]),
         "rpd_device_free": (C.c_int, [vp, vp]),
         "rpd_host_alloc": (C.c_int, [u64, C.POINTER(vp)]),
@@ -274,7 +275,7 @@ def exported_symbols() -> list[str]:
             "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
             "rpd_job_set_profiling", "rpd_job_kernel_time", "rpd_job_reset_kernel_times", "rpd_kernel_name",
             "rpd_job_mark", "rpd_job_mark_elapsed",
-            "rpd_atrous_wavelet", "rpd_joint_bilateral", "rpd_device_alloc", "rpd_device_free", "rpd_host_alloc",
+            "rpd_atrous_wavelet", "rpd_joint_bilateral", "rpd_atrous_wavelet_noalloc", "rpd_device_alloc", "rpd_device_free", "rpd_host_alloc",
             "rpd_host_free", "rpd_memcpy", "rpd_synth_fill", "rpd_last_error", "rpd_status_string"]
 
 
@@ -422,6 +423,17 @@ class Context:
         check(lib().rpd_joint_bilateral(self.handle, *[a.ctypes.data for a in args], w, h, sigma_c, sigma_n, sigma_p,
                                         sigma_a, *[o.ctypes.data for o in outs], MEM_HOST))
         return tuple(outs)
+
+
+NOALLOC_MAX_PIXELS = 4194304  # RPD_NOALLOC_MAX_PIXELS
+
+
+def atrous_noalloc(raw: "DeviceBuffer", normal: "DeviceBuffer", albedo: "DeviceBuffer", w: int, h: int,
+                   sigma_c: float, sigma_n: float, sigma_a: float, iterations: int, out: "DeviceBuffer",
+                   stream: int = 0) -> None:
+    """rpd_atrous_wavelet_noalloc on device buffers; asynchronous on `stream` (0: default)."""
+    check(lib().rpd_atrous_wavelet_noalloc(raw.ptr, normal.ptr, albedo.ptr, w, h, sigma_c, sigma_n, sigma_a,
+                                           iterations, out.ptr, stream or None))
 
 
 class Job:
