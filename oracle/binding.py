@@ -113,6 +113,83 @@ def ref() -> C.CDLL:
     return L
 
 
+_ref_filters = None
+
+
+def ref_filters() -> tuple[C.CDLL, C.CDLL]:
+    """The reference's own denoising/atrous_wavelet.cpp and joint_bilateral.cpp filter()
+    functions on in-memory images (oracle/ref/ref_filters.cpp)."""
+    global _ref_filters
+    if _ref_filters is None:
+        A = C.CDLL(str(HERE / "_ref" / "libref_atrous.so"))
+        J = C.CDLL(str(HERE / "_ref" / "libref_joint.so"))
+        A.ref_atrous.restype = C.c_int
+        A.ref_atrous.argtypes = [C.c_void_p] * 3 + [C.c_int] * 2 + [C.c_float] * 3 + [C.c_int, C.c_void_p]
+        J.ref_joint_bilateral.restype = C.c_int
+        J.ref_joint_bilateral.argtypes = [C.c_void_p] * 3 + [C.c_int] * 2 + [C.c_float] * 4 + [C.c_void_p] * 3
+        _ref_filters = (A, J)
+    return _ref_filters
+
+
+def ref_atrous(raw, normal, albedo, sigma_c, sigma_n, sigma_a, iterations) -> np.ndarray:
+    h, w, _ = raw.shape
+    out = np.empty((h, w, 3), dtype=np.float32)
+    a = [np.ascontiguousarray(x, dtype=np.float32) for x in (raw, normal, albedo)]
+    rc = ref_filters()[0].ref_atrous(*[x.ctypes.data for x in a], w, h, sigma_c, sigma_n, sigma_a, iterations,
+                                     out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"reference a-trous filter failed ({rc})")
+    return out
+
+
+def ref_joint_bilateral(raw, normal, albedo, sigma_c, sigma_n, sigma_p, sigma_a):
+    h, w, _ = raw.shape
+    outs = [np.empty((h, w, 3), dtype=np.float32) for _ in range(3)]
+    a = [np.ascontiguousarray(x, dtype=np.float32) for x in (raw, normal, albedo)]
+    rc = ref_filters()[1].ref_joint_bilateral(*[x.ctypes.data for x in a], w, h, sigma_c, sigma_n, sigma_p, sigma_a,
+                                              *[o.ctypes.data for o in outs])
+    if rc != 0:
+        raise RuntimeError(f"reference joint-bilateral filter failed ({rc})")
+    return tuple(outs)
+
+
+def port_atrous(raw, normal, albedo, sigma_c, sigma_n, sigma_a, iterations, threads: int = 1) -> np.ndarray:
+    h, w, _ = raw.shape
+    out = np.empty((h, w, 3), dtype=np.float32)
+    a = [np.ascontiguousarray(x, dtype=np.float32) for x in (raw, normal, albedo)]
+    port().orc_atrous_wavelet(*[x.ctypes.data for x in a], w, h, sigma_c, sigma_n, sigma_a, iterations,
+                              out.ctypes.data, threads)
+    return out
+
+
+def port_joint_bilateral(raw, normal, albedo, sigma_c, sigma_n, sigma_p, sigma_a, threads: int = 1):
+    h, w, _ = raw.shape
+    outs = [np.empty((h, w, 3), dtype=np.float32) for _ in range(3)]
+    a = [np.ascontiguousarray(x, dtype=np.float32) for x in (raw, normal, albedo)]
+    port().orc_joint_bilateral(*[x.ctypes.data for x in a], w, h, sigma_c, sigma_n, sigma_p, sigma_a,
+                               *[o.ctypes.data for o in outs], threads)
+    return tuple(outs)
+
+
+def config_dict(cfg: R.Config) -> dict:
+    return {name: getattr(cfg, name) for name, _ in R.Config._fields_}
+
+
+def config_from(d: dict) -> R.Config:
+    return R.default_config(**d)
+
+
+def synth_dict(p: R.SynthParams) -> dict:
+    return {name: getattr(p, name) for name, _ in R.SynthParams._fields_}
+
+
+def synth_from(d: dict) -> R.SynthParams:
+    p = R.SynthParams()
+    for k, v in d.items():
+        setattr(p, k, v)
+    return p
+
+
 def _counts_ptr(counts):
     if counts is None:
         return None, None

@@ -41,7 +41,23 @@ static inline int imaxs(int a, int b) { return (a < b) ? b : a; }
 static inline int imins(int a, int b) { return (b < a) ? b : a; }
 static inline int iclamps(int v, int lo, int hi) { return (v < lo) ? lo : ((hi < v) ? hi : v); }
 /* global.h:45-48 */
+/* The template lerp of shared/global.h:45-48; main.cpp calls it for Vec3f only
+ * (main.cpp:1115). */
 static inline float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+/* Every lerp(float, float, float) call of the reference (main.cpp:196,869-879,
+ * core/buffers.h:84-86, core/stats.h:90) resolves to std::lerp instead: stb_image.h, which
+ * shared/image.h:10-11 includes with its implementation, includes <math.h>, and in C++20
+ * libstdc++'s <math.h> brings std::lerp into the global namespace, where the non-template
+ * float overload beats the template above. This is the C++20 algorithm (P0811R3) as
+ * libstdc++ evaluates it: when a and b do not share a sign, t*b + (1-t)*a; t == 1 gives b
+ * exactly; otherwise a + t*(b-a), kept from passing b. */
+static inline float lerp_std(float a, float b, float t) {
+    if ((a <= 0.0f && b >= 0.0f) || (a >= 0.0f && b <= 0.0f)) return t * b + (1.0f - t) * a;
+    if (t == 1.0f) return b;
+    const float x = a + t * (b - a);
+    if ((t > 1.0f) == (b > a)) return (b < x) ? x : b;
+    return (b > x) ? x : b;
+}
 /* Eigen 3-vector reduction order */
 static inline float dot3(const float* a, const float* b) {
     return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]);
@@ -602,9 +618,9 @@ static inline float tiles_lookup(const orc_job* j, const float* tiles, int64_t i
     const float v10 = tiles[(size_t)y0 * j->nodes_x + x1];
     const float v01 = tiles[(size_t)y1 * j->nodes_x + x0];
     const float v11 = tiles[(size_t)y1 * j->nodes_x + x1];
-    const float top = lerpf(v00, v10, tx);
-    const float bottom = lerpf(v01, v11, tx);
-    return lerpf(top, bottom, ty);
+    const float top = lerp_std(v00, v10, tx);
+    const float bottom = lerp_std(v01, v11, tx);
+    return lerp_std(top, bottom, ty);
 }
 
 /* SensitivityTiles::expand_values (core/buffers.h:89-101) */
@@ -784,9 +800,9 @@ int orc_recompute_sensitivity(orc_job* j) {
 #endif
     for (int64_t idx = 0; idx < nn; ++idx) {
         float fin[7];
-        for (int f = 0; f < 7; ++f) fin[f] = lerpf(prior[f][idx], raw[f][idx], conf[f][idx]);
+        for (int f = 0; f < 7; ++f) fin[f] = lerp_std(prior[f][idx], raw[f][idx], conf[f][idx]);
         float screen[6];
-        for (int c = 0; c < 6; ++c) screen[c] = lerpf(prior[7 + c][idx], raw[7 + c][idx], conf[7 + c][idx]);
+        for (int c = 0; c < 6; ++c) screen[c] = lerp_std(prior[7 + c][idx], raw[7 + c][idx], conf[7 + c][idx]);
         T[N_PIXEL][idx] = fclamps(fin[R_PIXEL], 0.0f, 1.0f);
         T[N_BRDF][idx] = fclamps(fin[R_BRDF], 0.0f, 1.0f);
         T[N_LENS][idx] = fclamps(fin[R_LENS], 0.0f, 1.0f);
@@ -866,7 +882,7 @@ static float interpolate_table(const float* table, float df) {
     const int lo = iclamps((int)floorf(df), 1, 30);
     const int hi = iclamps((int)ceilf(df), 1, 30);
     if (lo == hi) return table[lo - 1];
-    return lerpf(table[lo - 1], table[hi - 1], (df - (float)lo) / (float)(hi - lo));
+    return lerp_std(table[lo - 1], table[hi - 1], (df - (float)lo) / (float)(hi - lo));
 }
 
 static float lookup_t_critical(float df, float alpha) {
@@ -1057,7 +1073,7 @@ int orc_statmc_denoise(orc_job* j) {
 static inline float conservative_variance_update(float value, float neighbor, float stabilizer) {
     const float blend = fclamps(fmaxs(0.0f, neighbor - value) / fmaxs(EPS_SMALL, value + neighbor + stabilizer),
                                 0.0f, 1.0f);
-    return lerpf(value, neighbor, blend);
+    return lerp_std(value, neighbor, blend);
 }
 
 int orc_variance_denoise(orc_job* j) {

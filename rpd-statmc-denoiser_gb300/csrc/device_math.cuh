@@ -22,8 +22,22 @@ __device__ __forceinline__ int imaxs(int a, int b) { return (a < b) ? b : a; }
 __device__ __forceinline__ int imins(int a, int b) { return (b < a) ? b : a; }
 __device__ __forceinline__ int iclamps(int v, int lo, int hi) { return (v < lo) ? lo : ((hi < v) ? hi : v); }
 
-// lerp (shared/global.h:45-48)
+// The template lerp of shared/global.h:45-48, which the reference calls for Vec3f only
+// (main.cpp:1115).
 __device__ __forceinline__ float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+// The reference's lerp(float, float, float) calls (main.cpp:196,869-879, core/buffers.h:84-86,
+// core/stats.h:90) resolve to std::lerp: stb_image.h (included with its implementation by
+// shared/image.h:10-11) includes <math.h>, whose C++20 libstdc++ form exports std::lerp to
+// the global namespace, and the non-template float overload wins. The C++20 algorithm
+// (P0811R3) as libstdc++ evaluates it: t*b + (1-t)*a when a and b do not share a sign, b
+// exactly at t == 1, otherwise a + t*(b-a) kept from passing b.
+__device__ __forceinline__ float lerp_std(float a, float b, float t) {
+    if ((a <= 0.0f && b >= 0.0f) || (a >= 0.0f && b <= 0.0f)) return __fadd_rn(__fmul_rn(t, b), __fmul_rn(1.0f - t, a));
+    if (t == 1.0f) return b;
+    const float x = __fadd_rn(a, __fmul_rn(t, b - a));
+    if ((t > 1.0f) == (b > a)) return (b < x) ? x : b;
+    return (b > x) ? x : b;
+}
 
 __device__ __forceinline__ float dot3(float a0, float a1, float a2, float b0, float b1, float b2) {
     return a0 * b0 + (a1 * b1 + a2 * b2);

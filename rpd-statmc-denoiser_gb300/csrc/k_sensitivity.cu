@@ -156,9 +156,9 @@ __global__ void k_node_combine(Geometry g, NodePlanes n) {
         n.prior[f][idx] = prior[f];
     }
     float fin[7];
-    for (int f = 0; f < 7; ++f) fin[f] = lerpf(prior[f], raw[f], conf[f]);
+    for (int f = 0; f < 7; ++f) fin[f] = lerp_std(prior[f], raw[f], conf[f]);
     float screen[6];
-    for (int c = 0; c < 6; ++c) screen[c] = lerpf(prior[7 + c], raw[7 + c], conf[7 + c]);
+    for (int c = 0; c < 6; ++c) screen[c] = lerp_std(prior[7 + c], raw[7 + c], conf[7 + c]);
     float** T = n.field;
     T[N_PIXEL][idx] = fclamps(fin[R_PIXEL], 0.0f, 1.0f);
     const float rnd[6] = {fclamps(fin[R_BRDF], 0.0f, 1.0f), fclamps(fin[R_LENS], 0.0f, 1.0f),
@@ -208,9 +208,9 @@ __device__ __forceinline__ float tiles_lookup(const Geometry& g, const float* ti
     const float v10 = tiles[int64_t(y0) * g.nodes_x + x1];
     const float v01 = tiles[int64_t(y1) * g.nodes_x + x0];
     const float v11 = tiles[int64_t(y1) * g.nodes_x + x1];
-    const float top = lerpf(v00, v10, tx);
-    const float bottom = lerpf(v01, v11, tx);
-    return lerpf(top, bottom, ty);
+    const float top = lerp_std(v00, v10, tx);
+    const float bottom = lerp_std(v01, v11, tx);
+    return lerp_std(top, bottom, ty);
 }
 
 __global__ void k_sens_pixels(Geometry g, NodePlanes n, PixelPlanes p) {

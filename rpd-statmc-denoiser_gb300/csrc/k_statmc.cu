@@ -48,7 +48,7 @@ __device__ __forceinline__ float interpolate_table(const float* table, float df)
     const int lo = iclamps(int(floorf(df)), 1, 30);
     const int hi = iclamps(int(ceilf(df)), 1, 30);
     if (lo == hi) return table[lo - 1];
-    return lerpf(table[lo - 1], table[hi - 1], (df - float(lo)) / float(hi - lo));
+    return lerp_std(table[lo - 1], table[hi - 1], (df - float(lo)) / float(hi - lo));
 }
 
 // lookup_t_critical (main.cpp:188-231)

@@ -26,7 +26,7 @@ struct VarParams {
 // rpf::conservative_variance_update (core/stats.h:85-91)
 __device__ __forceinline__ float conservative_variance_update(float value, float neighbor, float stabilizer) {
     const float blend = fclamps(fmaxs(0.0f, neighbor - value) / fmaxs(1e-8f, value + neighbor + stabilizer), 0.0f, 1.0f);
-    return lerpf(value, neighbor, blend);
+    return lerp_std(value, neighbor, blend);
 }
 
 __global__ void k_var_smooth(PixelPlanes p, VarParams prm, const float* src, float* dst) {

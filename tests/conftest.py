@@ -67,3 +67,54 @@ def small_config(w: int, h: int, **kw) -> R.Config:
                 var_iterations=2, seed=1234)
     base.update(kw)
     return R.default_config(**base)
+
+
+# ---- golden fixtures (tests/golden/make_golden.py) ----------------------------------------
+
+def load_golden(name: str):
+    """(meta dict, arrays dict) of one fixture."""
+    import json
+
+    with np.load(GOLDEN / name) as z:
+        arrays = {k: z[k] for k in z.files}
+    return json.loads(str(arrays.pop("meta"))), arrays
+
+
+def golden_samples(arrays: dict, prefix: str, planes: list[str], n_pixels: int) -> "R.HostSamples":
+    """HostSamples rebuilt from the planes stored under `prefix`."""
+    hs = R.HostSamples.__new__(R.HostSamples)
+    hs.planes = {p: np.ascontiguousarray(arrays[prefix + p]) for p in planes}
+    hs.n_samples = int(hs.planes["flags"].shape[-1])
+    hs.n_pixels = n_pixels
+    return hs
+
+
+def golden_config(meta: dict) -> "R.Config":
+    return B.config_from(meta["config"])
+
+
+def replay_adaptive(job, cfg, arrays: dict, spp: int, extra_for_pass, on_counts=None) -> None:
+    """render()'s adaptive sequence (main.cpp:1543-1559 minus the final radiance swap): the
+    base pass, then per adaptive pass denoise, variance, counts, the pass's extra samples
+    (`extra_for_pass(p, counts)` returns HostSamples and the counts they were drawn with),
+    sensitivity; then the final sensitivity, denoise, variance and finalize."""
+    w, h = cfg.image_width, cfg.image_height
+    s0 = extra_for_pass(-1, None)[0]
+    job.begin_frame()
+    job.push(s0, 0, w * h, spp)
+    job.end_pass()
+    job.recompute_sensitivity()
+    for p in range(cfg.adaptive_passes):
+        job.statmc_denoise()
+        job.variance_denoise()
+        counts = job.compute_adaptive_sample_counts()
+        if on_counts:
+            on_counts(p, job, counts)
+        extra, used = extra_for_pass(p, counts)
+        job.push(extra, 0, w * h, 0, counts=used)
+        job.end_pass()
+        job.recompute_sensitivity()
+    job.recompute_sensitivity()
+    job.statmc_denoise()
+    job.variance_denoise()
+    job.finalize()
