@@ -41,21 +41,23 @@ METRIC = "denoised Msamples/s at 1080p 16spp (plain)"
 UNIT = "Msamples/s"
 
 
-def workload_config(R, w=W, h=H):
+def workload_config(R, w=None, h=None):
     # path_tracer/config/cornell.yaml stage knobs + the plain-method overrides
     return R.default_config(
-        image_width=w, image_height=h, rpf_tile_size=16, color_window_radius=5, color_normal_threshold=0.6,
+        image_width=W if w is None else w, image_height=H if h is None else h, rpf_tile_size=16, color_window_radius=5, color_normal_threshold=0.6,
         color_depth_threshold=0.2, color_compat_alpha=0.01, color_sigma_max=4.0, var_window_radius=3,
         var_normal_threshold=0.6, var_compat_sigma=3.0, var_shrinkage_k=0.7, var_iterations=2, adaptive_spp=4,
         adaptive_base_samples=2, adaptive_sigma_max=4.0, adaptive_passes=0, seed=SEED)
 
 
 def config_json(R, cfg, extra=None):
-    d = {"workload": "plain method, 1920x1080, 16 spp, synthetic per-sample FP32 buffers (seed 1234)",
+    plane_gb = W * H * SPP * 62 / 1e9
+    d = {"workload": f"plain method, {W}x{H}, {SPP} spp, synthetic per-sample FP32 buffers (seed {SEED})",
          "width": cfg.image_width, "height": cfg.image_height, "spp": SPP, "rpf_tile_size": cfg.rpf_tile_size,
          "color_window_radius": cfg.color_window_radius, "var_window_radius": cfg.var_window_radius,
          "var_iterations": cfg.var_iterations, "adaptive_passes": 0,
-         "l2": "inputs larger than L2 (2.06 GB of sample planes per step vs 129 MB L2)",
+         "l2": f"inputs larger than L2 ({plane_gb:.2f} GB of sample planes per step vs 129 MB L2)"
+               if plane_gb > 0.129 else "inputs smaller than L2: not a bench configuration",
          "parallelism": "replicas"}
     if extra:
         d.update(extra)
@@ -311,7 +313,7 @@ def measured_peaks():
 
 def cpu_baseline(args, steps=1, warmup=0):
     """The reference CPU path (the C restatement in oracle/) on this host's cores, on a
-    1920x270 band (a quarter of the frame) of the same workload."""
+    band of a quarter of the frame's rows (1920x270 at 1080p) of the same workload."""
     import rpd_gb300 as R
     from oracle import binding as B
 
@@ -331,7 +333,7 @@ def cpu_baseline(args, steps=1, warmup=0):
     job.close()
     sec = sum(times) / len(times)
     return {"value": round(W * band_h * SPP / sec / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"1920x{band_h} band, 16 spp ({W * band_h * SPP} samples) per step, {len(times)} step(s), "
+            "sample": f"{W}x{band_h} band, {SPP} spp ({W * band_h * SPP} samples) per step, {len(times)} step(s), "
                       f"{sec:.2f} s per step"}
 
 
@@ -352,6 +354,7 @@ def run_reference(args):
 
 
 def main():
+    global W, H, SPP, METRIC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -359,7 +362,14 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # a smaller frame of the same workload, for profiling captures (the bench line is 1080p16)
+    ap.add_argument("--width", type=int, default=W)
+    ap.add_argument("--height", type=int, default=H)
+    ap.add_argument("--spp", type=int, default=SPP)
     args = ap.parse_args()
+    if (args.width, args.height, args.spp) != (W, H, SPP):
+        W, H, SPP = args.width, args.height, args.spp
+        METRIC = f"denoised Msamples/s at {W}x{H} {SPP}spp (plain)"
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -205,7 +205,8 @@ typedef enum rpd_stage {
 typedef enum rpd_kernel {
     RPD_KERNEL_OFFSETS = 0,         /* per-pixel sample offsets of a push */
     RPD_KERNEL_ACCUMULATE_PIXELS,   /* Welford statistics + features */
-    RPD_KERNEL_GRID,                /* RPD grid accumulation */
+    RPD_KERNEL_GRID,                /* RPD grid: totals and screen bins */
+    RPD_KERNEL_GRID_RANDOM,         /* RPD grid: random-dimension bins */
     RPD_KERNEL_MERGE,               /* pass grid merge */
     RPD_KERNEL_FEATURES,            /* feature cache */
     RPD_KERNEL_NODE_STATS,          /* per-node sensitivities, confidences, features */

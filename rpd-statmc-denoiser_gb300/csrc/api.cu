@@ -932,7 +932,7 @@ int rpd_job_mark_elapsed(rpd_job* job, int a, int b, float* ms) {
 
 const char* rpd_kernel_name(rpd_kernel k) {
     static const char* names[RPD_KERNEL_COUNT_] = {
-        "offsets", "accumulate_pixels", "grid", "merge", "features", "node_stats", "node_combine",
+        "offsets", "accumulate_pixels", "grid", "grid_random", "merge", "features", "node_stats", "node_combine",
         "sens_pixels", "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other"};
     return (k >= 0 && k < RPD_KERNEL_COUNT_) ? names[k] : "unknown";
 }

@@ -173,8 +173,12 @@ __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, 
         }
     }
     if (fm & RPD_SAMPLE_PIXEL_VALID) {
-        // the screen position stays inside the pixel with a margin: fl(x + u) - x in
-        // [0, 1 - 2^-10], so every node's screen coordinate rounds into the same bin
+        // the screen position stays inside the pixel: with a power-of-two support 4 <= S <= 2^11
+        // the screen bin is floor(fl(fl(x + u) - left) / (S/4)) (the division and the x4 are
+        // power-of-two scalings; left is an integer), the pixel's own bin whenever
+        // f = fl(x + u) - x lies in [0, 1 - 2^-12]: fl(X - left) is exact for left >= 0, and for
+        // the first node row/column (left = -S/2, X + S/2 < 2^12) it moves by at most 2^-13
+        // (main.cpp:352-356, core/stats.h:166-167)
         const float jx = (fx + in.pu[0]) - fx, jy = (fy + in.pu[1]) - fy;
         if (!(jx >= 0.0f && jx <= kUniformMax && jy >= 0.0f && jy <= kUniformMax)) a.pflags &= uint8_t(~kPixUniform);
     } else if (fm & (RPD_SAMPLE_LENS_VALID | RPD_SAMPLE_BRDF_VALID | RPD_SAMPLE_LIGHT_VALID | RPD_SAMPLE_ENV_VALID |

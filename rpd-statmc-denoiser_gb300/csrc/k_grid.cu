@@ -14,10 +14,10 @@
 //     exactly as the reference bins them);
 //   * only the random-dimension bins are updated per sample, from the packed key the
 //     statistics pass wrote.
-// Phase A walks the node's support pixels (lanes over pixels); phase B walks the support's
-// samples (lanes over consecutive samples of each support row: coalesced loads). Each lane
-// owns private accumulators, combined across the warp at the end of each phase in a fixed
-// order: deterministic, no atomics. Sums of y are double-float (pairs of floats, exact
+// k_grid_fast walks the node's support pixels (lanes over pixels) for the totals and the
+// screen bins; k_grid_random walks the support's samples (lanes over consecutive samples of
+// each support row: coalesced loads) for the random-dimension bins. Each lane owns private
+// accumulators, combined in a fixed order at the end: deterministic, no atomics. Sums of y are double-float (pairs of floats, exact
 // products via FMA; about 2^-44 relative — GB300 executes double precision at 1/55 of its
 // single-precision rate). With a power-of-two node step every weight is an exact multiple
 // of 1/step^2, so the bin weights are accumulated as exact integers.
@@ -216,43 +216,66 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, dou
     const int cols = xhi - xlo + 1;
     const int npix = cols * (yhi - ylo + 1);
 
-    // ---- phase A: per-pixel class sums -> totals and (uniform pixels) screen bins ---------
+    // ---- per-pixel class sums -> totals and (uniform pixels) screen bins ------------------
     bins.clear();
     Totals tot_x, tot_s;
-    for (int q = lane; q < npix; q += 32) {
-        const int x = xlo + q % cols, y = ylo + q / cols;
-        const int64_t idx = int64_t(y) * g.w + x;
-        if (idx < gpar.first || idx >= gpar.first + gpar.count) continue;
-        const float w = axis_factor(gpar, x, nx, g.nodes_x) * axis_factor(gpar, y, ny, g.nodes_y);
-        if (w <= 1e-8f) continue;  // BinnedDependency::add skips (core/stats.h:103)
-        const float cnt = gp.cls[grp][0][idx];
-        if (cnt == 0.0f) continue;
-        const float s1h = gp.cls[grp][1][idx], s1l = gp.cls[grp][2][idx];
-        const float s2h = gp.cls[grp][3][idx], s2l = gp.cls[grp][4][idx];
-        const uint8_t pf = gp.pflags[idx];
-        const bool mixed = grp > 0 && (pf & kPixMixed);
-        add_class(tot_x, w, cnt, s1h, s1l, s2h, s2l);
-        if (!mixed) add_class(tot_s, w, cnt, s1h, s1l, s2h, s2l);
-        if (gpar.uniform_ok && (pf & kPixUniform) && !mixed) {
-            const float su0 = fclamps((float(x) - support_left) / support, 0.0f, 1.0f);
-            const float sv0 = fclamps((float(y) - support_top) / support, 0.0f, 1.0f);
-            const int b = bin2d(su0, sv0);
-            bins.add_weight(b, w, cnt);
-            bins.add_sum(b, w, s1h, s1l);
-            continue;
+    for (int q0 = 0; q0 < npix; q0 += 32) {
+        const int q = q0 + lane;
+        bool slow = false;
+        int x = 0, y = 0;
+        int64_t idx = 0;
+        float w = 0.0f;
+        bool mixed = false;
+        if (q < npix) {
+            x = xlo + q % cols;
+            y = ylo + q / cols;
+            idx = int64_t(y) * g.w + x;
+            if (idx >= gpar.first && idx < gpar.first + gpar.count) {
+                w = axis_factor(gpar, x, nx, g.nodes_x) * axis_factor(gpar, y, ny, g.nodes_y);
+                const float cnt = w > 1e-8f ? gp.cls[grp][0][idx] : 0.0f;  // core/stats.h:103 skips w <= 1e-8
+                if (cnt != 0.0f) {
+                    const float s1h = gp.cls[grp][1][idx], s1l = gp.cls[grp][2][idx];
+                    const float s2h = gp.cls[grp][3][idx], s2l = gp.cls[grp][4][idx];
+                    const uint8_t pf = gp.pflags[idx];
+                    mixed = grp > 0 && (pf & kPixMixed);
+                    add_class(tot_x, w, cnt, s1h, s1l, s2h, s2l);
+                    if (!mixed) add_class(tot_s, w, cnt, s1h, s1l, s2h, s2l);
+                    if (gpar.uniform_ok && (pf & kPixUniform) && !mixed) {
+                        const float su0 = fclamps((float(x) - support_left) / support, 0.0f, 1.0f);
+                        const float sv0 = fclamps((float(y) - support_top) / support, 0.0f, 1.0f);
+                        const int b = bin2d(su0, sv0);
+                        bins.add_weight(b, w, cnt);
+                        bins.add_sum(b, w, s1h, s1l);
+                    } else {
+                        slow = true;
+                    }
+                }
+            }
         }
-        // screen bins sample by sample (and screen_X totals of mixed pixels)
-        const int64_t local = idx - gpar.first;
-        for (int64_t k = offsets[local]; k < offsets[local + 1]; ++k) {
-            const uint32_t key = gp.key[k];
-            if (!(key & pbit) || !(key & vbit)) continue;
-            const float yv = gp.lum[k];
-            const float su = fclamps((float(x) + s.pixel_u[0][k] - support_left) / support, 0.0f, 1.0f);
-            const float sv = fclamps((float(y) + s.pixel_u[1][k] - support_top) / support, 0.0f, 1.0f);
-            const int b = bin2d(su, sv);
-            bins.add_weight(b, w, 1.0f);
-            bins.add_sum(b, w, yv, 0.0f);
-            if (mixed) add_sample(tot_s, w, yv);
+        // pixels binned sample by sample (and the screen_X totals of mixed pixels): the whole
+        // warp walks each such pixel's samples, every lane into its own bins
+        unsigned pending = __ballot_sync(0xffffffffu, slow);
+        while (pending) {
+            const int src = __ffs(pending) - 1;
+            pending &= pending - 1;
+            const int64_t pidx = __shfl_sync(0xffffffffu, idx, src);
+            const float pw = __shfl_sync(0xffffffffu, w, src);
+            const bool pmixed = __shfl_sync(0xffffffffu, int(mixed), src) != 0;
+            const float fx = float(__shfl_sync(0xffffffffu, x, src));
+            const float fy = float(__shfl_sync(0xffffffffu, y, src));
+            const int64_t local = pidx - gpar.first;
+            const int64_t kend = offsets[local + 1];
+            for (int64_t k = offsets[local] + lane; k < kend; k += 32) {
+                const uint32_t key = gp.key[k];
+                if (!(key & pbit) || !(key & vbit)) continue;
+                const float yv = gp.lum[k];
+                const float su = fclamps((fx + s.pixel_u[0][k] - support_left) / support, 0.0f, 1.0f);
+                const float sv = fclamps((fy + s.pixel_u[1][k] - support_top) / support, 0.0f, 1.0f);
+                const int b = bin2d(su, sv);
+                bins.add_weight(b, pw, 1.0f);
+                bins.add_sum(b, pw, yv, 0.0f);
+                if (pmixed) add_sample(tot_s, pw, yv);
+            }
         }
     }
     // screen bins and totals: `pixel` for group 0, screen_X (and X's totals) otherwise
@@ -260,79 +283,278 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, dou
     reduce_totals_into(tot_s, base + dep_s * kDepStride);
     if (grp == 0) return;
     reduce_totals_into(tot_x, base + dep_x * kDepStride);
+}
 
-    // ---- phase B: random-dimension bins, lanes over consecutive samples -------------------
-    bins.clear();
-    const int shift = grp == 6 ? 20 : key_bin_shift(grp);
-    const uint32_t mask = grp == 6 ? 1u : 15u;
-    // the columns this node draws from: x factor > 0
-    int xa = xhi + 1, xb = xlo - 1;
+// ---- random-dimension bins (Dependency2D::add / BinnedDependency::add of brdf, lens,
+// light_uv, environment, light_select and rr; main.cpp:356-375) --------------------------
+//
+// One block per node, NW warps splitting the node's support rows. A lane walks consecutive
+// samples of a row segment (coalesced key/luminance loads) and updates, for each sample, the
+// bins of all six random dimensions at once: the key, the luminance and the node weight are
+// read and formed once per sample. Every lane owns private bins in shared memory
+// ([slot][lane], conflict free); the block combines warps and lanes in a fixed order at the
+// end, so the result is deterministic.
+constexpr int kRandDims = 6;
+constexpr int kRandSlots = 5 * 16 + 2;  // brdf, lens, light_uv, environment, light_select; rr has 2 bins
+__host__ __device__ constexpr int rand_slot0(int d) { return d * 16; }
+// d: 0 brdf, 1 lens, 2 light_uv, 3 environment, 4 light_select, 5 rr (grid group d + 1)
+__host__ __device__ constexpr int rand_dep(int d) {
+    return d == 0 ? D_BRDF : d == 1 ? D_LENS : d == 2 ? D_LIGHT_UV : d == 3 ? D_ENV : d == 4 ? D_LIGHT_SELECT : D_RR;
+}
+constexpr uint32_t kRandValidMask = (0x3fu << 22);  // key valid bits of the six dimensions
+
+struct RandParams {
+    GridParams gp;
+    uint32_t spp_magic;  // floor(k / spp) == umulhi(k, magic) for every in-segment k (0: search)
+    int spp_shift;       // spp is 2^shift (-1: not a power of two)
+    int cols;            // support columns of a node, 2 * step + 3 (shared-memory tables)
+};
+
+template <bool INT_W>
+struct RandLayout {
+    // per warp: weights [kRandSlots][32] (u32 exact integers or float2 double-float), then
+    // sums [kRandSlots][32] float2
+    static constexpr int kWeightBytes = kRandSlots * 32 * (INT_W ? 4 : 8);
+    static constexpr int kWarpBytes = kWeightBytes + kRandSlots * 32 * 8;
+};
+
+template <bool INT_W, int NW>
+__global__ void __launch_bounds__(NW * 32) k_grid_random(RandParams rp, double* pass_grid, const int64_t* offsets,
+                                                         GridPrep gp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using L = RandLayout<INT_W>;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const GridParams& gpar = rp.gp;
+    const Geometry& g = gpar.g;
+    const int64_t node = blockIdx.x;
+    const int nx = int(node % g.nodes_x), ny = int(node / g.nodes_x);
+    unsigned char* wbase = smem_raw + warp * L::kWarpBytes;
+    uint32_t* wint = reinterpret_cast<uint32_t*>(wbase);
+    float2* wdf = reinterpret_cast<float2*>(wbase);
+    float2* sums = reinterpret_cast<float2*>(wbase + L::kWeightBytes);
+    // column factors of the support (x factor * step, exact for a power-of-two step), and the
+    // offsets of each warp's current row segment (varying counts)
+    int64_t* seg = reinterpret_cast<int64_t*>(smem_raw + NW * L::kWarpBytes);
+    int64_t* myseg = seg + warp * (rp.cols + 1);
+    float* xf = reinterpret_cast<float*>(seg + NW * (rp.cols + 1));
+
+    const int xlo = imaxs(0, (nx - 1) * g.step - 1), xhi = imins(g.w - 1, (nx + 1) * g.step + 1);
+    const int ylo = imaxs(0, (ny - 1) * g.step - 1), yhi = imins(g.h - 1, (ny + 1) * g.step + 1);
+    for (int c = threadIdx.x; c < rp.cols; c += NW * 32)
+        xf[c] = (xlo + c <= xhi) ? axis_factor(gpar, xlo + c, nx, g.nodes_x) : 0.0f;
+    for (int k = 0; k < kRandSlots; ++k) {
+        if (INT_W) wint[k * 32 + lane] = 0u;
+        else wdf[k * 32 + lane] = make_float2(0.0f, 0.0f);
+        sums[k * 32 + lane] = make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    int xa = xhi + 1, xb = xlo - 1;  // the columns with x factor > 0
     for (int x = xlo; x <= xhi; ++x)
-        if (axis_factor(gpar, x, nx, g.nodes_x) > 0.0f) {
+        if (xf[x - xlo] > 0.0f) {
             xa = imins(xa, x);
             xb = imaxs(xb, x);
         }
-    for (int y = ylo; y <= yhi; ++y) {
+    const float wscale = float(g.step) * float(g.step);
+    const float inv_wscale = 1.0f / wscale;
+
+    for (int y = ylo + warp; y <= yhi; y += NW) {
         const float ay = axis_factor(gpar, y, ny, g.nodes_y);
         if (ay <= 0.0f || xa > xb) continue;
         int64_t p0 = int64_t(y) * g.w + xa, p1 = int64_t(y) * g.w + xb + 1;
         p0 = p0 < gpar.first ? gpar.first : p0;
         p1 = p1 > gpar.first + gpar.count ? gpar.first + gpar.count : p1;
         if (p0 >= p1) continue;
-        const int64_t k0 = offsets[p0 - gpar.first], k1 = offsets[p1 - gpar.first];
-        const int xrow0 = int(p0 - int64_t(y) * g.w);
-        for (int64_t k = k0 + lane; k < k1; k += 32) {
-            const uint32_t key = gp.key[k];
-            if (!(key & vbit)) continue;
-            const float yv = gp.lum[k];
-            int64_t pl;  // the sample's pixel within the row segment
-            if (gpar.spp > 0) {
-                pl = int64_t(__float2int_rz((float(k - k0) + 0.5f) * gpar.inv_spp));
-            } else {
-                int64_t lo = 0, hi = p1 - p0 - 1;
-                while (lo < hi) {
-                    const int64_t mid = (lo + hi + 1) >> 1;
-                    if (offsets[p0 - gpar.first + mid] <= k) lo = mid; else hi = mid - 1;
-                }
-                pl = lo;
+        const int npx = int(p1 - p0);
+        const int64_t* off = offsets + (p0 - gpar.first);
+        if (rp.spp_magic == 0u && rp.spp_shift < 0) {
+            __syncwarp();
+            for (int q = lane; q <= npx; q += 32) myseg[q] = off[q];
+            __syncwarp();
+        }
+        const int64_t k0 = off[0], k1 = off[npx];
+        const int col0 = int(p0 - int64_t(y) * g.w) - xlo;  // xf index of the segment's first pixel
+        const int n = int(k1 - k0);
+        constexpr int U = 4;  // samples per lane in flight
+        for (int kb = lane; kb < n; kb += 32 * U) {
+            uint32_t keys[U];
+            float ys[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int kk = kb + 32 * u;
+                keys[u] = kk < n ? gp.key[k0 + kk] : 0u;
+                ys[u] = kk < n ? gp.lum[k0 + kk] : 0.0f;
             }
-            const float w = axis_factor(gpar, xrow0 + int(pl), nx, g.nodes_x) * ay;
-            if (w <= 1e-8f) continue;
-            const int rb = int((key >> shift) & mask);
-            bins.add_weight(rb, w, 1.0f);
-            bins.add_sum(rb, w, yv, 0.0f);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t key = keys[u];
+                if (!(key & kRandValidMask)) continue;
+                const int kk = kb + 32 * u;
+                int pl;
+                if (rp.spp_shift >= 0) {
+                    pl = kk >> rp.spp_shift;
+                } else if (rp.spp_magic) {
+                    pl = int(__umulhi(uint32_t(kk), rp.spp_magic));
+                } else {
+                    int lo = 0, hi = npx - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (myseg[mid] - k0 <= kk) lo = mid; else hi = mid - 1;
+                    }
+                    pl = lo;
+                }
+                const float w = xf[col0 + pl] * ay;
+                if (w <= 1e-8f) continue;  // BinnedDependency::add skips (core/stats.h:103)
+                const uint32_t iw = INT_W ? uint32_t(w * wscale) : 0u;
+                const float wy = w * ys[u];
+                const float wye = __fmaf_rn(w, ys[u], -wy);
+                // the six dimensions own disjoint slot ranges: load all, update, store all
+                int slot[kRandDims];
+                bool on[kRandDims];
+                uint32_t wi[kRandDims];
+                float2 wd[kRandDims], sy[kRandDims];
+#pragma unroll
+                for (int d = 0; d < kRandDims; ++d) {
+                    on[d] = (key & key_valid_bit(d + 1)) != 0;
+                    const uint32_t bin = (key >> (d == 5 ? 20 : key_bin_shift(d + 1))) & (d == 5 ? 1u : 15u);
+                    slot[d] = (rand_slot0(d) + int(bin)) * 32 + lane;
+                }
+#pragma unroll
+                for (int d = 0; d < kRandDims; ++d) {
+                    if (!on[d]) continue;
+                    if (INT_W) wi[d] = wint[slot[d]];
+                    else wd[d] = wdf[slot[d]];
+                    sy[d] = sums[slot[d]];
+                }
+#pragma unroll
+                for (int d = 0; d < kRandDims; ++d) {
+                    if (!on[d]) continue;
+                    if (INT_W) wi[d] += iw;
+                    else df_add(wd[d].x, wd[d].y, w);
+                    df_add(sy[d].x, sy[d].y, wy);
+                    sy[d].y += wye;
+                }
+#pragma unroll
+                for (int d = 0; d < kRandDims; ++d) {
+                    if (!on[d]) continue;
+                    if (INT_W) wint[slot[d]] = wi[d];
+                    else wdf[slot[d]] = wd[d];
+                    sums[slot[d]] = sy[d];
+                }
+            }
         }
     }
-    bins.reduce_into(base + dep_x * kDepStride);
+    __syncthreads();
+    // combine: thread t owns values v = t, t + NW*32, ... of [weights(kRandSlots), sums(kRandSlots)],
+    // summed over warps in order and over lanes in a rotated order (32 different banks)
+    for (int v = threadIdx.x; v < 2 * kRandSlots; v += NW * 32) {
+        const bool is_w = v < kRandSlots;
+        const int slot = is_w ? v : v - kRandSlots;
+        int d = 0;
+        while (d < kRandDims - 1 && slot >= rand_slot0(d + 1)) ++d;
+        const int bin = slot - rand_slot0(d);
+        double out;
+        if (is_w && INT_W) {
+            uint64_t total = 0;
+            for (int wi = 0; wi < NW; ++wi) {
+                const uint32_t* src = reinterpret_cast<const uint32_t*>(smem_raw + wi * L::kWarpBytes) + slot * 32;
+                for (int i = 0; i < 32; ++i) total += src[(i + v) & 31];
+            }
+            out = double(total) * double(inv_wscale);
+        } else {
+            // four interleaved double-float partial sums, then combined in a fixed order
+            float h[4] = {0.0f, 0.0f, 0.0f, 0.0f}, l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (int wi = 0; wi < NW; ++wi) {
+                const unsigned char* b = smem_raw + wi * L::kWarpBytes;
+                const float2* src = reinterpret_cast<const float2*>(is_w ? b : b + L::kWeightBytes) + slot * 32;
+                for (int i = 0; i < 32; i += 4) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const float2 q = src[(i + j + v) & 31];
+                        df_add(h[j], l[j], q.x);
+                        l[j] += q.y;
+                    }
+                }
+            }
+            for (int j = 1; j < 4; ++j) {
+                df_add(h[0], l[0], h[j]);
+                l[0] += l[j];
+            }
+            out = double(h[0]) + double(l[0]);
+        }
+        if (out != 0.0) pass_grid[(node * kDeps + rand_dep(d)) * kDepStride + (is_w ? bin : 16 + bin)] += out;
+    }
+}
+
+}  // namespace
+
+namespace {
+
+// floor(k / spp) through a multiply-high: magic = ceil(2^32 / spp), checked for every k a
+// row segment can hold (returns 0 when it does not hold, and the kernel searches instead)
+uint32_t spp_magic_for(int spp, int max_k) {
+    if (spp <= 0) return 0u;
+    const uint64_t m = ((uint64_t(1) << 32) + uint64_t(spp) - 1) / uint64_t(spp);
+    if (m > 0xffffffffull) return 0u;
+    for (int k = 0; k < max_k; ++k)
+        if (int((uint64_t(k) * m) >> 32) != k / spp) return 0u;
+    return uint32_t(m);
+}
+
+template <bool INT_W, int NW>
+cudaError_t launch_random(Job& j, const RandParams& rp, const GridPrep& gp) {
+    const size_t smem = size_t(NW) * RandLayout<INT_W>::kWarpBytes + size_t(NW) * (rp.cols + 1) * 8 +
+                        size_t(rp.cols) * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem));
+    if (e != cudaSuccess) return e;
+    k_grid_random<INT_W, NW><<<unsigned(j.g.nn), NW * 32, smem, j.stream>>>(rp, j.n.pass_grid, j.offsets, gp);
+    j.launches += 1;
+    return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int64_t count, const GridPrep& gp,
                              int32_t spp, int32_t max_count) {
-    KernelScope ks(j, RPD_KERNEL_GRID);
     const int step = j.g.step;
     const bool pow2 = (step & (step - 1)) == 0;
     GridParams gpar{j.g, first, count, 0, pow2 ? 1 : 0, 1.0f / float(step), spp, spp > 0 ? 1.0f / float(spp) : 0.0f};
     const int sup = j.g.support;
-    gpar.uniform_ok = (sup >= 4 && (sup & (sup - 1)) == 0) ? 1 : 0;
+    gpar.uniform_ok = (sup >= 4 && sup <= 2048 && (sup & (sup - 1)) == 0) ? 1 : 0;
     // exact integer bin weights need a power-of-two step and a per-bin total below 2^32:
     // at most support^2 pixels * max_count samples * step^2
     const double bound = double(sup + 3) * double(sup + 3) * double(std::max(max_count, 1)) * double(step) * double(step);
+    const bool int_w = pow2 && bound < 4.0e9;
     cudaError_t e;
-    if (pow2 && bound < 4.0e9) {
-        const size_t smem = size_t(kGroups) * LaneBins<true>::kSlots * 32 * sizeof(float);
-        e = cudaFuncSetAttribute(k_grid_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-        k_grid_fast<true><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, j.n.pass_grid, s, j.offsets, gp);
-    } else {
-        const size_t smem = size_t(kGroups) * LaneBins<false>::kSlots * 32 * sizeof(float);
-        e = cudaFuncSetAttribute(k_grid_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-        k_grid_fast<false><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, j.n.pass_grid, s, j.offsets, gp);
+    {
+        KernelScope ks(j, RPD_KERNEL_GRID);
+        if (int_w) {
+            const size_t smem = size_t(kGroups) * LaneBins<true>::kSlots * 32 * sizeof(float);
+            e = cudaFuncSetAttribute(k_grid_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if (e != cudaSuccess) return e;
+            k_grid_fast<true><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, j.n.pass_grid, s, j.offsets, gp);
+        } else {
+            const size_t smem = size_t(kGroups) * LaneBins<false>::kSlots * 32 * sizeof(float);
+            e = cudaFuncSetAttribute(k_grid_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if (e != cudaSuccess) return e;
+            k_grid_fast<false><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, j.n.pass_grid, s, j.offsets, gp);
+        }
+        j.launches += 1;
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    j.launches += 1;
-    return cudaGetLastError();
+    KernelScope ks(j, RPD_KERNEL_GRID_RANDOM);
+    RandParams rp{gpar, 0u, -1, 2 * step + 3};
+    if (spp > 0) {
+        if ((spp & (spp - 1)) == 0) {
+            int sh = 0;
+            while ((1 << sh) < spp) ++sh;
+            rp.spp_shift = sh;
+        } else {
+            rp.spp_magic = spp_magic_for(spp, (2 * step + 3) * spp);
+        }
+    }
+    return int_w ? launch_random<true, 2>(j, rp, gp) : launch_random<false, 2>(j, rp, gp);
 }
 
 }  // namespace rpd

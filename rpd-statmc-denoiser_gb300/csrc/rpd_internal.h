@@ -212,7 +212,7 @@ struct DeviceSamples {           // rpd_sample_soa with pointers in HBM
 // (hi, lo) and sum y^2 (hi, lo) over the pixel's finite samples.
 constexpr uint8_t kPixUniform = 0x1;  // every screen position lies inside its pixel
 constexpr uint8_t kPixMixed = 0x2;    // some sample has a random dimension but no screen position
-constexpr float kUniformMax = 1.0f - 1.0f / 1024.0f;
+constexpr float kUniformMax = 1.0f - 1.0f / 4096.0f;  // largest in-pixel offset of a uniform pixel
 __host__ __device__ constexpr uint8_t class_bit(int c) {
     return c == 0 ? RPD_SAMPLE_PIXEL_VALID : c == 1 ? RPD_SAMPLE_BRDF_VALID : c == 2 ? RPD_SAMPLE_LENS_VALID
          : c == 3 ? RPD_SAMPLE_LIGHT_VALID : c == 4 ? RPD_SAMPLE_ENV_VALID : c == 5 ? RPD_SAMPLE_LIGHT_SELECT_VALID

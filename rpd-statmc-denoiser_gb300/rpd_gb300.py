@@ -41,7 +41,7 @@ RGB_FIELDS = {"DENOISED", "RADIANCE_SUM", "NORMAL_SUM", "ALBEDO_SUM", "STATS_COL
               "STATS_SQRT_SQUARE_DIFF"}
 INT_FIELDS = {"HIT_COUNT", "SAMPLE_COUNT", "STATS_N", "ADAPTIVE_COUNTS"}
 STAGES = ["ACCUMULATE", "SENSITIVITY", "STATMC", "VARIANCE", "ADAPTIVE"]
-KERNELS = ["offsets", "accumulate_pixels", "grid", "merge", "features", "node_stats", "node_combine", "sens_pixels",
+KERNELS = ["offsets", "accumulate_pixels", "grid", "grid_random", "merge", "features", "node_stats", "node_combine", "sens_pixels",
            "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other"]
 STAGE = {name: i for i, name in enumerate(STAGES)}
 
