@@ -178,6 +178,8 @@ def run_gpu(args):
     dev = R.DeviceSamples(ctx, n, np_)
     ctx.synth_fill(params, 0, np_, SPP, dev)
     job = R.Job(ctx, cfg)
+    if args.grid_shape:
+        job.set_tuning("grid_shape", args.grid_shape)
 
     def step(samples):
         job.begin_frame()
@@ -366,6 +368,7 @@ def main():
     ap.add_argument("--width", type=int, default=W)
     ap.add_argument("--height", type=int, default=H)
     ap.add_argument("--spp", type=int, default=SPP)
+    ap.add_argument("--grid-shape", type=int, default=0, help="random-dimension grid launch shape 1..5 (0: default)")
     args = ap.parse_args()
     if (args.width, args.height, args.spp) != (W, H, SPP):
         W, H, SPP = args.width, args.height, args.spp

@@ -260,6 +260,13 @@ int rpd_job_set_config(rpd_job* job, const rpd_config* cfg);
 #define RPD_EXACT_GRID   0x1
 #define RPD_EXACT_WINDOW 0x2
 int rpd_job_set_exact(rpd_job* job, int flags);
+/* Launch-shape knobs (no counterpart in the reference; results do not depend on them).
+ * RPD_TUNE_GRID_SHAPE: warps per node of the random-dimension grid pass, as row groups x
+ * dimension sets: 1 = 2x1, 2 = 2x2, 3 = 2x3, 4 = 1x2, 5 = 1x3, 6 = 1x1 (default). More dimension sets
+ * keep fewer bins per warp (more resident warps) but walk the samples once per set. */
+#define RPD_TUNE_GRID_SHAPE 0
+int rpd_job_set_tuning(rpd_job* job, int knob, int value);
+int rpd_job_get_tuning(rpd_job* job, int knob, int* value);
 /* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */
 int rpd_job_begin_frame(rpd_job* job);
 

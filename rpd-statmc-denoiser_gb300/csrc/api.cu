@@ -523,6 +523,24 @@ int rpd_job_set_exact(rpd_job* job, int flags) {
     return RPD_OK;
 }
 
+int rpd_job_set_tuning(rpd_job* job, int knob, int value) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (knob != RPD_TUNE_GRID_SHAPE) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
+    if (value < 1 || value > 6) return fail(RPD_ERR_INVALID_ARGUMENT, "grid shape must be 1..6");
+    j->grid_shape = value;
+    return RPD_OK;
+}
+
+int rpd_job_get_tuning(rpd_job* job, int knob, int* value) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!value) return fail(RPD_ERR_INVALID_ARGUMENT, "null value");
+    if (knob != RPD_TUNE_GRID_SHAPE) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
+    *value = j->grid_shape;
+    return RPD_OK;
+}
+
 int rpd_job_begin_frame(rpd_job* job) {
     Job* j = reinterpret_cast<Job*>(job);
     CHECK_JOB(j);

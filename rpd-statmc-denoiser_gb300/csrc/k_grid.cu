@@ -288,20 +288,40 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, dou
 // ---- random-dimension bins (Dependency2D::add / BinnedDependency::add of brdf, lens,
 // light_uv, environment, light_select and rr; main.cpp:356-375) --------------------------
 //
-// One block per node, NW warps splitting the node's support rows. A lane walks consecutive
-// samples of a row segment (coalesced key/luminance loads) and updates, for each sample, the
-// bins of all six random dimensions at once: the key, the luminance and the node weight are
-// read and formed once per sample. Every lane owns private bins in shared memory
-// ([slot][lane], conflict free); the block combines warps and lanes in a fixed order at the
-// end, so the result is deterministic.
+// One block per node: RW row groups x DS dimension sets of warps. A warp walks the samples of
+// its row group's support rows as one flat stream (lanes over consecutive samples: coalesced,
+// 16-byte loads of 4 samples when possible) and updates, for each sample, the bins of the
+// dimensions of its set. Every lane owns private bins in shared memory ([slot][lane], conflict
+// free; a dimension the sample does not carry updates a per-lane trash slot instead, so the
+// update has no branches). The block combines row groups and lanes in a fixed order at the
+// end: deterministic, no atomics.
 constexpr int kRandDims = 6;
 constexpr int kRandSlots = 5 * 16 + 2;  // brdf, lens, light_uv, environment, light_select; rr has 2 bins
-__host__ __device__ constexpr int rand_slot0(int d) { return d * 16; }
 // d: 0 brdf, 1 lens, 2 light_uv, 3 environment, 4 light_select, 5 rr (grid group d + 1)
+__host__ __device__ constexpr int rand_slot0(int d) { return d * 16; }
 __host__ __device__ constexpr int rand_dep(int d) {
     return d == 0 ? D_BRDF : d == 1 ? D_LENS : d == 2 ? D_LIGHT_UV : d == 3 ? D_ENV : d == 4 ? D_LIGHT_SELECT : D_RR;
 }
+__host__ __device__ constexpr int rand_shift(int d) { return d == 5 ? 20 : key_bin_shift(d + 1); }
+__host__ __device__ constexpr uint32_t rand_mask(int d) { return d == 5 ? 1u : 15u; }
 constexpr uint32_t kRandValidMask = (0x3fu << 22);  // key valid bits of the six dimensions
+
+// The six dimensions split into DS sets (one warp of a row group each): fewer private bins per
+// warp (more resident warps) at the price of walking the samples once per set.
+template <int DS>
+__host__ __device__ constexpr int dim_set(int d) {
+    return DS == 1 ? 0 : DS == 2 ? ((d == 0 || d == 1 || d == 5) ? 0 : 1)
+                                 : ((d == 0 || d == 5) ? 0 : (d == 1 || d == 4) ? 1 : 2);
+}
+// first slot of dimension d within its set's region
+template <int DS>
+__host__ __device__ constexpr int dim_slot0(int d) {
+    return DS == 1 ? d * 16 : DS == 2 ? (d == 0 ? 0 : d == 1 ? 16 : d == 5 ? 32 : d == 2 ? 0 : d == 3 ? 16 : 32)
+                                      : ((d == 0 || d == 1 || d == 2) ? 0 : 16);
+}
+// slots of the largest set, plus the trash slot
+template <int DS>
+__host__ __device__ constexpr int set_slots() { return DS == 1 ? kRandSlots : DS == 2 ? 48 : 32; }
 
 struct RandParams {
     GridParams gp;
@@ -310,43 +330,243 @@ struct RandParams {
     int cols;            // support columns of a node, 2 * step + 3 (shared-memory tables)
 };
 
-template <bool INT_W>
+template <bool INT_W, int DS>
 struct RandLayout {
-    // per warp: weights [kRandSlots][32] (u32 exact integers or float2 double-float), then
-    // sums [kRandSlots][32] float2
-    static constexpr int kWeightBytes = kRandSlots * 32 * (INT_W ? 4 : 8);
-    static constexpr int kWarpBytes = kWeightBytes + kRandSlots * 32 * 8;
+    // per warp: weights [slots][32] (u32 exact integers or float2 double-float), then
+    // sums [slots][32] float2; slot kTrash absorbs the updates of absent dimensions
+    static constexpr int kTrash = set_slots<DS>();
+    static constexpr int kSlots = kTrash + 1;
+    static constexpr int kWeightBytes = kSlots * 32 * (INT_W ? 4 : 8);
+    static constexpr int kWarpBytes = kWeightBytes + kSlots * 32 * 8;
 };
 
-template <bool INT_W, int NW>
-__global__ void __launch_bounds__(NW * 32) k_grid_random(RandParams rp, double* pass_grid, const int64_t* offsets,
-                                                         GridPrep gp) {
+// Per-warp table of the row segments a warp walks (one chunk of up to 32 support rows).
+struct RowTable {
+    int64_t k0[32];    // first sample of the segment
+    int base[33];      // prefix of the segment lengths (flat sample index of the segment start)
+    int col0[32];      // column-factor index of the segment's first pixel
+    float ay[32];      // the row's y factor
+    int p0[32];        // first pixel of the segment, relative to the push (varying counts)
+    int npx[32];       // pixels in the segment
+};
+
+// Everything a warp's walk needs.
+template <bool INT_W, int DS>
+struct WalkCtx {
+    uint32_t* wint;
+    float2* wdf;
+    float2* sums;
+    RowTable* rt;
+    const float* xf;
+    int lane;
+    float wscale;
+};
+
+// One sample: add w (weights) and w*y (sums) to the bin of every dimension of set SET the
+// sample carries. Absent dimensions (and w <= 1e-8, which BinnedDependency::add skips,
+// core/stats.h:103) go to the trash slot with the same arithmetic.
+template <bool INT_W, int DS, int SET>
+__device__ __forceinline__ void rand_update(const WalkCtx<INT_W, DS>& c, uint32_t key, float w, uint32_t iw,
+                                            float y) {
+    using L = RandLayout<INT_W, DS>;
+    const bool wok = w > 1e-8f;
+    const float wy = w * y;
+    const float wye = __fmaf_rn(w, y, -wy);
+    int slot[kRandDims];
+    uint32_t wi[kRandDims];
+    float2 wd[kRandDims], sy[kRandDims];
+#pragma unroll
+    for (int d = 0; d < kRandDims; ++d) {
+        if (dim_set<DS>(d) != SET) continue;
+        const bool on = wok && (key & key_valid_bit(d + 1)) != 0;
+        const int bin = int((key >> rand_shift(d)) & rand_mask(d));
+        slot[d] = (on ? dim_slot0<DS>(d) + bin : L::kTrash) * 32 + c.lane;
+    }
+    // the dimensions own disjoint slot ranges (the trash slot is only ever a sink): load all,
+    // update, store all
+#pragma unroll
+    for (int d = 0; d < kRandDims; ++d) {
+        if (dim_set<DS>(d) != SET) continue;
+        if (INT_W) wi[d] = c.wint[slot[d]];
+        else wd[d] = c.wdf[slot[d]];
+        sy[d] = c.sums[slot[d]];
+    }
+#pragma unroll
+    for (int d = 0; d < kRandDims; ++d) {
+        if (dim_set<DS>(d) != SET) continue;
+        if (INT_W) wi[d] += iw;
+        else df_add(wd[d].x, wd[d].y, w);
+        df_add(sy[d].x, sy[d].y, wy);
+        sy[d].y += wye;
+    }
+#pragma unroll
+    for (int d = 0; d < kRandDims; ++d) {
+        if (dim_set<DS>(d) != SET) continue;
+        if (INT_W) c.wint[slot[d]] = wi[d];
+        else c.wdf[slot[d]] = wd[d];
+        c.sums[slot[d]] = sy[d];
+    }
+}
+
+// The flat walk of one row-segment chunk (total samples) for dimension set SET.
+template <bool INT_W, int DS, int SET, bool VEC>
+__device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const RandParams& rp, const GridPrep& gp,
+                                          const int64_t* offsets, int total) {
+    const RowTable* rt = c.rt;
+    const int lane = c.lane;
+    int r = 0;  // current segment of this lane (monotone along its walk)
+    if (VEC) {
+        // quads of 4 consecutive samples of one pixel (the samples per pixel are a power of two
+        // >= 4 and every segment starts 16-byte aligned): one 16-byte load of keys and one of
+        // luminances per quad, 2 quads per lane in flight
+        constexpr int U = 2;
+        const int nq = total >> 2;
+        auto fetchq = [&](int q, uint4& kq, float4& yq, float& w) {
+            kq = make_uint4(0u, 0u, 0u, 0u);
+            yq = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            w = 0.0f;
+            if (q >= nq) return;
+            const int t = q << 2;
+            while (t >= rt->base[r + 1]) ++r;
+            const int kk = t - rt->base[r];
+            const int64_t k = rt->k0[r] + kk;
+            kq = *reinterpret_cast<const uint4*>(gp.key + k);
+            yq = *reinterpret_cast<const float4*>(gp.lum + k);
+            w = c.xf[rt->col0[r] + (kk >> rp.spp_shift)] * rt->ay[r];
+        };
+        uint4 nk[U];
+        float4 nyv[U];
+        float nw[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) fetchq(lane + 32 * u, nk[u], nyv[u], nw[u]);
+        for (int q0 = 0; q0 < nq; q0 += 32 * U) {
+            uint4 ck[U];
+            float4 cy[U];
+            float cw[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                ck[u] = nk[u];
+                cy[u] = nyv[u];
+                cw[u] = nw[u];
+            }
+            if (q0 + 32 * U < nq) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) fetchq(q0 + 32 * U + lane + 32 * u, nk[u], nyv[u], nw[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t iw = INT_W ? uint32_t(cw[u] * c.wscale) : 0u;
+                rand_update<INT_W, DS, SET>(c, ck[u].x, cw[u], iw, cy[u].x);
+                rand_update<INT_W, DS, SET>(c, ck[u].y, cw[u], iw, cy[u].y);
+                rand_update<INT_W, DS, SET>(c, ck[u].z, cw[u], iw, cy[u].z);
+                rand_update<INT_W, DS, SET>(c, ck[u].w, cw[u], iw, cy[u].w);
+            }
+        }
+    } else {
+        constexpr int U = 4;  // samples per lane in flight
+        auto fetch = [&](int t, uint32_t& key, float& y, float& w) {
+            key = 0u;
+            y = 0.0f;
+            w = 0.0f;
+            if (t >= total) return;
+            while (t >= rt->base[r + 1]) ++r;
+            const int kk = t - rt->base[r];
+            const int64_t k = rt->k0[r] + kk;
+            key = gp.key[k];
+            y = gp.lum[k];
+            int pl;
+            if (rp.spp_shift >= 0) {
+                pl = kk >> rp.spp_shift;
+            } else if (rp.spp_magic) {
+                pl = int(__umulhi(uint32_t(kk), rp.spp_magic));
+            } else {
+                const int64_t* off = offsets + rt->p0[r];
+                int lo = 0, hi = rt->npx[r] - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (off[mid] <= k) lo = mid; else hi = mid - 1;
+                }
+                pl = lo;
+            }
+            w = c.xf[rt->col0[r] + pl] * rt->ay[r];
+        };
+        uint32_t nk[U];
+        float nyv[U], nw[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) fetch(lane + 32 * u, nk[u], nyv[u], nw[u]);
+        for (int t0 = 0; t0 < total; t0 += 32 * U) {
+            uint32_t ck[U];
+            float cy[U], cw[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                ck[u] = nk[u];
+                cy[u] = nyv[u];
+                cw[u] = nw[u];
+            }
+            if (t0 + 32 * U < total) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) fetch(t0 + 32 * U + lane + 32 * u, nk[u], nyv[u], nw[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                rand_update<INT_W, DS, SET>(c, ck[u], cw[u], INT_W ? uint32_t(cw[u] * c.wscale) : 0u, cy[u]);
+        }
+    }
+}
+
+template <bool INT_W, int RW, int DS, bool VEC>
+__global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, double* pass_grid,
+                                                              const int64_t* offsets, GridPrep gp) {
+    constexpr int NW = RW * DS;
+    constexpr int VPT = (2 * kRandSlots + NW * 32 - 1) / (NW * 32);  // combined values per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using L = RandLayout<INT_W>;
+    using L = RandLayout<INT_W, DS>;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    const int dset = warp % DS;     // the dimension set of this warp
+    const int rgroup = warp / DS;   // its row group
     const GridParams& gpar = rp.gp;
     const Geometry& g = gpar.g;
     const int64_t node = blockIdx.x;
     const int nx = int(node % g.nodes_x), ny = int(node / g.nodes_x);
     unsigned char* wbase = smem_raw + warp * L::kWarpBytes;
-    uint32_t* wint = reinterpret_cast<uint32_t*>(wbase);
-    float2* wdf = reinterpret_cast<float2*>(wbase);
-    float2* sums = reinterpret_cast<float2*>(wbase + L::kWeightBytes);
-    // column factors of the support (x factor * step, exact for a power-of-two step), and the
-    // offsets of each warp's current row segment (varying counts)
-    int64_t* seg = reinterpret_cast<int64_t*>(smem_raw + NW * L::kWarpBytes);
-    int64_t* myseg = seg + warp * (rp.cols + 1);
-    float* xf = reinterpret_cast<float*>(seg + NW * (rp.cols + 1));
+    WalkCtx<INT_W, DS> c;
+    c.wint = reinterpret_cast<uint32_t*>(wbase);
+    c.wdf = reinterpret_cast<float2*>(wbase);
+    c.sums = reinterpret_cast<float2*>(wbase + L::kWeightBytes);
+    c.rt = reinterpret_cast<RowTable*>(smem_raw + NW * L::kWarpBytes) + warp;
+    float* xf = reinterpret_cast<float*>(reinterpret_cast<RowTable*>(smem_raw + NW * L::kWarpBytes) + NW);
+    c.xf = xf;
+    c.lane = lane;
+    c.wscale = float(g.step) * float(g.step);
+    RowTable* rt = c.rt;
 
+    // the grid entries this thread adds to at the end, read now so the loads overlap the walk
+    double prev[VPT];
+    int64_t gidx[VPT];
+#pragma unroll
+    for (int vi = 0; vi < VPT; ++vi) {
+        const int v = threadIdx.x + vi * NW * 32;
+        gidx[vi] = -1;
+        prev[vi] = 0.0;
+        if (v < 2 * kRandSlots) {
+            const bool is_w = v < kRandSlots;
+            const int gslot = is_w ? v : v - kRandSlots;
+            int d = 0;
+            while (d < kRandDims - 1 && gslot >= rand_slot0(d + 1)) ++d;
+            const int bin = gslot - rand_slot0(d);
+            gidx[vi] = (node * kDeps + rand_dep(d)) * kDepStride + (is_w ? bin : 16 + bin);
+            prev[vi] = pass_grid[gidx[vi]];
+        }
+    }
     const int xlo = imaxs(0, (nx - 1) * g.step - 1), xhi = imins(g.w - 1, (nx + 1) * g.step + 1);
     const int ylo = imaxs(0, (ny - 1) * g.step - 1), yhi = imins(g.h - 1, (ny + 1) * g.step + 1);
-    for (int c = threadIdx.x; c < rp.cols; c += NW * 32)
-        xf[c] = (xlo + c <= xhi) ? axis_factor(gpar, xlo + c, nx, g.nodes_x) : 0.0f;
-    for (int k = 0; k < kRandSlots; ++k) {
-        if (INT_W) wint[k * 32 + lane] = 0u;
-        else wdf[k * 32 + lane] = make_float2(0.0f, 0.0f);
-        sums[k * 32 + lane] = make_float2(0.0f, 0.0f);
+    for (int col = threadIdx.x; col < rp.cols; col += NW * 32)
+        xf[col] = (xlo + col <= xhi) ? axis_factor(gpar, xlo + col, nx, g.nodes_x) : 0.0f;
+    for (int k = 0; k < L::kSlots; ++k) {
+        if (INT_W) c.wint[k * 32 + lane] = 0u;
+        else c.wdf[k * 32 + lane] = make_float2(0.0f, 0.0f);
+        c.sums[k * 32 + lane] = make_float2(0.0f, 0.0f);
     }
     __syncthreads();
     int xa = xhi + 1, xb = xlo - 1;  // the columns with x factor > 0
@@ -355,134 +575,101 @@ __global__ void __launch_bounds__(NW * 32) k_grid_random(RandParams rp, double* 
             xa = imins(xa, x);
             xb = imaxs(xb, x);
         }
-    const float wscale = float(g.step) * float(g.step);
-    const float inv_wscale = 1.0f / wscale;
+    const int nrows = (yhi - ylo) / RW + 1;  // rows ylo + rgroup + RW * j
 
-    for (int y = ylo + warp; y <= yhi; y += NW) {
-        const float ay = axis_factor(gpar, y, ny, g.nodes_y);
-        if (ay <= 0.0f || xa > xb) continue;
-        int64_t p0 = int64_t(y) * g.w + xa, p1 = int64_t(y) * g.w + xb + 1;
-        p0 = p0 < gpar.first ? gpar.first : p0;
-        p1 = p1 > gpar.first + gpar.count ? gpar.first + gpar.count : p1;
-        if (p0 >= p1) continue;
-        const int npx = int(p1 - p0);
-        const int64_t* off = offsets + (p0 - gpar.first);
-        if (rp.spp_magic == 0u && rp.spp_shift < 0) {
-            __syncwarp();
-            for (int q = lane; q <= npx; q += 32) myseg[q] = off[q];
-            __syncwarp();
-        }
-        const int64_t k0 = off[0], k1 = off[npx];
-        const int col0 = int(p0 - int64_t(y) * g.w) - xlo;  // xf index of the segment's first pixel
-        const int n = int(k1 - k0);
-        constexpr int U = 4;  // samples per lane in flight
-        for (int kb = lane; kb < n; kb += 32 * U) {
-            uint32_t keys[U];
-            float ys[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int kk = kb + 32 * u;
-                keys[u] = kk < n ? gp.key[k0 + kk] : 0u;
-                ys[u] = kk < n ? gp.lum[k0 + kk] : 0.0f;
+    for (int c0 = 0; c0 < nrows; c0 += 32) {
+        // ---- this chunk's row segments, one lane per row ----
+        const int y = ylo + rgroup + RW * (c0 + lane);
+        int n = 0;
+        if (c0 + lane < nrows && y <= yhi && xa <= xb) {
+            const float ay = axis_factor(gpar, y, ny, g.nodes_y);
+            int64_t p0 = int64_t(y) * g.w + xa, p1 = int64_t(y) * g.w + xb + 1;
+            p0 = p0 < gpar.first ? gpar.first : p0;
+            p1 = p1 > gpar.first + gpar.count ? gpar.first + gpar.count : p1;
+            if (ay > 0.0f && p0 < p1) {
+                const int64_t k0 = offsets[p0 - gpar.first];
+                n = int(offsets[p1 - gpar.first] - k0);
+                rt->k0[lane] = k0;
+                rt->col0[lane] = int(p0 - int64_t(y) * g.w) - xlo;
+                rt->ay[lane] = ay;
+                rt->p0[lane] = int(p0 - gpar.first);
+                rt->npx[lane] = int(p1 - p0);
             }
+        }
+        int incl = n;  // inclusive scan of the segment lengths
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += v;
+        }
+        rt->base[lane + 1] = incl;
+        if (lane == 0) rt->base[0] = 0;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        if (dset == 0) rand_walk<INT_W, DS, 0, VEC>(c, rp, gp, offsets, total);
+        if (DS > 1 && dset == 1) rand_walk<INT_W, DS, 1, VEC>(c, rp, gp, offsets, total);
+        if (DS > 2 && dset == 2) rand_walk<INT_W, DS, 2, VEC>(c, rp, gp, offsets, total);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // combine: thread t owns values v = t + vi * NW*32 of [weights(kRandSlots), sums(kRandSlots)],
+    // each summed over the row groups in order and over the 32 lanes in a rotated order
+    // (32 different banks), two interleaved double-float chains per value
+    int vslot[VPT], vset[VPT];
+    bool vw[VPT];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const uint32_t key = keys[u];
-                if (!(key & kRandValidMask)) continue;
-                const int kk = kb + 32 * u;
-                int pl;
-                if (rp.spp_shift >= 0) {
-                    pl = kk >> rp.spp_shift;
-                } else if (rp.spp_magic) {
-                    pl = int(__umulhi(uint32_t(kk), rp.spp_magic));
+    for (int vi = 0; vi < VPT; ++vi) {
+        const int v = threadIdx.x + vi * NW * 32;
+        const bool is_w = v < kRandSlots;
+        const int gslot = is_w ? v : v - kRandSlots;
+        int d = 0;
+        while (d < kRandDims - 1 && gslot >= rand_slot0(d + 1)) ++d;
+        vslot[vi] = dim_slot0<DS>(d) + (gslot - rand_slot0(d));
+        vset[vi] = dim_set<DS>(d);
+        vw[vi] = is_w;
+    }
+    uint64_t itot[VPT];
+    float h[VPT][2], l[VPT][2];
+#pragma unroll
+    for (int vi = 0; vi < VPT; ++vi) {
+        itot[vi] = 0;
+        h[vi][0] = h[vi][1] = l[vi][0] = l[vi][1] = 0.0f;
+    }
+    for (int rg = 0; rg < RW; ++rg) {
+        for (int i = 0; i < 32; i += 2) {
+#pragma unroll
+            for (int vi = 0; vi < VPT; ++vi) {
+                if (gidx[vi] < 0) continue;
+                const unsigned char* b = smem_raw + (rg * DS + vset[vi]) * L::kWarpBytes;
+                const int v = threadIdx.x + vi * NW * 32;
+                if (vw[vi] && INT_W) {
+                    const uint32_t* src = reinterpret_cast<const uint32_t*>(b) + vslot[vi] * 32;
+                    itot[vi] += uint64_t(src[(i + v) & 31]) + uint64_t(src[(i + 1 + v) & 31]);
                 } else {
-                    int lo = 0, hi = npx - 1;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (myseg[mid] - k0 <= kk) lo = mid; else hi = mid - 1;
+                    const float2* src =
+                        reinterpret_cast<const float2*>(vw[vi] ? b : b + L::kWeightBytes) + vslot[vi] * 32;
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const float2 q = src[(i + j + v) & 31];
+                        df_add(h[vi][j], l[vi][j], q.x);
+                        l[vi][j] += q.y;
                     }
-                    pl = lo;
-                }
-                const float w = xf[col0 + pl] * ay;
-                if (w <= 1e-8f) continue;  // BinnedDependency::add skips (core/stats.h:103)
-                const uint32_t iw = INT_W ? uint32_t(w * wscale) : 0u;
-                const float wy = w * ys[u];
-                const float wye = __fmaf_rn(w, ys[u], -wy);
-                // the six dimensions own disjoint slot ranges: load all, update, store all
-                int slot[kRandDims];
-                bool on[kRandDims];
-                uint32_t wi[kRandDims];
-                float2 wd[kRandDims], sy[kRandDims];
-#pragma unroll
-                for (int d = 0; d < kRandDims; ++d) {
-                    on[d] = (key & key_valid_bit(d + 1)) != 0;
-                    const uint32_t bin = (key >> (d == 5 ? 20 : key_bin_shift(d + 1))) & (d == 5 ? 1u : 15u);
-                    slot[d] = (rand_slot0(d) + int(bin)) * 32 + lane;
-                }
-#pragma unroll
-                for (int d = 0; d < kRandDims; ++d) {
-                    if (!on[d]) continue;
-                    if (INT_W) wi[d] = wint[slot[d]];
-                    else wd[d] = wdf[slot[d]];
-                    sy[d] = sums[slot[d]];
-                }
-#pragma unroll
-                for (int d = 0; d < kRandDims; ++d) {
-                    if (!on[d]) continue;
-                    if (INT_W) wi[d] += iw;
-                    else df_add(wd[d].x, wd[d].y, w);
-                    df_add(sy[d].x, sy[d].y, wy);
-                    sy[d].y += wye;
-                }
-#pragma unroll
-                for (int d = 0; d < kRandDims; ++d) {
-                    if (!on[d]) continue;
-                    if (INT_W) wint[slot[d]] = wi[d];
-                    else wdf[slot[d]] = wd[d];
-                    sums[slot[d]] = sy[d];
                 }
             }
         }
     }
-    __syncthreads();
-    // combine: thread t owns values v = t, t + NW*32, ... of [weights(kRandSlots), sums(kRandSlots)],
-    // summed over warps in order and over lanes in a rotated order (32 different banks)
-    for (int v = threadIdx.x; v < 2 * kRandSlots; v += NW * 32) {
-        const bool is_w = v < kRandSlots;
-        const int slot = is_w ? v : v - kRandSlots;
-        int d = 0;
-        while (d < kRandDims - 1 && slot >= rand_slot0(d + 1)) ++d;
-        const int bin = slot - rand_slot0(d);
-        double out;
-        if (is_w && INT_W) {
-            uint64_t total = 0;
-            for (int wi = 0; wi < NW; ++wi) {
-                const uint32_t* src = reinterpret_cast<const uint32_t*>(smem_raw + wi * L::kWarpBytes) + slot * 32;
-                for (int i = 0; i < 32; ++i) total += src[(i + v) & 31];
-            }
-            out = double(total) * double(inv_wscale);
-        } else {
-            // four interleaved double-float partial sums, then combined in a fixed order
-            float h[4] = {0.0f, 0.0f, 0.0f, 0.0f}, l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            for (int wi = 0; wi < NW; ++wi) {
-                const unsigned char* b = smem_raw + wi * L::kWarpBytes;
-                const float2* src = reinterpret_cast<const float2*>(is_w ? b : b + L::kWeightBytes) + slot * 32;
-                for (int i = 0; i < 32; i += 4) {
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const float2 q = src[(i + j + v) & 31];
-                        df_add(h[j], l[j], q.x);
-                        l[j] += q.y;
-                    }
-                }
-            }
-            for (int j = 1; j < 4; ++j) {
-                df_add(h[0], l[0], h[j]);
-                l[0] += l[j];
-            }
-            out = double(h[0]) + double(l[0]);
+    for (int vi = 0; vi < VPT; ++vi) {
+        if (gidx[vi] < 0) continue;
+        double out;
+        if (vw[vi] && INT_W) {
+            out = double(itot[vi]) / double(c.wscale);
+        } else {
+            df_add(h[vi][0], l[vi][0], h[vi][1]);
+            l[vi][0] += l[vi][1];
+            out = double(h[vi][0]) + double(l[vi][0]);
         }
-        if (out != 0.0) pass_grid[(node * kDeps + rand_dep(d)) * kDepStride + (is_w ? bin : 16 + bin)] += out;
+        if (out != 0.0) pass_grid[gidx[vi]] = prev[vi] + out;
     }
 }
 
@@ -501,16 +688,39 @@ uint32_t spp_magic_for(int spp, int max_k) {
     return uint32_t(m);
 }
 
-template <bool INT_W, int NW>
-cudaError_t launch_random(Job& j, const RandParams& rp, const GridPrep& gp) {
-    const size_t smem = size_t(NW) * RandLayout<INT_W>::kWarpBytes + size_t(NW) * (rp.cols + 1) * 8 +
+template <bool INT_W, int RW, int DS, bool VEC>
+cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) {
+    constexpr int NW = RW * DS;
+    const size_t smem = size_t(NW) * RandLayout<INT_W, DS>::kWarpBytes + size_t(NW) * sizeof(RowTable) +
                         size_t(rp.cols) * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem));
+    cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, RW, DS, VEC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    k_grid_random<INT_W, NW><<<unsigned(j.g.nn), NW * 32, smem, j.stream>>>(rp, j.n.pass_grid, j.offsets, gp);
+    k_grid_random<INT_W, RW, DS, VEC><<<unsigned(j.g.nn), NW * 32, smem, j.stream>>>(rp, j.n.pass_grid, j.offsets,
+                                                                                     gp);
     j.launches += 1;
     return cudaGetLastError();
+}
+
+// quads need samples per pixel a multiple of 4 (and a power of two, for the shift) with
+// 16-byte aligned key and luminance planes
+template <bool INT_W, int RW, int DS>
+cudaError_t launch_random(Job& j, const RandParams& rp, const GridPrep& gp) {
+    const bool vec = rp.spp_shift >= 2 && (reinterpret_cast<uintptr_t>(gp.key) & 15u) == 0 &&
+                     (reinterpret_cast<uintptr_t>(gp.lum) & 15u) == 0;
+    return vec ? launch_random_vec<INT_W, RW, DS, true>(j, rp, gp) : launch_random_vec<INT_W, RW, DS, false>(j, rp, gp);
+}
+
+template <bool INT_W>
+cudaError_t launch_random_shape(Job& j, const RandParams& rp, const GridPrep& gp, int shape) {
+    switch (shape) {
+    case 1: return launch_random<INT_W, 2, 1>(j, rp, gp);
+    case 2: return launch_random<INT_W, 2, 2>(j, rp, gp);
+    case 3: return launch_random<INT_W, 2, 3>(j, rp, gp);
+    case 4: return launch_random<INT_W, 1, 2>(j, rp, gp);
+    case 5: return launch_random<INT_W, 1, 3>(j, rp, gp);
+    default: return launch_random<INT_W, 1, 1>(j, rp, gp);
+    }
 }
 
 }  // namespace
@@ -554,7 +764,7 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
             rp.spp_magic = spp_magic_for(spp, (2 * step + 3) * spp);
         }
     }
-    return int_w ? launch_random<true, 2>(j, rp, gp) : launch_random<false, 2>(j, rp, gp);
+    return int_w ? launch_random_shape<true>(j, rp, gp, j.grid_shape) : launch_random_shape<false>(j, rp, gp, j.grid_shape);
 }
 
 }  // namespace rpd

@@ -138,6 +138,7 @@ struct Job {
     int64_t offsets_cap = 0;
     bool exact_grid = false;     // RPD_EXACT_GRID: double-precision grid in the reference's order
     bool exact_window = false;   // RPD_EXACT_WINDOW: double-precision StatMC window
+    int grid_shape = 6;          // launch shape of the random-dimension grid pass (row groups x dimension sets)
     bool pass_open = false;
     bool features_valid = false;
     bool cache_valid = false;

@@ -226,6 +226,8 @@ def lib() -> C.CDLL:
         "rpd_job_destroy": (None, [vp]),
         "rpd_job_set_config": (C.c_int, [vp, C.POINTER(Config)]),
         "rpd_job_set_exact": (C.c_int, [vp, C.c_int]),
+        "rpd_job_set_tuning": (C.c_int, [vp, C.c_int, C.c_int]),
+        "rpd_job_get_tuning": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
         "rpd_job_begin_frame": (C.c_int, [vp]),
         "rpd_job_push_samples": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp, C.c_int]),
         "rpd_job_end_pass": (C.c_int, [vp]),
@@ -270,6 +272,7 @@ def exported_symbols() -> list[str]:
     """Names declared in include/rpd_gb300.h that the library must export."""
     return ["rpd_config_defaults", "rpd_config_validate", "rpd_ctx_create", "rpd_ctx_destroy", "rpd_job_footprint",
             "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config", "rpd_job_set_exact",
+            "rpd_job_set_tuning", "rpd_job_get_tuning",
             "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_end_pass", "rpd_recompute_sensitivity",
             "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
             "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
@@ -458,6 +461,16 @@ class Job:
 
     def set_exact(self, grid: bool = False, window: bool = False) -> None:
         check(lib().rpd_job_set_exact(self.handle, (1 if grid else 0) | (2 if window else 0)))
+
+    TUNING = {"grid_shape": 0}
+
+    def set_tuning(self, knob: str, value: int) -> None:
+        check(lib().rpd_job_set_tuning(self.handle, self.TUNING[knob], int(value)))
+
+    def get_tuning(self, knob: str) -> int:
+        v = C.c_int()
+        check(lib().rpd_job_get_tuning(self.handle, self.TUNING[knob], C.byref(v)))
+        return v.value
 
     def begin_frame(self) -> None:
         check(lib().rpd_job_begin_frame(self.handle))

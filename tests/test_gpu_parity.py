@@ -262,3 +262,21 @@ def test_plain_256x256_4spp(gpu_ctx):
     s = B.synth_fill(R.synth_params(w, h, 1234, miss_regions=3), 0, w * h, spp)
     g, o = run_both(gpu_ctx, cfg, s, spp, threads=1)
     check_pipeline(g, o, exact_grid=False)
+
+
+@pytest.mark.parametrize("shape", [1, 2, 3, 4, 5, 6])
+def test_grid_launch_shapes_agree(gpu_ctx, shape):
+    """Every launch shape of the random-dimension grid pass gives the oracle's grid (the
+    shapes change only the order of the double-float sums)."""
+    w, h, spp = 50, 34, 6
+    cfg = small_config(w, h, rpf_tile_size=8)
+    s = B.synth_fill(R.synth_params(w, h, 5, miss_regions=2), 0, w * h, spp)
+    g = R.Job(gpu_ctx, cfg)
+    g.set_tuning("grid_shape", shape)
+    assert g.get_tuning("grid_shape") == shape
+    o = B.OracleJob(cfg, threads=1)
+    for job in (g, o):
+        B.run_pipeline(job, s, spp)
+    check_pipeline(g, o, exact_grid=False)
+    g.close()
+    o.close()
