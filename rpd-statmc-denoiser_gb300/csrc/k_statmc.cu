@@ -237,25 +237,35 @@ __global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcPara
 
 // ---- fast tiled path ----------------------------------------------------------------------
 
-enum TileField {
-    F_NX = 0, F_NY, F_NZ, F_D, F_AX, F_AY, F_AZ, F_SM0, F_SM1, F_SM2, F_SV0, F_SV1, F_SV2,
-    F_A0, F_A1, F_A2, F_N, F_CM0, F_CM1, F_CM2, F_VM, F_R0, F_R1, F_R2, F_R3, F_R4, F_R5, F_COUNT
-};
+// Halo tile planes, float4 per pixel (structure of float4 arrays: a warp reading 32
+// neighbours at one offset reads 512 contiguous bytes, conflict free):
+//   P_GATE (nx, ny, nz, depth)         normal / depth gates
+//   P_ALB  (ax, ay, az, n)             albedo gate, sample count (as float)
+//   P_SM   (sqrt mean rgb, rpd[4])     Welch means
+//   P_SV   (sqrt var stable rgb, rpd[5]) Welch variances
+//   P_A    (sv^2 / (n - 1) rgb, var of the mean)
+//   P_RPD  (rpd[0..3])
+//   P_CM   (colour mean rgb, 0)
+enum TilePlane { P_GATE = 0, P_ALB, P_SM, P_SV, P_A, P_RPD, P_CM, P_COUNT };
 
 constexpr int kTileX = 32;
 constexpr float kBand = 1.0f / 32768.0f;          // 2^-15 relative guard band
 constexpr float kQAccept = 5.991464547107979f;     // 2 ln 20: exp(-q/2) > 0.05
 constexpr double kWsBand = 1.0 / 65536.0;          // guard band of weight_sum >= 1.1
+constexpr float kDepthBand = 1.0f / 1048576.0f;    // 2^-20: depth quotient decided by a product
 
-__device__ __forceinline__ float tile_t_lookup(const float* table, float df, const StatmcParams& prm) {
+// t critical value of the fast path. The table branch interpolates (tab[lo-1], tab[lo]) with
+// lo = round(df - 1/2) taken from the float's bits (df in [1, 30.5): no conversion unit); at
+// an integer df this may pick the lower cell with fraction 1, the same value to an ulp. The
+// pairs hold (tab[i], tab[i+1] - tab[i]) and (tab[29], 0), so df in [30, 30.5) gives tab[29]
+// as lookup_t_critical does.
+__device__ __forceinline__ float tile_t_lookup(const float2* pairs, float df, const StatmcParams& prm) {
     df = fmaxf(df, 1.0f);
     if (prm.table < 2 && df < 30.5f) {
-        const float lo_f = floorf(df);
-        const int lo = iclamps(int(lo_f), 1, 30);
-        const int hi = iclamps(int(ceilf(df)), 1, 30);
-        const float a = table[lo - 1];
-        if (lo == hi) return a;
-        return __fmaf_rn(table[hi - 1] - a, df - float(lo), a);
+        const float fl = (df - 0.5f) + 12582912.0f;  // 1.5 * 2^23: integer part in the low bits
+        const int lo = imaxs(__float_as_int(fl) - 0x4B400000, 1);
+        const float2 ab = pairs[lo - 1];
+        return __fmaf_rn(ab.y, df - float(lo), ab.x);
     }
     float z = prm.z;
     if (df < 30.0f) z = z * sqrtf(__fdividef(df, fmaxf(1.0f, df - 1.0f)));
@@ -263,47 +273,51 @@ __device__ __forceinline__ float tile_t_lookup(const float* table, float df, con
 }
 
 __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcParams prm) {
-    extern __shared__ float smem[];
+    extern __shared__ float4 smem4[];
     const int r = prm.r;
     const int tw = kTileX + 2 * r, th = prm.by + 2 * r;
     const int tn = tw * th;
-    float* T = smem;                       // F_COUNT planes of tn floats
-    float* table = smem + F_COUNT * tn;    // 32 floats of the active t table
+    const int side = 2 * r + 1;
+    float4* T = smem4;                                                  // P_COUNT planes of tn
+    float2* pairs = reinterpret_cast<float2*>(smem4 + P_COUNT * tn);    // 32 t-table pairs
+    float* spatial_tab = reinterpret_cast<float*>(pairs + 32);          // side * side
     const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * prm.by;
     const int tid = threadIdx.y * kTileX + threadIdx.x;
     const int nthreads = kTileX * prm.by;
 
-    if (tid < 32) table[tid] = tid < 30 ? (prm.table == 0 ? c_t05[tid] : c_t01[tid]) : 0.0f;
+    if (tid < 32) {
+        const float* tab = prm.table == 0 ? c_t05 : c_t01;
+        pairs[tid] = tid < 29 ? make_float2(tab[tid], tab[tid + 1] - tab[tid])
+                              : make_float2(tid == 29 ? tab[29] : 0.0f, 0.0f);
+    }
+    for (int e = tid; e < side * side; e += nthreads) {
+        const int dx = e % side - r, dy = e / side - r;
+        spatial_tab[e] = __frcp_rn(1.0f + float(dx * dx + dy * dy));  // 1 / (1 + d^2), main.cpp:1096
+    }
     for (int e = tid; e < tn; e += nthreads) {
         const int gx = x0 - r + e % tw, gy = y0 - r + e / tw;
         bool inside = gx >= 0 && gx < prm.w && gy >= 0 && gy < prm.h;
         const int64_t q = inside ? int64_t(gy) * prm.w + gx : 0;
         const bool hit = inside && p.hit_count[q] > 0;
         // a neighbour outside the image or without a primary hit fails the normal gate
-        T[F_NX * tn + e] = hit ? p.f_normal[0][q] : 0.0f;
-        T[F_NY * tn + e] = hit ? p.f_normal[1][q] : 0.0f;
-        T[F_NZ * tn + e] = hit ? p.f_normal[2][q] : 0.0f;
+        T[P_GATE * tn + e] = make_float4(hit ? p.f_normal[0][q] : 0.0f, hit ? p.f_normal[1][q] : 0.0f,
+                                         hit ? p.f_normal[2][q] : 0.0f, inside ? p.f_depth[q] : 0.0f);
         if (!inside) continue;
-        T[F_D * tn + e] = p.f_depth[q];
-        T[F_AX * tn + e] = p.f_albedo[0][q];
-        T[F_AY * tn + e] = p.f_albedo[1][q];
-        T[F_AZ * tn + e] = p.f_albedo[2][q];
         const int n_raw = p.n[q];
         const int nj = imaxs(1, n_raw);
         float var = pixel_variance(p.square_diff[q], n_raw);
         if (!isfinite(var)) var = 1e-8f;
         var = fclamps(var, 1e-8f, prm.var2_max);
         const float nm1 = fmaxf(float(nj - 1), 1.0f);
-        for (int c = 0; c < 3; ++c) {
-            const float sv = p.sqrt_var_stable[c][q];
-            T[(F_SM0 + c) * tn + e] = p.sqrt_mean[c][q];
-            T[(F_SV0 + c) * tn + e] = sv;
-            T[(F_A0 + c) * tn + e] = __fdividef(sv * sv, nm1);
-            T[(F_CM0 + c) * tn + e] = p.color_mean[c][q];
-        }
-        T[F_N * tn + e] = float(nj);
-        T[F_VM * tn + e] = fmaxs(1e-8f, var / float(nj));
-        for (int c = 0; c < 6; ++c) T[(F_R0 + c) * tn + e] = p.rpd[c][q];
+        float sv[3];
+        for (int c = 0; c < 3; ++c) sv[c] = p.sqrt_var_stable[c][q];
+        T[P_ALB * tn + e] = make_float4(p.f_albedo[0][q], p.f_albedo[1][q], p.f_albedo[2][q], float(nj));
+        T[P_SM * tn + e] = make_float4(p.sqrt_mean[0][q], p.sqrt_mean[1][q], p.sqrt_mean[2][q], p.rpd[4][q]);
+        T[P_SV * tn + e] = make_float4(sv[0], sv[1], sv[2], p.rpd[5][q]);
+        T[P_A * tn + e] = make_float4(__fdividef(sv[0] * sv[0], nm1), __fdividef(sv[1] * sv[1], nm1),
+                                      __fdividef(sv[2] * sv[2], nm1), fmaxs(1e-8f, var / float(nj)));
+        T[P_RPD * tn + e] = make_float4(p.rpd[0][q], p.rpd[1][q], p.rpd[2][q], p.rpd[3][q]);
+        T[P_CM * tn + e] = make_float4(p.color_mean[0][q], p.color_mean[1][q], p.color_mean[2][q], 0.0f);
     }
     __syncthreads();
 
@@ -318,19 +332,11 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
         return;
     }
     const int ei = (threadIdx.y + r) * tw + threadIdx.x + r;
-    const float ni0 = T[F_NX * tn + ei], ni1 = T[F_NY * tn + ei], ni2 = T[F_NZ * tn + ei];
-    const float di = T[F_D * tn + ei];
-    const float ai0 = T[F_AX * tn + ei], ai1 = T[F_AY * tn + ei], ai2 = T[F_AZ * tn + ei];
-    float smi[3], svi[3], Ai[3];
-    for (int c = 0; c < 3; ++c) {
-        smi[c] = T[(F_SM0 + c) * tn + ei];
-        svi[c] = T[(F_SV0 + c) * tn + ei];
-        Ai[c] = T[(F_A0 + c) * tn + ei];
-    }
-    const float nif = T[F_N * tn + ei];
+    const float4 gi = T[P_GATE * tn + ei], ali = T[P_ALB * tn + ei];
+    const float4 smi4 = T[P_SM * tn + ei], svi4 = T[P_SV * tn + ei], ai4 = T[P_A * tn + ei], ri4 = T[P_RPD * tn + ei];
+    const float smi[3] = {smi4.x, smi4.y, smi4.z}, svi[3] = {svi4.x, svi4.y, svi4.z};
+    const float nif = ali.w;
     const int n_i = int(nif);
-    float rpd_i[6];
-    for (int c = 0; c < 6; ++c) rpd_i[c] = T[(F_R0 + c) * tn + ei];
     {
         // the debug planes (main.cpp:1021-1023)
         const int n_raw = p.n[idx];
@@ -343,7 +349,7 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
         p.var_ratio[idx] = (var_i > 1e-8f) ? (vm * float(n_i)) / var_i : 0.0f;
     }
     const float dthr = prm.depth_threshold;
-    const float dabs_i = fabsf(di);
+    const float dabs_i = fabsf(gi.w);
 
     // double-float accumulators across rows: colour (3), weight, weight^2, weight^2*var
     float acc_hi[6] = {0, 0, 0, 0, 0, 0}, acc_lo[6] = {0, 0, 0, 0, 0, 0};
@@ -351,73 +357,85 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
     for (int dy = -r; dy <= r; ++dy) {
         float row[6] = {0, 0, 0, 0, 0, 0};
         const int erow = (threadIdx.y + r + dy) * tw + threadIdx.x + r;
+        const float* srow = spatial_tab + (dy + r) * side + r;
         for (int dx = -r; dx <= r; ++dx) {
             const int e = erow + dx;
-            const float nj0 = T[F_NX * tn + e], nj1 = T[F_NY * tn + e], nj2 = T[F_NZ * tn + e];
-            if (dot3(ni0, ni1, ni2, nj0, nj1, nj2) < prm.normal_threshold) continue;
-            // relative_depth_delta(di, dj) > threshold, decided exactly
-            const float dj = T[F_D * tn + e];
+            const float4 gj = T[P_GATE * tn + e];
+            if (dot3(gi.x, gi.y, gi.z, gj.x, gj.y, gj.z) < prm.normal_threshold) continue;
+            // relative_depth_delta(di, dj) > threshold: fl(num / m) against dthr, decided by
+            // the product dthr * m away from the threshold and by the IEEE quotient near it
             float m = dabs_i;
-            if (m < fabsf(dj)) m = fabsf(dj);
+            if (m < fabsf(gj.w)) m = fabsf(gj.w);
             if (m < 1e-8f) m = 1e-8f;
-            const float num = fabsf(di - dj);
-            const float approx = __fdividef(num, m);
+            const float num = fabsf(gi.w - gj.w);
+            const float tm = dthr * m;
             bool far;
-            if (fabsf(approx - dthr) <= dthr * (1.0f / 1048576.0f) + 1e-30f) far = __fdiv_rn(num, m) > dthr;
-            else far = approx > dthr;
+            if (!(tm >= 1e-30f)) far = __fdiv_rn(num, m) > dthr;  // tiny or zero threshold: no product test
+            else if (num > tm * (1.0f + kDepthBand)) far = true;
+            else if (num < tm * (1.0f - kDepthBand)) far = false;
+            else far = __fdiv_rn(num, m) > dthr;
             if (far) continue;
-            const float da0 = ai0 - T[F_AX * tn + e], da1 = ai1 - T[F_AY * tn + e], da2 = ai2 - T[F_AZ * tn + e];
+            const float4 aj = T[P_ALB * tn + e];
+            const float da0 = ali.x - aj.x, da1 = ali.y - aj.y, da2 = ali.z - aj.z;
             if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) continue;
 
-            const float njf = T[F_N * tn + e];
+            const float4 smj = T[P_SM * tn + e], svj = T[P_SV * tn + e], aaj = T[P_A * tn + e];
+            const float njf = aj.w;
             bool exact = false;
-            float qmax = 0.0f;
-            for (int c = 0; c < 3; ++c) {
-                const float vj = T[(F_SV0 + c) * tn + e];
-                const float vs = svi[c] + vj;
-                const float md = smi[c] - T[(F_SM0 + c) * tn + e];
-                const float t2 = __fdividef(md * md, vs);
-                const float den = Ai[c] + T[(F_A0 + c) * tn + e];
-                exact |= fabsf(den - 1e-8f) <= 1e-8f * kBand;
-                const float df = den > 1e-8f ? __fdividef(vs * vs, den) : nif + njf - 2.0f;
-                exact |= fabsf(df - prm.df_break) <= prm.df_break * kBand;
-                const float tc = tile_t_lookup(table, df, prm);
-                qmax = fmaxf(qmax, __fdividef(t2, tc * tc));
+            // per channel t^2 / t_crit^2 = md^2 / (vs * tc^2); the largest is found by cross
+            // products and divided once, together with the RPD relaxation
+            float qn = 0.0f, qd = 1.0f;
+            {
+                const float sj[3] = {smj.x, smj.y, smj.z}, vj[3] = {svj.x, svj.y, svj.z};
+                const float aj3[3] = {aaj.x, aaj.y, aaj.z}, ai3[3] = {ai4.x, ai4.y, ai4.z};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float vs = svi[c] + vj[c];
+                    const float md = smi[c] - sj[c];
+                    const float den = ai3[c] + aj3[c];
+                    exact |= fabsf(den - 1e-8f) <= 1e-8f * kBand;
+                    const float df = den > 1e-8f ? __fdividef(vs * vs, den) : nif + njf - 2.0f;
+                    exact |= fabsf(df - prm.df_break) <= prm.df_break * kBand;
+                    const float tc = tile_t_lookup(pairs, df, prm);
+                    const float n2 = md * md, d2 = vs * tc * tc;
+                    if (n2 * qd > qn * d2) {
+                        qn = n2;
+                        qd = d2;
+                    }
+                }
             }
-            float shared = 0.0f;
-            for (int c = 0; c < 6; ++c) shared = fmaxs(shared, fmins(rpd_i[c], T[(F_R0 + c) * tn + e]));
+            const float4 rj = T[P_RPD * tn + e];
+            float shared = fmaxs(fmaxs(fmins(ri4.x, rj.x), fmins(ri4.y, rj.y)),
+                                 fmaxs(fmins(ri4.z, rj.z), fmins(ri4.w, rj.w)));
+            shared = fmaxs(shared, fmaxs(fmins(smi4.w, smj.w), fmins(svi4.w, svj.w)));
             shared = fclamps(shared, 0.0f, 1.0f);
             const float adjustment = fclamps(prm.rpd_scale * shared, 0.0f, 1.0f);
-            const float q = __fdividef(qmax, 1.0f + adjustment);
+            const float q = __fdividef(qn, qd * (1.0f + adjustment));
             const bool center = dx == 0 && dy == 0;
             exact |= fabsf(q - 25.0f) <= 25.0f * kBand;
             exact |= !center && fabsf(q - kQAccept) <= kQAccept * kBand;
-            const float spatial = __frcp_rn(1.0f + float(dx * dx + dy * dy));
             float wj;
             if (exact) {
-                float svj[3], smj[3];
-                for (int c = 0; c < 3; ++c) {
-                    svj[c] = T[(F_SV0 + c) * tn + e];
-                    smj[c] = T[(F_SM0 + c) * tn + e];
-                }
-                const double qd = exact_q(svi, smi, n_i, svj, smj, int(njf), prm.alpha, adjustment);
-                if (qd > 25.0) continue;
+                const float sjx[3] = {smj.x, smj.y, smj.z}, vjx[3] = {svj.x, svj.y, svj.z};
+                const double qx = exact_q(svi, smi, n_i, vjx, sjx, int(njf), prm.alpha, adjustment);
+                if (qx > 25.0) continue;
                 const double sw = 1.0 / (1.0 + double(dx * dx + dy * dy));
-                const double wd = sw * exp(-0.5 * qd);
+                const double wd = sw * exp(-0.5 * qx);
                 if (!center && wd > 0.05 * sw) ++accepted;
                 wj = float(wd);
             } else {
                 if (q > 25.0f) continue;
                 if (!center && q < kQAccept) ++accepted;
-                wj = spatial * __expf(-0.5f * q);
+                wj = srow[dx] * __expf(-0.5f * q);
             }
+            const float4 cmj = T[P_CM * tn + e];
             const float w2 = wj * wj;
-            row[0] = __fmaf_rn(wj, T[F_CM0 * tn + e], row[0]);
-            row[1] = __fmaf_rn(wj, T[F_CM1 * tn + e], row[1]);
-            row[2] = __fmaf_rn(wj, T[F_CM2 * tn + e], row[2]);
+            row[0] = __fmaf_rn(wj, cmj.x, row[0]);
+            row[1] = __fmaf_rn(wj, cmj.y, row[1]);
+            row[2] = __fmaf_rn(wj, cmj.z, row[2]);
             row[3] += wj;
             row[4] += w2;
-            row[5] = __fmaf_rn(w2, T[F_VM * tn + e], row[5]);
+            row[5] = __fmaf_rn(w2, aaj.w, row[5]);
         }
         for (int k = 0; k < 6; ++k) {  // TwoSum into the double-float accumulators
             const float s = acc_hi[k] + row[k];
@@ -437,8 +455,9 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
         exact_pixel(p, prm, idx);
         return;
     }
-    const float var_mean_i = T[F_VM * tn + ei];
-    const float cmi[3] = {T[F_CM0 * tn + ei], T[F_CM1 * tn + ei], T[F_CM2 * tn + ei]};
+    const float var_mean_i = ai4.w;
+    const float4 cmi4 = T[P_CM * tn + ei];
+    const float cmi[3] = {cmi4.x, cmi4.y, cmi4.z};
     float mean_nb[3] = {cmi[0], cmi[1], cmi[2]};
     double var_neighbors = double(var_mean_i);
     if (weight_sum > double(1e-8f)) {
@@ -475,7 +494,9 @@ float sqrt_gate_threshold(float t) {
 }
 
 size_t tile_bytes(int r, int by) {
-    return (size_t(kTileX + 2 * r) * size_t(by + 2 * r) * F_COUNT + 32) * sizeof(float);
+    const size_t side = size_t(2 * r + 1);
+    return size_t(kTileX + 2 * r) * size_t(by + 2 * r) * P_COUNT * sizeof(float4) + 32 * sizeof(float2) +
+           side * side * sizeof(float);
 }
 
 }  // namespace
