@@ -1,0 +1,111 @@
+// A clone of the reference's render() StatMC sequence (path_tracer/main.cpp:1543-1564) written
+// against include/rpd_statmc.hpp: the four stage functions keep their reference names and
+// signatures, and the per-sample accumulation becomes pushes of synthetic samples.
+//
+//   render_clone W H SPP PASSES   -> prints the mean denoised value and the adaptive total
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "rpd_statmc.hpp"
+#include "rpd_synth.h"
+
+// The RenderConfig fields the stage reads, named as in path_tracer/core/config.h:15-49.
+struct RenderConfig {
+    int image_width = 64, image_height = 48;
+    int rpf_tile_size = 16, color_window_radius = 5;
+    float color_normal_threshold = 0.6f, color_depth_threshold = 0.2f, color_compat_alpha = 0.01f;
+    float color_sigma_max = 4.0f;
+    int var_window_radius = 3;
+    float var_normal_threshold = 0.6f, var_depth_threshold = 0.25f, var_compat_sigma = 3.0f, var_shrinkage_k = 0.7f;
+    int var_iterations = 2, adaptive_base_samples = 1, adaptive_spp = 4;
+    float adaptive_sigma_max = 4.0f;
+    int adaptive_passes = 2, adaptive_importance_smoothing_radius = 1;
+    float rpf_shrinkage_scale = 1.0f, rpf_confidence_samples = 128.0f;
+    bool debug_statmc_outputs = false;
+};
+
+struct HostPlanes {
+    std::vector<float> f[18];
+    std::vector<uint8_t> flags, category;
+    rpd_sample_soa soa{};
+    HostPlanes(int64_t n_samples, int64_t n_pixels) {
+        for (auto& v : f) v.resize(size_t(n_samples));
+        f[17].resize(size_t(n_pixels) * 3);
+        flags.resize(size_t(n_samples));
+        category.resize(size_t(n_samples));
+        int k = 0;
+        for (int c = 0; c < 3; ++c) soa.radiance[c] = f[k++].data();
+        for (int c = 0; c < 3; ++c) soa.normal[c] = f[k++].data();
+        soa.depth = f[k++].data();
+        for (int c = 0; c < 2; ++c) soa.pixel_u[c] = f[k++].data();
+        for (int c = 0; c < 2; ++c) soa.lens_u[c] = f[k++].data();
+        for (int c = 0; c < 2; ++c) soa.brdf_u[c] = f[k++].data();
+        for (int c = 0; c < 2; ++c) soa.light_u[c] = f[k++].data();
+        for (int c = 0; c < 3; ++c) soa.pixel_albedo[c] = f[17].data() + size_t(c) * size_t(n_pixels);
+        soa.flags = flags.data();
+        soa.category = category.data();
+    }
+};
+
+int main(int argc, char** argv) {
+    RenderConfig config;
+    int spp = 4;
+    if (argc > 3) {
+        config.image_width = std::atoi(argv[1]);
+        config.image_height = std::atoi(argv[2]);
+        spp = std::atoi(argv[3]);
+    }
+    if (argc > 4) config.adaptive_passes = std::atoi(argv[4]);
+    const int w = config.image_width, h = config.image_height;
+    const int64_t np = int64_t(w) * h;
+    try {
+        rpd::Context ctx(0, 0);
+        rpd::current_seed() = 1234;
+        rpd::Job job(ctx, rpd::to_rpd_config(config, rpd::current_seed()));
+        rpd::set_current_job(&job);
+        rpd_synth_params prm;
+        rpd_synth_defaults(&prm, w, h, 1234);
+
+        // render_image_statmc (main.cpp:649-737): the first pass
+        job.begin_frame();
+        {
+            HostPlanes s(np * spp, np);
+            rpd::check(rpd_synth_fill(ctx.get(), &prm, 0, np, spp, nullptr, nullptr, &s.soa, RPD_MEM_HOST));
+            job.push(s.soa, 0, np, spp);
+        }
+        job.end_pass();
+        rpd::recompute_sensitivity(config);
+        std::vector<int32_t> n_so_far(size_t(np), spp);
+        int64_t adaptive_total = 0;
+        for (int i = 0; i < config.adaptive_passes && config.adaptive_spp > 0; ++i) {  // main.cpp:1547-1552
+            rpd::statmc_denoise(config);
+            rpd::variance_denoise(config);
+            std::vector<int> counts = rpd::compute_adaptive_sample_counts(config);
+            int64_t extra = 0;
+            for (int c : counts) extra += c;
+            adaptive_total += extra;
+            HostPlanes s(extra, np);  // render_image_adaptive (main.cpp:1451-1538)
+            rpd::check(rpd_synth_fill(ctx.get(), &prm, 0, np, 0, counts.data(), n_so_far.data(), &s.soa,
+                                      RPD_MEM_HOST));
+            job.push(s.soa, 0, np, 0, counts.data());
+            job.end_pass();
+            for (int64_t p = 0; p < np; ++p) n_so_far[size_t(p)] += counts[size_t(p)];
+            rpd::recompute_sensitivity(config);
+        }
+        rpd::recompute_sensitivity(config);
+        rpd::statmc_denoise(config);
+        rpd::variance_denoise(config);
+        job.finalize();
+        const std::vector<float> den = job.read<float>(RPD_FIELD_DENOISED);
+        double mean = 0.0;
+        for (float v : den) mean += v;
+        mean /= double(den.size());
+        std::printf("denoised_mean %.9g adaptive_total %lld\n", mean, (long long)adaptive_total);
+        rpd::set_current_job(nullptr);
+    } catch (const rpd::Error& e) {
+        std::fprintf(stderr, "rpd error %d: %s\n", e.status, e.what());
+        return 1;
+    }
+    return 0;
+}
