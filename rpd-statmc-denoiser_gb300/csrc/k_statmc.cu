@@ -86,25 +86,50 @@ __global__ void k_sqrt_var_mean(PixelPlanes p, int64_t np) {
     }
 }
 
-__global__ void k_sqrt_var_stable(PixelPlanes p, int w, int h) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= int64_t(w) * h) return;
-    const int cy = int(i / w), cx = int(i % w);
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, weight_sum = 0.0;
-    for (int dy = -1; dy <= 1; ++dy) {
-        const int y = iclamps(cy + dy, 0, h - 1);
-        for (int dx = -1; dx <= 1; ++dx) {
-            const int x = iclamps(cx + dx, 0, w - 1);
-            const double weight = 1.0 / (1.0 + double(dx * dx + dy * dy));
-            const int64_t q = int64_t(y) * w + x;
-            a0 += double(p.sqrt_var_mean[0][q]) * weight;
-            a1 += double(p.sqrt_var_mean[1][q]) * weight;
-            a2 += double(p.sqrt_var_mean[2][q]) * weight;
-            weight_sum += weight;
+// sample_vec3_local_average (main.cpp:170-184) of the sqrt variance of the mean, then the
+// component max (981-990). The reference accumulates in double: v * weight with weights 1/3
+// (corners, 1.0 / 3.0 rounded), 1/2 and 1 (both exact), nine additions in (dy, dx) order, one
+// division by the summed weights. A 32 x 8 block stages, per pixel of its (clamped) 34 x 10 halo,
+// the three products each channel can need (v, v * 0.5, v * (1.0 / 3.0)) in double once, so a
+// pixel pays only its nine additions and the division on GB300's slow double pipe.
+constexpr int kSvTx = 32, kSvTy = 8;
+__global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p, int w, int h, double weight_sum) {
+    __shared__ double tile[3][3][(kSvTy + 2) * (kSvTx + 2)];  // [channel][v, v/2, v/3][pixel]
+    const int tw = kSvTx + 2, tn = (kSvTy + 2) * (kSvTx + 2);
+    const int x0 = blockIdx.x * kSvTx, y0 = blockIdx.y * kSvTy;
+    const int tid = threadIdx.y * kSvTx + threadIdx.x;
+    const double third = 1.0 / (1.0 + 2.0);
+    for (int e = tid; e < tn; e += kSvTx * kSvTy) {
+        const int gx = iclamps(x0 - 1 + e % tw, 0, w - 1), gy = iclamps(y0 - 1 + e / tw, 0, h - 1);
+        const int64_t q = int64_t(gy) * w + gx;
+        for (int c = 0; c < 3; ++c) {
+            const double v = double(p.sqrt_var_mean[c][q]);
+            tile[c][0][e] = v;
+            tile[c][1][e] = v * 0.5;
+            tile[c][2][e] = v * third;
         }
     }
-    const float avg[3] = {float(a0 / weight_sum), float(a1 / weight_sum), float(a2 / weight_sum)};
-    for (int c = 0; c < 3; ++c) p.sqrt_var_stable[c][i] = fmaxs(p.sqrt_var_mean[c][i], avg[c]);
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const int64_t i = int64_t(y) * w + x;
+    const int e = (threadIdx.y + 1) * tw + threadIdx.x + 1;
+    for (int c = 0; c < 3; ++c) {
+        const double* t1 = tile[c][0];
+        const double* th = tile[c][1];
+        const double* tt = tile[c][2];
+        double a = 0.0;
+        a += tt[e - tw - 1];
+        a += th[e - tw];
+        a += tt[e - tw + 1];
+        a += th[e - 1];
+        a += t1[e];
+        a += th[e + 1];
+        a += tt[e + tw - 1];
+        a += th[e + tw];
+        a += tt[e + tw + 1];
+        p.sqrt_var_stable[c][i] = fmaxs(p.sqrt_var_mean[c][i], float(a / weight_sum));
+    }
 }
 
 struct StatmcParams {
@@ -240,7 +265,8 @@ __global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcPara
 // Halo tile planes, float4 per pixel (structure of float4 arrays: a warp reading 32
 // neighbours at one offset reads 512 contiguous bytes, conflict free):
 //   P_GATE (nx, ny, nz, depth)         normal / depth gates
-//   P_ALB  (ax, ay, az, n)             albedo gate, sample count (as float)
+//   P_ALB  (ax, ay, az, n)             albedo gate, sample count as float (0: outside the
+//                                      image or no primary hit, which the reference skips)
 //   P_SM   (sqrt mean rgb, rpd[4])     Welch means
 //   P_SV   (sqrt var stable rgb, rpd[5]) Welch variances
 //   P_A    (sv^2 / (n - 1) rgb, var of the mean)
@@ -299,10 +325,12 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
         bool inside = gx >= 0 && gx < prm.w && gy >= 0 && gy < prm.h;
         const int64_t q = inside ? int64_t(gy) * prm.w + gx : 0;
         const bool hit = inside && p.hit_count[q] > 0;
-        // a neighbour outside the image or without a primary hit fails the normal gate
-        T[P_GATE * tn + e] = make_float4(hit ? p.f_normal[0][q] : 0.0f, hit ? p.f_normal[1][q] : 0.0f,
-                                         hit ? p.f_normal[2][q] : 0.0f, inside ? p.f_depth[q] : 0.0f);
-        if (!inside) continue;
+        T[P_GATE * tn + e] = hit ? make_float4(p.f_normal[0][q], p.f_normal[1][q], p.f_normal[2][q], p.f_depth[q])
+                                 : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!hit) {
+            T[P_ALB * tn + e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            continue;
+        }
         const int n_raw = p.n[q];
         const int nj = imaxs(1, n_raw);
         float var = pixel_variance(p.square_diff[q], n_raw);
@@ -362,6 +390,8 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
             const int e = erow + dx;
             const float4 gj = T[P_GATE * tn + e];
             if (dot3(gi.x, gi.y, gi.z, gj.x, gj.y, gj.z) < prm.normal_threshold) continue;
+            const float4 aj = T[P_ALB * tn + e];
+            if (!(aj.w > 0.0f)) continue;  // outside the image or no primary hit
             // relative_depth_delta(di, dj) > threshold: fl(num / m) against dthr, decided by
             // the product dthr * m away from the threshold and by the IEEE quotient near it
             float m = dabs_i;
@@ -375,7 +405,6 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
             else if (num < tm * (1.0f - kDepthBand)) far = false;
             else far = __fdiv_rn(num, m) > dthr;
             if (far) continue;
-            const float4 aj = T[P_ALB * tn + e];
             const float da0 = ali.x - aj.x, da1 = ali.y - aj.y, da2 = ali.z - aj.z;
             if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) continue;
 
@@ -506,7 +535,12 @@ cudaError_t launch_statmc(Job& j) {
     {
         KernelScope ks(j, RPD_KERNEL_SQRT_VARIANCE);
         k_sqrt_var_mean<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np);
-        k_sqrt_var_stable<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, j.g.w, j.g.h);
+        // the summed weights of the 3x3 average, accumulated as the reference accumulates them
+        double weight_sum = 0.0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) weight_sum += 1.0 / (1.0 + double(dx * dx + dy * dy));
+        const dim3 sgrid((j.g.w + kSvTx - 1) / kSvTx, (j.g.h + kSvTy - 1) / kSvTy);
+        k_sqrt_var_stable<<<sgrid, dim3(kSvTx, kSvTy), 0, j.stream>>>(j.p, j.g.w, j.g.h, weight_sum);
     }
     KernelScope ks(j, RPD_KERNEL_STATMC_WINDOW);
     StatmcParams prm{};

@@ -29,34 +29,86 @@ __device__ __forceinline__ float conservative_variance_update(float value, float
     return lerp_std(value, neighbor, blend);
 }
 
-__global__ void k_var_smooth(PixelPlanes p, VarParams prm, const float* src, float* dst) {
-    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= int64_t(prm.w) * prm.h) return;
+// One Jacobi iteration (main.cpp:1198-1249). A 32 x 8 block stages its (32+2r) x (8+2r) halo
+// in shared memory: (unit normal, depth) as float4 and the current variance, -1 for pixels
+// outside the image or without a primary hit (the reference's bounds and hit_count tests). The
+// per-neighbour
+// float operations are the reference's, in its order; the two quotient gates are decided by a
+// product or a reciprocal square root away from their thresholds and by the IEEE quotient near
+// them, and the spatial weights 1 / (1 + d^2) come from a table.
+constexpr int kVarTx = 32, kVarTy = 8;
+constexpr float kGateBand = 1.0f / 1048576.0f;  // 2^-20
+
+__global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth(PixelPlanes p, VarParams prm, const float* src,
+                                                                float* dst) {
+    extern __shared__ float4 vsm[];
+    const int r = prm.radius;
+    const int tw = kVarTx + 2 * r, th = kVarTy + 2 * r, tn = tw * th;
+    const int side = 2 * r + 1;
+    float4* G = vsm;                                          // (normal, depth)
+    float* V = reinterpret_cast<float*>(vsm + tn);            // max(EPS_SMALL, src)
+    float* W = V + tn;                                        // 1 / (1 + d^2)
+    const int x0 = blockIdx.x * kVarTx, y0 = blockIdx.y * kVarTy;
+    const int tid = threadIdx.y * kVarTx + threadIdx.x;
+    for (int e = tid; e < side * side; e += kVarTx * kVarTy) {
+        const int dx = e % side - r, dy = e / side - r;
+        W[e] = 1.0f / (1.0f + float(dx * dx + dy * dy));
+    }
+    for (int e = tid; e < tn; e += kVarTx * kVarTy) {
+        const int gx = x0 - r + e % tw, gy = y0 - r + e / tw;
+        const bool inside = gx >= 0 && gx < prm.w && gy >= 0 && gy < prm.h;
+        const int64_t q = inside ? int64_t(gy) * prm.w + gx : 0;
+        const bool hit = inside && p.hit_count[q] > 0;
+        G[e] = hit ? make_float4(p.f_normal[0][q], p.f_normal[1][q], p.f_normal[2][q], p.f_depth[q])
+                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        V[e] = hit ? fmaxs(1e-8f, src[q]) : -1.0f;
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= prm.w || y >= prm.h) return;
+    const int64_t idx = int64_t(y) * prm.w + x;
     if (p.hit_count[idx] == 0) {
         dst[idx] = src[idx];
         return;
     }
-    const int y = int(idx / prm.w), x = int(idx % prm.w);
-    const float ni0 = p.f_normal[0][idx], ni1 = p.f_normal[1][idx], ni2 = p.f_normal[2][idx];
-    const float depth_i = p.f_depth[idx];
-    const float var_i = fmaxs(1e-8f, src[idx]);
+    const int ei = (threadIdx.y + r) * tw + threadIdx.x + r;
+    const float4 gi = G[ei];
+    const float var_i = V[ei];
+    const float dabs_i = fabsf(gi.w);
+    const float dthr = prm.depth_threshold;
     float weight_sum = 0.0f, weighted_sum = 0.0f;
-    for (int dy = -prm.radius; dy <= prm.radius; ++dy) {
-        const int yy = y + dy;
-        if (yy < 0 || yy >= prm.h) continue;
-        for (int dx = -prm.radius; dx <= prm.radius; ++dx) {
-            const int xx = x + dx;
-            if (xx < 0 || xx >= prm.w || (dx == 0 && dy == 0)) continue;
-            const int64_t jn = int64_t(yy) * prm.w + xx;
-            if (p.hit_count[jn] == 0) continue;
-            if (dot3(ni0, ni1, ni2, p.f_normal[0][jn], p.f_normal[1][jn], p.f_normal[2][jn]) < prm.normal_threshold)
-                continue;
-            if (relative_depth_delta(depth_i, p.f_depth[jn]) > prm.depth_threshold) continue;
-            const float var_j = fmaxs(1e-8f, src[jn]);
-            const float relative_difference = fabsf(var_i - var_j) / fmaxs(1e-8f, sqrtf(var_i * var_j));
-            if (relative_difference > prm.compat_sigma) continue;
-            const float dist2 = float(dx * dx + dy * dy);
-            const float w_j = 1.0f / (1.0f + dist2);
+    for (int dy = -r; dy <= r; ++dy) {
+        const int erow = ei + dy * tw;
+        const float* wrow = W + (dy + r) * side + r;
+        for (int dx = -r; dx <= r; ++dx) {
+            if (dx == 0 && dy == 0) continue;
+            const float var_j = V[erow + dx];
+            if (var_j < 0.0f) continue;  // outside the image or no primary hit
+            const float4 gj = G[erow + dx];
+            if (dot3(gi.x, gi.y, gi.z, gj.x, gj.y, gj.z) < prm.normal_threshold) continue;
+            // relative_depth_delta(depth_i, depth_j) > threshold (main.cpp:266-268)
+            float m = dabs_i;
+            if (m < fabsf(gj.w)) m = fabsf(gj.w);
+            if (m < 1e-8f) m = 1e-8f;
+            const float num = fabsf(gi.w - gj.w);
+            const float tm = dthr * m;
+            bool far;
+            if (!(tm >= 1e-30f)) far = num / m > dthr;
+            else if (num > tm * (1.0f + kGateBand)) far = true;
+            else if (num < tm * (1.0f - kGateBand)) far = false;
+            else far = num / m > dthr;
+            if (far) continue;
+            // |var_i - var_j| / max(EPS_SMALL, sqrt(var_i * var_j)) > compat_sigma
+            const float diff = fabsf(var_i - var_j);
+            const float prod = var_i * var_j;
+            const float approx = diff * rsqrtf(prod);
+            bool incompatible;
+            if (fabsf(approx - prm.compat_sigma) > prm.compat_sigma * kGateBand && prod >= 1e-16f && prod < 1e36f)
+                incompatible = approx > prm.compat_sigma;
+            else
+                incompatible = diff / fmaxs(1e-8f, sqrtf(prod)) > prm.compat_sigma;
+            if (incompatible) continue;
+            const float w_j = wrow[dx];
             weighted_sum += w_j * var_j;
             weight_sum += w_j;
         }
@@ -86,8 +138,15 @@ cudaError_t launch_variance(Job& j) {
     k_var_init<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np, max_variance, curr);
     VarParams prm{j.g.w, j.g.h, j.cfg.var_window_radius, j.cfg.var_normal_threshold, j.cfg.var_depth_threshold,
                   j.cfg.var_compat_sigma, j.cfg.var_shrinkage_k};
+    const int r = prm.radius;
+    const size_t smem = size_t(kVarTx + 2 * r) * size_t(kVarTy + 2 * r) * (sizeof(float4) + sizeof(float)) +
+                        size_t(2 * r + 1) * size_t(2 * r + 1) * sizeof(float);
+    if (smem > size_t(200) * 1024) return cudaErrorInvalidValue;  // radius beyond the shared-memory tile
+    cudaError_t e = cudaFuncSetAttribute(k_var_smooth, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    const dim3 vgrid((j.g.w + kVarTx - 1) / kVarTx, (j.g.h + kVarTy - 1) / kVarTy);
     for (int it = 0; it < j.cfg.var_iterations; ++it) {
-        k_var_smooth<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm, curr, next);
+        k_var_smooth<<<vgrid, dim3(kVarTx, kVarTy), smem, j.stream>>>(j.p, prm, curr, next);
         float* t = curr;
         curr = next;
         next = t;

@@ -37,11 +37,17 @@ def gpu_ctx():
 
 
 def fbits(a: np.ndarray) -> np.ndarray:
-    """Bit pattern view for exact float comparisons."""
+    """Bit pattern view for exact float comparisons. Every NaN maps to one pattern: NaN
+    payloads and signs are not part of the contract (x86 propagates an operand's payload where
+    the GPU returns its canonical NaN)."""
     if a.dtype == np.float32:
-        return a.view(np.uint32)
+        b = a.view(np.uint32).copy()
+        b[np.isnan(a)] = 0x7FC00000
+        return b
     if a.dtype == np.float64:
-        return a.view(np.uint64)
+        b = a.view(np.uint64).copy()
+        b[np.isnan(a)] = 0x7FF8000000000000
+        return b
     return a
 
 

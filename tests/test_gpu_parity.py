@@ -280,3 +280,28 @@ def test_grid_launch_shapes_agree(gpu_ctx, shape):
     check_pipeline(g, o, exact_grid=False)
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_non_finite_features(gpu_ctx, exact):
+    """NaN normals, infinite and NaN depths and NaN albedo in some pixels: every gate
+    treats them as the reference's float comparisons do."""
+    w, h, spp = 36, 28, 4
+    cfg = small_config(w, h, var_window_radius=2)
+    s = B.synth_fill(R.synth_params(w, h, 19, miss_regions=2), 0, w * h, spp)
+    rng = np.random.default_rng(3)
+    pix = rng.choice(w * h, size=40, replace=False)
+    for i, px in enumerate(pix):
+        k = slice(px * spp, (px + 1) * spp)
+        if i % 4 == 0:
+            s.planes["normal"][0][k] = np.nan
+        elif i % 4 == 1:
+            s.planes["depth"][k] = np.inf
+        elif i % 4 == 2:
+            s.planes["depth"][k] = np.nan
+        else:
+            s.planes["pixel_albedo"][1][px] = np.nan
+    g, o = run_both(gpu_ctx, cfg, s, spp, exact=exact)
+    check_pipeline(g, o, exact_grid=exact)
+    g.close()
+    o.close()
