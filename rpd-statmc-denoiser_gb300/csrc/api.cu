@@ -51,7 +51,7 @@ Geometry make_geometry(const rpd_config& c) {
 
 // Assigns (offset-encoded) plane pointers; returns the arena size.
 uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5] = nullptr,
-              uint8_t** pflags = nullptr) {
+              float4** pat4 = nullptr, float2** pat2 = nullptr) {
     Layout L;
     const int64_t np = g.np, nn = g.nn;
     L.add(p.mean, np);
@@ -100,11 +100,13 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5]
     L.add(n.n_depth, nn);
     for (int c = 0; c < 3; ++c) L.add(n.n_albedo[c], nn);
     float* cls_tmp[kClasses][5];
-    uint8_t* pflags_tmp = nullptr;
+    float4* pat4_tmp = nullptr;
+    float2* pat2_tmp = nullptr;
     float* (*C)[5] = cls ? cls : cls_tmp;
     for (int c = 0; c < kClasses; ++c)
         for (int f = 0; f < 5; ++f) L.add(C[c][f], np);
-    L.add(pflags ? *pflags : pflags_tmp, np);
+    L.add(pat4 ? *pat4 : pat4_tmp, np);
+    L.add(pat2 ? *pat2 : pat2_tmp, np);
     return (L.bytes + 255) & ~uint64_t(255);
 }
 
@@ -424,7 +426,7 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
     j->ctx = c;
     j->cfg = *cfg;
     j->g = make_geometry(*cfg);
-    j->arena_bytes = plan(j->g, j->p, j->n, j->cls, &j->pflags);
+    j->arena_bytes = plan(j->g, j->p, j->n, j->cls, &j->pat4, &j->pat2);
     {
         std::lock_guard<std::mutex> lock(c->mu);
         if (c->in_use.load() + j->arena_bytes > c->budget) {
@@ -445,7 +447,8 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
     rebase_all(j->p, j->n, static_cast<char*>(j->arena));
     for (int c = 0; c < kClasses; ++c)
         for (int f = 0; f < 5; ++f) rebase(j->cls[c][f], static_cast<char*>(j->arena));
-    rebase(j->pflags, static_cast<char*>(j->arena));
+    rebase(j->pat4, static_cast<char*>(j->arena));
+    rebase(j->pat2, static_cast<char*>(j->arena));
     cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
     for (int s = 0; s < RPD_STAGE_COUNT_ && e == cudaSuccess; ++s) {
         e = cudaEventCreate(&j->ev_start[s]);
@@ -545,7 +548,16 @@ int rpd_job_begin_frame(rpd_job* job) {
     Job* j = reinterpret_cast<Job*>(job);
     CHECK_JOB(j);
     RPD_CUDA(cudaSetDevice(j->ctx->device));
-    RPD_CUDA(cudaMemsetAsync(j->arena, 0, j->arena_bytes, j->stream));
+    // only the per-pixel accumulators start from zero (render_image_statmc's buffers.init and
+    // pixel_stats reset): they are contiguous from the Welford mean to the depth sum. Every
+    // other plane is written whole by the stage that produces it; the frame grid is assigned by
+    // the first merge; the pass grid is cleared by each merge (and here if a pass was left open).
+    const char* acc0 = reinterpret_cast<const char*>(j->p.mean);
+    const char* acc1 = reinterpret_cast<const char*>(j->p.depth + j->g.np);
+    RPD_CUDA(cudaMemsetAsync(j->p.mean, 0, size_t(acc1 - acc0), j->stream));
+    if (j->pass_open)
+        RPD_CUDA(cudaMemsetAsync(j->n.pass_grid, 0, size_t(j->g.nn) * kDeps * kDepStride * sizeof(double), j->stream));
+    j->grid_fresh = true;
     j->pass_open = false;
     j->features_valid = false;
     j->cache_valid = false;
@@ -678,7 +690,8 @@ int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first, i
         gp.key = reinterpret_cast<uint32_t*>(j->lum + ((std::max<int64_t>(nsamp, 1) + 63) / 64) * 64);
         for (int c = 0; c < kClasses; ++c)
             for (int f = 0; f < 5; ++f) gp.cls[c][f] = j->cls[c][f];
-        gp.pflags = j->pflags;
+        gp.pat4 = j->pat4;
+        gp.pat2 = j->pat2;
         gp.lum = j->lum;
     }
     RPD_CUDA(launch_accumulate_pixels(*j, d, first, count, gp, counts ? 0 : spp));
@@ -840,6 +853,12 @@ int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory 
     default: break;
     }
     if (f >= RPD_FIELD_NODE_ALL && f <= RPD_FIELD_NODE_RR_CONF) src = j->n.field[f - RPD_FIELD_NODE_ALL];
+    if (f == RPD_FIELD_GRID && j->grid_fresh) {  // no pass merged into this frame's grid yet: zeros
+        if (where == RPD_MEM_HOST) std::memset(dst, 0, bytes);
+        else RPD_CUDA(cudaMemsetAsync(dst, 0, bytes, j->stream));
+        RPD_CUDA(cudaStreamSynchronize(j->stream));
+        return RPD_OK;
+    }
     if (src) {
         RPD_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, j->stream));
         RPD_CUDA(cudaStreamSynchronize(j->stream));

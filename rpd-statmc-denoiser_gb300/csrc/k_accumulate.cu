@@ -95,9 +95,10 @@ struct PixelAcc {
     float cm[3], sm[3], sq[3], rad[3], nor[3], alb[3], dep;
     int hits, nsamples;
     // validity-class sums for the grid pass: samples whose class bits equal the pixel's
-    // first pattern share one set of sums; others go to per-class sums
+    // pattern (the first nonzero class bits) share one set of sums; others go to per-class
+    // sums and make the pixel deviant
     uint8_t pat;
-    bool have_pat;
+    bool have_pat, dev;
     float pc, p1h, p1l, p2h, p2l;
     float cc[kClasses], s1h[kClasses], s1l[kClasses], s2h[kClasses], s2l[kClasses];
     uint8_t pflags;
@@ -153,16 +154,19 @@ __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, 
     const uint8_t cls_bits = fm & 0xfe;
     const float y2 = lum * lum;
     const float y2e = __fmaf_rn(lum, lum, -y2);
-    if (!a.have_pat) {
+    if (cls_bits != 0 && !a.have_pat) {
         a.have_pat = true;
         a.pat = cls_bits;
     }
-    if (cls_bits == a.pat) {
+    if (cls_bits == 0) {
+        // no validity class: nothing for the grid's totals
+    } else if (cls_bits == a.pat) {
         a.pc += 1.0f;
         df_add(a.p1h, a.p1l, lum);
         df_add(a.p2h, a.p2l, y2);
         a.p2l += y2e;
     } else {
+        a.dev = true;
         #pragma unroll
         for (int c = 0; c < kClasses; ++c) {
             if (!(cls_bits & class_bit(c))) continue;
@@ -210,14 +214,14 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
     PixelAcc a;
     a.pflags = kPixUniform;
     a.have_pat = false;
+    a.dev = false;
     a.pat = 0;
     a.pc = a.p1h = a.p1l = a.p2h = a.p2l = 0.0f;
     for (int c = 0; c < kClasses; ++c) a.cc[c] = a.s1h[c] = a.s1l[c] = a.s2h[c] = a.s2l[c] = 0.0f;
     if (k0 == k1) {
         if (prep) {
-            for (int c = 0; c < kClasses; ++c)
-                for (int f = 0; f < 5; ++f) gp.cls[c][f][idx] = 0.0f;
-            gp.pflags[idx] = a.pflags;
+            gp.pat4[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            gp.pat2[idx] = make_float2(0.0f, __uint_as_float(uint32_t(a.pflags) << 8));
         }
         return;
     }
@@ -331,22 +335,28 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
     p.hit_count[idx] = a.hits;
     p.sample_count[idx] = a.nsamples;
     if (prep) {
-        for (int c = 0; c < kClasses; ++c) {
-            float h1 = a.s1h[c], l1 = a.s1l[c], h2 = a.s2h[c], l2 = a.s2l[c], cnt = a.cc[c];
-            if (a.have_pat && (a.pat & class_bit(c))) {
-                cnt += a.pc;
-                df_add(h1, l1, a.p1h);
-                l1 += a.p1l;
-                df_add(h2, l2, a.p2h);
-                l2 += a.p2l;
+        gp.pat4[idx] = make_float4(a.pc, a.p1h, a.p1l, a.p2h);
+        const uint32_t bits = uint32_t(a.have_pat ? a.pat : 0) |
+                              (uint32_t(a.pflags | (a.dev ? kPixDeviant : 0)) << 8);
+        gp.pat2[idx] = make_float2(a.p2l, __uint_as_float(bits));
+        if (a.dev) {
+            // full per-class sums: the deviating samples plus the pattern's
+            for (int c = 0; c < kClasses; ++c) {
+                float h1 = a.s1h[c], l1 = a.s1l[c], h2 = a.s2h[c], l2 = a.s2l[c], cnt = a.cc[c];
+                if (a.have_pat && (a.pat & class_bit(c))) {
+                    cnt += a.pc;
+                    df_add(h1, l1, a.p1h);
+                    l1 += a.p1l;
+                    df_add(h2, l2, a.p2h);
+                    l2 += a.p2l;
+                }
+                gp.cls[c][0][idx] = cnt;
+                gp.cls[c][1][idx] = h1;
+                gp.cls[c][2][idx] = l1;
+                gp.cls[c][3][idx] = h2;
+                gp.cls[c][4][idx] = l2;
             }
-            gp.cls[c][0][idx] = cnt;
-            gp.cls[c][1][idx] = h1;
-            gp.cls[c][2][idx] = l1;
-            gp.cls[c][3][idx] = h2;
-            gp.cls[c][4][idx] = l2;
         }
-        gp.pflags[idx] = a.pflags;
     }
 }
 
@@ -499,10 +509,20 @@ __global__ void __launch_bounds__(128) k_grid_ordered(Geometry g, double* pass_g
     acc[35] = y2_sum;
 }
 
+// grid += pass (the first pass of a frame: grid = 0 + pass), then clear the pass grid. The
+// fast path's pass grid holds double-float pairs (hi, lo) in the bytes of each double.
+template <bool DF, bool FRESH>
 __global__ void k_merge_grid(double* grid, double* pass_grid, int64_t n) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    grid[i] += pass_grid[i];
+    double v;
+    if (DF) {
+        const float2 p = reinterpret_cast<const float2*>(pass_grid)[i];
+        v = double(p.x) + double(p.y);
+    } else {
+        v = pass_grid[i];
+    }
+    grid[i] = FRESH ? 0.0 + v : grid[i] + v;
     pass_grid[i] = 0.0;
 }
 
@@ -606,7 +626,12 @@ cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first
 cudaError_t launch_merge_grid(Job& j) {
     KernelScope ks(j, RPD_KERNEL_MERGE);
     const int64_t n = j.g.nn * kDeps * kDepStride;
-    k_merge_grid<<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
+    const bool df = !j.exact_grid;
+    if (df && j.grid_fresh) k_merge_grid<true, true><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
+    else if (df) k_merge_grid<true, false><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
+    else if (j.grid_fresh) k_merge_grid<false, true><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
+    else k_merge_grid<false, false><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
+    j.grid_fresh = false;
     j.launches += 1;
     return cudaGetLastError();
 }

@@ -49,6 +49,24 @@ struct DF {
     float h = 0.0f, l = 0.0f;
 };
 
+// The fast path's pass grid holds every entry as a double-float (hi, lo) pair in the 8 bytes
+// of a double; the merge into the frame grid turns it into a double (k_merge_grid).
+__device__ __forceinline__ void df_accum(float2* e, float h, float l) {
+    float2 v = *e;
+    df_add(v.x, v.y, h);
+    v.y += l;
+    *e = v;
+}
+
+// An integer bin weight (a multiple of 1/step^2, below 2^32 by the launch's bound) as a
+// double-float: the float of the integer plus the float of its remainder, scaled exactly.
+__device__ __forceinline__ float2 int_weight_df(uint64_t total, float inv_wscale) {
+    const uint32_t t = uint32_t(total);
+    const float hi = __uint2float_rz(t);          // an integer <= t
+    const uint32_t rem = t - __float2uint_rz(hi);  // below 2^8, exact in float
+    return make_float2(hi * inv_wscale, float(rem) * inv_wscale);
+}
+
 struct Totals {
     DF w, w2, y, y2;
 };
@@ -117,18 +135,15 @@ struct LaneBins {
         at(kSy + 16 + bin) = yl;
     }
     // Sum the 32 lanes in a fixed (rotated) order; lane v owns value v: weight[v] for v < 16,
-    // sum_y[v - 16] otherwise. Adds the result to acc[v].
-    __device__ void reduce_into(double* acc) {
+    // sum_y[v - 16] otherwise. Returns the lane's value as a double-float.
+    __device__ float2 reduce_value() {
         __syncwarp();
         const int v = lane;
-        double out;
+        float2 out;
         if (INT_W && v < 16) {
             uint64_t total = 0;
-            for (int i = 0; i < 32; ++i) {
-                const int src = (i + v) & 31;
-                total += reinterpret_cast<const uint32_t*>(base)[v * 32 + src];
-            }
-            out = double(total) / double(wscale);
+            for (int i = 0; i < 32; ++i) total += reinterpret_cast<const uint32_t*>(base)[v * 32 + ((i + v) & 31)];
+            out = int_weight_df(total, 1.0f / wscale);
         } else {
             const int hi_slot = v < 16 ? v : kSy + (v - 16);
             float h = 0.0f, l = 0.0f;
@@ -137,14 +152,21 @@ struct LaneBins {
                 df_add(h, l, base[hi_slot * 32 + src]);
                 l += base[(hi_slot + 16) * 32 + src];
             }
-            out = double(h) + double(l);
+            out = make_float2(h, l);
         }
-        acc[v] += out;
         __syncwarp();
+        return out;
+    }
+    // As reduce_value, adding the result to the pass-grid entry acc[v].
+    __device__ void reduce_into(float2* acc) {
+        const float2 out = reduce_value();
+        if (out.x != 0.0f || out.y != 0.0f) df_accum(acc + lane, out.x, out.y);
     }
 };
 
-__device__ void reduce_totals_into(Totals t, double* acc) {
+// Warp sum of the lanes' totals (fixed shuffle tree); the result is valid in lane 0 as
+// double-floats (w_sum, w2_sum, y_sum, y2_sum).
+__device__ void reduce_totals(Totals t, float2* out4) {
     float v[8] = {t.w.h, t.w.l, t.w2.h, t.w2.l, t.y.h, t.y.l, t.y2.h, t.y2.l};
     for (int off = 16; off > 0; off >>= 1) {
         for (int q = 0; q < 4; ++q) {
@@ -154,11 +176,16 @@ __device__ void reduce_totals_into(Totals t, double* acc) {
             v[2 * q + 1] += ol;
         }
     }
+    for (int q = 0; q < 4; ++q) out4[q] = make_float2(v[2 * q], v[2 * q + 1]);
+}
+
+// As reduce_totals, adding the result to the pass-grid entries acc[32..35].
+__device__ void reduce_totals_into(Totals t, float2* acc) {
+    float2 r[4];
+    reduce_totals(t, r);
     if ((threadIdx.x & 31) == 0) {
-        acc[32] += double(v[0]) + double(v[1]);
-        acc[33] += double(v[2]) + double(v[3]);
-        acc[34] += double(v[4]) + double(v[5]);
-        acc[35] += double(v[6]) + double(v[7]);
+        for (int q = 0; q < 4; ++q)
+            if (r[q].x != 0.0f || r[q].y != 0.0f) df_accum(acc + 32 + q, r[q].x, r[q].y);
     }
 }
 
@@ -184,8 +211,36 @@ __device__ __forceinline__ float axis_factor(const GridParams& gp, int c, int n,
     return 0.0f;
 }
 
+// A pixel's pattern sums, pattern and flags (see GridPrep).
+struct PixPattern {
+    float c, s1h, s1l, s2h, s2l;
+    uint8_t pat, pf;
+};
+__device__ __forceinline__ PixPattern load_pattern(const GridPrep& gp, int64_t idx) {
+    const float4 a = gp.pat4[idx];
+    const float2 b = gp.pat2[idx];
+    const uint32_t bits = __float_as_uint(b.y);
+    return PixPattern{a.x, a.y, a.z, a.w, b.x, uint8_t(bits & 0xffu), uint8_t(bits >> 8)};
+}
+
+// The (count, sum y hi/lo, sum y^2 hi/lo) of class c for pixel idx (see GridPrep).
+__device__ __forceinline__ void class_sums(const GridPrep& gp, int c, int64_t idx, const PixPattern& pp,
+                                           float* out) {
+    if (pp.pf & kPixDeviant) {
+        for (int f = 0; f < 5; ++f) out[f] = gp.cls[c][f][idx];
+    } else if (pp.pat & class_bit(c)) {
+        out[0] = pp.c;
+        out[1] = pp.s1h;
+        out[2] = pp.s1l;
+        out[3] = pp.s2h;
+        out[4] = pp.s2l;
+    } else {
+        for (int f = 0; f < 5; ++f) out[f] = 0.0f;
+    }
+}
+
 template <bool INT_W>
-__global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, double* pass_grid, DeviceSamples s,
+__global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, float2* pass_grid, DeviceSamples s,
                                                             const int64_t* offsets, GridPrep gp) {
     extern __shared__ float sm[];
     const int lane = threadIdx.x & 31;
@@ -206,7 +261,7 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, dou
     case 6: dep_x = D_RR; dep_s = D_SCREEN_RR; break;
     default: break;
     }
-    double* base = pass_grid + node * kDeps * kDepStride;
+    float2* base = pass_grid + node * kDeps * kDepStride;
     const float support = float(g.support);
     const float half_support = 0.5f * support;
     const float support_left = float(nx * g.step) - half_support;
@@ -232,11 +287,13 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, dou
             idx = int64_t(y) * g.w + x;
             if (idx >= gpar.first && idx < gpar.first + gpar.count) {
                 w = axis_factor(gpar, x, nx, g.nodes_x) * axis_factor(gpar, y, ny, g.nodes_y);
-                const float cnt = w > 1e-8f ? gp.cls[grp][0][idx] : 0.0f;  // core/stats.h:103 skips w <= 1e-8
+                const PixPattern pp = load_pattern(gp, idx);
+                const uint8_t pf = pp.pf;
+                float cs[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                if (w > 1e-8f) class_sums(gp, grp, idx, pp, cs);  // core/stats.h:103 skips w <= 1e-8
+                const float cnt = cs[0];
                 if (cnt != 0.0f) {
-                    const float s1h = gp.cls[grp][1][idx], s1l = gp.cls[grp][2][idx];
-                    const float s2h = gp.cls[grp][3][idx], s2l = gp.cls[grp][4][idx];
-                    const uint8_t pf = gp.pflags[idx];
+                    const float s1h = cs[1], s1l = cs[2], s2h = cs[3], s2l = cs[4];
                     mixed = grp > 0 && (pf & kPixMixed);
                     add_class(tot_x, w, cnt, s1h, s1l, s2h, s2l);
                     if (!mixed) add_class(tot_s, w, cnt, s1h, s1l, s2h, s2l);
@@ -285,6 +342,264 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, dou
     reduce_totals_into(tot_x, base + dep_x * kDepStride);
 }
 
+// ---- totals and screen bins, pattern form (the default) ----------------------------------
+//
+// One warp per node. Pixels of the node's pattern P0 (the pattern of its first non-deviant
+// support pixel) carry the same class sums for every class in P0, so their totals are formed
+// once (TP) and their screen bins once (bins A: per pixel for uniform pixels, sample by sample
+// otherwise); each class then takes TP and bins A if it is in P0. Every other pixel (deviant,
+// or of another pattern) goes to a list handled class by class as the per-class kernel does
+// (bins B). All sums are lane-private and combined in a fixed order: deterministic.
+__device__ __forceinline__ int axis_ifactor(int c, int n, int nodes, int sh) {
+    // x factor * step of a power-of-two step (c < (nodes - 1) * step for every image pixel)
+    const int c0 = imins(c >> sh, nodes - 1);
+    const int t = c - (c0 << sh);
+    return c0 == n ? (1 << sh) - t : (c0 + 1 == n ? t : 0);
+}
+
+template <bool INT_W>
+__global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pass_grid, DeviceSamples s,
+                                                    const int64_t* offsets, GridPrep gp) {
+    extern __shared__ float sm[];
+    constexpr int kS = LaneBins<INT_W>::kSlots;
+    const int lane = threadIdx.x;
+    const int64_t node = blockIdx.x;
+    const Geometry& g = gpar.g;
+    const int nx = int(node % g.nodes_x), ny = int(node / g.nodes_x);
+    const float wscale = float(g.step) * float(g.step);
+    LaneBins<INT_W> binsA{sm, lane, wscale};
+    int* xlist = reinterpret_cast<int*>(sm + kS * 32);
+    float2* base = pass_grid + node * kDeps * kDepStride;
+    const float support = float(g.support);
+    const float half_support = 0.5f * support;
+    const float support_left = float(nx * g.step) - half_support;
+    const float support_top = float(ny * g.step) - half_support;
+    const int xlo = imaxs(0, (nx - 1) * g.step - 1), xhi = imins(g.w - 1, (nx + 1) * g.step + 1);
+    const int ylo = imaxs(0, (ny - 1) * g.step - 1), yhi = imins(g.h - 1, (ny + 1) * g.step + 1);
+    const int cols = xhi - xlo + 1;
+    const int npix = cols * (yhi - ylo + 1);
+    const int sh = __ffs(g.step) - 1;                 // log2(step) when the step is a power of two
+    const int bsh = __ffs(g.support) - 3;             // log2(support / 4) when uniform_ok
+    const int sl = nx * g.step - g.support / 2, st = ny * g.step - g.support / 2;  // integer when uniform_ok
+    const float inv_wscale = 1.0f / wscale;
+    const uint32_t pbit = key_valid_bit(0);
+
+    auto weight = [&](int x, int y) -> float {
+        if (gpar.pow2_step)
+            return float(axis_ifactor(x, nx, g.nodes_x, sh) * axis_ifactor(y, ny, g.nodes_y, sh)) * inv_wscale;
+        return axis_factor(gpar, x, nx, g.nodes_x) * axis_factor(gpar, y, ny, g.nodes_y);
+    };
+    // the pixel's nominal screen bin (every sample's, for a uniform pixel)
+    auto uniform_bin = [&](int x, int y) -> int {
+        const int dx = x - sl, dy = y - st;
+        const int bx = dx < 0 ? 0 : imins(dx >> bsh, 3), by = dy < 0 ? 0 : imins(dy >> bsh, 3);
+        return by * 4 + bx;
+    };
+    // samples of pixel (px, py) binned one by one by the whole warp (main.cpp:349-357): every
+    // lane into its own bins; also the screen totals of a mixed pixel (samples with the
+    // position and the class)
+    auto bin_samples = [&](LaneBins<INT_W>& bins, int64_t pidx, float pw, int px, int py, uint32_t vbit,
+                           bool pmixed, Totals& ts) {
+        const float fx = float(px), fy = float(py);
+        const int64_t local = pidx - gpar.first;
+        const int64_t kend = offsets[local + 1];
+        for (int64_t k = offsets[local] + lane; k < kend; k += 32) {
+            const uint32_t key = gp.key[k];
+            if (!(key & pbit) || !(key & vbit)) continue;
+            const float yv = gp.lum[k];
+            const float su = fclamps((fx + s.pixel_u[0][k] - support_left) / support, 0.0f, 1.0f);
+            const float sv = fclamps((fy + s.pixel_u[1][k] - support_top) / support, 0.0f, 1.0f);
+            const int b = bin2d(su, sv);
+            bins.add_weight(b, pw, 1.0f);
+            bins.add_sum(b, pw, yv, 0.0f);
+            if (pmixed) add_sample(ts, pw, yv);
+        }
+    };
+
+    // ---- P0: the pattern of the first non-deviant support pixel with a pattern ----
+    uint8_t P0 = 0;
+    for (int q0 = 0; q0 < npix; q0 += 32) {
+        const int q = q0 + lane;
+        uint8_t pat = 0;
+        if (q < npix) {
+            const int64_t idx = int64_t(ylo + q / cols) * g.w + xlo + q % cols;
+            if (idx >= gpar.first && idx < gpar.first + gpar.count) {
+                const uint32_t bits = __float_as_uint(gp.pat2[idx].y);
+                if (!((bits >> 8) & kPixDeviant)) pat = uint8_t(bits & 0xffu);
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, pat != 0);
+        if (m) {
+            P0 = uint8_t(__shfl_sync(0xffffffffu, int(pat), __ffs(m) - 1));
+            break;
+        }
+    }
+    const bool p0pix = (P0 & RPD_SAMPLE_PIXEL_VALID) != 0;
+
+    // ---- main pass: P0 pixels into TP / bins A, the rest into the list ----
+    binsA.clear();
+    Totals TP, unused;
+    int nlist = 0;
+    int x = xlo + lane % cols, y = ylo + lane / cols;  // position of q = q0 + lane
+    // the pattern record of q, loaded one iteration ahead so the loads overlap the work
+    auto fetch = [&](int q, int px, int py, PixPattern& pp, bool& in) {
+        const int64_t idx = int64_t(py) * g.w + px;
+        in = q < npix && idx >= gpar.first && idx < gpar.first + gpar.count;
+        if (in) pp = load_pattern(gp, idx);
+        else pp = PixPattern{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0};
+    };
+    PixPattern nxt;
+    bool nin;
+    fetch(lane, x, y, nxt, nin);
+    for (int q0 = 0; q0 < npix; q0 += 32) {
+        const PixPattern pp = nxt;
+        const bool in = nin;
+        const int cx = x, cy = y;
+        x += 32;
+        while (x > xhi) {
+            x -= cols;
+            ++y;
+        }
+        if (q0 + 32 < npix) fetch(q0 + 32 + lane, x, y, nxt, nin);
+        bool exc = false, slow = false;
+        const int64_t idx = int64_t(cy) * g.w + cx;
+        float w = 0.0f;
+        if (in) {
+            w = weight(cx, cy);
+            if (w > 1e-8f) {  // BinnedDependency::add skips w <= 1e-8 (core/stats.h:103)
+                const bool dev = (pp.pf & kPixDeviant) != 0;
+                if (!dev && pp.pat == P0 && pp.pat != 0) {
+                    add_class(TP, w, pp.c, pp.s1h, pp.s1l, pp.s2h, pp.s2l);
+                    if (p0pix) {
+                        if (gpar.uniform_ok && (pp.pf & kPixUniform)) {
+                            const int b = uniform_bin(cx, cy);
+                            binsA.add_weight(b, w, pp.c);
+                            binsA.add_sum(b, w, pp.s1h, pp.s1l);
+                        } else {
+                            slow = true;
+                        }
+                    }
+                } else if (dev || pp.pat != 0) {
+                    exc = true;
+                }
+            }
+        }
+        const int q = q0 + lane;
+        const unsigned me = __ballot_sync(0xffffffffu, exc);
+        if (exc) xlist[nlist + __popc(me & ((1u << lane) - 1))] = q;
+        nlist += __popc(me);
+        unsigned pending = __ballot_sync(0xffffffffu, slow);
+        while (pending) {
+            const int src = __ffs(pending) - 1;
+            pending &= pending - 1;
+            const int64_t pidx = __shfl_sync(0xffffffffu, idx, src);
+            const float pw = __shfl_sync(0xffffffffu, w, src);
+            const int px = __shfl_sync(0xffffffffu, cx, src), py = __shfl_sync(0xffffffffu, cy, src);
+            bin_samples(binsA, pidx, pw, px, py, pbit, false, unused);
+        }
+    }
+    __syncwarp();
+    float2 tp[4];
+    reduce_totals(TP, tp);
+    const float2 va = binsA.reduce_value();
+    LaneBins<INT_W>& binsB = binsA;  // bins A are folded into va: reuse their storage
+
+    // ---- class by class: P0's share plus the listed pixels ----
+    for (int cl = 0; cl < kClasses; ++cl) {
+        const bool inP0 = (P0 & class_bit(cl)) != 0;
+        const bool p0screen = inP0 && p0pix;  // P0 pixels enter the screen sums of this class
+        const uint32_t vbit = key_valid_bit(cl);
+        Totals tx, ts;
+        float2 vb = make_float2(0.0f, 0.0f);
+        if (nlist > 0) {
+            binsB.clear();
+            for (int i0 = 0; i0 < nlist; i0 += 32) {
+                const int i = i0 + lane;
+                bool slow = false, mixed = false;
+                int px = 0, py = 0;
+                int64_t idx = 0;
+                float w = 0.0f;
+                if (i < nlist) {
+                    const int q = xlist[i];
+                    px = xlo + q % cols;
+                    py = ylo + q / cols;
+                    idx = int64_t(py) * g.w + px;
+                    w = weight(px, py);
+                    const PixPattern pp = load_pattern(gp, idx);
+                    const uint8_t pf = pp.pf;
+                    float cs[5];
+                    class_sums(gp, cl, idx, pp, cs);
+                    if (cs[0] != 0.0f) {
+                        mixed = cl > 0 && (pf & kPixMixed);
+                        add_class(tx, w, cs[0], cs[1], cs[2], cs[3], cs[4]);
+                        if (!mixed) add_class(ts, w, cs[0], cs[1], cs[2], cs[3], cs[4]);
+                        if (gpar.uniform_ok && (pf & kPixUniform) && !mixed) {
+                            const int b = uniform_bin(px, py);
+                            binsB.add_weight(b, w, cs[0]);
+                            binsB.add_sum(b, w, cs[1], cs[2]);
+                        } else {
+                            slow = true;
+                        }
+                    }
+                }
+                unsigned pending = __ballot_sync(0xffffffffu, slow);
+                while (pending) {
+                    const int src = __ffs(pending) - 1;
+                    pending &= pending - 1;
+                    const int64_t pidx = __shfl_sync(0xffffffffu, idx, src);
+                    const float pw = __shfl_sync(0xffffffffu, w, src);
+                    const bool pmixed = __shfl_sync(0xffffffffu, int(mixed), src) != 0;
+                    const int sx = __shfl_sync(0xffffffffu, px, src), sy = __shfl_sync(0xffffffffu, py, src);
+                    bin_samples(binsB, pidx, pw, sx, sy, vbit, pmixed, ts);
+                }
+            }
+            vb = binsB.reduce_value();
+        }
+        int dep_x = D_PIXEL, dep_s = D_PIXEL;
+        switch (cl) {
+        case 1: dep_x = D_BRDF; dep_s = D_SCREEN_BRDF; break;
+        case 2: dep_x = D_LENS; dep_s = D_SCREEN_LENS; break;
+        case 3: dep_x = D_LIGHT_UV; dep_s = D_SCREEN_LIGHT_UV; break;
+        case 4: dep_x = D_ENV; dep_s = D_SCREEN_ENV; break;
+        case 5: dep_x = D_LIGHT_SELECT; dep_s = D_SCREEN_LIGHT_SELECT; break;
+        case 6: dep_x = D_RR; dep_s = D_SCREEN_RR; break;
+        default: break;
+        }
+        // screen bins (the pixel dependency for class 0): lane v owns bin value v
+        float bh = vb.x, bl = vb.y;
+        if (p0screen) {
+            df_add(bh, bl, va.x);
+            bl += va.y;
+        }
+        if (bh != 0.0f || bl != 0.0f) df_accum(base + dep_s * kDepStride + lane, bh, bl);
+        float2 t4[4];
+        reduce_totals(ts, t4);
+        if (lane == 0) {
+            for (int k = 0; k < 4; ++k) {
+                float h = t4[k].x, l = t4[k].y;
+                if (p0screen) {
+                    df_add(h, l, tp[k].x);
+                    l += tp[k].y;
+                }
+                if (h != 0.0f || l != 0.0f) df_accum(base + dep_s * kDepStride + 32 + k, h, l);
+            }
+        }
+        if (cl > 0) {
+            reduce_totals(tx, t4);
+            if (lane == 0) {
+                for (int k = 0; k < 4; ++k) {
+                    float h = t4[k].x, l = t4[k].y;
+                    if (inP0) {
+                        df_add(h, l, tp[k].x);
+                        l += tp[k].y;
+                    }
+                    if (h != 0.0f || l != 0.0f) df_accum(base + dep_x * kDepStride + 32 + k, h, l);
+                }
+            }
+        }
+    }
+}
+
 // ---- random-dimension bins (Dependency2D::add / BinnedDependency::add of brdf, lens,
 // light_uv, environment, light_select and rr; main.cpp:356-375) --------------------------
 //
@@ -304,7 +619,6 @@ __host__ __device__ constexpr int rand_dep(int d) {
 }
 __host__ __device__ constexpr int rand_shift(int d) { return d == 5 ? 20 : key_bin_shift(d + 1); }
 __host__ __device__ constexpr uint32_t rand_mask(int d) { return d == 5 ? 1u : 15u; }
-constexpr uint32_t kRandValidMask = (0x3fu << 22);  // key valid bits of the six dimensions
 
 // The six dimensions split into DS sets (one warp of a row group each): fewer private bins per
 // warp (more resident warps) at the price of walking the samples once per set.
@@ -515,7 +829,7 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
 }
 
 template <bool INT_W, int RW, int DS, bool VEC>
-__global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, double* pass_grid,
+__global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, float2* pass_grid,
                                                               const int64_t* offsets, GridPrep gp) {
     constexpr int NW = RW * DS;
     constexpr int VPT = (2 * kRandSlots + NW * 32 - 1) / (NW * 32);  // combined values per thread
@@ -542,13 +856,13 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, dou
     RowTable* rt = c.rt;
 
     // the grid entries this thread adds to at the end, read now so the loads overlap the walk
-    double prev[VPT];
+    float2 prev[VPT];
     int64_t gidx[VPT];
 #pragma unroll
     for (int vi = 0; vi < VPT; ++vi) {
         const int v = threadIdx.x + vi * NW * 32;
         gidx[vi] = -1;
-        prev[vi] = 0.0;
+        prev[vi] = make_float2(0.0f, 0.0f);
         if (v < 2 * kRandSlots) {
             const bool is_w = v < kRandSlots;
             const int gslot = is_w ? v : v - kRandSlots;
@@ -661,15 +975,23 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, dou
 #pragma unroll
     for (int vi = 0; vi < VPT; ++vi) {
         if (gidx[vi] < 0) continue;
-        double out;
+        float oh, ol;
         if (vw[vi] && INT_W) {
-            out = double(itot[vi]) / double(c.wscale);
+            const float2 t = int_weight_df(itot[vi], 1.0f / c.wscale);
+            oh = t.x;
+            ol = t.y;
         } else {
             df_add(h[vi][0], l[vi][0], h[vi][1]);
             l[vi][0] += l[vi][1];
-            out = double(h[vi][0]) + double(l[vi][0]);
+            oh = h[vi][0];
+            ol = l[vi][0];
         }
-        if (out != 0.0) pass_grid[gidx[vi]] = prev[vi] + out;
+        if (oh != 0.0f || ol != 0.0f) {
+            float2 e = prev[vi];
+            df_add(e.x, e.y, oh);
+            e.y += ol;
+            pass_grid[gidx[vi]] = e;
+        }
     }
 }
 
@@ -696,8 +1018,8 @@ cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) 
     cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, RW, DS, VEC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    k_grid_random<INT_W, RW, DS, VEC><<<unsigned(j.g.nn), NW * 32, smem, j.stream>>>(rp, j.n.pass_grid, j.offsets,
-                                                                                     gp);
+    k_grid_random<INT_W, RW, DS, VEC><<<unsigned(j.g.nn), NW * 32, smem, j.stream>>>(
+        rp, reinterpret_cast<float2*>(j.n.pass_grid), j.offsets, gp);
     j.launches += 1;
     return cudaGetLastError();
 }
@@ -739,16 +1061,31 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
     cudaError_t e;
     {
         KernelScope ks(j, RPD_KERNEL_GRID);
-        if (int_w) {
+        const int side = 2 * step + 3;
+        const size_t list_bytes = size_t(side) * size_t(side) * sizeof(int);
+        if (list_bytes <= size_t(64) * 1024) {
+            // pattern form: one warp per node
+            const size_t smem = size_t(int_w ? LaneBins<true>::kSlots : LaneBins<false>::kSlots) * 32 * sizeof(float) +
+                                list_bytes;
+            if (int_w) {
+                e = cudaFuncSetAttribute(k_grid_screen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+                if (e != cudaSuccess) return e;
+                k_grid_screen<true><<<unsigned(j.g.nn), 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+            } else {
+                e = cudaFuncSetAttribute(k_grid_screen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+                if (e != cudaSuccess) return e;
+                k_grid_screen<false><<<unsigned(j.g.nn), 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+            }
+        } else if (int_w) {
             const size_t smem = size_t(kGroups) * LaneBins<true>::kSlots * 32 * sizeof(float);
             e = cudaFuncSetAttribute(k_grid_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if (e != cudaSuccess) return e;
-            k_grid_fast<true><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, j.n.pass_grid, s, j.offsets, gp);
+            k_grid_fast<true><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
         } else {
             const size_t smem = size_t(kGroups) * LaneBins<false>::kSlots * 32 * sizeof(float);
             e = cudaFuncSetAttribute(k_grid_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if (e != cudaSuccess) return e;
-            k_grid_fast<false><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, j.n.pass_grid, s, j.offsets, gp);
+            k_grid_fast<false><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
         }
         j.launches += 1;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -132,14 +132,16 @@ struct Job {
     uint64_t staging_bytes = 0;
     float* lum = nullptr;        // per-sample luminance of the current push (fast grid pass)
     uint64_t lum_cap = 0;
-    float* cls[kClasses][5]{};   // per-pixel validity-class sums (arena)
-    uint8_t* pflags = nullptr;   // per-pixel screen-uniform / mixed flags (arena)
+    float* cls[kClasses][5]{};   // per-pixel validity-class sums of deviant pixels (arena)
+    float4* pat4 = nullptr;      // per-pixel pattern sums (count, sum y hi, lo, sum y^2 hi) (arena)
+    float2* pat2 = nullptr;      // per-pixel (sum y^2 lo, pattern | flags << 8 as bits) (arena)
     int64_t* offsets = nullptr;  // per-pixel sample offsets of the current push
     int64_t offsets_cap = 0;
     bool exact_grid = false;     // RPD_EXACT_GRID: double-precision grid in the reference's order
     bool exact_window = false;   // RPD_EXACT_WINDOW: double-precision StatMC window
     int grid_shape = 6;          // launch shape of the random-dimension grid pass (row groups x dimension sets)
     bool pass_open = false;
+    bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)
     bool features_valid = false;
     bool cache_valid = false;
     bool have_samples = false;
@@ -213,15 +215,23 @@ struct DeviceSamples {           // rpd_sample_soa with pointers in HBM
 // (hi, lo) and sum y^2 (hi, lo) over the pixel's finite samples.
 constexpr uint8_t kPixUniform = 0x1;  // every screen position lies inside its pixel
 constexpr uint8_t kPixMixed = 0x2;    // some sample has a random dimension but no screen position
+constexpr uint8_t kPixDeviant = 0x4;  // some sample's validity pattern differs from the pixel's pattern
 constexpr float kUniformMax = 1.0f - 1.0f / 4096.0f;  // largest in-pixel offset of a uniform pixel
 __host__ __device__ constexpr uint8_t class_bit(int c) {
     return c == 0 ? RPD_SAMPLE_PIXEL_VALID : c == 1 ? RPD_SAMPLE_BRDF_VALID : c == 2 ? RPD_SAMPLE_LENS_VALID
          : c == 3 ? RPD_SAMPLE_LIGHT_VALID : c == 4 ? RPD_SAMPLE_ENV_VALID : c == 5 ? RPD_SAMPLE_LIGHT_SELECT_VALID
          : RPD_SAMPLE_RR_VALID;
 }
+// Per-pixel inputs of the grid pass, written by the statistics pass for the pixels of a push.
+// A pixel's pattern is the validity-class bits (flags & 0xfe) of its first finite sample that
+// has any; pat4/pat2 hold the (count, sum y, sum y^2) double-float sums over its finite samples
+// with exactly that pattern, and the pattern and the pixel flags (kPix*) as the bits of
+// pat2.y: pattern | flags << 8. A pixel with other patterns too is deviant (kPixDeviant) and
+// then also has full per-class sums in cls[0..6].
 struct GridPrep {
     float* cls[kClasses][5];  // W*H planes
-    uint8_t* pflags;          // W*H
+    float4* pat4;             // W*H
+    float2* pat2;             // W*H
     float* lum;               // per sample of the push (NaN when the radiance is not finite)
     uint32_t* key;            // per sample of the push: packed random-dimension bins + validity
     int width;
