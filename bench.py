@@ -177,20 +177,29 @@ def run_gpu(args):
     params = R.synth_params(W, H, SEED + rank)
     dev = R.DeviceSamples(ctx, n, np_)
     ctx.synth_fill(params, 0, np_, SPP, dev)
+    samples = dev
+    quality = None
+    if args.precision == "fp16":
+        # the precision form: the same frame in compact storage; its error against the FP32 push
+        samples = R.DeviceSamples16.encode(ctx, dev, depth_scale=1.0)
+        quality = compact_quality(R, ctx, cfg, dev, samples)
     job = R.Job(ctx, cfg)
     if args.grid_shape:
         job.set_tuning("grid_shape", args.grid_shape)
 
     def step(samples):
         job.begin_frame()
-        job.push(samples, 0, np_, SPP)
+        if getattr(samples, "compact_host", False):
+            job.push16(samples, 0, np_, SPP, where=R.MEM_HOST)
+        else:
+            job.push(samples, 0, np_, SPP)
         job.end_pass()
         job.recompute_sensitivity()
         job.statmc_denoise()
         job.variance_denoise()
 
     for _ in range(args.warmup):
-        step(dev)
+        step(samples)
     job.sync()
     # device-resident timed region
     job.set_profiling(True)
@@ -201,7 +210,7 @@ def run_gpu(args):
     with ClockSampler(local) as clocks:
         job.mark(0)
         for _ in range(args.steps):
-            step(dev)
+            step(samples)
         job.mark(1)
         elapsed = job.elapsed_ms(0, 1)
     launches = job.launches() - launches0
@@ -214,7 +223,7 @@ def run_gpu(args):
     # end-to-end through the C ABI from pinned host buffers
     e2e = None
     if not args.no_e2e:
-        host = pinned_host_copy(R, ctx, dev)
+        host = pinned_host_copy(R, ctx, samples)
         denoised = np.empty((H, W, 3), dtype=np.float32)
         for _ in range(max(1, args.warmup)):
             step(host)
@@ -256,10 +265,16 @@ def run_gpu(args):
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": config_json(R, cfg),
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks.summary(), "roofline": roofline,
         "kernels_ms_per_step": kernels_ms,
+        "storage": "fp16/snorm16/unorm16 per-sample planes (32 B/sample), fp32 accumulation"
+                   if args.precision == "fp16" else "fp32 per-sample planes (62 B/sample)",
     }
+    if quality is not None:
+        out["quality"] = quality
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, steps=1)
     job.close()
+    if samples is not dev:
+        samples.free()
     dev.free()
     ctx.close()
     if rank == 0:
@@ -270,7 +285,11 @@ def pinned_host_copy(R, ctx, dev):
     """Copy device sample planes into page-locked host planes (for the end-to-end leg)."""
     import ctypes as C
 
+    compact = isinstance(dev, R.DeviceSamples16)
+
     class PinnedSamples:
+        compact_host = compact
+
         def __init__(self):
             self.ptrs = []
             self.planes = {}
@@ -287,9 +306,12 @@ def pinned_host_copy(R, ctx, dev):
                 self.planes[name] = arrs
 
         def soa(self):
-            s = R.SampleSoA()
+            s = R.SampleSoA16() if compact else R.SampleSoA()
+            if compact:
+                s.depth_scale = dev.depth_scale
+            table = R.PLANES16 if compact else R.PLANES
             for name, arrs in self.planes.items():
-                if len(arrs) == 1 and R.PLANES[name][0] == 1:
+                if len(arrs) == 1 and table[name][0] == 1:
                     setattr(s, name, arrs[0])
                 else:
                     f = getattr(s, name)
@@ -303,6 +325,26 @@ def pinned_host_copy(R, ctx, dev):
             self.ptrs = []
 
     return PinnedSamples()
+
+
+def compact_quality(R, ctx, cfg, dev, dev16):
+    """relMSE = mean((x - r)^2 / (r^2 + 1e-2)) and max relative error of the compact-storage
+    frame against the same frame pushed as FP32 planes."""
+    out = []
+    for samples in (dev, dev16):
+        job = R.Job(ctx, cfg)
+        job.begin_frame()
+        job.push(samples, 0, W * H, SPP)
+        job.end_pass()
+        job.recompute_sensitivity()
+        job.statmc_denoise()
+        job.variance_denoise()
+        out.append(job.read("DENOISED").astype(np.float64))
+        job.close()
+    r, x = out
+    return {"reference": "the same frame pushed as FP32 planes (the oracle-pinned path)",
+            "rel_mse": float(np.mean((x - r) ** 2 / (r * r + 1e-2))),
+            "max_rel_err": float(np.max(np.abs(x - r) / np.maximum(np.abs(r), 1e-3)))}
 
 
 def measured_peaks():
@@ -368,11 +410,15 @@ def main():
     ap.add_argument("--width", type=int, default=W)
     ap.add_argument("--height", type=int, default=H)
     ap.add_argument("--spp", type=int, default=SPP)
-    ap.add_argument("--grid-shape", type=int, default=0, help="random-dimension grid launch shape 1..5 (0: default)")
+    ap.add_argument("--grid-shape", type=int, default=0, help="random-dimension grid launch shape 1..6 (0: default)")
+    ap.add_argument("--precision", choices=["fp32", "fp16"], default="fp32",
+                    help="fp16: the precision form (compact per-sample storage, single-precision accumulation)")
     args = ap.parse_args()
     if (args.width, args.height, args.spp) != (W, H, SPP):
         W, H, SPP = args.width, args.height, args.spp
         METRIC = f"denoised Msamples/s at {W}x{H} {SPP}spp (plain)"
+    if args.precision == "fp16":
+        METRIC = METRIC.replace("(plain)", "(fp16 storage)")
     if args.impl == "reference":
         run_reference(args)
     else:

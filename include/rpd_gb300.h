@@ -282,6 +282,42 @@ int rpd_job_begin_frame(rpd_job* job);
 int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first_pixel,
                          int64_t pixel_count, int32_t spp, const int32_t* counts,
                          rpd_memory where);
+/*
+ * Compact per-sample storage (the precision form; no counterpart in the reference): the same
+ * record in 32 bytes per sample instead of 62-74, decoded to float by the statistics pass,
+ * which then accumulates in single precision exactly as for rpd_sample_soa:
+ *   sqrt_radiance   IEEE binary16 of sqrt(max(radiance, 0)) per channel (a non-finite
+ *                   radiance stays non-finite and drops the sample); radiance = s * s
+ *   normal          snorm16, n = max(q / 32767, -1)
+ *   depth           binary16 of depth / depth_scale; depth = d * depth_scale
+ *   pixel_albedo    binary16 per pixel (per-sample albedo is not carried)
+ *   *_u             unorm16, u = q / 65536 (the 4x4 bins of Dependency2D::add are those
+ *                   of the unquantised u: floor(u * 4) == floor(q / 16384))
+ *   flags, category as in rpd_sample_soa.
+ */
+typedef struct rpd_sample_soa16 {
+    const uint16_t* sqrt_radiance[3];
+    const int16_t* normal[3];
+    const uint16_t* depth;
+    const uint16_t* pixel_albedo[3];
+    const uint16_t* pixel_u[2];
+    const uint16_t* lens_u[2];
+    const uint16_t* brdf_u[2];
+    const uint16_t* light_u[2];
+    const uint16_t* env_u[2];
+    const uint8_t* flags;
+    const uint8_t* category;
+    float depth_scale;
+} rpd_sample_soa16;
+int rpd_job_push_samples16(rpd_job* job, const rpd_sample_soa16* s, int64_t first_pixel,
+                           int64_t pixel_count, int32_t spp, const int32_t* counts,
+                           rpd_memory where);
+/* Encode device-resident rpd_sample_soa planes (n_samples samples, n_pixels pixels) into
+ * device-resident rpd_sample_soa16 planes (out's pointers; out->depth_scale is used). The
+ * per-pixel albedo comes from in->pixel_albedo. */
+int rpd_encode_samples16(rpd_ctx* ctx, const rpd_sample_soa* in, int64_t n_samples, int64_t n_pixels,
+                         const rpd_sample_soa16* out);
+
 /* End of a render pass: merge_rpf_grids_into (main.cpp:378-388, 730, 1531) and cache
  * invalidation (main.cpp:1533). */
 int rpd_job_end_pass(rpd_job* job);

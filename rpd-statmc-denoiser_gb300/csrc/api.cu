@@ -565,6 +565,9 @@ int rpd_job_begin_frame(rpd_job* job) {
     return RPD_OK;
 }
 
+static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
+                     rpd_memory where, int64_t total);
+
 int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first, int64_t count, int32_t spp,
                          const int32_t* counts, rpd_memory where) {
     Job* j = reinterpret_cast<Job*>(job);
@@ -670,6 +673,156 @@ int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first, i
     if (!d.normal[0] || !d.normal[1] || !d.normal[2] || !d.depth ||
         (!d.albedo[0] && !d.pixel_albedo[0]))
         return fail(RPD_ERR_INVALID_ARGUMENT, "normal, depth and albedo (per sample or per pixel) are required");
+    return push_tail(j, d, first, count, spp, counts, where, total);
+}
+
+// The part of a push shared by both sample formats: the offsets are computed, d points at
+// device planes. Runs the statistics pass and the grid pass.
+int rpd_job_push_samples16(rpd_job* job, const rpd_sample_soa16* s, int64_t first, int64_t count, int32_t spp,
+                           const int32_t* counts, rpd_memory where) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!s) return fail(RPD_ERR_INVALID_ARGUMENT, "null sample planes");
+    if (first < 0 || count < 0 || first + count > j->g.np)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "pixel span [" + std::to_string(first) + ", " +
+                                                  std::to_string(first + count) + ") is outside the image");
+    if (!counts && spp < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "negative spp");
+    if (j->exact_grid) return fail(RPD_ERR_STATE, "the exact grid mode needs rpd_sample_soa planes");
+    if (count == 0) return RPD_OK;
+    for (int c = 0; c < 3; ++c)
+        if (!s->sqrt_radiance[c] || !s->normal[c] || !s->pixel_albedo[c])
+            return fail(RPD_ERR_INVALID_ARGUMENT, "sqrt_radiance, normal and pixel_albedo planes are required");
+    if (!s->depth || !s->flags) return fail(RPD_ERR_INVALID_ARGUMENT, "depth and flags planes are required");
+    if (!(s->depth_scale > 0.0f) || !std::isfinite(s->depth_scale))
+        return fail(RPD_ERR_INVALID_ARGUMENT, "depth_scale must be finite and positive");
+    {
+        auto pair_ok = [](const uint16_t* const* v) { return (v[0] == nullptr) == (v[1] == nullptr); };
+        if (!pair_ok(s->pixel_u) || !pair_ok(s->lens_u) || !pair_ok(s->brdf_u) || !pair_ok(s->light_u) ||
+            !pair_ok(s->env_u))
+            return fail(RPD_ERR_INVALID_ARGUMENT, "a multi-component sample plane is only partly given");
+    }
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    int st = ensure_offsets(*j, count);
+    if (st != RPD_OK) return st;
+    StageTimer timer(*j, RPD_STAGE_ACCUMULATE);
+    int64_t total = 0;
+    if (counts) {
+        if (where == RPD_MEM_HOST) {
+            for (int64_t i = 0; i < count; ++i) {
+                if (counts[i] < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "negative per-pixel sample count");
+                total += counts[i];
+            }
+        }
+    } else {
+        total = int64_t(count) * spp;
+    }
+    DeviceSamples d{};
+    d.compact = 1;
+    d.c16.depth_scale = s->depth_scale;
+    if (where == RPD_MEM_HOST) {
+        struct Plane { const void* src; uint64_t bytes; const void** dst; };
+        std::vector<Plane> planes;
+        auto hplane = [&](const void* src, const void* const* dst, int64_t n, int elem) {
+            if (src) planes.push_back({src, uint64_t(n) * uint64_t(elem), const_cast<const void**>(dst)});
+        };
+        for (int c = 0; c < 3; ++c) {
+            hplane(s->sqrt_radiance[c], reinterpret_cast<const void* const*>(&d.c16.sqrt_radiance[c]), total, 2);
+            hplane(s->normal[c], reinterpret_cast<const void* const*>(&d.c16.normal[c]), total, 2);
+            hplane(s->pixel_albedo[c], reinterpret_cast<const void* const*>(&d.c16.pixel_albedo[c]), count, 2);
+        }
+        hplane(s->depth, reinterpret_cast<const void* const*>(&d.c16.depth), total, 2);
+        for (int c = 0; c < 2; ++c) {
+            hplane(s->pixel_u[c], reinterpret_cast<const void* const*>(&d.c16.pixel_u[c]), total, 2);
+            hplane(s->lens_u[c], reinterpret_cast<const void* const*>(&d.c16.lens_u[c]), total, 2);
+            hplane(s->brdf_u[c], reinterpret_cast<const void* const*>(&d.c16.brdf_u[c]), total, 2);
+            hplane(s->light_u[c], reinterpret_cast<const void* const*>(&d.c16.light_u[c]), total, 2);
+            hplane(s->env_u[c], reinterpret_cast<const void* const*>(&d.c16.env_u[c]), total, 2);
+        }
+        hplane(s->flags, reinterpret_cast<const void* const*>(&d.flags), total, 1);
+        hplane(s->category, reinterpret_cast<const void* const*>(&d.category), total, 1);
+        const int32_t* d_counts = nullptr;
+        if (counts) planes.push_back({counts, uint64_t(count) * 4, reinterpret_cast<const void**>(&d_counts)});
+        uint64_t need = 0;
+        for (auto& p : planes) need = ((need + 255) & ~uint64_t(255)) + p.bytes;
+        st = grow_device(*j, &j->staging, &j->staging_bytes, need + 256);
+        if (st != RPD_OK) return st;
+        uint64_t off = 0;
+        for (auto& p : planes) {
+            off = (off + 255) & ~uint64_t(255);
+            char* dst = static_cast<char*>(j->staging) + off;
+            if (p.bytes) RPD_CUDA(cudaMemcpyAsync(dst, p.src, p.bytes, cudaMemcpyHostToDevice, j->stream));
+            *p.dst = dst;
+            off += p.bytes;
+        }
+        if (counts) RPD_CUDA(launch_offsets_scan(*j, d_counts, count));
+        else RPD_CUDA(launch_offsets_uniform(*j, count, spp));
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            d.c16.sqrt_radiance[c] = s->sqrt_radiance[c];
+            d.c16.normal[c] = s->normal[c];
+            d.c16.pixel_albedo[c] = s->pixel_albedo[c];
+        }
+        d.c16.depth = s->depth;
+        for (int c = 0; c < 2; ++c) {
+            d.c16.pixel_u[c] = s->pixel_u[c];
+            d.c16.lens_u[c] = s->lens_u[c];
+            d.c16.brdf_u[c] = s->brdf_u[c];
+            d.c16.light_u[c] = s->light_u[c];
+            d.c16.env_u[c] = s->env_u[c];
+        }
+        d.flags = s->flags;
+        d.category = s->category;
+        if (counts) RPD_CUDA(launch_offsets_scan(*j, counts, count));
+        else RPD_CUDA(launch_offsets_uniform(*j, count, spp));
+    }
+    return push_tail(j, d, first, count, spp, counts, where, total);
+}
+
+int rpd_encode_samples16(rpd_ctx* ctx, const rpd_sample_soa* in, int64_t n_samples, int64_t n_pixels,
+                         const rpd_sample_soa16* out) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !in || !out || n_samples < 0 || n_pixels < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "bad encode arguments");
+    if (!(out->depth_scale > 0.0f) || !std::isfinite(out->depth_scale))
+        return fail(RPD_ERR_INVALID_ARGUMENT, "depth_scale must be finite and positive");
+    for (int k = 0; k < 3; ++k)
+        if (!in->radiance[k] || !in->normal[k] || !out->sqrt_radiance[k] || !out->normal[k])
+            return fail(RPD_ERR_INVALID_ARGUMENT, "radiance and normal planes are required on both sides");
+    if (!in->depth || !out->depth) return fail(RPD_ERR_INVALID_ARGUMENT, "depth planes are required on both sides");
+    DeviceSamples d{};
+    for (int k = 0; k < 3; ++k) {
+        d.radiance[k] = in->radiance[k];
+        d.normal[k] = in->normal[k];
+        d.pixel_albedo[k] = in->pixel_albedo[k];
+    }
+    d.depth = in->depth;
+    DeviceSamples16 o{};
+    for (int k = 0; k < 3; ++k) {
+        o.sqrt_radiance[k] = out->sqrt_radiance[k];
+        o.normal[k] = out->normal[k];
+        o.pixel_albedo[k] = out->pixel_albedo[k];
+    }
+    o.depth = out->depth;
+    o.depth_scale = out->depth_scale;
+    auto dim = [](const float* const* a, const uint16_t* const* b, const float** da, const uint16_t** db) {
+        if (a[0] && b[0]) {
+            da[0] = a[0]; da[1] = a[1];
+            db[0] = b[0]; db[1] = b[1];
+        }
+    };
+    dim(in->pixel_u, out->pixel_u, d.pixel_u, o.pixel_u);
+    dim(in->lens_u, out->lens_u, d.lens_u, o.lens_u);
+    dim(in->brdf_u, out->brdf_u, d.brdf_u, o.brdf_u);
+    dim(in->light_u, out->light_u, d.light_u, o.light_u);
+    dim(in->env_u, out->env_u, d.env_u, o.env_u);
+    RPD_CUDA(cudaSetDevice(c->device));
+    RPD_CUDA(launch_encode_samples16(d, n_samples, n_pixels, o, c->util_stream));
+    RPD_CUDA(cudaStreamSynchronize(c->util_stream));
+    return RPD_OK;
+}
+
+static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
+                     rpd_memory where, int64_t total) {
+    int st = RPD_OK;
     const bool rpd = j->cfg.rpf_shrinkage_scale > 0.0f;
     if (rpd && !d.category) return fail(RPD_ERR_INVALID_ARGUMENT, "category plane is required when RPD is enabled");
     GridPrep gp{};

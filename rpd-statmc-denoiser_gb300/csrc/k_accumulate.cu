@@ -12,6 +12,8 @@
 //   k_merge_grid         merge_rpf_grids_into (main.cpp:378-388).
 //   k_feature_cache      ensure_feature_cache (main.cpp:94-122).
 //   k_finalize           FrameBuffers::finalize (core/buffers.h:152-167).
+#include <cuda_fp16.h>
+
 #include "rpd_internal.h"
 #include "device_math.cuh"
 
@@ -194,9 +196,23 @@ __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, 
 __device__ __forceinline__ float4 ld4(const float* p, int64_t k) { return *reinterpret_cast<const float4*>(p + k); }
 __device__ __forceinline__ float lane4(const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
 
+// rpd_sample_soa16 decoding (include/rpd_gb300.h)
+__device__ __forceinline__ float h2f(uint16_t h) { return __half2float(__ushort_as_half(h)); }
+__device__ __forceinline__ float snorm16(int16_t q) { return fmaxf(float(q) * (1.0f / 32767.0f), -1.0f); }
+__device__ __forceinline__ float unorm16(uint16_t q) { return float(q) * (1.0f / 65536.0f); }
+__device__ __forceinline__ float sq(float v) { return v * v; }
+// four consecutive 16-bit values (8-byte aligned) as sample i of the load
+__device__ __forceinline__ uint2 ld4h(const void* p, int64_t k) {
+    return *reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(p) + k);
+}
+__device__ __forceinline__ uint16_t lane4h(const uint2& v, int i) {
+    return uint16_t((i < 2 ? v.x : v.y) >> (16 * (i & 1)));
+}
+
 // VEC4: every present plane is 16-byte aligned at the pixel's first sample and the pixel's
-// sample count is a multiple of 4, so each plane is read four samples per load.
-template <bool VEC4>
+// sample count is a multiple of 4, so each plane is read four samples per load. COMPACT: the
+// planes are rpd_sample_soa16's (s.c16), decoded to float here.
+template <bool VEC4, bool COMPACT>
 __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets,
                                                            int32_t spp, int64_t first, int64_t count, GridPrep gp) {
     const int64_t local = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -205,11 +221,16 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
     const int64_t k0 = offsets ? offsets[local] : local * spp;
     const int64_t k1 = offsets ? offsets[local + 1] : (local + 1) * spp;
     const bool prep = gp.lum != nullptr;
-    const uint8_t plane_mask = uint8_t(0xffu & ~((s.pixel_u[0] ? 0 : RPD_SAMPLE_PIXEL_VALID) |
-                                                 (s.lens_u[0] ? 0 : RPD_SAMPLE_LENS_VALID) |
-                                                 (s.brdf_u[0] ? 0 : RPD_SAMPLE_BRDF_VALID) |
-                                                 (s.light_u[0] ? 0 : RPD_SAMPLE_LIGHT_VALID) |
-                                                 (s.env_u[0] ? 0 : RPD_SAMPLE_ENV_VALID)));
+    const bool has_pu = COMPACT ? s.c16.pixel_u[0] != nullptr : s.pixel_u[0] != nullptr;
+    const bool has_lu = COMPACT ? s.c16.lens_u[0] != nullptr : s.lens_u[0] != nullptr;
+    const bool has_bu = COMPACT ? s.c16.brdf_u[0] != nullptr : s.brdf_u[0] != nullptr;
+    const bool has_li = COMPACT ? s.c16.light_u[0] != nullptr : s.light_u[0] != nullptr;
+    const bool has_eu = COMPACT ? s.c16.env_u[0] != nullptr : s.env_u[0] != nullptr;
+    const uint8_t plane_mask = uint8_t(0xffu & ~((has_pu ? 0 : RPD_SAMPLE_PIXEL_VALID) |
+                                                 (has_lu ? 0 : RPD_SAMPLE_LENS_VALID) |
+                                                 (has_bu ? 0 : RPD_SAMPLE_BRDF_VALID) |
+                                                 (has_li ? 0 : RPD_SAMPLE_LIGHT_VALID) |
+                                                 (has_eu ? 0 : RPD_SAMPLE_ENV_VALID)));
     const float fx = float(idx % gp.width), fy = float(idx / gp.width);
     PixelAcc a;
     a.pflags = kPixUniform;
@@ -239,14 +260,92 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
     a.dep = p.depth[idx];
     a.hits = p.hit_count[idx];
     a.nsamples = p.sample_count[idx];
-    const bool per_sample_albedo = s.albedo[0] != nullptr;
+    const bool per_sample_albedo = !COMPACT && s.albedo[0] != nullptr;
     float palb[3] = {0.0f, 0.0f, 0.0f};
-    if (!per_sample_albedo && s.pixel_albedo[0]) {
+    if (COMPACT) {
+        if (s.c16.pixel_albedo[0])
+            for (int c = 0; c < 3; ++c) palb[c] = h2f(s.c16.pixel_albedo[c][local]);
+    } else if (!per_sample_albedo && s.pixel_albedo[0]) {
         for (int c = 0; c < 3; ++c) palb[c] = s.pixel_albedo[c][local];
     }
     const bool dims = prep;  // the random dimensions are only read for the grid pass
 
-    if (VEC4) {
+    if (COMPACT) {
+        const DeviceSamples16& h = s.c16;
+        const float dscale = h.depth_scale;
+        if (VEC4) {
+            for (int64_t k = k0; k < k1; k += 4) {
+                uint2 L[3], N[3], D, PU[2], LU[2], BU[2], LI[2], EU[2];
+                for (int c = 0; c < 3; ++c) {
+                    L[c] = ld4h(h.sqrt_radiance[c], k);
+                    N[c] = ld4h(h.normal[c], k);
+                }
+                D = ld4h(h.depth, k);
+                const uint2 z = make_uint2(0u, 0u);
+                for (int c = 0; c < 2; ++c) {
+                    PU[c] = (dims && has_pu) ? ld4h(h.pixel_u[c], k) : z;
+                    LU[c] = (dims && has_lu) ? ld4h(h.lens_u[c], k) : z;
+                    BU[c] = (dims && has_bu) ? ld4h(h.brdf_u[c], k) : z;
+                    LI[c] = (dims && has_li) ? ld4h(h.light_u[c], k) : z;
+                    EU[c] = (dims && has_eu) ? ld4h(h.env_u[c], k) : z;
+                }
+                const uint32_t F4 = *reinterpret_cast<const uint32_t*>(s.flags + k);
+                const uint32_t C4 = (dims && s.category) ? *reinterpret_cast<const uint32_t*>(s.category + k) : 0u;
+                float lum4[4];
+                uint32_t key4[4];
+                #pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    SampleIn in;
+                    for (int c = 0; c < 3; ++c) {
+                        in.L[c] = sq(h2f(lane4h(L[c], i)));
+                        in.n[c] = snorm16(int16_t(lane4h(N[c], i)));
+                        in.alb[c] = 0.0f;
+                    }
+                    in.d = h2f(lane4h(D, i)) * dscale;
+                    for (int c = 0; c < 2; ++c) {
+                        in.pu[c] = unorm16(lane4h(PU[c], i));
+                        in.lu[c] = unorm16(lane4h(LU[c], i));
+                        in.bu[c] = unorm16(lane4h(BU[c], i));
+                        in.liu[c] = unorm16(lane4h(LI[c], i));
+                        in.eu[c] = unorm16(lane4h(EU[c], i));
+                    }
+                    in.f = uint8_t(F4 >> (8 * i));
+                    in.cat = uint8_t(C4 >> (8 * i));
+                    process_sample(a, in, false, palb, prep, plane_mask, fx, fy, lum4[i], key4[i]);
+                }
+                if (prep) {
+                    *reinterpret_cast<float4*>(gp.lum + k) = make_float4(lum4[0], lum4[1], lum4[2], lum4[3]);
+                    *reinterpret_cast<uint4*>(gp.key + k) = make_uint4(key4[0], key4[1], key4[2], key4[3]);
+                }
+            }
+        } else {
+            for (int64_t k = k0; k < k1; ++k) {
+                SampleIn in;
+                for (int c = 0; c < 3; ++c) {
+                    in.L[c] = sq(h2f(h.sqrt_radiance[c][k]));
+                    in.n[c] = snorm16(h.normal[c][k]);
+                    in.alb[c] = 0.0f;
+                }
+                in.d = h2f(h.depth[k]) * dscale;
+                for (int c = 0; c < 2; ++c) {
+                    in.pu[c] = (dims && has_pu) ? unorm16(h.pixel_u[c][k]) : 0.0f;
+                    in.lu[c] = (dims && has_lu) ? unorm16(h.lens_u[c][k]) : 0.0f;
+                    in.bu[c] = (dims && has_bu) ? unorm16(h.brdf_u[c][k]) : 0.0f;
+                    in.liu[c] = (dims && has_li) ? unorm16(h.light_u[c][k]) : 0.0f;
+                    in.eu[c] = (dims && has_eu) ? unorm16(h.env_u[c][k]) : 0.0f;
+                }
+                in.f = s.flags[k];
+                in.cat = (dims && s.category) ? s.category[k] : 0;
+                float lum;
+                uint32_t key;
+                process_sample(a, in, false, palb, prep, plane_mask, fx, fy, lum, key);
+                if (prep) {
+                    gp.lum[k] = lum;
+                    gp.key[k] = key;
+                }
+            }
+        }
+    } else if (VEC4) {
         for (int64_t k = k0; k < k1; k += 4) {
             float4 L[3], N[3], A[3], D, PU[2], LU[2], BU[2], LI[2], EU[2];
             for (int c = 0; c < 3; ++c) {
@@ -597,20 +696,34 @@ cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count) 
 cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,
                                      const GridPrep& gp, int32_t spp) {
     KernelScope ks(j, RPD_KERNEL_ACCUMULATE_PIXELS);
-    auto aligned = [](const void* ptr) { return (reinterpret_cast<uintptr_t>(ptr) & 15u) == 0; };
-    bool vec4 = spp > 0 && spp % 4 == 0 && aligned(s.depth) && aligned(s.flags) &&
-                (!s.category || aligned(s.category));
-    for (int c = 0; c < 3; ++c)
-        vec4 = vec4 && aligned(s.radiance[c]) && aligned(s.normal[c]) && (!s.albedo[0] || aligned(s.albedo[c]));
-    for (int c = 0; c < 2; ++c)
-        vec4 = vec4 && (!s.pixel_u[0] || aligned(s.pixel_u[c])) && (!s.lens_u[0] || aligned(s.lens_u[c])) &&
-               (!s.brdf_u[0] || aligned(s.brdf_u[c])) && (!s.light_u[0] || aligned(s.light_u[c])) &&
-               (!s.env_u[0] || aligned(s.env_u[c]));
-    vec4 = vec4 && (!gp.lum || (aligned(gp.lum) && aligned(gp.key)));
-    if (vec4)
-        k_accumulate_pixels<true><<<grid_for(count, 128), 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
-    else
-        k_accumulate_pixels<false><<<grid_for(count, 128), 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+    auto aligned = [](const void* ptr, uintptr_t a) { return (reinterpret_cast<uintptr_t>(ptr) & (a - 1)) == 0; };
+    bool vec4 = spp > 0 && spp % 4 == 0 && aligned(s.flags, 16) && (!s.category || aligned(s.category, 16));
+    if (s.compact) {
+        const DeviceSamples16& h = s.c16;
+        for (int c = 0; c < 3; ++c) vec4 = vec4 && aligned(h.sqrt_radiance[c], 8) && aligned(h.normal[c], 8);
+        vec4 = vec4 && aligned(h.depth, 8);
+        for (int c = 0; c < 2; ++c)
+            vec4 = vec4 && (!h.pixel_u[0] || aligned(h.pixel_u[c], 8)) && (!h.lens_u[0] || aligned(h.lens_u[c], 8)) &&
+                   (!h.brdf_u[0] || aligned(h.brdf_u[c], 8)) && (!h.light_u[0] || aligned(h.light_u[c], 8)) &&
+                   (!h.env_u[0] || aligned(h.env_u[c], 8));
+    } else {
+        vec4 = vec4 && aligned(s.depth, 16);
+        for (int c = 0; c < 3; ++c)
+            vec4 = vec4 && aligned(s.radiance[c], 16) && aligned(s.normal[c], 16) && (!s.albedo[0] || aligned(s.albedo[c], 16));
+        for (int c = 0; c < 2; ++c)
+            vec4 = vec4 && (!s.pixel_u[0] || aligned(s.pixel_u[c], 16)) && (!s.lens_u[0] || aligned(s.lens_u[c], 16)) &&
+                   (!s.brdf_u[0] || aligned(s.brdf_u[c], 16)) && (!s.light_u[0] || aligned(s.light_u[c], 16)) &&
+                   (!s.env_u[0] || aligned(s.env_u[c], 16));
+    }
+    vec4 = vec4 && (!gp.lum || (aligned(gp.lum, 16) && aligned(gp.key, 16)));
+    const unsigned blocks = grid_for(count, 128);
+    if (s.compact) {
+        if (vec4) k_accumulate_pixels<true, true><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else k_accumulate_pixels<false, true><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+    } else {
+        if (vec4) k_accumulate_pixels<true, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else k_accumulate_pixels<false, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+    }
     j.launches += 1;
     return cudaGetLastError();
 }

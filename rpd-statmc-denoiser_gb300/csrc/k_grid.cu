@@ -71,6 +71,11 @@ struct Totals {
     DF w, w2, y, y2;
 };
 
+// The screen position (pixel_u) of sample k, from either sample-plane format.
+__device__ __forceinline__ float sample_pu(const DeviceSamples& s, int c, int64_t k) {
+    return s.compact ? float(s.c16.pixel_u[c][k]) * (1.0f / 65536.0f) : s.pixel_u[c][k];
+}
+
 // Dependency2D::add bin (core/stats.h:166-168)
 __device__ __forceinline__ int bin2d(float u, float v) {
     const int x = iclamps(int(u * 4.0f), 0, 3);
@@ -326,8 +331,8 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, flo
                 const uint32_t key = gp.key[k];
                 if (!(key & pbit) || !(key & vbit)) continue;
                 const float yv = gp.lum[k];
-                const float su = fclamps((fx + s.pixel_u[0][k] - support_left) / support, 0.0f, 1.0f);
-                const float sv = fclamps((fy + s.pixel_u[1][k] - support_top) / support, 0.0f, 1.0f);
+                const float su = fclamps((fx + sample_pu(s, 0, k) - support_left) / support, 0.0f, 1.0f);
+                const float sv = fclamps((fy + sample_pu(s, 1, k) - support_top) / support, 0.0f, 1.0f);
                 const int b = bin2d(su, sv);
                 bins.add_weight(b, pw, 1.0f);
                 bins.add_sum(b, pw, yv, 0.0f);
@@ -407,8 +412,8 @@ __global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pas
             const uint32_t key = gp.key[k];
             if (!(key & pbit) || !(key & vbit)) continue;
             const float yv = gp.lum[k];
-            const float su = fclamps((fx + s.pixel_u[0][k] - support_left) / support, 0.0f, 1.0f);
-            const float sv = fclamps((fy + s.pixel_u[1][k] - support_top) / support, 0.0f, 1.0f);
+            const float su = fclamps((fx + sample_pu(s, 0, k) - support_left) / support, 0.0f, 1.0f);
+            const float sv = fclamps((fy + sample_pu(s, 1, k) - support_top) / support, 0.0f, 1.0f);
             const int b = bin2d(su, sv);
             bins.add_weight(b, pw, 1.0f);
             bins.add_sum(b, pw, yv, 0.0f);

@@ -194,7 +194,22 @@ int cuda_fail(cudaError_t e, const char* what);
     } while (0)
 
 // ---- kernels (launch wrappers; each returns cudaError_t of the launch) -------------------
+struct DeviceSamples16 {         // rpd_sample_soa16 with pointers in HBM
+    const uint16_t* sqrt_radiance[3];
+    const int16_t* normal[3];
+    const uint16_t* depth;
+    const uint16_t* pixel_albedo[3];
+    const uint16_t* pixel_u[2];
+    const uint16_t* lens_u[2];
+    const uint16_t* brdf_u[2];
+    const uint16_t* light_u[2];
+    const uint16_t* env_u[2];
+    float depth_scale;
+};
+
 struct DeviceSamples {           // rpd_sample_soa with pointers in HBM
+    int compact;                 // 1: the planes are rpd_sample_soa16's, in c16 (flags and category below)
+    DeviceSamples16 c16;
     const float* radiance[3];
     const float* normal[3];
     const float* depth;
@@ -249,6 +264,8 @@ __host__ __device__ constexpr int key_bin_shift(int group) {
     return group == 1 ? 4 : group == 2 ? 0 : group == 3 ? 8 : group == 4 ? 12 : 16;
 }
 
+cudaError_t launch_encode_samples16(const DeviceSamples& in, int64_t n_samples, int64_t n_pixels,
+                                    const DeviceSamples16& out, cudaStream_t stream);
 cudaError_t launch_offsets_uniform(Job& j, int64_t count, int32_t spp);
 cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count);
 cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,

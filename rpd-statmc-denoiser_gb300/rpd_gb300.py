@@ -117,6 +117,16 @@ class SampleSoA(C.Structure):
     ]
 
 
+class SampleSoA16(C.Structure):
+    """rpd_sample_soa16: the compact per-sample record (precision form)."""
+    _fields_ = [
+        ("sqrt_radiance", C.c_void_p * 3), ("normal", C.c_void_p * 3), ("depth", C.c_void_p),
+        ("pixel_albedo", C.c_void_p * 3), ("pixel_u", C.c_void_p * 2), ("lens_u", C.c_void_p * 2),
+        ("brdf_u", C.c_void_p * 2), ("light_u", C.c_void_p * 2), ("env_u", C.c_void_p * 2),
+        ("flags", C.c_void_p), ("category", C.c_void_p), ("depth_scale", C.c_float),
+    ]
+
+
 class SynthParams(C.Structure):
     """rpd_synth_params (include/rpd_synth.h)."""
     _fields_ = [
@@ -230,6 +240,8 @@ def lib() -> C.CDLL:
         "rpd_job_get_tuning": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
         "rpd_job_begin_frame": (C.c_int, [vp]),
         "rpd_job_push_samples": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp, C.c_int]),
+        "rpd_job_push_samples16": (C.c_int, [vp, C.POINTER(SampleSoA16), i64, i64, i32, vp, C.c_int]),
+        "rpd_encode_samples16": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, C.POINTER(SampleSoA16)]),
         "rpd_job_end_pass": (C.c_int, [vp]),
         "rpd_recompute_sensitivity": (C.c_int, [vp]),
         "rpd_statmc_denoise": (C.c_int, [vp]),
@@ -273,7 +285,7 @@ def exported_symbols() -> list[str]:
     return ["rpd_config_defaults", "rpd_config_validate", "rpd_ctx_create", "rpd_ctx_destroy", "rpd_job_footprint",
             "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config", "rpd_job_set_exact",
             "rpd_job_set_tuning", "rpd_job_get_tuning",
-            "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_end_pass", "rpd_recompute_sensitivity",
+            "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_push_samples16", "rpd_encode_samples16", "rpd_job_end_pass", "rpd_recompute_sensitivity",
             "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
             "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
             "rpd_job_set_profiling", "rpd_job_kernel_time", "rpd_job_reset_kernel_times", "rpd_kernel_name",
@@ -387,6 +399,73 @@ class DeviceSamples:
         self.bufs = {}
 
 
+# Compact planes: name -> (components, dtype, per)
+PLANES16 = {
+    "sqrt_radiance": (3, np.uint16, "sample"), "normal": (3, np.int16, "sample"), "depth": (1, np.uint16, "sample"),
+    "pixel_albedo": (3, np.uint16, "pixel"), "pixel_u": (2, np.uint16, "sample"), "lens_u": (2, np.uint16, "sample"),
+    "brdf_u": (2, np.uint16, "sample"), "light_u": (2, np.uint16, "sample"), "env_u": (2, np.uint16, "sample"),
+    "flags": (1, np.uint8, "sample"), "category": (1, np.uint8, "sample"),
+}
+# the compact planes that carry a given rpd_sample_soa plane
+FROM32 = {"radiance": "sqrt_radiance", "normal": "normal", "depth": "depth", "pixel_albedo": "pixel_albedo",
+          "pixel_u": "pixel_u", "lens_u": "lens_u", "brdf_u": "brdf_u", "light_u": "light_u", "env_u": "env_u",
+          "flags": "flags", "category": "category"}
+
+
+class DeviceSamples16:
+    """rpd_sample_soa16 planes in HBM (the precision form's storage)."""
+
+    def __init__(self, ctx: "Context", n_samples: int, n_pixels: int, planes: tuple[str, ...], depth_scale=1.0):
+        self.ctx = ctx
+        self.n_samples, self.n_pixels = int(n_samples), int(n_pixels)
+        self.depth_scale = float(depth_scale)
+        self.bufs: dict[str, list[DeviceBuffer]] = {}
+        for name in planes:
+            comps, dt, per = PLANES16[name]
+            n = self.n_samples if per == "sample" else self.n_pixels
+            self.bufs[name] = [DeviceBuffer(ctx, max(1, n) * np.dtype(dt).itemsize) for _ in range(comps)]
+
+    @classmethod
+    def encode(cls, ctx: "Context", dev: "DeviceSamples", depth_scale: float = 1.0) -> "DeviceSamples16":
+        """rpd_encode_samples16 of device-resident FP32 planes; flags/category are copied."""
+        planes = tuple(FROM32[n] for n in dev.bufs if n in FROM32)
+        out = cls(ctx, dev.n_samples, dev.n_pixels, planes, depth_scale)
+        check(lib().rpd_encode_samples16(ctx.handle, C.byref(dev.soa()), dev.n_samples, dev.n_pixels,
+                                         C.byref(out.soa())))
+        for name in ("flags", "category"):
+            if name in dev.bufs:
+                src, dst = dev.bufs[name][0], out.bufs[name][0]
+                check(lib().rpd_memcpy(ctx.handle, dst.ptr, src.ptr, dev.n_samples, 2))
+        return out
+
+    def soa(self) -> SampleSoA16:
+        s = SampleSoA16()
+        for name, bl in self.bufs.items():
+            if PLANES16[name][0] == 1:
+                setattr(s, name, bl[0].ptr)
+            else:
+                field = getattr(s, name)
+                for c, b in enumerate(bl):
+                    field[c] = b.ptr
+        s.depth_scale = self.depth_scale
+        return s
+
+    @property
+    def nbytes(self) -> int:
+        total = 0
+        for name in self.bufs:
+            comps, dt, per = PLANES16[name]
+            n = self.n_samples if per == "sample" else self.n_pixels
+            total += comps * n * np.dtype(dt).itemsize
+        return total
+
+    def free(self) -> None:
+        for bl in self.bufs.values():
+            for b in bl:
+                b.free()
+        self.bufs = {}
+
+
 class Context:
     """rpd_ctx: one GPU and the HBM budget jobs are admitted against."""
 
@@ -476,6 +555,8 @@ class Job:
         check(lib().rpd_job_begin_frame(self.handle))
 
     def push(self, samples, first: int, count: int, spp: int = 0, counts=None) -> None:
+        if isinstance(samples, DeviceSamples16):
+            return self.push16(samples, first, count, spp, counts)
         where = MEM_DEVICE if isinstance(samples, DeviceSamples) else MEM_HOST
         s = samples.soa()
         if counts is None:
@@ -486,6 +567,33 @@ class Job:
         else:
             cp = counts.ptr
         check(lib().rpd_job_push_samples(self.handle, C.byref(s), first, count, spp, cp, where))
+
+    def push16(self, samples, first: int, count: int, spp: int = 0, counts=None, where: int = MEM_DEVICE) -> None:
+        """rpd_job_push_samples16 of compact planes (device-resident unless `where` says host)."""
+        if where == MEM_HOST:
+            cp = None if counts is None else np.ascontiguousarray(counts, dtype=np.int32)
+            check(lib().rpd_job_push_samples16(self.handle, C.byref(samples.soa()), first, count, spp,
+                                               None if cp is None else cp.ctypes.data, MEM_HOST))
+            return
+        if counts is None:
+            cp = None
+        elif isinstance(counts, np.ndarray):
+            counts = np.ascontiguousarray(counts, dtype=np.int32)
+            cp = counts.ctypes.data
+        else:
+            cp = counts.ptr
+        if isinstance(counts, np.ndarray):
+            # device planes with host counts: stage the counts on the device
+            buf = DeviceBuffer(self.ctx, max(1, counts.nbytes))
+            buf.upload(counts)
+            try:
+                check(lib().rpd_job_push_samples16(self.handle, C.byref(samples.soa()), first, count, spp, buf.ptr,
+                                                   MEM_DEVICE))
+                self.sync()
+            finally:
+                buf.free()
+            return
+        check(lib().rpd_job_push_samples16(self.handle, C.byref(samples.soa()), first, count, spp, cp, MEM_DEVICE))
 
     def end_pass(self) -> None:
         check(lib().rpd_job_end_pass(self.handle))

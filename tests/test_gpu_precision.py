@@ -1,0 +1,102 @@
+"""The precision form: compact per-sample storage (rpd_sample_soa16: binary16 sqrt-radiance,
+snorm16 normals, binary16 depth, unorm16 random dimensions), decoded and accumulated in
+single precision. Its error is measured against the same frame pushed as FP32 planes (the
+path the oracle pins), as relMSE = mean((x - r)^2 / (r^2 + 1e-2)) over pixels and channels;
+the bar is 1e-3. The random-dimension bins are the unquantised ones, so their weights match
+exactly."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import R, assert_bitwise, small_config
+
+pytestmark = pytest.mark.gpu
+
+REL_MSE_BAR = 1e-3
+RANDOM_DEPS = [R.DEP_NAMES.index(n) for n in ("brdf", "lens", "light_uv", "light_select", "rr")]
+
+
+def rel_mse(x, r):
+    x = x.astype(np.float64)
+    r = r.astype(np.float64)
+    return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+
+
+def run(job, samples, w, h, spp):
+    job.begin_frame()
+    job.push(samples, 0, w * h, spp)
+    job.end_pass()
+    job.recompute_sensitivity()
+    job.statmc_denoise()
+    job.variance_denoise()
+
+
+@pytest.mark.parametrize("w,h,spp,tile", [(96, 64, 8, 16), (61, 37, 4, 8), (40, 30, 5, 6)])
+def test_compact_storage_against_fp32(gpu_ctx, w, h, spp, tile):
+    cfg = small_config(w, h, rpf_tile_size=tile)
+    p = R.synth_params(w, h, 23)
+    dev = R.DeviceSamples(gpu_ctx, w * h * spp, w * h)
+    gpu_ctx.synth_fill(p, 0, w * h, spp, dev)
+    dev16 = R.DeviceSamples16.encode(gpu_ctx, dev, depth_scale=4.0)
+    assert dev16.nbytes < 0.55 * dev.nbytes
+    a, b = R.Job(gpu_ctx, cfg), R.Job(gpu_ctx, cfg)
+    run(a, dev, w, h, spp)
+    run(b, dev16, w, h, spp)
+    for f in ("STATS_N", "HIT_COUNT", "SAMPLE_COUNT"):
+        assert_bitwise(a.read(f), b.read(f), f)
+    err = rel_mse(b.read("DENOISED"), a.read("DENOISED"))
+    assert err <= REL_MSE_BAR, err
+    ga, gb = a.read("GRID"), b.read("GRID")
+    for d in RANDOM_DEPS:  # bin weights of the random dimensions: identical bins, identical weights
+        np.testing.assert_array_equal(ga[:, d, :16], gb[:, d, :16])
+    for j in (a, b):
+        j.close()
+    dev.free()
+    dev16.free()
+
+
+def test_compact_adaptive_pass(gpu_ctx):
+    w, h, spp = 48, 40, 4
+    cfg = small_config(w, h, adaptive_spp=4, adaptive_base_samples=1)
+    p = R.synth_params(w, h, 29)
+    dev = R.DeviceSamples(gpu_ctx, w * h * spp, w * h)
+    gpu_ctx.synth_fill(p, 0, w * h, spp, dev)
+    dev16 = R.DeviceSamples16.encode(gpu_ctx, dev)
+    a, b = R.Job(gpu_ctx, cfg), R.Job(gpu_ctx, cfg)
+    run(a, dev, w, h, spp)
+    run(b, dev16, w, h, spp)
+    ca, cb = a.compute_adaptive_sample_counts(), b.compute_adaptive_sample_counts()
+    assert ca.sum() == cb.sum() == cfg.adaptive_spp * w * h
+    # the importance follows the stabilised variance, which moves by the storage error
+    assert float(np.abs(ca - cb).sum()) <= 0.05 * ca.sum()
+    extra_n = int(cb.sum())
+    ex = R.DeviceSamples(gpu_ctx, extra_n, w * h)
+    gpu_ctx.synth_fill(p, 0, w * h, 0, ex, counts=cb, start_n=np.full(w * h, spp, np.int32))
+    ex16 = R.DeviceSamples16.encode(gpu_ctx, ex)
+    b.push(ex16, 0, w * h, 0, counts=cb)
+    b.end_pass()
+    b.recompute_sensitivity()
+    b.statmc_denoise()
+    assert np.all(np.isfinite(b.read("DENOISED")))
+    assert int(b.read("SAMPLE_COUNT").sum()) == w * h * spp + extra_n
+    for j in (a, b):
+        j.close()
+    for d in (dev, dev16, ex, ex16):
+        d.free()
+
+
+def test_compact_rejects_exact_grid(gpu_ctx):
+    w, h, spp = 16, 16, 4
+    cfg = small_config(w, h)
+    dev = R.DeviceSamples(gpu_ctx, w * h * spp, w * h)
+    gpu_ctx.synth_fill(R.synth_params(w, h, 3), 0, w * h, spp, dev)
+    dev16 = R.DeviceSamples16.encode(gpu_ctx, dev)
+    job = R.Job(gpu_ctx, cfg)
+    job.set_exact(grid=True, window=False)
+    job.begin_frame()
+    with pytest.raises(R.RpdError, match="exact grid mode"):
+        job.push(dev16, 0, w * h, spp)
+    job.close()
+    dev.free()
+    dev16.free()
