@@ -220,29 +220,56 @@ def run_gpu(args):
     ms_per_step = elapsed_max / args.steps
     value = world * n / (ms_per_step * 1e-3) / 1e6
 
-    # end-to-end through the C ABI from pinned host buffers
+    # end-to-end through the C ABI from pinned host buffers: every step pushes the frame's
+    # planes from host memory (copied to HBM inside the push) and reads the denoised image back.
+    # Two jobs alternate, as a caller streaming frames would use them: while one job's push
+    # copies frame i+1 (the host->device link runs at ~210 GB/s on this machine), the other
+    # job's stages of frame i run on the GPU.
     e2e = None
     if not args.no_e2e:
         host = pinned_host_copy(R, ctx, samples)
         denoised = np.empty((H, W, 3), dtype=np.float32)
-        for _ in range(max(1, args.warmup)):
-            step(host)
-            job.read("DENOISED")
-        job.sync()
+        jobs = [job, R.Job(ctx, cfg)]
+        if args.grid_shape:
+            jobs[1].set_tuning("grid_shape", args.grid_shape)
+
+        def start(jb):
+            jb.begin_frame()
+            if getattr(host, "compact_host", False):
+                jb.push16(host, 0, np_, SPP, where=R.MEM_HOST)
+            else:
+                jb.push(host, 0, np_, SPP)
+            jb.end_pass()
+            jb.recompute_sensitivity()
+            jb.statmc_denoise()
+            jb.variance_denoise()
+
+        def finish(jb):
+            R.check(R.lib().rpd_job_read(jb.handle, R.FIELD["DENOISED"], denoised.ctypes.data, denoised.nbytes,
+                                         R.MEM_HOST))
+
+        for i in range(max(2, args.warmup)):
+            start(jobs[i % 2])
+            finish(jobs[i % 2])
+        for jb in jobs:
+            jb.sync()
         barrier(dist)
         t0 = time.perf_counter()
-        job.mark(2)
-        for _ in range(args.steps):
-            step(host)
-            R.check(R.lib().rpd_job_read(job.handle, R.FIELD["DENOISED"], denoised.ctypes.data, denoised.nbytes,
-                                         R.MEM_HOST))
-        job.mark(3)
-        e2e_ms = job.elapsed_ms(2, 3)
+        pending = None
+        for i in range(args.steps):
+            jb = jobs[i % 2]
+            start(jb)
+            if pending is not None:
+                finish(pending)
+            pending = jb
+        finish(pending)
         wall_ms = (time.perf_counter() - t0) * 1e3
-        e2e_ms = max_over_ranks(dist, max(e2e_ms, wall_ms))
+        e2e_ms = max_over_ranks(dist, wall_ms)
         e2e = {"value": round(world * n / (e2e_ms / args.steps * 1e-3) / 1e6, 3), "unit": UNIT,
                "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(denoised.nbytes),
-               "ms_per_step": round(e2e_ms / args.steps, 3)}
+               "ms_per_step": round(e2e_ms / args.steps, 3),
+               "pipeline": "two jobs alternating: frame i+1's host->device copy overlaps frame i's stages"}
+        jobs[1].close()
         host.free()
 
     # roofline of the dominant kernel

@@ -265,6 +265,9 @@ int rpd_job_set_exact(rpd_job* job, int flags);
  * dimension sets: 1 = 2x1, 2 = 2x2, 3 = 2x3, 4 = 1x2, 5 = 1x3, 6 = 1x1 (default). More dimension sets
  * keep fewer bins per warp (more resident warps) but walk the samples once per set. */
 #define RPD_TUNE_GRID_SHAPE 0
+/* RPD_TUNE_HOST_BAND_MB: a host-memory push is copied to HBM in row bands of about this many
+ * megabytes (default 96), each band's copy overlapping the previous band's passes. */
+#define RPD_TUNE_HOST_BAND_MB 1
 int rpd_job_set_tuning(rpd_job* job, int knob, int value);
 int rpd_job_get_tuning(rpd_job* job, int knob, int* value);
 /* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */

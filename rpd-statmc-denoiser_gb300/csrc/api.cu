@@ -450,6 +450,10 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
     rebase(j->pat4, static_cast<char*>(j->arena));
     rebase(j->pat2, static_cast<char*>(j->arena));
     cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&j->copy_stream, cudaStreamNonBlocking);
+    for (int b = 0; b < Job::kMaxBands && e == cudaSuccess; ++b)
+        e = cudaEventCreateWithFlags(&j->band_copied[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->staging_free, cudaEventDisableTiming);
     for (int s = 0; s < RPD_STAGE_COUNT_ && e == cudaSuccess; ++s) {
         e = cudaEventCreate(&j->ev_start[s]);
         if (e == cudaSuccess) e = cudaEventCreate(&j->ev_stop[s]);
@@ -469,6 +473,7 @@ void rpd_job_destroy(rpd_job* job) {
     if (!j) return;
     cudaSetDevice(j->ctx->device);
     if (j->stream) cudaStreamSynchronize(j->stream);
+    if (j->copy_stream) cudaStreamSynchronize(j->copy_stream);
     if (j->arena) {
         cudaFree(j->arena);
         j->ctx->in_use -= j->arena_bytes;
@@ -497,6 +502,10 @@ void rpd_job_destroy(rpd_job* job) {
     for (auto e : j->event_pool) cudaEventDestroy(e);
     for (auto e : j->marks)
         if (e) cudaEventDestroy(e);
+    for (int b = 0; b < Job::kMaxBands; ++b)
+        if (j->band_copied[b]) cudaEventDestroy(j->band_copied[b]);
+    if (j->staging_free) cudaEventDestroy(j->staging_free);
+    if (j->copy_stream) cudaStreamDestroy(j->copy_stream);
     if (j->stream) cudaStreamDestroy(j->stream);
     delete j;
 }
@@ -529,18 +538,26 @@ int rpd_job_set_exact(rpd_job* job, int flags) {
 int rpd_job_set_tuning(rpd_job* job, int knob, int value) {
     Job* j = reinterpret_cast<Job*>(job);
     CHECK_JOB(j);
-    if (knob != RPD_TUNE_GRID_SHAPE) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
-    if (value < 1 || value > 6) return fail(RPD_ERR_INVALID_ARGUMENT, "grid shape must be 1..6");
-    j->grid_shape = value;
-    return RPD_OK;
+    if (knob == RPD_TUNE_GRID_SHAPE) {
+        if (value < 1 || value > 6) return fail(RPD_ERR_INVALID_ARGUMENT, "grid shape must be 1..6");
+        j->grid_shape = value;
+        return RPD_OK;
+    }
+    if (knob == RPD_TUNE_HOST_BAND_MB) {
+        if (value < 1 || value > 65536) return fail(RPD_ERR_INVALID_ARGUMENT, "host band size must be 1..65536 MB");
+        j->band_bytes = int64_t(value) << 20;
+        return RPD_OK;
+    }
+    return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
 int rpd_job_get_tuning(rpd_job* job, int knob, int* value) {
     Job* j = reinterpret_cast<Job*>(job);
     CHECK_JOB(j);
     if (!value) return fail(RPD_ERR_INVALID_ARGUMENT, "null value");
-    if (knob != RPD_TUNE_GRID_SHAPE) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
-    *value = j->grid_shape;
+    if (knob == RPD_TUNE_GRID_SHAPE) *value = j->grid_shape;
+    else if (knob == RPD_TUNE_HOST_BAND_MB) *value = int(j->band_bytes >> 20);
+    else return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
     return RPD_OK;
 }
 
@@ -567,6 +584,98 @@ int rpd_job_begin_frame(rpd_job* job) {
 
 static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
                      rpd_memory where, int64_t total);
+
+// One host-memory plane of a push: its source, bytes per element, whether it has one element
+// per pixel (else per sample) and where its device pointer goes in a DeviceSamples.
+struct HostPlane {
+    const void* src;
+    uint32_t elem;
+    bool per_pixel;
+    size_t field;
+};
+
+// A host push in row bands: every band's planes are copied on the job's copy stream into the
+// staging buffer (one region per band), and each band's statistics and grid passes start on the
+// job stream as soon as its copy is done, overlapping the copies of the later bands (a pass
+// pushed in bands accumulates exactly as one push). The copies wait only for the previous host
+// push's passes to release the staging. Returns when every copy has completed, so the caller
+// may reuse its host planes.
+static int push_host_banded(Job* j, const std::vector<HostPlane>& planes, const DeviceSamples& proto, int64_t first,
+                            int64_t count, int32_t spp, const int32_t* counts, int64_t total) {
+    std::vector<int64_t> pre;
+    if (counts) {
+        pre.resize(size_t(count) + 1);
+        pre[0] = 0;
+        for (int64_t i = 0; i < count; ++i) pre[size_t(i) + 1] = pre[size_t(i)] + counts[i];
+    }
+    auto sample_at = [&](int64_t p) { return counts ? pre[size_t(p)] : p * int64_t(spp); };
+    uint64_t per_sample = 0;
+    for (const auto& hp : planes)
+        if (!hp.per_pixel) per_sample += hp.elem;
+    const uint64_t total_bytes = uint64_t(total) * per_sample;
+    // bands of about j->band_bytes, at most kMaxBands, on image-row boundaries
+    const int w = j->g.w;
+    const int64_t rows = (first + count - 1) / w - first / w + 1;
+    int64_t nbands = int64_t(total_bytes / uint64_t(j->band_bytes));
+    nbands = std::max<int64_t>(1, std::min<int64_t>({nbands, int64_t(Job::kMaxBands), rows}));
+    const int64_t rows_per_band = (rows + nbands - 1) / nbands;
+    struct Band { int64_t p0, p1, k0, k1; uint64_t off; };
+    std::vector<Band> bands;
+    uint64_t need = 0;
+    for (int64_t p0 = 0; p0 < count;) {
+        const int64_t row0 = (first + p0) / w;
+        const int64_t p1 = std::min<int64_t>(count, (row0 + rows_per_band) * w - first);
+        Band b{p0, p1, sample_at(p0), sample_at(p1), (need + 255) & ~uint64_t(255)};
+        need = b.off;
+        for (const auto& hp : planes)
+            need = ((need + 255) & ~uint64_t(255)) + uint64_t(hp.per_pixel ? p1 - p0 : b.k1 - b.k0) * hp.elem;
+        if (counts) need = ((need + 255) & ~uint64_t(255)) + uint64_t(p1 - p0) * 4;
+        bands.push_back(b);
+        p0 = p1;
+    }
+    if (j->staging_bytes < need + 256) {
+        RPD_CUDA(cudaStreamSynchronize(j->stream));  // the previous push's passes are done with it
+        int st = grow_device(*j, &j->staging, &j->staging_bytes, need + 256);
+        if (st != RPD_OK) return st;
+    }
+    RPD_CUDA(cudaStreamWaitEvent(j->copy_stream, j->staging_free, 0));
+    char* base = static_cast<char*>(j->staging);
+    std::vector<DeviceSamples> dev(bands.size(), proto);
+    std::vector<const int32_t*> dcounts(bands.size(), nullptr);
+    for (size_t bi = 0; bi < bands.size(); ++bi) {
+        const Band& b = bands[bi];
+        uint64_t off = b.off;
+        for (const auto& hp : planes) {
+            off = (off + 255) & ~uint64_t(255);
+            const int64_t e0 = hp.per_pixel ? b.p0 : b.k0, n = hp.per_pixel ? b.p1 - b.p0 : b.k1 - b.k0;
+            const uint64_t bytes = uint64_t(n) * hp.elem;
+            if (bytes)
+                RPD_CUDA(cudaMemcpyAsync(base + off, static_cast<const char*>(hp.src) + uint64_t(e0) * hp.elem, bytes,
+                                         cudaMemcpyHostToDevice, j->copy_stream));
+            *reinterpret_cast<const void**>(reinterpret_cast<char*>(&dev[bi]) + hp.field) = base + off;
+            off += bytes;
+        }
+        if (counts) {
+            off = (off + 255) & ~uint64_t(255);
+            RPD_CUDA(cudaMemcpyAsync(base + off, counts + b.p0, uint64_t(b.p1 - b.p0) * 4, cudaMemcpyHostToDevice,
+                                     j->copy_stream));
+            dcounts[bi] = reinterpret_cast<const int32_t*>(base + off);
+        }
+        RPD_CUDA(cudaEventRecord(j->band_copied[bi], j->copy_stream));
+    }
+    for (size_t bi = 0; bi < bands.size(); ++bi) {
+        const Band& b = bands[bi];
+        RPD_CUDA(cudaStreamWaitEvent(j->stream, j->band_copied[bi], 0));
+        if (counts) RPD_CUDA(launch_offsets_scan(*j, dcounts[bi], b.p1 - b.p0));
+        else RPD_CUDA(launch_offsets_uniform(*j, b.p1 - b.p0, spp));
+        const int st = push_tail(j, dev[bi], first + b.p0, b.p1 - b.p0, spp, counts ? counts + b.p0 : nullptr,
+                                 RPD_MEM_HOST, b.k1 - b.k0);
+        if (st != RPD_OK) return st;
+    }
+    RPD_CUDA(cudaEventRecord(j->staging_free, j->stream));
+    RPD_CUDA(cudaStreamSynchronize(j->copy_stream));
+    return RPD_OK;
+}
 
 int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first, int64_t count, int32_t spp,
                          const int32_t* counts, rpd_memory where) {
@@ -612,44 +721,33 @@ int rpd_job_push_samples(rpd_job* job, const rpd_sample_soa* s, int64_t first, i
 
     DeviceSamples d{};
     if (where == RPD_MEM_HOST) {
-        // one staging arena: the planes that are present, then the counts
-        struct Plane { const void* src; uint64_t bytes; const void** dst; };
-        std::vector<Plane> planes;
-        auto fplane = [&](const float* src, const float** dst, int64_t n) {
-            if (src) planes.push_back({src, uint64_t(n) * 4, reinterpret_cast<const void**>(dst)});
+        if (!s->normal[0] || !s->depth || (!s->albedo[0] && !s->pixel_albedo[0]))
+            return fail(RPD_ERR_INVALID_ARGUMENT, "normal, depth and albedo (per sample or per pixel) are required");
+        if (j->cfg.rpf_shrinkage_scale > 0.0f && !s->category)
+            return fail(RPD_ERR_INVALID_ARGUMENT, "category plane is required when RPD is enabled");
+        std::vector<HostPlane> planes;
+        auto add = [&](const void* src, uint32_t elem, bool per_pixel, const void* const& field) {
+            if (src)
+                planes.push_back({src, elem, per_pixel,
+                                  size_t(reinterpret_cast<const char*>(&field) - reinterpret_cast<const char*>(&d))});
         };
         for (int c = 0; c < 3; ++c) {
-            fplane(s->radiance[c], &d.radiance[c], total);
-            fplane(s->normal[c], &d.normal[c], total);
-            fplane(s->albedo[c], &d.albedo[c], total);
-            fplane(s->pixel_albedo[c], &d.pixel_albedo[c], count);
+            add(s->radiance[c], 4, false, reinterpret_cast<const void* const&>(d.radiance[c]));
+            add(s->normal[c], 4, false, reinterpret_cast<const void* const&>(d.normal[c]));
+            add(s->albedo[c], 4, false, reinterpret_cast<const void* const&>(d.albedo[c]));
+            add(s->pixel_albedo[c], 4, true, reinterpret_cast<const void* const&>(d.pixel_albedo[c]));
         }
-        fplane(s->depth, &d.depth, total);
+        add(s->depth, 4, false, reinterpret_cast<const void* const&>(d.depth));
         for (int c = 0; c < 2; ++c) {
-            fplane(s->pixel_u[c], &d.pixel_u[c], total);
-            fplane(s->lens_u[c], &d.lens_u[c], total);
-            fplane(s->brdf_u[c], &d.brdf_u[c], total);
-            fplane(s->light_u[c], &d.light_u[c], total);
-            fplane(s->env_u[c], &d.env_u[c], total);
+            add(s->pixel_u[c], 4, false, reinterpret_cast<const void* const&>(d.pixel_u[c]));
+            add(s->lens_u[c], 4, false, reinterpret_cast<const void* const&>(d.lens_u[c]));
+            add(s->brdf_u[c], 4, false, reinterpret_cast<const void* const&>(d.brdf_u[c]));
+            add(s->light_u[c], 4, false, reinterpret_cast<const void* const&>(d.light_u[c]));
+            add(s->env_u[c], 4, false, reinterpret_cast<const void* const&>(d.env_u[c]));
         }
-        planes.push_back({s->flags, uint64_t(total), reinterpret_cast<const void**>(&d.flags)});
-        if (s->category) planes.push_back({s->category, uint64_t(total), reinterpret_cast<const void**>(&d.category)});
-        const int32_t* d_counts = nullptr;
-        if (counts) planes.push_back({counts, uint64_t(count) * 4, reinterpret_cast<const void**>(&d_counts)});
-        uint64_t need = 0;
-        for (auto& p : planes) need = ((need + 255) & ~uint64_t(255)) + p.bytes;
-        st = grow_device(*j, &j->staging, &j->staging_bytes, need + 256);
-        if (st != RPD_OK) return st;
-        uint64_t off = 0;
-        for (auto& p : planes) {
-            off = (off + 255) & ~uint64_t(255);
-            char* dst = static_cast<char*>(j->staging) + off;
-            if (p.bytes) RPD_CUDA(cudaMemcpyAsync(dst, p.src, p.bytes, cudaMemcpyHostToDevice, j->stream));
-            *p.dst = dst;
-            off += p.bytes;
-        }
-        if (counts) RPD_CUDA(launch_offsets_scan(*j, d_counts, count));
-        else RPD_CUDA(launch_offsets_uniform(*j, count, spp));
+        add(s->flags, 1, false, reinterpret_cast<const void* const&>(d.flags));
+        add(s->category, 1, false, reinterpret_cast<const void* const&>(d.category));
+        return push_host_banded(j, planes, d, first, count, spp, counts, total);
     } else {
         for (int c = 0; c < 3; ++c) {
             d.radiance[c] = s->radiance[c];
@@ -720,42 +818,30 @@ int rpd_job_push_samples16(rpd_job* job, const rpd_sample_soa16* s, int64_t firs
     d.compact = 1;
     d.c16.depth_scale = s->depth_scale;
     if (where == RPD_MEM_HOST) {
-        struct Plane { const void* src; uint64_t bytes; const void** dst; };
-        std::vector<Plane> planes;
-        auto hplane = [&](const void* src, const void* const* dst, int64_t n, int elem) {
-            if (src) planes.push_back({src, uint64_t(n) * uint64_t(elem), const_cast<const void**>(dst)});
+        if (j->cfg.rpf_shrinkage_scale > 0.0f && !s->category)
+            return fail(RPD_ERR_INVALID_ARGUMENT, "category plane is required when RPD is enabled");
+        std::vector<HostPlane> planes;
+        auto add = [&](const void* src, uint32_t elem, bool per_pixel, const void* const& field) {
+            if (src)
+                planes.push_back({src, elem, per_pixel,
+                                  size_t(reinterpret_cast<const char*>(&field) - reinterpret_cast<const char*>(&d))});
         };
         for (int c = 0; c < 3; ++c) {
-            hplane(s->sqrt_radiance[c], reinterpret_cast<const void* const*>(&d.c16.sqrt_radiance[c]), total, 2);
-            hplane(s->normal[c], reinterpret_cast<const void* const*>(&d.c16.normal[c]), total, 2);
-            hplane(s->pixel_albedo[c], reinterpret_cast<const void* const*>(&d.c16.pixel_albedo[c]), count, 2);
+            add(s->sqrt_radiance[c], 2, false, reinterpret_cast<const void* const&>(d.c16.sqrt_radiance[c]));
+            add(s->normal[c], 2, false, reinterpret_cast<const void* const&>(d.c16.normal[c]));
+            add(s->pixel_albedo[c], 2, true, reinterpret_cast<const void* const&>(d.c16.pixel_albedo[c]));
         }
-        hplane(s->depth, reinterpret_cast<const void* const*>(&d.c16.depth), total, 2);
+        add(s->depth, 2, false, reinterpret_cast<const void* const&>(d.c16.depth));
         for (int c = 0; c < 2; ++c) {
-            hplane(s->pixel_u[c], reinterpret_cast<const void* const*>(&d.c16.pixel_u[c]), total, 2);
-            hplane(s->lens_u[c], reinterpret_cast<const void* const*>(&d.c16.lens_u[c]), total, 2);
-            hplane(s->brdf_u[c], reinterpret_cast<const void* const*>(&d.c16.brdf_u[c]), total, 2);
-            hplane(s->light_u[c], reinterpret_cast<const void* const*>(&d.c16.light_u[c]), total, 2);
-            hplane(s->env_u[c], reinterpret_cast<const void* const*>(&d.c16.env_u[c]), total, 2);
+            add(s->pixel_u[c], 2, false, reinterpret_cast<const void* const&>(d.c16.pixel_u[c]));
+            add(s->lens_u[c], 2, false, reinterpret_cast<const void* const&>(d.c16.lens_u[c]));
+            add(s->brdf_u[c], 2, false, reinterpret_cast<const void* const&>(d.c16.brdf_u[c]));
+            add(s->light_u[c], 2, false, reinterpret_cast<const void* const&>(d.c16.light_u[c]));
+            add(s->env_u[c], 2, false, reinterpret_cast<const void* const&>(d.c16.env_u[c]));
         }
-        hplane(s->flags, reinterpret_cast<const void* const*>(&d.flags), total, 1);
-        hplane(s->category, reinterpret_cast<const void* const*>(&d.category), total, 1);
-        const int32_t* d_counts = nullptr;
-        if (counts) planes.push_back({counts, uint64_t(count) * 4, reinterpret_cast<const void**>(&d_counts)});
-        uint64_t need = 0;
-        for (auto& p : planes) need = ((need + 255) & ~uint64_t(255)) + p.bytes;
-        st = grow_device(*j, &j->staging, &j->staging_bytes, need + 256);
-        if (st != RPD_OK) return st;
-        uint64_t off = 0;
-        for (auto& p : planes) {
-            off = (off + 255) & ~uint64_t(255);
-            char* dst = static_cast<char*>(j->staging) + off;
-            if (p.bytes) RPD_CUDA(cudaMemcpyAsync(dst, p.src, p.bytes, cudaMemcpyHostToDevice, j->stream));
-            *p.dst = dst;
-            off += p.bytes;
-        }
-        if (counts) RPD_CUDA(launch_offsets_scan(*j, d_counts, count));
-        else RPD_CUDA(launch_offsets_uniform(*j, count, spp));
+        add(s->flags, 1, false, reinterpret_cast<const void* const&>(d.flags));
+        add(s->category, 1, false, reinterpret_cast<const void* const&>(d.category));
+        return push_host_banded(j, planes, d, first, count, spp, counts, total);
     } else {
         for (int c = 0; c < 3; ++c) {
             d.c16.sqrt_radiance[c] = s->sqrt_radiance[c];

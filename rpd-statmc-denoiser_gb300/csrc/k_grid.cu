@@ -197,6 +197,8 @@ __device__ void reduce_totals_into(Totals t, float2* acc) {
 struct GridParams {
     Geometry g;
     int64_t first, count;
+    int64_t node0;        // first node of the launch (the node rows whose supports meet the push)
+    int64_t count_nodes;  // nodes of the launch
     int uniform_ok;  // power-of-two support >= 4
     int pow2_step;   // the node step is a power of two: x / step is exact
     float inv_step;
@@ -250,7 +252,7 @@ __global__ void __launch_bounds__(kGroups * 32) k_grid_fast(GridParams gpar, flo
     extern __shared__ float sm[];
     const int lane = threadIdx.x & 31;
     const int grp = threadIdx.x >> 5;
-    const int64_t node = blockIdx.x;
+    const int64_t node = gpar.node0 + blockIdx.x;
     const Geometry& g = gpar.g;
     const int nx = int(node % g.nodes_x), ny = int(node / g.nodes_x);
     LaneBins<INT_W> bins{sm + grp * LaneBins<INT_W>::kSlots * 32, lane, float(g.step) * float(g.step)};
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pas
     extern __shared__ float sm[];
     constexpr int kS = LaneBins<INT_W>::kSlots;
     const int lane = threadIdx.x;
-    const int64_t node = blockIdx.x;
+    const int64_t node = gpar.node0 + blockIdx.x;
     const Geometry& g = gpar.g;
     const int nx = int(node % g.nodes_x), ny = int(node / g.nodes_x);
     const float wscale = float(g.step) * float(g.step);
@@ -846,7 +848,7 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
     const int rgroup = warp / DS;   // its row group
     const GridParams& gpar = rp.gp;
     const Geometry& g = gpar.g;
-    const int64_t node = blockIdx.x;
+    const int64_t node = rp.gp.node0 + blockIdx.x;
     const int nx = int(node % g.nodes_x), ny = int(node / g.nodes_x);
     unsigned char* wbase = smem_raw + warp * L::kWarpBytes;
     WalkCtx<INT_W, DS> c;
@@ -1023,7 +1025,8 @@ cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) 
     cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, RW, DS, VEC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    k_grid_random<INT_W, RW, DS, VEC><<<unsigned(j.g.nn), NW * 32, smem, j.stream>>>(
+    const unsigned nblocks = unsigned(rp.gp.count_nodes);
+    k_grid_random<INT_W, RW, DS, VEC><<<nblocks, NW * 32, smem, j.stream>>>(
         rp, reinterpret_cast<float2*>(j.n.pass_grid), j.offsets, gp);
     j.launches += 1;
     return cudaGetLastError();
@@ -1056,7 +1059,15 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
                              int32_t spp, int32_t max_count) {
     const int step = j.g.step;
     const bool pow2 = (step & (step - 1)) == 0;
-    GridParams gpar{j.g, first, count, 0, pow2 ? 1 : 0, 1.0f / float(step), spp, spp > 0 ? 1.0f / float(spp) : 0.0f};
+    GridParams gpar{j.g, first, count, 0, 0, 0, pow2 ? 1 : 0, 1.0f / float(step), spp, spp > 0 ? 1.0f / float(spp) : 0.0f};
+    {
+        // node rows whose support rows (ny-1)*step-1 .. (ny+1)*step+1 meet the push's rows
+        const int y0 = int(first / j.g.w), y1 = int((first + count - 1) / j.g.w);
+        const int ny0 = std::max(0, (y0 - 1) / step - 1), ny1 = std::min(j.g.nodes_y - 1, (y1 + 1) / step + 1);
+        gpar.node0 = int64_t(ny0) * j.g.nodes_x;
+        gpar.count_nodes = int64_t(ny1 - ny0 + 1) * j.g.nodes_x;
+    }
+    const unsigned nblocks = unsigned(gpar.count_nodes);
     const int sup = j.g.support;
     gpar.uniform_ok = (sup >= 4 && sup <= 2048 && (sup & (sup - 1)) == 0) ? 1 : 0;
     // exact integer bin weights need a power-of-two step and a per-bin total below 2^32:
@@ -1075,22 +1086,22 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
             if (int_w) {
                 e = cudaFuncSetAttribute(k_grid_screen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
                 if (e != cudaSuccess) return e;
-                k_grid_screen<true><<<unsigned(j.g.nn), 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+                k_grid_screen<true><<<nblocks, 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
             } else {
                 e = cudaFuncSetAttribute(k_grid_screen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
                 if (e != cudaSuccess) return e;
-                k_grid_screen<false><<<unsigned(j.g.nn), 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+                k_grid_screen<false><<<nblocks, 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
             }
         } else if (int_w) {
             const size_t smem = size_t(kGroups) * LaneBins<true>::kSlots * 32 * sizeof(float);
             e = cudaFuncSetAttribute(k_grid_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if (e != cudaSuccess) return e;
-            k_grid_fast<true><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+            k_grid_fast<true><<<nblocks, kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
         } else {
             const size_t smem = size_t(kGroups) * LaneBins<false>::kSlots * 32 * sizeof(float);
             e = cudaFuncSetAttribute(k_grid_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if (e != cudaSuccess) return e;
-            k_grid_fast<false><<<unsigned(j.g.nn), kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+            k_grid_fast<false><<<nblocks, kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
         }
         j.launches += 1;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;

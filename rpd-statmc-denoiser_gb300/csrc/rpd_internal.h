@@ -130,6 +130,14 @@ struct Job {
     // staging for host-side pushes (grown on demand)
     void* staging = nullptr;
     uint64_t staging_bytes = 0;
+    // host pushes copy row bands on their own stream into the staging buffer, so that the copy
+    // of one band overlaps the statistics and grid passes of the previous ones; the staging
+    // is reused by the next host push once this push's passes have read it
+    static constexpr int kMaxBands = 16;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t band_copied[kMaxBands]{};
+    cudaEvent_t staging_free = nullptr;
+    int64_t band_bytes = int64_t(96) << 20;  // target size of a band (RPD_TUNE_HOST_BAND_MB)
     float* lum = nullptr;        // per-sample luminance of the current push (fast grid pass)
     uint64_t lum_cap = 0;
     float* cls[kClasses][5]{};   // per-pixel validity-class sums of deviant pixels (arena)

@@ -541,7 +541,7 @@ class Job:
     def set_exact(self, grid: bool = False, window: bool = False) -> None:
         check(lib().rpd_job_set_exact(self.handle, (1 if grid else 0) | (2 if window else 0)))
 
-    TUNING = {"grid_shape": 0}
+    TUNING = {"grid_shape": 0, "host_band_mb": 1}
 
     def set_tuning(self, knob: str, value: int) -> None:
         check(lib().rpd_job_set_tuning(self.handle, self.TUNING[knob], int(value)))

@@ -305,3 +305,39 @@ def test_non_finite_features(gpu_ctx, exact):
     check_pipeline(g, o, exact_grid=exact)
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("counts_mode", [False, True], ids=["uniform", "counts"])
+def test_banded_host_push_equals_device_push(gpu_ctx, counts_mode):
+    """A host push copied in several row bands (each band's copy overlapping the previous
+    band's passes) gives exactly the result of one device-resident push."""
+    w, h, spp = 80, 60, 8
+    cfg = small_config(w, h, rpf_tile_size=8)
+    p = R.synth_params(w, h, 41, miss_regions=2)
+    counts = None
+    if counts_mode:
+        counts = np.random.default_rng(5).integers(0, 12, size=w * h).astype(np.int32)
+        host = B.synth_fill(p, 0, w * h, 0, counts=counts)
+    else:
+        host = B.synth_fill(p, 0, w * h, spp)
+    dev = R.DeviceSamples.from_host(gpu_ctx, host)
+    a = R.Job(gpu_ctx, cfg)
+    a.set_tuning("host_band_mb", 1)  # 2.4 MB of planes: two bands
+    b = R.Job(gpu_ctx, cfg)
+    for job, src in ((a, host), (b, dev)):
+        job.begin_frame()
+        job.push(src, 0, w * h, 0 if counts_mode else spp, counts=counts)
+        job.end_pass()
+        job.recompute_sensitivity()
+        job.statmc_denoise()
+        job.variance_denoise()
+    for f in ["STATS_MEAN", "STATS_N", "RADIANCE_SUM", "VARIANCE_DENOISED", "GRID", "DENOISED"]:
+        if f == "GRID":
+            assert_grid_close(a.read(f), b.read(f), rel=1e-12)
+        elif f == "DENOISED":
+            assert max_rel_err(a.read(f), b.read(f), FLOOR) <= 1e-6
+        else:
+            assert_bitwise(a.read(f), b.read(f), f)
+    a.close()
+    b.close()
+    dev.free()
