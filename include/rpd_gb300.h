@@ -268,6 +268,9 @@ int rpd_job_set_exact(rpd_job* job, int flags);
 /* RPD_TUNE_HOST_BAND_MB: a host-memory push is copied to HBM in row bands of about this many
  * megabytes (default 96), each band's copy overlapping the previous band's passes. */
 #define RPD_TUNE_HOST_BAND_MB 1
+/* RPD_TUNE_STATMC_ROWS: pixel rows per block of the StatMC window kernel: 2, 4 or 8 (0, the
+ * default: the tallest whose halo tile fits in shared memory). */
+#define RPD_TUNE_STATMC_ROWS 2
 int rpd_job_set_tuning(rpd_job* job, int knob, int value);
 int rpd_job_get_tuning(rpd_job* job, int knob, int* value);
 /* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */
@@ -384,6 +387,37 @@ int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, con
 int rpd_atrous_wavelet_noalloc(const float* raw, const float* normal, const float* albedo,
                                int32_t width, int32_t height, float sigma_c, float sigma_n,
                                float sigma_a, int32_t iterations, float* out, void* stream);
+
+/* ---- the batched form (no counterpart in the reference) ------------------------------ */
+
+/* Autotune a job's launch shapes (RPD_TUNE_GRID_SHAPE, RPD_TUNE_STATMC_ROWS) on the frame in
+ * device-resident planes (exactly one of s32 / s16; spp samples per pixel): every candidate is
+ * timed on this frame and the fastest kept. The choice is cached per frame class (size, spp,
+ * tile, window radii, storage) for the process, so later jobs of the class skip the timing.
+ * Leaves the frame denoised (begin_frame .. variance_denoise). */
+int rpd_job_autotune(rpd_job* job, const rpd_sample_soa* s32, const rpd_sample_soa16* s16, int32_t spp);
+
+/* A batch: frames of different jobs (uneven sizes allowed) run as one CUDA graph. */
+typedef struct rpd_batch_s rpd_batch;
+int rpd_batch_create(rpd_ctx* ctx, rpd_batch** out);
+/* Add a frame: `job` runs begin_frame, one push of device-resident planes (exactly one of s32 /
+ * s16, spp samples per pixel), end_pass, recompute_sensitivity, statmc_denoise and
+ * variance_denoise. A job appears once per batch. */
+int rpd_batch_add(rpd_batch* b, rpd_job* job, const rpd_sample_soa* s32, const rpd_sample_soa16* s16,
+                  int32_t spp);
+/* Run every frame. The first run executes the frames once directly (sizing every buffer), then
+ * captures all of them, each on its job's stream, into one CUDA graph; every run launches that
+ * graph: one launch for the whole batch, frames of different jobs running concurrently. The
+ * graph keeps the planes' addresses (update their contents, not the pointers). Asynchronous;
+ * rpd_batch_sync waits, rpd_batch_last_ms gives the device time of the last launch. */
+int rpd_batch_run(rpd_batch* b);
+int rpd_batch_sync(rpd_batch* b);
+int rpd_batch_last_ms(rpd_batch* b, float* ms);
+uint64_t rpd_batch_kernel_count(rpd_batch* b);  /* kernel nodes in one run */
+/* Frames run in `lanes` concurrent chains (default 4), largest frames first, each frame to the
+ * least-loaded chain. Set before the first run. */
+int rpd_batch_set_lanes(rpd_batch* b, int lanes);
+void rpd_batch_destroy(rpd_batch* b);
 
 /* ---- memory helpers for callers without a CUDA toolchain ---------------------------- */
 

@@ -548,6 +548,12 @@ int rpd_job_set_tuning(rpd_job* job, int knob, int value) {
         j->band_bytes = int64_t(value) << 20;
         return RPD_OK;
     }
+    if (knob == RPD_TUNE_STATMC_ROWS) {
+        if (value != 0 && value != 2 && value != 4 && value != 8)
+            return fail(RPD_ERR_INVALID_ARGUMENT, "StatMC tile rows must be 0, 2, 4 or 8");
+        j->statmc_by = value;
+        return RPD_OK;
+    }
     return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
@@ -557,6 +563,7 @@ int rpd_job_get_tuning(rpd_job* job, int knob, int* value) {
     if (!value) return fail(RPD_ERR_INVALID_ARGUMENT, "null value");
     if (knob == RPD_TUNE_GRID_SHAPE) *value = j->grid_shape;
     else if (knob == RPD_TUNE_HOST_BAND_MB) *value = int(j->band_bytes >> 20);
+    else if (knob == RPD_TUNE_STATMC_ROWS) *value = j->statmc_by;
     else return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
     return RPD_OK;
 }

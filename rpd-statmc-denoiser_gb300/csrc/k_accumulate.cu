@@ -212,7 +212,7 @@ __device__ __forceinline__ uint16_t lane4h(const uint2& v, int i) {
 // VEC4: every present plane is 16-byte aligned at the pixel's first sample and the pixel's
 // sample count is a multiple of 4, so each plane is read four samples per load. COMPACT: the
 // planes are rpd_sample_soa16's (s.c16), decoded to float here.
-template <bool VEC4, bool COMPACT>
+template <bool VEC4, bool COMPACT, bool WIDE>
 __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets,
                                                            int32_t spp, int64_t first, int64_t count, GridPrep gp) {
     const int64_t local = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -274,48 +274,73 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
         const DeviceSamples16& h = s.c16;
         const float dscale = h.depth_scale;
         if (VEC4) {
-            for (int64_t k = k0; k < k1; k += 4) {
-                uint2 L[3], N[3], D, PU[2], LU[2], BU[2], LI[2], EU[2];
+            // V samples per plane load: 8 (16-byte loads) when WIDE, else 4 (8-byte loads)
+            constexpr int V = WIDE ? 8 : 4;
+            constexpr int NW = V / 2;  // 32-bit words per load
+            struct Wv { uint32_t w[NW]; };
+            auto ldv = [](const void* ptr, int64_t k) {
+                Wv r;
+                if (WIDE) {
+                    const uint4 v = *reinterpret_cast<const uint4*>(static_cast<const uint16_t*>(ptr) + k);
+                    r.w[0] = v.x; r.w[NW > 1 ? 1 : 0] = v.y;
+                    if (NW > 2) { r.w[NW > 2 ? 2 : 0] = v.z; r.w[NW > 3 ? 3 : 0] = v.w; }
+                } else {
+                    const uint2 v = *reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(ptr) + k);
+                    r.w[0] = v.x; r.w[NW > 1 ? 1 : 0] = v.y;
+                }
+                return r;
+            };
+            auto lane16 = [](const Wv& v, int i) { return uint16_t(v.w[i >> 1] >> (16 * (i & 1))); };
+            for (int64_t k = k0; k < k1; k += V) {
+                Wv L[3], N[3], D, PU[2], LU[2], BU[2], LI[2], EU[2];
                 for (int c = 0; c < 3; ++c) {
-                    L[c] = ld4h(h.sqrt_radiance[c], k);
-                    N[c] = ld4h(h.normal[c], k);
+                    L[c] = ldv(h.sqrt_radiance[c], k);
+                    N[c] = ldv(h.normal[c], k);
                 }
-                D = ld4h(h.depth, k);
-                const uint2 z = make_uint2(0u, 0u);
+                D = ldv(h.depth, k);
+                Wv z;
+                for (int q = 0; q < NW; ++q) z.w[q] = 0u;
                 for (int c = 0; c < 2; ++c) {
-                    PU[c] = (dims && has_pu) ? ld4h(h.pixel_u[c], k) : z;
-                    LU[c] = (dims && has_lu) ? ld4h(h.lens_u[c], k) : z;
-                    BU[c] = (dims && has_bu) ? ld4h(h.brdf_u[c], k) : z;
-                    LI[c] = (dims && has_li) ? ld4h(h.light_u[c], k) : z;
-                    EU[c] = (dims && has_eu) ? ld4h(h.env_u[c], k) : z;
+                    PU[c] = (dims && has_pu) ? ldv(h.pixel_u[c], k) : z;
+                    LU[c] = (dims && has_lu) ? ldv(h.lens_u[c], k) : z;
+                    BU[c] = (dims && has_bu) ? ldv(h.brdf_u[c], k) : z;
+                    LI[c] = (dims && has_li) ? ldv(h.light_u[c], k) : z;
+                    EU[c] = (dims && has_eu) ? ldv(h.env_u[c], k) : z;
                 }
-                const uint32_t F4 = *reinterpret_cast<const uint32_t*>(s.flags + k);
-                const uint32_t C4 = (dims && s.category) ? *reinterpret_cast<const uint32_t*>(s.category + k) : 0u;
-                float lum4[4];
-                uint32_t key4[4];
+                uint32_t F[NW / 2 > 0 ? NW / 2 : 1], Cg[NW / 2 > 0 ? NW / 2 : 1];
+                for (int q = 0; q < V / 4; ++q) {
+                    F[q] = *reinterpret_cast<const uint32_t*>(s.flags + k + 4 * q);
+                    Cg[q] = (dims && s.category) ? *reinterpret_cast<const uint32_t*>(s.category + k + 4 * q) : 0u;
+                }
+                float lumv[V];
+                uint32_t keyv[V];
                 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
+                for (int i = 0; i < V; ++i) {
                     SampleIn in;
                     for (int c = 0; c < 3; ++c) {
-                        in.L[c] = sq(h2f(lane4h(L[c], i)));
-                        in.n[c] = snorm16(int16_t(lane4h(N[c], i)));
+                        in.L[c] = sq(h2f(lane16(L[c], i)));
+                        in.n[c] = snorm16(int16_t(lane16(N[c], i)));
                         in.alb[c] = 0.0f;
                     }
-                    in.d = h2f(lane4h(D, i)) * dscale;
+                    in.d = h2f(lane16(D, i)) * dscale;
                     for (int c = 0; c < 2; ++c) {
-                        in.pu[c] = unorm16(lane4h(PU[c], i));
-                        in.lu[c] = unorm16(lane4h(LU[c], i));
-                        in.bu[c] = unorm16(lane4h(BU[c], i));
-                        in.liu[c] = unorm16(lane4h(LI[c], i));
-                        in.eu[c] = unorm16(lane4h(EU[c], i));
+                        in.pu[c] = unorm16(lane16(PU[c], i));
+                        in.lu[c] = unorm16(lane16(LU[c], i));
+                        in.bu[c] = unorm16(lane16(BU[c], i));
+                        in.liu[c] = unorm16(lane16(LI[c], i));
+                        in.eu[c] = unorm16(lane16(EU[c], i));
                     }
-                    in.f = uint8_t(F4 >> (8 * i));
-                    in.cat = uint8_t(C4 >> (8 * i));
-                    process_sample(a, in, false, palb, prep, plane_mask, fx, fy, lum4[i], key4[i]);
+                    in.f = uint8_t(F[i >> 2] >> (8 * (i & 3)));
+                    in.cat = uint8_t(Cg[i >> 2] >> (8 * (i & 3)));
+                    process_sample(a, in, false, palb, prep, plane_mask, fx, fy, lumv[i], keyv[i]);
                 }
                 if (prep) {
-                    *reinterpret_cast<float4*>(gp.lum + k) = make_float4(lum4[0], lum4[1], lum4[2], lum4[3]);
-                    *reinterpret_cast<uint4*>(gp.key + k) = make_uint4(key4[0], key4[1], key4[2], key4[3]);
+                    for (int q = 0; q < V / 4; ++q) {
+                        *reinterpret_cast<float4*>(gp.lum + k + 4 * q) =
+                            make_float4(lumv[4 * q], lumv[4 * q + 1], lumv[4 * q + 2], lumv[4 * q + 3]);
+                        *reinterpret_cast<uint4*>(gp.key + k + 4 * q) =
+                            make_uint4(keyv[4 * q], keyv[4 * q + 1], keyv[4 * q + 2], keyv[4 * q + 3]);
+                    }
                 }
             }
         } else {
@@ -718,11 +743,26 @@ cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t fir
     vec4 = vec4 && (!gp.lum || (aligned(gp.lum, 16) && aligned(gp.key, 16)));
     const unsigned blocks = grid_for(count, 128);
     if (s.compact) {
-        if (vec4) k_accumulate_pixels<true, true><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
-        else k_accumulate_pixels<false, true><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        // 16-byte loads of 8 samples when every present plane allows them
+        bool wide = vec4 && spp % 8 == 0;
+        const DeviceSamples16& h = s.c16;
+        for (int c = 0; c < 3; ++c) wide = wide && aligned(h.sqrt_radiance[c], 16) && aligned(h.normal[c], 16);
+        wide = wide && aligned(h.depth, 16);
+        for (int c = 0; c < 2; ++c)
+            wide = wide && (!h.pixel_u[0] || aligned(h.pixel_u[c], 16)) && (!h.lens_u[0] || aligned(h.lens_u[c], 16)) &&
+                   (!h.brdf_u[0] || aligned(h.brdf_u[c], 16)) && (!h.light_u[0] || aligned(h.light_u[c], 16)) &&
+                   (!h.env_u[0] || aligned(h.env_u[c], 16));
+        if (wide)
+            k_accumulate_pixels<true, true, true><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else if (vec4)
+            k_accumulate_pixels<true, true, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else
+            k_accumulate_pixels<false, true, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     } else {
-        if (vec4) k_accumulate_pixels<true, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
-        else k_accumulate_pixels<false, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        if (vec4)
+            k_accumulate_pixels<true, false, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else
+            k_accumulate_pixels<false, false, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     }
     j.launches += 1;
     return cudaGetLastError();

@@ -569,6 +569,8 @@ cudaError_t launch_statmc(Job& j) {
             break;
         }
     }
+    // a tuned tile height (RPD_TUNE_STATMC_ROWS) when its tile fits
+    if (j.statmc_by > 0 && j.statmc_by <= by) by = j.statmc_by;
     if (j.exact_window || by == 0) {
         k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
     } else {

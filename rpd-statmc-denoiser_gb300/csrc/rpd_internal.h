@@ -148,6 +148,7 @@ struct Job {
     bool exact_grid = false;     // RPD_EXACT_GRID: double-precision grid in the reference's order
     bool exact_window = false;   // RPD_EXACT_WINDOW: double-precision StatMC window
     int grid_shape = 6;          // launch shape of the random-dimension grid pass (row groups x dimension sets)
+    int statmc_by = 0;           // StatMC tile height (0: the largest that fits)
     bool pass_open = false;
     bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)
     bool features_valid = false;

@@ -242,6 +242,15 @@ def lib() -> C.CDLL:
         "rpd_job_push_samples": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp, C.c_int]),
         "rpd_job_push_samples16": (C.c_int, [vp, C.POINTER(SampleSoA16), i64, i64, i32, vp, C.c_int]),
         "rpd_encode_samples16": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, C.POINTER(SampleSoA16)]),
+        "rpd_job_autotune": (C.c_int, [vp, C.POINTER(SampleSoA), C.POINTER(SampleSoA16), i32]),
+        "rpd_batch_create": (C.c_int, [vp, C.POINTER(vp)]),
+        "rpd_batch_add": (C.c_int, [vp, vp, C.POINTER(SampleSoA), C.POINTER(SampleSoA16), i32]),
+        "rpd_batch_run": (C.c_int, [vp]),
+        "rpd_batch_sync": (C.c_int, [vp]),
+        "rpd_batch_last_ms": (C.c_int, [vp, C.POINTER(C.c_float)]),
+        "rpd_batch_kernel_count": (u64, [vp]),
+        "rpd_batch_set_lanes": (C.c_int, [vp, C.c_int]),
+        "rpd_batch_destroy": (None, [vp]),
         "rpd_job_end_pass": (C.c_int, [vp]),
         "rpd_recompute_sensitivity": (C.c_int, [vp]),
         "rpd_statmc_denoise": (C.c_int, [vp]),
@@ -285,7 +294,9 @@ def exported_symbols() -> list[str]:
     return ["rpd_config_defaults", "rpd_config_validate", "rpd_ctx_create", "rpd_ctx_destroy", "rpd_job_footprint",
             "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config", "rpd_job_set_exact",
             "rpd_job_set_tuning", "rpd_job_get_tuning",
-            "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_push_samples16", "rpd_encode_samples16", "rpd_job_end_pass", "rpd_recompute_sensitivity",
+            "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_push_samples16", "rpd_encode_samples16",
+            "rpd_job_autotune", "rpd_batch_create", "rpd_batch_add", "rpd_batch_run", "rpd_batch_sync",
+            "rpd_batch_last_ms", "rpd_batch_kernel_count", "rpd_batch_set_lanes", "rpd_batch_destroy", "rpd_job_end_pass", "rpd_recompute_sensitivity",
             "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
             "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
             "rpd_job_set_profiling", "rpd_job_kernel_time", "rpd_job_reset_kernel_times", "rpd_kernel_name",
@@ -518,6 +529,49 @@ def atrous_noalloc(raw: "DeviceBuffer", normal: "DeviceBuffer", albedo: "DeviceB
                                            iterations, out.ptr, stream or None))
 
 
+def _frame_args(samples):
+    if isinstance(samples, DeviceSamples16):
+        return None, C.byref(samples.soa())
+    return C.byref(samples.soa()), None
+
+
+class Batch:
+    """rpd_batch: frames of several jobs captured into one CUDA graph."""
+
+    def __init__(self, ctx: "Context"):
+        h = C.c_void_p()
+        check(lib().rpd_batch_create(ctx.handle, C.byref(h)))
+        self.handle = h.value
+        self.keep = []
+
+    def add(self, job: "Job", samples, spp: int) -> None:
+        s32, s16 = _frame_args(samples)
+        self.keep.append(samples)
+        check(lib().rpd_batch_add(self.handle, job.handle, s32, s16, spp))
+
+    def run(self) -> None:
+        check(lib().rpd_batch_run(self.handle))
+
+    def sync(self) -> None:
+        check(lib().rpd_batch_sync(self.handle))
+
+    def last_ms(self) -> float:
+        v = C.c_float()
+        check(lib().rpd_batch_last_ms(self.handle, C.byref(v)))
+        return float(v.value)
+
+    def kernel_count(self) -> int:
+        return int(lib().rpd_batch_kernel_count(self.handle))
+
+    def set_lanes(self, lanes: int) -> None:
+        check(lib().rpd_batch_set_lanes(self.handle, int(lanes)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().rpd_batch_destroy(self.handle)
+            self.handle = None
+
+
 class Job:
     """rpd_job: one frame's state in HBM and the reference's stage entry points."""
 
@@ -541,7 +595,12 @@ class Job:
     def set_exact(self, grid: bool = False, window: bool = False) -> None:
         check(lib().rpd_job_set_exact(self.handle, (1 if grid else 0) | (2 if window else 0)))
 
-    TUNING = {"grid_shape": 0, "host_band_mb": 1}
+    TUNING = {"grid_shape": 0, "host_band_mb": 1, "statmc_rows": 2}
+
+    def autotune(self, samples, spp: int) -> None:
+        """rpd_job_autotune on device-resident planes (leaves the frame denoised)."""
+        s32, s16 = _frame_args(samples)
+        check(lib().rpd_job_autotune(self.handle, s32, s16, spp))
 
     def set_tuning(self, knob: str, value: int) -> None:
         check(lib().rpd_job_set_tuning(self.handle, self.TUNING[knob], int(value)))
