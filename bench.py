@@ -523,6 +523,145 @@ def run_batched(args):
         print(json.dumps(out))
 
 
+def serving_knobs(R):
+    """The serving workload's stage knobs: the plain method's, with three adaptive passes of 4
+    extra samples per pixel on average and a floor of 1."""
+    return workload_config(R, 1, 1).replace(adaptive_passes=3, adaptive_spp=4, adaptive_base_samples=1)
+
+
+def request_stream(count: int, rate: float, seed: int):
+    """A Poisson stream: (arrival s, width, height, spp, seed) with sizes and spp drawn as in the
+    mixed-size job stream."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    out = []
+    for i in range(count):
+        w, h = SIZES[int(rng.integers(len(SIZES)))]
+        out.append((float(t[i]), w, h, SPPS[int(rng.integers(len(SPPS)))], seed + 7919 * (i + 1)))
+    return out
+
+
+def run_serving(args):
+    """The serving form: a Poisson stream of requests (sizes and spp of the mixed stream, three
+    adaptive passes each, extra samples generated on the device) submitted to rpd_server in
+    real time; the server admits them against a 120 GB HBM budget and overlaps them on the GPU.
+    Against the plain per-frame drop-in (render()'s call sequence from the host, FP32 planes, one
+    request after another) on a bounded prefix of the same stream."""
+    import threading
+
+    import rpd_gb300 as R
+
+    world, rank, local, dist = dist_setup()
+    ctx = R.Context(local, 0)
+    knobs = serving_knobs(R)
+    n_req = args.steps
+    stream = request_stream(n_req, args.rate, SEED + 1000 * rank)
+    srv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=args.inflight, storage=args.storage)
+    # warm-up: a few requests of every size (creates the cached jobs, fills the buffer pool)
+    for k in range(max(1, args.warmup)):
+        for (w, h) in SIZES:
+            srv.submit(w, h, SPPS[k % len(SPPS)], 17 + k, tag=0)
+    srv.drain(600000)
+    srv.poll(4096)
+    st0 = srv.stats()
+    barrier(dist)
+    # the arrival process, in real time, from a host thread
+    def submitter(t0):
+        for (t, w, h, spp, seed) in stream:
+            delay = t0 + t - time.perf_counter()
+            if delay > 0.002:
+                time.sleep(delay - 0.001)
+            while time.perf_counter() < t0 + t:
+                pass
+            srv.submit(w, h, spp, seed, tag=seed)
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        th = threading.Thread(target=submitter, args=(t0,))
+        th.start()
+        th.join()
+        srv.drain(3600000)
+    done = [c for c in srv.poll(n_req + 16) if c["tag"] != 0]
+    st1 = srv.stats()
+    assert len(done) == n_req and all(c["status"] == 0 for c in done), "serving run incomplete"
+    first = min(c["submit_ms"] for c in done)
+    last = max(c["done_ms"] for c in done)
+    wall_s = max_over_ranks(dist, (last - first) * 1e-3)
+    samples = sum(c["samples"] for c in done)
+    lat = np.array([c["done_ms"] - c["submit_ms"] for c in done])
+    queue_ms = np.array([c["admit_ms"] - c["submit_ms"] for c in done])
+    value = world * samples / wall_s / 1e6
+    srv.close()
+
+    # quality: served results against the plain FP32 drop-in on a few requests
+    rel = []
+    qsrv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=4, storage=args.storage)
+    picks = [stream[i] for i in range(min(4, n_req))]
+    bufs = []
+    for (_, w, h, spp, seed) in picks:
+        b = R.PinnedBuffer(w * h * 12)
+        bufs.append(b)
+        qsrv.submit(w, h, spp, seed, out=b.ptr, tag=seed)
+    qsrv.drain(600000)
+    qsrv.close()
+    for (_, w, h, spp, seed), b in zip(picks, bufs):
+        img, _ = R.plain_request(ctx, knobs, w, h, spp, seed)
+        ref = img.astype(np.float64)
+        x = b.array(np.float32, (h, w, 3)).astype(np.float64)
+        rel.append(float(np.mean((x - ref) ** 2 / (ref * ref + 1e-2))))
+        b.free()
+
+    # the plain per-frame drop-in on a bounded prefix of the stream, one request after another
+    # (jobs cached per size, as a caller of the drop-in would keep them)
+    plain_jobs = {}
+    plain_samples = 0
+    n_plain = min(n_req, args.plain_requests)
+    for (_, w, h, spp, seed) in stream[:2]:
+        R.plain_request(ctx, knobs, w, h, spp, seed)  # warm-up
+    t_plain = time.perf_counter()
+    for (_, w, h, spp, seed) in stream[:n_plain]:
+        if (w, h) not in plain_jobs:
+            plain_jobs[(w, h)] = R.Job(ctx, knobs.replace(image_width=w, image_height=h))
+        _, ns = R.plain_request(ctx, knobs, w, h, spp, seed, job=plain_jobs[(w, h)])
+        plain_samples += ns
+    t_plain = time.perf_counter() - t_plain
+    for j in plain_jobs.values():
+        j.close()
+    plain_value = plain_samples / t_plain / 1e6
+    out = {"metric": f"denoised Msamples/s, served stream ({n_req} requests, Poisson {args.rate:g} req/s, "
+                     f"3 adaptive passes, {args.storage} storage)",
+           "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": n_req, "warmup": args.warmup,
+           "ms_per_step": round(wall_s * 1e3 / n_req, 4), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "config": {"workload": f"{n_req} requests, Poisson arrivals at {args.rate:g}/s, sizes from {SIZES}, spp "
+                                  f"from {SPPS}, adaptive_passes 3, adaptive_spp 4, base samples 1; samples of every "
+                                  f"pass generated on the device (seed {SEED})",
+                      "step": "one request", "hbm_budget_gb": args.budget_gb, "max_inflight": args.inflight,
+                      "storage": args.storage, "samples": samples, "wall_s": round(wall_s, 4),
+                      "l2": "sample planes of every request larger than L2 except the 256x256 ones",
+                      "parallelism": "replicas"},
+           "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3),
+                          "mean": round(float(lat.mean()), 3), "max": round(float(lat.max()), 3),
+                          "queue_p50": round(float(np.percentile(queue_ms, 50)), 3),
+                          "queue_p99": round(float(np.percentile(queue_ms, 99)), 3)},
+           "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": int(np.mean([c["width"] * c["height"] * 12 for c in done])),
+                   "form": "submit to denoised image in host memory; the per-sample input is generated on the "
+                           "device from each request's seed, so nothing crosses host->device"},
+           "plain": {"value": round(plain_value, 3), "requests": n_plain, "samples": plain_samples,
+                     "s": round(t_plain, 3),
+                     "form": "render()'s call sequence per request from the host, FP32 planes generated on the "
+                             "device, adaptive counts read back, one request after another"},
+           "speedup_vs_plain": round(value / plain_value, 3),
+           "quality": {"reference": "the plain FP32 drop-in on the same requests", "rel_mse_eps": 1e-2,
+                       "rel_mse_mean": float(np.mean(rel)), "rel_mse_max": float(np.max(rel))},
+           "server": {"bytes_peak": st1["bytes_peak"], "bytes_budget": st1["bytes_budget"],
+                      "jobs_cached": st1["jobs_cached"]},
+           "gpu_launches": int(st1["launches"] - st0["launches"]), "clocks": clocks.summary()}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def run_reference(args):
     world, rank, _, dist = dist_setup()
     if rank != 0:
@@ -555,10 +694,16 @@ def main():
     ap.add_argument("--grid-shape", type=int, default=0, help="random-dimension grid launch shape 1..6 (0: default)")
     ap.add_argument("--precision", choices=["fp32", "fp16"], default="fp32",
                     help="fp16: the precision form (compact per-sample storage, single-precision accumulation)")
-    ap.add_argument("--form", choices=["plain", "batched"], default="plain",
-                    help="batched: uneven frames in one graph-captured launch (fp16 storage, autotuned shapes)")
+    ap.add_argument("--form", choices=["plain", "batched", "serving"], default="plain",
+                    help="batched: uneven frames in one graph-captured launch (fp16 storage, autotuned shapes); "
+                         "serving: a Poisson stream of requests through rpd_server (--steps requests)")
     ap.add_argument("--frames", type=int, default=48, help="frames of the batched form")
     ap.add_argument("--lanes", type=int, default=4, help="concurrent frame chains of the batched form")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
+    ap.add_argument("--budget-gb", type=int, default=120, help="serving: HBM admission budget")
+    ap.add_argument("--inflight", type=int, default=32, help="serving: requests on the GPU at once")
+    ap.add_argument("--storage", choices=["fp16", "fp32"], default="fp16", help="serving: sample storage")
+    ap.add_argument("--plain-requests", type=int, default=200, help="serving: stream prefix run through the plain drop-in")
     args = ap.parse_args()
     if (args.width, args.height, args.spp) != (W, H, SPP):
         W, H, SPP = args.width, args.height, args.spp
@@ -569,6 +714,8 @@ def main():
         run_reference(args)
     elif args.form == "batched":
         run_batched(args)
+    elif args.form == "serving":
+        run_serving(args)
     else:
         run_gpu(args)
 

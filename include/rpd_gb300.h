@@ -36,7 +36,8 @@ typedef enum rpd_status {
     RPD_ERR_CUDA = 5,             /* CUDA runtime error (message has the CUDA text) */
     RPD_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up */
     RPD_ERR_STATE = 7,            /* call out of order (e.g. denoise before any samples) */
-    RPD_ERR_NO_DEVICE = 8         /* no CUDA device, or the device is not sm_103 */
+    RPD_ERR_NO_DEVICE = 8,        /* no CUDA device, or the device is not sm_103 */
+    RPD_ERR_CANCELLED = 9         /* a queued serving request was cancelled */
 } rpd_status;
 
 /* Where the pointers handed to a call live. */
@@ -271,6 +272,9 @@ int rpd_job_set_exact(rpd_job* job, int flags);
 /* RPD_TUNE_STATMC_ROWS: pixel rows per block of the StatMC window kernel: 2, 4 or 8 (0, the
  * default: the tallest whose halo tile fits in shared memory). */
 #define RPD_TUNE_STATMC_ROWS 2
+/* RPD_TUNE_ALLOCATOR: 0 (default) the parallel allocation of the adaptive counts, 1 the
+ * one-thread kernel in the reference's order. Both give the same counts. */
+#define RPD_TUNE_ALLOCATOR 3
 int rpd_job_set_tuning(rpd_job* job, int knob, int value);
 int rpd_job_get_tuning(rpd_job* job, int knob, int* value);
 /* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */
@@ -335,6 +339,22 @@ int rpd_variance_denoise(rpd_job* job);
 /* Extra sample count per pixel for one adaptive pass; written to counts_out (W*H int32
  * in `where` memory; may be NULL, the result stays readable as RPD_FIELD_ADAPTIVE_COUNTS). */
 int rpd_compute_adaptive_sample_counts(rpd_job* job, int32_t* counts_out, rpd_memory where);
+/* Outcome of the job's last adaptive allocation (synchronises the job's stream): out[0] 1 when
+ * the parallel allocation finished, out[1] 1 when it handed the allocation to the serial
+ * kernel, out[2] 1 when a grid barrier timed out, out[3] water-filling passes, out[4]
+ * fixed-point rounds beyond the first of each pass, out[5] chunks walked exactly, out[6] why
+ * it handed over (0 it did not, 1 an importance outside [0, FLT_MAX], 2 no room for exact
+ * chunk values, 3 a pass that did not settle, 4 a barrier timeout, 5 no cooperative launch). */
+int rpd_job_allocator_stats(rpd_job* job, int32_t* out7);
+/* Device timestamps (ns since its launch) of the last parallel allocation at each of its grid
+ * barriers: up to max values into ns, the count in *n_out. */
+int rpd_job_allocator_timeline(rpd_job* job, uint64_t* ns, int32_t max, int32_t* n_out);
+/* The allocation step of compute_adaptive_sample_counts (main.cpp:1372-1438) on a caller's
+ * importance map (W*H floats, the map after any smoothing; finite and >= 0): counts_out gets
+ * the floor plus the extra samples exactly as the reference allocates them from that map. The
+ * map becomes the job's RPD_FIELD_ADAPTIVE_IMPORTANCE. */
+int rpd_adaptive_allocate(rpd_job* job, const float* importance, rpd_memory where, int32_t* counts_out,
+                          rpd_memory out_where);
 /* FrameBuffers::finalize (core/buffers.h:152-167) on the radiance/feature sums. */
 int rpd_finalize(rpd_job* job);
 
@@ -445,6 +465,74 @@ int rpd_synth_fill(rpd_ctx* ctx, const struct rpd_synth_params* params, int64_t 
 
 const char* rpd_last_error(void);
 const char* rpd_status_string(int status);
+
+/* ---- serving: continuous batching of denoise requests (serve.cu) ----------------------
+ *
+ * A request loop over one GPU. Requests of any size and first-pass spp are submitted at any
+ * time; a scheduler thread admits them in arrival order as slots (max_inflight) and HBM budget
+ * free up, runs each one's whole pipeline — the first pass, config.adaptive_passes adaptive
+ * passes, the final StatMC and variance passes (render(), main.cpp:1543-1564) — on its own
+ * stream with its state resident in HBM, and copies the denoised image to host memory. Requests
+ * overlap on the device. The per-sample source is the seeded generator of rpd_synth.h evaluated
+ * on the device (the first pass draws ordinals 0..spp-1 of each pixel, adaptive pass p draws
+ * from p << 16 on), so a request is fully described by its size, spp and seed. A request's
+ * result does not depend on what else runs. */
+typedef struct rpd_server rpd_server;
+
+typedef enum rpd_storage {
+    RPD_STORAGE_FP32 = 0,   /* rpd_sample_soa planes */
+    RPD_STORAGE_FP16 = 1    /* rpd_sample_soa16 planes (sqrt-radiance binary16, snorm16 normals, ...) */
+} rpd_storage;
+
+typedef struct rpd_server_config {
+    rpd_config knobs;            /* stage knobs of every request; the image size comes per request */
+    uint64_t hbm_budget_bytes;   /* admission budget for request state and buffers (0: the context's) */
+    int32_t max_inflight;        /* requests on the GPU at once, 1..256 */
+    int32_t storage;             /* rpd_storage of the sample buffers */
+} rpd_server_config;
+
+typedef struct rpd_request {
+    int32_t width, height;
+    int32_t spp;                 /* samples per pixel of the first pass, 0..65535 */
+    uint32_t seed;               /* seed of the synthetic workload (rpd_synth_defaults at this size) */
+    float* denoised_out;         /* width*height*3 floats (interleaved RGB), page-locked host memory
+                                  * (rpd_host_alloc) or device memory; NULL: the result is copied to
+                                  * a buffer of the server and not kept */
+    int32_t out_where;           /* rpd_memory of denoised_out */
+    uint64_t tag;                /* returned in the completion */
+} rpd_request;
+
+typedef struct rpd_completion {
+    uint64_t id, tag;
+    int32_t status;              /* RPD_OK, RPD_ERR_CANCELLED or the error that stopped the request */
+    int32_t width, height, spp;
+    int64_t samples;             /* samples denoised: the first pass plus every adaptive pass */
+    double submit_ms, admit_ms, done_ms;  /* server clock (ms since rpd_server_create) */
+} rpd_completion;
+
+typedef struct rpd_server_stats {
+    int64_t submitted, completed, rejected, queued, inflight;
+    uint64_t bytes_reserved, bytes_peak, bytes_budget;
+    int64_t jobs_cached;
+    double now_ms;               /* server clock */
+    int64_t launches;            /* kernels enqueued for requests so far */
+} rpd_server_stats;
+
+void rpd_server_config_defaults(rpd_server_config* cfg);
+int rpd_server_create(rpd_ctx* ctx, const rpd_server_config* cfg, rpd_server** out);
+/* Queues a request. A request that cannot fit the budget even alone is refused here with
+ * RPD_ERR_OVER_BUDGET; a bad size or config with RPD_ERR_INVALID_ARGUMENT / _CONFIG. */
+int rpd_server_submit(rpd_server* srv, const rpd_request* req, uint64_t* id_out);
+/* Moves up to max finished requests (in completion order) to out; *n_out gets the number. */
+int rpd_server_poll(rpd_server* srv, rpd_completion* out, int32_t max, int32_t* n_out);
+/* Waits until nothing is queued or running (timeout_ms < 0: no limit); RPD_ERR_TIMEOUT else. */
+int rpd_server_drain(rpd_server* srv, int32_t timeout_ms);
+/* Cancels a queued request (its completion carries RPD_ERR_CANCELLED); one already on the GPU
+ * runs to the end (RPD_ERR_STATE). */
+int rpd_server_cancel(rpd_server* srv, uint64_t id);
+int rpd_server_get_stats(rpd_server* srv, rpd_server_stats* out);
+/* Finishes every submitted request, then releases the server. */
+void rpd_server_destroy(rpd_server* srv);
 
 #ifdef __cplusplus
 }

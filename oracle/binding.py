@@ -61,6 +61,7 @@ def port() -> C.CDLL:
         "orc_statmc_denoise": (C.c_int, [vp]),
         "orc_variance_denoise": (C.c_int, [vp]),
         "orc_compute_adaptive_sample_counts": (C.c_int, [vp, vp]),
+        "orc_allocate_counts_map": (None, [vp, i64, C.POINTER(R.Config), vp]),
         "orc_finalize": (C.c_int, [vp]),
         "orc_job_read": (C.c_int, [vp, C.c_int, vp, C.c_size_t]),
         "orc_stage_ms": (C.c_double, [vp, C.c_int]),
@@ -151,6 +152,15 @@ def ref_joint_bilateral(raw, normal, albedo, sigma_c, sigma_n, sigma_p, sigma_a)
     if rc != 0:
         raise RuntimeError(f"reference joint-bilateral filter failed ({rc})")
     return tuple(outs)
+
+
+def port_allocate(importance: np.ndarray, cfg) -> np.ndarray:
+    """The allocation of compute_adaptive_sample_counts (main.cpp:1372-1438) on a given final
+    importance map, in the reference's order."""
+    imp = np.ascontiguousarray(importance, dtype=np.float32).ravel()
+    counts = np.empty(imp.size, dtype=np.int32)
+    port().orc_allocate_counts_map(imp.ctypes.data, imp.size, C.byref(cfg), counts.ctypes.data)
+    return counts
 
 
 def port_atrous(raw, normal, albedo, sigma_c, sigma_n, sigma_a, iterations, threads: int = 1) -> np.ndarray:

@@ -1153,6 +1153,90 @@ int orc_variance_denoise(orc_job* j) {
 
 /* ---- compute_adaptive_sample_counts (main.cpp:1273-1446) ------------------------------ */
 
+/* The budget-preserving allocation of compute_adaptive_sample_counts (main.cpp:1372-1438) on a
+ * final importance map: counts holds the floor per pixel on entry and the counts on return.
+ * sum_importance is std::accumulate over the map (main.cpp:1370), in pixel order. */
+void orc_allocate_counts(const float* importance, int64_t np, const rpd_config* cfg, double sum_importance,
+                         int32_t* sc) {
+    const int extra_sample_total = (int)(cfg->adaptive_spp * np);
+    const int floor_per_pixel = iclamps(cfg->adaptive_base_samples, 0, cfg->adaptive_spp);
+    const int reserved_samples = (int)(floor_per_pixel * np);
+    if (extra_sample_total <= 0) return;
+    {
+        int remaining_samples = imaxs(0, extra_sample_total - reserved_samples);
+        if (sum_importance <= 0.0 || remaining_samples <= 0) {
+            return;
+        }
+        float* desired_add = (float*)zalloc((size_t)np * 4);
+        int32_t* active = (int32_t*)malloc((size_t)np * 4);
+        int32_t* next_active = (int32_t*)malloc((size_t)np * 4);
+        int64_t n_active = np;
+        for (int64_t i = 0; i < np; ++i) active[i] = (int32_t)i;
+        double remaining_importance = sum_importance;
+        const int max_extra_per_pixel = imaxs(4, 8 * imaxs(1, cfg->adaptive_spp));
+        while (n_active > 0 && remaining_samples > 0 && remaining_importance > (double)EPS_SMALL) {
+            int clipped = 0;
+            int64_t n_next = 0;
+            for (int64_t a = 0; a < n_active; ++a) {
+                const int32_t idx = active[a];
+                const double share = (double)importance[idx] / remaining_importance;
+                const double desired = share * (double)remaining_samples;
+                if (desired > (double)max_extra_per_pixel) {
+                    desired_add[idx] = (float)max_extra_per_pixel;
+                    remaining_samples -= max_extra_per_pixel;
+                    remaining_importance -= (double)importance[idx];
+                    clipped = 1;
+                } else {
+                    next_active[n_next++] = idx;
+                }
+            }
+            if (!clipped) {
+                for (int64_t a = 0; a < n_next; ++a) {
+                    const int32_t idx = next_active[a];
+                    desired_add[idx] = (float)((double)importance[idx] / remaining_importance * (double)remaining_samples);
+                }
+                break;
+            }
+            int32_t* t = active; active = next_active; next_active = t;
+            n_active = n_next;
+        }
+        int assigned = 0;
+        float* residual = (float*)zalloc((size_t)np * 4);
+        double residual_sum = 0.0;
+        for (int64_t i = 0; i < np; ++i) {
+            const int add = (int)floorf(desired_add[i]);
+            sc[i] += add;
+            assigned += add;
+            residual[i] = fmaxs(0.0f, desired_add[i] - (float)add);
+            residual_sum += (double)residual[i];
+        }
+        const int remaining = imaxs(0, extra_sample_total - reserved_samples - assigned);
+        if (remaining > 0 && residual_sum > (double)EPS_SMALL) {
+            const double offset = (double)hash_to_unit_float(cfg->seed ^ 0x4d595df4u);
+            double cumulative = 0.0;
+            int64_t cursor = 0;
+            for (int k = 0; k < remaining; ++k) {
+                const double target = (((double)k + offset) / (double)remaining) * residual_sum;
+                while (cursor < np && cumulative + (double)residual[cursor] < target) {
+                    cumulative += (double)residual[cursor];
+                    ++cursor;
+                }
+                if (cursor < np) sc[cursor]++;
+            }
+        }
+        free(residual); free(desired_add); free(active); free(next_active);
+    }
+}
+
+/* orc_allocate_counts with the sum taken here, for callers holding only the map. */
+void orc_allocate_counts_map(const float* importance, int64_t np, const rpd_config* cfg, int32_t* counts) {
+    const int floor_per_pixel = iclamps(cfg->adaptive_base_samples, 0, cfg->adaptive_spp);
+    for (int64_t i = 0; i < np; ++i) counts[i] = floor_per_pixel;
+    double sum_importance = 0.0;
+    for (int64_t i = 0; i < np; ++i) sum_importance = sum_importance + (double)importance[i];
+    orc_allocate_counts(importance, np, cfg, sum_importance, counts);
+}
+
 int orc_compute_adaptive_sample_counts(orc_job* j, int32_t* counts_out) {
     const double t0 = now_ms();
     set_omp(j->threads);
@@ -1160,7 +1244,6 @@ int orc_compute_adaptive_sample_counts(orc_job* j, int32_t* counts_out) {
     const int64_t np = (int64_t)j->np;
     const int extra_sample_total = j->cfg.adaptive_spp * w * h;
     const int floor_per_pixel = iclamps(j->cfg.adaptive_base_samples, 0, j->cfg.adaptive_spp);
-    const int reserved_samples = floor_per_pixel * w * h;
     int32_t* sc = j->last_counts;
     for (int64_t i = 0; i < np; ++i) sc[i] = floor_per_pixel;
     if (extra_sample_total <= 0) goto done;
@@ -1224,69 +1307,8 @@ int orc_compute_adaptive_sample_counts(orc_job* j, int32_t* counts_out) {
         }
         memcpy(j->adaptive_importance, importance, (size_t)np * 4);
 
-        int remaining_samples = imaxs(0, extra_sample_total - reserved_samples);
-        if (sum_importance <= 0.0 || remaining_samples <= 0) {
-            free(importance); free(vs);
-            goto done;
-        }
-        float* desired_add = (float*)zalloc((size_t)np * 4);
-        int32_t* active = (int32_t*)malloc((size_t)np * 4);
-        int32_t* next_active = (int32_t*)malloc((size_t)np * 4);
-        int64_t n_active = np;
-        for (int64_t i = 0; i < np; ++i) active[i] = (int32_t)i;
-        double remaining_importance = sum_importance;
-        const int max_extra_per_pixel = imaxs(4, 8 * imaxs(1, j->cfg.adaptive_spp));
-        while (n_active > 0 && remaining_samples > 0 && remaining_importance > (double)EPS_SMALL) {
-            int clipped = 0;
-            int64_t n_next = 0;
-            for (int64_t a = 0; a < n_active; ++a) {
-                const int32_t idx = active[a];
-                const double share = (double)importance[idx] / remaining_importance;
-                const double desired = share * (double)remaining_samples;
-                if (desired > (double)max_extra_per_pixel) {
-                    desired_add[idx] = (float)max_extra_per_pixel;
-                    remaining_samples -= max_extra_per_pixel;
-                    remaining_importance -= (double)importance[idx];
-                    clipped = 1;
-                } else {
-                    next_active[n_next++] = idx;
-                }
-            }
-            if (!clipped) {
-                for (int64_t a = 0; a < n_next; ++a) {
-                    const int32_t idx = next_active[a];
-                    desired_add[idx] = (float)((double)importance[idx] / remaining_importance * (double)remaining_samples);
-                }
-                break;
-            }
-            int32_t* t = active; active = next_active; next_active = t;
-            n_active = n_next;
-        }
-        int assigned = 0;
-        float* residual = (float*)zalloc((size_t)np * 4);
-        double residual_sum = 0.0;
-        for (int64_t i = 0; i < np; ++i) {
-            const int add = (int)floorf(desired_add[i]);
-            sc[i] += add;
-            assigned += add;
-            residual[i] = fmaxs(0.0f, desired_add[i] - (float)add);
-            residual_sum += (double)residual[i];
-        }
-        const int remaining = imaxs(0, extra_sample_total - reserved_samples - assigned);
-        if (remaining > 0 && residual_sum > (double)EPS_SMALL) {
-            const double offset = (double)hash_to_unit_float(j->cfg.seed ^ 0x4d595df4u);
-            double cumulative = 0.0;
-            int64_t cursor = 0;
-            for (int k = 0; k < remaining; ++k) {
-                const double target = (((double)k + offset) / (double)remaining) * residual_sum;
-                while (cursor < np && cumulative + (double)residual[cursor] < target) {
-                    cumulative += (double)residual[cursor];
-                    ++cursor;
-                }
-                if (cursor < np) sc[cursor]++;
-            }
-        }
-        free(residual); free(desired_add); free(active); free(next_active); free(importance); free(vs);
+        orc_allocate_counts(importance, np, &j->cfg, sum_importance, sc);
+        free(importance); free(vs);
     }
 done:
     if (counts_out) memcpy(counts_out, sc, (size_t)np * 4);

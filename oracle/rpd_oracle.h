@@ -44,6 +44,12 @@ int orc_job_end_pass(orc_job* job);
 int orc_recompute_sensitivity(orc_job* job);
 int orc_statmc_denoise(orc_job* job);
 int orc_variance_denoise(orc_job* job);
+/* compute_adaptive_sample_counts' allocation (main.cpp:1372-1438) on a final importance map:
+ * counts holds the floor per pixel on entry; sum_importance is the in-order double sum. */
+void orc_allocate_counts(const float* importance, int64_t np, const rpd_config* cfg, double sum_importance,
+                         int32_t* counts);
+/* The same from the map alone: counts is set to the floor, the sum taken in pixel order. */
+void orc_allocate_counts_map(const float* importance, int64_t np, const rpd_config* cfg, int32_t* counts);
 int orc_compute_adaptive_sample_counts(orc_job* job, int32_t* counts_out);
 int orc_finalize(orc_job* job);
 int orc_job_read(orc_job* job, int field, void* dst, size_t bytes);

@@ -90,6 +90,8 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5]
     L.add(p.counts, np);
     L.add(p.active_a, np);
     L.add(p.active_b, np);
+    L.add(p.alloc_state, np);
+    L.add(p.alloc_work, int64_t(allocator_work_bytes(np)));
     L.add(n.grid, nn * kDeps * kDepStride);
     L.add(n.pass_grid, nn * kDeps * kDepStride);
     for (int f = 0; f < N_FIELDS; ++f) L.add(n.field[f], nn);
@@ -151,6 +153,8 @@ void rebase_all(PixelPlanes& p, NodePlanes& n, char* base) {
     rebase(p.counts, base);
     rebase(p.active_a, base);
     rebase(p.active_b, base);
+    rebase(p.alloc_state, base);
+    rebase(p.alloc_work, base);
     rebase(n.grid, base);
     rebase(n.pass_grid, base);
     for (int f = 0; f < N_FIELDS; ++f) rebase(n.field[f], base);
@@ -294,6 +298,7 @@ const char* rpd_status_string(int s) {
     case RPD_ERR_TIMEOUT: return "device wait timed out";
     case RPD_ERR_STATE: return "call out of order";
     case RPD_ERR_NO_DEVICE: return "no sm_103 device";
+    case RPD_ERR_CANCELLED: return "cancelled";
     default: return "unknown status";
     }
 }
@@ -386,7 +391,9 @@ int rpd_ctx_create(int device, uint64_t budget, rpd_ctx** out) {
     c->device = device;
     c->budget = budget ? budget : uint64_t(free_b);
     cudaError_t e = cudaStreamCreateWithFlags(&c->util_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->alloc_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
+        if (c->util_stream) cudaStreamDestroy(c->util_stream);
         delete c;
         return cuda_fail(e, "cudaStreamCreate");
     }
@@ -399,6 +406,7 @@ void rpd_ctx_destroy(rpd_ctx* ctx) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->util_stream) cudaStreamDestroy(c->util_stream);
+    if (c->alloc_stream) cudaStreamDestroy(c->alloc_stream);
     delete c;
 }
 
@@ -454,6 +462,8 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
     for (int b = 0; b < Job::kMaxBands && e == cudaSuccess; ++b)
         e = cudaEventCreateWithFlags(&j->band_copied[b], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->staging_free, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->alloc_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->alloc_done, cudaEventDisableTiming);
     for (int s = 0; s < RPD_STAGE_COUNT_ && e == cudaSuccess; ++s) {
         e = cudaEventCreate(&j->ev_start[s]);
         if (e == cudaSuccess) e = cudaEventCreate(&j->ev_stop[s]);
@@ -505,6 +515,8 @@ void rpd_job_destroy(rpd_job* job) {
     for (int b = 0; b < Job::kMaxBands; ++b)
         if (j->band_copied[b]) cudaEventDestroy(j->band_copied[b]);
     if (j->staging_free) cudaEventDestroy(j->staging_free);
+    if (j->alloc_ready) cudaEventDestroy(j->alloc_ready);
+    if (j->alloc_done) cudaEventDestroy(j->alloc_done);
     if (j->copy_stream) cudaStreamDestroy(j->copy_stream);
     if (j->stream) cudaStreamDestroy(j->stream);
     delete j;
@@ -554,6 +566,11 @@ int rpd_job_set_tuning(rpd_job* job, int knob, int value) {
         j->statmc_by = value;
         return RPD_OK;
     }
+    if (knob == RPD_TUNE_ALLOCATOR) {
+        if (value != 0 && value != 1) return fail(RPD_ERR_INVALID_ARGUMENT, "allocator must be 0 or 1");
+        j->serial_allocator = value == 1;
+        return RPD_OK;
+    }
     return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
@@ -564,6 +581,7 @@ int rpd_job_get_tuning(rpd_job* job, int knob, int* value) {
     if (knob == RPD_TUNE_GRID_SHAPE) *value = j->grid_shape;
     else if (knob == RPD_TUNE_HOST_BAND_MB) *value = int(j->band_bytes >> 20);
     else if (knob == RPD_TUNE_STATMC_ROWS) *value = j->statmc_by;
+    else if (knob == RPD_TUNE_ALLOCATOR) *value = j->serial_allocator ? 1 : 0;
     else return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
     return RPD_OK;
 }
@@ -922,9 +940,9 @@ static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int
     gp.width = j->g.w;
     const bool fast_grid = rpd && !j->exact_grid;
     if (fast_grid) {
-        // the per-sample total is needed on the host to size the luminance plane
+        // the per-sample total (or a bound on it) is needed on the host to size the luminance plane
         int64_t nsamp = total;
-        if (counts && where != RPD_MEM_HOST) {
+        if (counts && where != RPD_MEM_HOST && total <= 0) {
             RPD_CUDA(cudaMemcpyAsync(&nsamp, j->offsets + count, 8, cudaMemcpyDeviceToHost, j->stream));
             RPD_CUDA(cudaStreamSynchronize(j->stream));
         }
@@ -1031,6 +1049,45 @@ int rpd_compute_adaptive_sample_counts(rpd_job* job, int32_t* out, rpd_memory wh
                                  where == RPD_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, j->stream));
         if (where == RPD_MEM_HOST) RPD_CUDA(cudaStreamSynchronize(j->stream));
     }
+    return RPD_OK;
+}
+
+int rpd_job_allocator_timeline(rpd_job* job, uint64_t* ns, int32_t max, int32_t* n_out) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!ns || !n_out || max < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "bad timeline arguments");
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    return allocator_timeline(*j, ns, max, n_out);
+}
+
+int rpd_adaptive_allocate(rpd_job* job, const float* importance, rpd_memory where, int32_t* counts_out,
+                          rpd_memory out_where) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!importance) return fail(RPD_ERR_INVALID_ARGUMENT, "null importance map");
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    const uint64_t bytes = uint64_t(j->g.np) * 4;
+    RPD_CUDA(cudaMemcpyAsync(j->p.importance, importance, bytes,
+                             where == RPD_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, j->stream));
+    {
+        StageTimer timer(*j, RPD_STAGE_ADAPTIVE);
+        RPD_CUDA(launch_allocate_map(*j));
+    }
+    if (counts_out) {
+        RPD_CUDA(cudaMemcpyAsync(counts_out, j->p.counts, bytes,
+                                 out_where == RPD_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                                 j->stream));
+        if (out_where == RPD_MEM_HOST) RPD_CUDA(cudaStreamSynchronize(j->stream));
+    }
+    return RPD_OK;
+}
+
+int rpd_job_allocator_stats(rpd_job* job, int32_t* out) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!out) return fail(RPD_ERR_INVALID_ARGUMENT, "null output");
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    RPD_CUDA(allocator_stats(*j, out));
     return RPD_OK;
 }
 
@@ -1432,3 +1489,30 @@ int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, con
 }
 
 }  // extern "C"
+
+namespace rpd {
+
+int job_reserve(Job& j, int64_t max_push_samples) {
+    int st = ensure_offsets(j, j.g.np);
+    if (st != RPD_OK) return st;
+    if (j.cfg.rpf_shrinkage_scale > 0.0f && !j.exact_grid) {
+        void* lum = j.lum;
+        st = grow_device(j, &lum, &j.lum_cap, uint64_t(std::max<int64_t>(max_push_samples, 1)) * 8 + 256);
+        j.lum = static_cast<float*>(lum);
+    }
+    return st;
+}
+
+int push_device_async(Job& j, const DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
+                      int64_t total_bound) {
+    int st = ensure_offsets(j, count);
+    if (st != RPD_OK) return st;
+    StageTimer timer(j, RPD_STAGE_ACCUMULATE);
+    if (counts) RPD_CUDA(launch_offsets_scan(j, counts, count));
+    else RPD_CUDA(launch_offsets_uniform(j, count, spp));
+    DeviceSamples dd = d;
+    return push_tail(&j, dd, first, count, spp, counts, RPD_MEM_DEVICE,
+                     counts ? std::max<int64_t>(total_bound, 1) : int64_t(count) * spp);
+}
+
+}  // namespace rpd

@@ -1,13 +1,12 @@
 // compute_adaptive_sample_counts (main.cpp:1273-1446).
 //
-//   k_importance       variance source and importance = sqrt (1303-1327)
+//   k_importance        variance source and importance = sqrt (1303-1327)
 //   k_smooth_importance edge-aware smoothing (1331-1368)
-//   k_allocate_serial  the budget-preserving allocation (1329-1438). Its integers depend on
-//                      sequential double-precision sums (std::accumulate, the running
-//                      remaining_importance of the water-filling and the cursor of the
-//                      systematic residual sampling), so it runs as one device thread in
-//                      the reference's order: the counts are bit-identical for identical
-//                      importance values.
+//   k_allocate_coop     the budget-preserving allocation (1329-1438) in parallel, with the
+//                       reference's integers bit for bit (k_allocate.cu)
+//   k_allocate_serial   the same allocation as one device thread in the reference's order. It
+//                       runs behind the parallel kernel and returns at once unless that kernel
+//                       flagged a case outside its method (or RPD_TUNE_ALLOCATOR selects it).
 #include <algorithm>
 
 #include "rpd_internal.h"
@@ -81,9 +80,14 @@ struct AllocParams {
     uint32_t seed;
 };
 
-__global__ void k_allocate_serial(PixelPlanes p, AllocParams a, const float* importance) {
+__global__ void k_allocate_serial(PixelPlanes p, AllocParams a, const float* importance, const int* guard,
+                                  int floor_per_pixel) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int64_t np = a.np;
+    if (guard) {
+        if (*(volatile const int*)guard == 0) return;  // the parallel allocation completed
+        for (int64_t i = 0; i < np; ++i) p.counts[i] = floor_per_pixel;
+    }
     double sum_importance = 0.0;
     for (int64_t i = 0; i < np; ++i) sum_importance = sum_importance + double(importance[i]);
     int remaining_samples = imaxs(0, a.extra_sample_total - a.reserved_samples);
@@ -160,6 +164,28 @@ __global__ void k_copy(const float* src, float* dst, int64_t n) {
 
 }  // namespace
 
+namespace {
+
+// The allocation from the final importance map in j.p.importance (main.cpp:1372-1438); the
+// counts hold the floor already.
+cudaError_t launch_allocation(Job& j, int extra_sample_total, int floor_per_pixel) {
+    const int64_t np = j.g.np;
+    const float* importance = j.p.importance;
+    AllocParams a{np, extra_sample_total, floor_per_pixel * j.g.w * j.g.h,
+                  std::max(4, 8 * std::max(1, j.cfg.adaptive_spp)), j.cfg.seed};
+    const int* guard = nullptr;
+    if (!j.serial_allocator) {
+        const cudaError_t e = launch_allocate_parallel(j, importance, a.extra_sample_total, a.reserved_samples,
+                                                       a.max_extra_per_pixel, a.seed, &guard);
+        if (e != cudaSuccess) return e;
+    }
+    k_allocate_serial<<<1, 1, 0, j.stream>>>(j.p, a, importance, guard, floor_per_pixel);
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_adaptive(Job& j) {
     KernelScope ks(j, RPD_KERNEL_ADAPTIVE);
     const int64_t np = j.g.np;
@@ -171,7 +197,6 @@ cudaError_t launch_adaptive(Job& j) {
     if (extra_sample_total <= 0) return cudaGetLastError();
     k_importance<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np, j.cfg.adaptive_sigma_max);
     j.launches += 1;
-    const float* importance = j.p.importance;
     const int radius = j.cfg.adaptive_importance_smoothing_radius;
     if (radius > 0) {
         k_smooth_importance<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, w, h, radius, j.p.importance,
@@ -179,11 +204,18 @@ cudaError_t launch_adaptive(Job& j) {
         k_copy<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p.importance_tmp, j.p.importance, np);
         j.launches += 2;
     }
-    AllocParams a{np, extra_sample_total, floor_per_pixel * w * h,
-                  std::max(4, 8 * std::max(1, j.cfg.adaptive_spp)), j.cfg.seed};
-    k_allocate_serial<<<1, 1, 0, j.stream>>>(j.p, a, importance);
+    return launch_allocation(j, extra_sample_total, floor_per_pixel);
+}
+
+cudaError_t launch_allocate_map(Job& j) {
+    KernelScope ks(j, RPD_KERNEL_ADAPTIVE);
+    const int64_t np = j.g.np;
+    const int extra_sample_total = j.cfg.adaptive_spp * j.g.w * j.g.h;
+    const int floor_per_pixel = std::clamp(j.cfg.adaptive_base_samples, 0, j.cfg.adaptive_spp);
+    k_fill_counts<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p.counts, np, floor_per_pixel);
     j.launches += 1;
-    return cudaGetLastError();
+    if (extra_sample_total <= 0) return cudaGetLastError();
+    return launch_allocation(j, extra_sample_total, floor_per_pixel);
 }
 
 }  // namespace rpd

@@ -87,6 +87,9 @@ struct PixelPlanes {
     int32_t* counts;
     int32_t* active_a;
     int32_t* active_b;
+    // scratch of the parallel allocation (k_allocate.cu)
+    uint8_t* alloc_state;
+    unsigned char* alloc_work;
 };
 
 struct NodePlanes {
@@ -113,6 +116,9 @@ struct Ctx {
     std::atomic<uint64_t> in_use{0};
     std::mutex mu;
     cudaStream_t util_stream = nullptr;
+    // every job's parallel allocation runs on this stream, one at a time: two cooperative
+    // launches that each hold part of the GPU must not wait on each other's blocks
+    cudaStream_t alloc_stream = nullptr;
     std::unordered_map<void*, uint64_t> user_allocs;  // rpd_device_alloc bookkeeping
 };
 
@@ -137,6 +143,8 @@ struct Job {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t band_copied[kMaxBands]{};
     cudaEvent_t staging_free = nullptr;
+    cudaEvent_t alloc_ready = nullptr;  // the job's stream reached the allocation
+    cudaEvent_t alloc_done = nullptr;   // the allocation stream finished it
     int64_t band_bytes = int64_t(96) << 20;  // target size of a band (RPD_TUNE_HOST_BAND_MB)
     float* lum = nullptr;        // per-sample luminance of the current push (fast grid pass)
     uint64_t lum_cap = 0;
@@ -149,6 +157,7 @@ struct Job {
     bool exact_window = false;   // RPD_EXACT_WINDOW: double-precision StatMC window
     int grid_shape = 6;          // launch shape of the random-dimension grid pass (row groups x dimension sets)
     int statmc_by = 0;           // StatMC tile height (0: the largest that fits)
+    bool serial_allocator = false;  // RPD_TUNE_ALLOCATOR = 1: the one-thread allocation kernel only
     bool pass_open = false;
     bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)
     bool features_valid = false;
@@ -290,6 +299,17 @@ cudaError_t launch_rpd_cache(Job& j);
 cudaError_t launch_statmc(Job& j);
 cudaError_t launch_variance(Job& j);
 cudaError_t launch_adaptive(Job& j);
+// The allocation alone, from the importance map already in j.p.importance.
+cudaError_t launch_allocate_map(Job& j);
+// The parallel allocation (k_allocate.cu): bytes of its scratch for np pixels, and the launch;
+// *fallback_flag gets the device flag telling the serial kernel to redo the allocation.
+uint64_t allocator_work_bytes(int64_t np);
+cudaError_t launch_allocate_parallel(Job& j, const float* importance, int extra_sample_total, int reserved_samples,
+                                     int max_extra, uint32_t seed, const int** fallback_flag);
+// The last parallel allocation's outcome (rpd_job_allocator_stats), after a stream sync.
+cudaError_t allocator_stats(Job& j, int32_t* out);
+// Device times (ns from the launch) of the last parallel allocation's barriers.
+int allocator_timeline(Job& j, uint64_t* ns, int32_t max, int32_t* n);
 cudaError_t launch_finalize(Job& j);
 cudaError_t launch_expand(Job& j, const float* node_field, float* out);
 cudaError_t launch_atrous(const float* raw, const float* normal, const float* albedo, int w, int h,
@@ -298,6 +318,14 @@ cudaError_t launch_atrous(const float* raw, const float* normal, const float* al
 cudaError_t launch_joint_bilateral(const float* raw, const float* normal, const float* albedo, int w, int h,
                                    float sigma_c, float sigma_n, float sigma_p, float sigma_a, float* gaussian,
                                    float* bilateral, float* joint, cudaStream_t stream, uint64_t* launches);
+
+// Pushes without host synchronisation (the serving loop, serve.cu). job_reserve sizes the
+// offsets for every pixel and the per-sample scratch for pushes of up to max_push_samples, so
+// that later pushes allocate nothing; push_device_async takes device planes and, with device
+// counts, a bound on the push's sample total instead of reading the total back.
+int job_reserve(Job& j, int64_t max_push_samples);
+int push_device_async(Job& j, const DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
+                      int64_t total_bound);
 
 inline unsigned grid_for(int64_t n, int block) {
     return static_cast<unsigned>((n + block - 1) / block);

@@ -137,6 +137,36 @@ class SynthParams(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    """rpd_server_config."""
+    _fields_ = [("knobs", Config), ("hbm_budget_bytes", C.c_uint64), ("max_inflight", C.c_int32),
+                ("storage", C.c_int32)]
+
+
+class Request(C.Structure):
+    """rpd_request."""
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("seed", C.c_uint32),
+                ("denoised_out", C.c_void_p), ("out_where", C.c_int32), ("tag", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    """rpd_completion."""
+    _fields_ = [("id", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("width", C.c_int32),
+                ("height", C.c_int32), ("spp", C.c_int32), ("samples", C.c_int64), ("submit_ms", C.c_double),
+                ("admit_ms", C.c_double), ("done_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    """rpd_server_stats."""
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("rejected", C.c_int64), ("queued", C.c_int64),
+                ("inflight", C.c_int64), ("bytes_reserved", C.c_uint64), ("bytes_peak", C.c_uint64),
+                ("bytes_budget", C.c_uint64), ("jobs_cached", C.c_int64), ("now_ms", C.c_double),
+                ("launches", C.c_int64)]
+
+
+STORAGE = {"fp32": 0, "fp16": 1}
+
+
 def synth_params(width: int, height: int, seed: int, **kw) -> SynthParams:
     """Defaults of the full-size synthetic workload (rpd_synth_defaults)."""
     p = SynthParams(width=width, height=height, seed=seed, regions=48, dependent_regions=24, mu_min=-2.0,
@@ -238,6 +268,9 @@ def lib() -> C.CDLL:
         "rpd_job_set_exact": (C.c_int, [vp, C.c_int]),
         "rpd_job_set_tuning": (C.c_int, [vp, C.c_int, C.c_int]),
         "rpd_job_get_tuning": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
+        "rpd_job_allocator_stats": (C.c_int, [vp, C.POINTER(C.c_int32)]),
+        "rpd_adaptive_allocate": (C.c_int, [vp, vp, C.c_int, vp, C.c_int]),
+        "rpd_job_allocator_timeline": (C.c_int, [vp, C.POINTER(C.c_uint64), i32, C.POINTER(i32)]),
         "rpd_job_begin_frame": (C.c_int, [vp]),
         "rpd_job_push_samples": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp, C.c_int]),
         "rpd_job_push_samples16": (C.c_int, [vp, C.POINTER(SampleSoA16), i64, i64, i32, vp, C.c_int]),
@@ -278,6 +311,14 @@ def lib() -> C.CDLL:
         "rpd_memcpy": (C.c_int, [vp, vp, vp, u64, C.c_int]),
         "rpd_synth_fill": (C.c_int, [vp, C.POINTER(SynthParams), i64, i64, i32, vp, vp, C.POINTER(SampleSoA),
                                      C.c_int]),
+        "rpd_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
+        "rpd_server_create": (C.c_int, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
+        "rpd_server_submit": (C.c_int, [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+        "rpd_server_poll": (C.c_int, [vp, C.POINTER(Completion), i32, C.POINTER(i32)]),
+        "rpd_server_drain": (C.c_int, [vp, i32]),
+        "rpd_server_cancel": (C.c_int, [vp, u64]),
+        "rpd_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStats)]),
+        "rpd_server_destroy": (None, [vp]),
         "rpd_last_error": (C.c_char_p, []),
         "rpd_status_string": (C.c_char_p, [C.c_int]),
     }
@@ -293,7 +334,9 @@ def exported_symbols() -> list[str]:
     """Names declared in include/rpd_gb300.h that the library must export."""
     return ["rpd_config_defaults", "rpd_config_validate", "rpd_ctx_create", "rpd_ctx_destroy", "rpd_job_footprint",
             "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config", "rpd_job_set_exact",
-            "rpd_job_set_tuning", "rpd_job_get_tuning",
+            "rpd_job_set_tuning", "rpd_job_get_tuning", "rpd_job_allocator_stats", "rpd_adaptive_allocate", "rpd_job_allocator_timeline",
+            "rpd_server_config_defaults", "rpd_server_create", "rpd_server_submit", "rpd_server_poll",
+            "rpd_server_drain", "rpd_server_cancel", "rpd_server_get_stats", "rpd_server_destroy",
             "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_push_samples16", "rpd_encode_samples16",
             "rpd_job_autotune", "rpd_batch_create", "rpd_batch_add", "rpd_batch_run", "rpd_batch_sync",
             "rpd_batch_last_ms", "rpd_batch_kernel_count", "rpd_batch_set_lanes", "rpd_batch_destroy", "rpd_job_end_pass", "rpd_recompute_sensitivity",
@@ -595,7 +638,7 @@ class Job:
     def set_exact(self, grid: bool = False, window: bool = False) -> None:
         check(lib().rpd_job_set_exact(self.handle, (1 if grid else 0) | (2 if window else 0)))
 
-    TUNING = {"grid_shape": 0, "host_band_mb": 1, "statmc_rows": 2}
+    TUNING = {"grid_shape": 0, "host_band_mb": 1, "statmc_rows": 2, "allocator": 3}
 
     def autotune(self, samples, spp: int) -> None:
         """rpd_job_autotune on device-resident planes (leaves the frame denoised)."""
@@ -609,6 +652,29 @@ class Job:
         v = C.c_int()
         check(lib().rpd_job_get_tuning(self.handle, self.TUNING[knob], C.byref(v)))
         return v.value
+
+    def adaptive_allocate(self, importance: np.ndarray) -> np.ndarray:
+        """rpd_adaptive_allocate on a host importance map; returns the counts."""
+        imp = np.ascontiguousarray(importance, dtype=np.float32).ravel()
+        out = np.empty(self.cfg.image_width * self.cfg.image_height, dtype=np.int32)
+        if imp.size != out.size:
+            raise ValueError("importance map size does not match the frame")
+        check(lib().rpd_adaptive_allocate(self.handle, imp.ctypes.data, MEM_HOST, out.ctypes.data, MEM_HOST))
+        return out
+
+    def allocator_timeline(self) -> list[float]:
+        """Microseconds from the last parallel allocation's launch to each of its barriers."""
+        buf = (C.c_uint64 * 96)()
+        n = C.c_int32()
+        check(lib().rpd_job_allocator_timeline(self.handle, buf, 96, C.byref(n)))
+        return [buf[i] / 1e3 for i in range(n.value)]
+
+    def allocator_stats(self) -> dict:
+        """Outcome of the last adaptive allocation (rpd_job_allocator_stats)."""
+        out = (C.c_int32 * 7)()
+        check(lib().rpd_job_allocator_stats(self.handle, out))
+        keys = ("parallel_done", "fallback", "timeout", "passes", "rounds", "exact_chunks", "reason")
+        return dict(zip(keys, (int(v) for v in out)))
 
     def begin_frame(self) -> None:
         check(lib().rpd_job_begin_frame(self.handle))
@@ -711,3 +777,130 @@ class Job:
             check(lib().rpd_job_kernel_time(self.handle, i, C.byref(ms), C.byref(n)))
             out[name] = (ms.value, n.value)
         return out
+
+
+class Server:
+    """rpd_server: the serving loop (continuous batching of denoise requests)."""
+
+    def __init__(self, ctx: Context, knobs: Config, budget_bytes: int = 0, max_inflight: int = 16,
+                 storage: str = "fp16"):
+        cfg = ServerConfig()
+        lib().rpd_server_config_defaults(C.byref(cfg))
+        cfg.knobs = knobs
+        cfg.hbm_budget_bytes = budget_bytes
+        cfg.max_inflight = max_inflight
+        cfg.storage = STORAGE[storage]
+        h = C.c_void_p()
+        check(lib().rpd_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+
+    def submit(self, width: int, height: int, spp: int, seed: int, out=None, tag: int = 0) -> int:
+        """Queue a request; `out` is a pinned host or device buffer of width*height*3 floats
+        (a DeviceBuffer, or an integer address of pinned memory), or None."""
+        r = Request()
+        r.width, r.height, r.spp, r.seed, r.tag = width, height, spp, seed & 0xFFFFFFFF, tag
+        if isinstance(out, DeviceBuffer):
+            r.denoised_out, r.out_where = out.ptr, MEM_DEVICE
+        elif out is not None:
+            r.denoised_out, r.out_where = int(out), MEM_HOST
+        rid = C.c_uint64()
+        check(lib().rpd_server_submit(self.handle, C.byref(r), C.byref(rid)))
+        return rid.value
+
+    def poll(self, max_n: int = 256) -> list[dict]:
+        buf = (Completion * max_n)()
+        n = C.c_int32()
+        check(lib().rpd_server_poll(self.handle, buf, max_n, C.byref(n)))
+        keys = [f for f, _ in Completion._fields_]
+        return [{k: getattr(buf[i], k) for k in keys} for i in range(n.value)]
+
+    def drain(self, timeout_ms: int = -1) -> None:
+        check(lib().rpd_server_drain(self.handle, timeout_ms))
+
+    def cancel(self, rid: int) -> None:
+        check(lib().rpd_server_cancel(self.handle, rid))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().rpd_server_get_stats(self.handle, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self) -> None:
+        if self.handle:
+            lib().rpd_server_destroy(self.handle)
+            self.handle = None
+
+
+
+# The planes the serving loop generates per sample (plus the per-pixel albedo).
+SERVED_PLANES = ("radiance", "normal", "depth", "pixel_albedo", "pixel_u", "lens_u", "brdf_u", "light_u", "flags",
+                 "category")
+
+
+def plain_request(ctx: Context, knobs: Config, width: int, height: int, spp: int, seed: int,
+                  job: "Job | None" = None) -> tuple[np.ndarray, int]:
+    """One synthetic request through the plain per-frame drop-in: render()'s call sequence
+    (path_tracer/main.cpp:1543-1564) on one job from the host, FP32 planes generated on the
+    device with the same ordinals the serving loop draws (first pass 0..spp-1, adaptive pass p
+    from p << 16), the adaptive counts read back to the host as compute_adaptive_sample_counts
+    returns them. Returns the denoised image (H, W, 3) and the samples denoised."""
+    cfg = knobs.replace(image_width=width, image_height=height)
+    n = width * height
+    passes = cfg.adaptive_passes if cfg.adaptive_spp > 0 else 0
+    own = job is None
+    if own:
+        job = Job(ctx, cfg)
+    dev = DeviceSamples(ctx, n * max(spp, cfg.adaptive_spp if passes else 0, 1), n, planes=SERVED_PLANES)
+    counts_dev = DeviceBuffer(ctx, n * 4)
+    start_dev = DeviceBuffer(ctx, n * 4)
+    try:
+        params = synth_params(width, height, seed)
+        samples = n * spp
+        ctx.synth_fill(params, 0, n, spp, dev)
+        job.begin_frame()
+        job.push(dev, 0, n, spp)
+        job.end_pass()
+        job.recompute_sensitivity()
+        for p in range(1, passes + 1):
+            job.statmc_denoise()
+            job.variance_denoise()
+            counts = job.compute_adaptive_sample_counts()
+            samples += int(counts.sum())
+            counts_dev.upload(counts)
+            start_dev.upload(np.full(n, p << 16, dtype=np.int32))
+            ctx.synth_fill(params, 0, n, 0, dev, counts=counts_dev, start_n=start_dev)
+            job.push(dev, 0, n, 0, counts=counts_dev)
+            job.end_pass()
+            job.recompute_sensitivity()
+        job.recompute_sensitivity()
+        job.statmc_denoise()
+        job.variance_denoise()
+        job.finalize()
+        return job.read("DENOISED"), samples
+    finally:
+        dev.free()
+        counts_dev.free()
+        start_dev.free()
+        if own:
+            job.close()
+
+
+class PinnedBuffer:
+    """Page-locked host memory (rpd_host_alloc) viewed as a numpy array."""
+
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        check(lib().rpd_host_alloc(int(nbytes), C.byref(p)))
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+
+    def array(self, dtype=np.float32, shape=None) -> np.ndarray:
+        n = self.nbytes // np.dtype(dtype).itemsize
+        buf = (C.c_char * self.nbytes).from_address(self.ptr)
+        a = np.frombuffer(buf, dtype=dtype, count=n)
+        return a.reshape(shape) if shape is not None else a
+
+    def free(self) -> None:
+        if self.ptr:
+            lib().rpd_host_free(self.ptr)
+            self.ptr = None
