@@ -592,10 +592,12 @@ def run_serving(args):
     value = world * samples / wall_s / 1e6
     srv.close()
 
-    # quality: served results against the plain FP32 drop-in on a few requests
-    rel = []
+    # quality on the stream's first small requests: the served result against the plain FP32
+    # drop-in on the same request, and both against the plain method at 1024 spp (converged)
+    def relmse(x, ref):
+        return float(np.mean((x - ref) ** 2 / (ref * ref + 1e-2)))
+    picks = [r for r in stream if r[1] * r[2] <= 640 * 360][:4]
     qsrv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=4, storage=args.storage)
-    picks = [stream[i] for i in range(min(4, n_req))]
     bufs = []
     for (_, w, h, spp, seed) in picks:
         b = R.PinnedBuffer(w * h * 12)
@@ -603,11 +605,16 @@ def run_serving(args):
         qsrv.submit(w, h, spp, seed, out=b.ptr, tag=seed)
     qsrv.drain(600000)
     qsrv.close()
+    q_plain, q_served_conv, q_plain_conv = [], [], []
     for (_, w, h, spp, seed), b in zip(picks, bufs):
-        img, _ = R.plain_request(ctx, knobs, w, h, spp, seed)
-        ref = img.astype(np.float64)
+        plain_img, _ = R.plain_request(ctx, knobs, w, h, spp, seed)
+        conv_img, _ = R.plain_request(ctx, knobs.replace(adaptive_passes=0), w, h, 1024, seed)
         x = b.array(np.float32, (h, w, 3)).astype(np.float64)
-        rel.append(float(np.mean((x - ref) ** 2 / (ref * ref + 1e-2))))
+        p_ = plain_img.astype(np.float64)
+        y = conv_img.astype(np.float64)
+        q_plain.append(relmse(x, p_))
+        q_served_conv.append(relmse(x, y))
+        q_plain_conv.append(relmse(p_, y))
         b.free()
 
     # the plain per-frame drop-in on a bounded prefix of the stream, one request after another
@@ -652,8 +659,14 @@ def run_serving(args):
                      "form": "render()'s call sequence per request from the host, FP32 planes generated on the "
                              "device, adaptive counts read back, one request after another"},
            "speedup_vs_plain": round(value / plain_value, 3),
-           "quality": {"reference": "the plain FP32 drop-in on the same requests", "rel_mse_eps": 1e-2,
-                       "rel_mse_mean": float(np.mean(rel)), "rel_mse_max": float(np.max(rel))},
+           "quality": {"requests": [list(r[1:4]) for r in picks], "rel_mse_eps": 1e-2,
+                       "vs_plain_fp32": {"mean": float(np.mean(q_plain)), "max": float(np.max(q_plain))},
+                       "served_vs_converged": float(np.mean(q_served_conv)),
+                       "plain_vs_converged": float(np.mean(q_plain_conv)),
+                       "note": "with adaptive passes the compact storage also moves the adaptive counts a "
+                               "little (the systematic residual sampling follows a running sum), so some "
+                               "pixels draw one sample more or less than in the FP32 run; converged = the "
+                               "plain FP32 method at 1024 spp"},
            "server": {"bytes_peak": st1["bytes_peak"], "bytes_budget": st1["bytes_budget"],
                       "jobs_cached": st1["jobs_cached"]},
            "gpu_launches": int(st1["launches"] - st0["launches"]), "clocks": clocks.summary()}

@@ -567,8 +567,9 @@ int rpd_job_set_tuning(rpd_job* job, int knob, int value) {
         return RPD_OK;
     }
     if (knob == RPD_TUNE_ALLOCATOR) {
-        if (value != 0 && value != 1) return fail(RPD_ERR_INVALID_ARGUMENT, "allocator must be 0 or 1");
+        if (value < 0 || value > 4096) return fail(RPD_ERR_INVALID_ARGUMENT, "allocator must be 0..4096");
         j->serial_allocator = value == 1;
+        j->allocator_blocks = value >= 2 ? value : 0;
         return RPD_OK;
     }
     return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
@@ -581,7 +582,7 @@ int rpd_job_get_tuning(rpd_job* job, int knob, int* value) {
     if (knob == RPD_TUNE_GRID_SHAPE) *value = j->grid_shape;
     else if (knob == RPD_TUNE_HOST_BAND_MB) *value = int(j->band_bytes >> 20);
     else if (knob == RPD_TUNE_STATMC_ROWS) *value = j->statmc_by;
-    else if (knob == RPD_TUNE_ALLOCATOR) *value = j->serial_allocator ? 1 : 0;
+    else if (knob == RPD_TUNE_ALLOCATOR) *value = j->serial_allocator ? 1 : j->allocator_blocks;
     else return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
     return RPD_OK;
 }
@@ -946,12 +947,15 @@ static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int
             RPD_CUDA(cudaMemcpyAsync(&nsamp, j->offsets + count, 8, cudaMemcpyDeviceToHost, j->stream));
             RPD_CUDA(cudaStreamSynchronize(j->stream));
         }
-        // luminance and key planes of the push, one allocation
+        // luminance, key (and, with per-pixel counts, column) planes of the push, one allocation
+        const int64_t ns64 = ((std::max<int64_t>(nsamp, 1) + 63) / 64) * 64;
+        const bool with_col = counts != nullptr && j->g.w <= 65535;
         void* lum = j->lum;
-        st = grow_device(*j, &lum, &j->lum_cap, uint64_t(std::max<int64_t>(nsamp, 1)) * 8 + 256);
+        st = grow_device(*j, &lum, &j->lum_cap, uint64_t(ns64) * (with_col ? 10 : 8) + 256);
         if (st != RPD_OK) return st;
         j->lum = static_cast<float*>(lum);
-        gp.key = reinterpret_cast<uint32_t*>(j->lum + ((std::max<int64_t>(nsamp, 1) + 63) / 64) * 64);
+        gp.key = reinterpret_cast<uint32_t*>(j->lum + ns64);
+        gp.col = with_col ? reinterpret_cast<uint16_t*>(gp.key + ns64) : nullptr;
         for (int c = 0; c < kClasses; ++c)
             for (int f = 0; f < 5; ++f) gp.cls[c][f] = j->cls[c][f];
         gp.pat4 = j->pat4;
@@ -1497,7 +1501,8 @@ int job_reserve(Job& j, int64_t max_push_samples) {
     if (st != RPD_OK) return st;
     if (j.cfg.rpf_shrinkage_scale > 0.0f && !j.exact_grid) {
         void* lum = j.lum;
-        st = grow_device(j, &lum, &j.lum_cap, uint64_t(std::max<int64_t>(max_push_samples, 1)) * 8 + 256);
+        const int64_t ns64 = ((std::max<int64_t>(max_push_samples, 1) + 63) / 64) * 64;
+        st = grow_device(j, &lum, &j.lum_cap, uint64_t(ns64) * 10 + 256);
         j.lum = static_cast<float*>(lum);
     }
     return st;

@@ -367,6 +367,7 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
                 if (prep) {
                     gp.lum[k] = lum;
                     gp.key[k] = key;
+                    if (gp.col) gp.col[k] = uint16_t(idx % gp.width);
                 }
             }
         }
@@ -440,6 +441,7 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
             if (prep) {
                 gp.lum[k] = lum;
                 gp.key[k] = key;
+                if (gp.col) gp.col[k] = uint16_t(idx % gp.width);
             }
         }
     }

@@ -52,17 +52,20 @@ namespace rpd {
 
 namespace {
 
-constexpr int kAT = 512;                // threads per block
+constexpr int kAT = 256;                // threads per block
 constexpr int kAV = 8;                  // consecutive pixels per thread
 constexpr int kAL = kAT * kAV;          // pixels per chunk
 constexpr int kAWarps = kAT / 32;
 constexpr int kTile = 128;              // chunk records staged in shared memory by the walk
 constexpr int kMaxOwned = 128;          // chunks per block
+constexpr int kDefaultBlocks = 1 << 20;  // blocks of the cooperative launch: one per SM unless capped
 constexpr int kMaxRounds = 64;          // fixed-point rounds per water-filling pass
 constexpr long long kTwo52 = 1ll << 52;
 constexpr long long kTwo53 = 1ll << 53;
+constexpr unsigned long long kSat = 1ull << 62;  // saturation of exact integer sums
 constexpr long long kBarrierCycles = 4000000000ll;  // about two seconds at the SM clock
 constexpr int kNoExp = INT_MIN;
+constexpr int kNoRegion = INT_MIN;  // a chain without an exact region
 constexpr int kStamps = 96;
 
 // The action of one addend (or a run of them) on S: for input parity p, S += step[p] and the
@@ -143,22 +146,74 @@ __device__ __forceinline__ EF ef_make(float x, int E, int sign) {
 __device__ __forceinline__ double pow2d(int k) {  // 2^k for -1022 <= k <= 1023
     return __longlong_as_double((long long)(k + 1023) << 52);
 }
+// The binade arithmetic works on the bits of the double, with no double-precision instruction
+// (GB300 issues those at 2 per SM per clock): a positive normal s = S * 2^(E-52) with S in
+// [2^52, 2^53) has exponent field E + 1023 and mantissa field S - 2^52.
 __device__ __forceinline__ int exponent_of(double s) {
     return int((__double_as_longlong(s) >> 52) & 0x7ff) - 1023;
 }
-// A value the binade arithmetic handles (positive, far from the ends of the double range).
+// A value the binade arithmetic handles: positive and normal, far from the ends of the range.
 __device__ __forceinline__ bool binade_ok(double s) {
-    if (!(s > 0.0)) return false;
-    const int e = exponent_of(s);
-    return e > -900 && e < 900;
+    const long long b = __double_as_longlong(s);
+    const int e = int((b >> 52) & 0x7ff) - 1023;  // the sign bit lands in bit 11 of the field
+    return b > 0 && e > -900 && e < 900;
 }
 __device__ __forceinline__ bool stays_in_binade(long long S, int sign) {
     // adding: every exact sum stays below 2^(E+1); subtracting: every exact difference stays
     // at or above 2^E (S >= 2^52 + 1 keeps the unrounded value above the binade's floor)
     return sign > 0 ? S < kTwo53 : S > kTwo52;
 }
-__device__ __forceinline__ long long scaled(double s, int E) { return (long long)(s * pow2d(52 - E)); }
-__device__ __forceinline__ double unscaled(long long S, int E) { return double(S) * pow2d(E - 52); }
+// S of s, for s in the binade of exponent E
+__device__ __forceinline__ long long scaled(double s, int) {
+    return (__double_as_longlong(s) & (kTwo52 - 1)) | kTwo52;
+}
+// the double S * 2^(E-52), for S in [2^52, 2^53)
+__device__ __forceinline__ double unscaled(long long S, int E) {
+    return __longlong_as_double((static_cast<long long>(E + 1023) << 52) | (S - kTwo52));
+}
+// float(s) rounded toward zero, from the bits (the clip test's screen only needs 2^-23)
+__device__ __forceinline__ float float_trunc(double s) {
+    const long long b = __double_as_longlong(s);
+    const int e = int((b >> 52) & 0x7ff) - 1023;
+    if (b <= 0 || e < -126 || e > 127) return float(s);
+    return __uint_as_float((unsigned(e + 127) << 23) | unsigned((b >> 29) & 0x7fffff));
+}
+
+// ---- the exact region of a sum from zero -------------------------------------------------------
+// While every partial sum of nonnegative floats from 0 stays below 2^(53-F), where 2^-F is the
+// smallest unit in last place among the addends, no addition rounds: every partial sum is an
+// integer multiple of 2^-F below 2^53 units, which a double holds exactly. There the chain value is
+// the exact sum, evaluated as a 64-bit integer count of 2^-F units in any order.
+__device__ __forceinline__ int float_exp(float x) {  // x = m * 2^e with the integer mantissa m
+    const unsigned eb = (__float_as_uint(x) >> 23) & 0xffu;
+    return eb ? int(eb) - 150 : -149;
+}
+// x * 2^F for x >= 0 (F >= -e for every addend), saturated at 2^62
+__device__ __forceinline__ unsigned long long int_units(float x, int F) {
+    const unsigned bits = __float_as_uint(x) & 0x7fffffffu;
+    if (bits == 0u) return 0ull;
+    const unsigned eb = bits >> 23;
+    const unsigned long long m = eb ? (unsigned long long)((bits & 0x7fffffu) | 0x800000u) : bits;
+    const int sh = float_exp(x) + F;
+    if (sh < 0 || sh > 38) return kSat;
+    return m << sh;
+}
+__device__ __forceinline__ unsigned long long sat_add(unsigned long long a, unsigned long long b) {
+    const unsigned long long t = a + b;  // both at most 2^62: no wrap
+    return t > kSat ? kSat : t;
+}
+// P * 2^-F for P < 2^53 (exact), from the bits
+__device__ __forceinline__ double units_to_double(unsigned long long P, int F) {
+    if (P == 0ull) return 0.0;
+    const int top = 63 - __clzll((long long)P);
+    const unsigned long long mant = (P << (52 - top)) & (unsigned long long)(kTwo52 - 1);
+    return __longlong_as_double(((long long)(top - F + 1023) << 52) | (long long)mant);
+}
+// F of a chain from the largest (1000 - e) the addends reported (0: no nonzero addend)
+__device__ __forceinline__ int region_f(int code) {
+    const int F = code - 1000;
+    return (code > 0 && F >= -900 && F <= 900) ? F : kNoRegion;
+}
 
 struct __align__(16) ChunkRec {
     long long i0[2];   // chunk action for the candidate exponents E[0], E[1]
@@ -168,13 +223,18 @@ struct __align__(16) ChunkRec {
     double approx;     // approximate sum of the chunk's addends (predictions only)
     int clips;         // clipped pixels of the chunk (water-filling chain)
     int len;           // pixels in the chunk
+    unsigned long long isum;  // exact sum of the chunk's addends in units of 2^-F (saturated)
     // written by the walk
     double start;      // exact chain value before the chunk
-    int mode;          // 0/1: walked with candidate mode; 2: walked exactly, values in the pool
+    int mode;          // 0/1: walked with candidate mode; 2: walked exactly, values in the pool;
+                       // 3: inside the exact region
     int slot;          // pool slot of an exactly walked chunk
     int nb;            // clipped pixels before the chunk
     int pad;
+    unsigned long long pstart;  // units before the chunk (mode 3)
 };
+
+static_assert(sizeof(ChunkRec) % 16 == 0, "the walk copies records as 16-byte words");
 
 struct AllocScalars {
     unsigned bar_count;
@@ -191,6 +251,7 @@ struct AllocScalars {
     int done;                    // the parallel allocation finished
     int reason;                  // why it handed over: 1 input, 2 pool, 3 rounds, 4 barrier, 5 no launch
     int n_stamps;
+    int region_code[2];          // largest 1000 - e over the nonzero importances (0) and residuals (1)
     int pad;
     unsigned long long stamps[kStamps];  // %globaltimer (ns) at the start and after each barrier
 };
@@ -329,6 +390,30 @@ __device__ double block_sum_d(double v, Shared& sh) {
     return t;
 }
 
+__device__ float block_sum_f(float v, Shared& sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+    if (lane == 0) sh.warp_i[warp] = __float_as_int(v);
+    __syncthreads();
+    float t = 0.0f;
+    for (int w = 0; w < kAWarps; ++w) t += __int_as_float(sh.warp_i[w]);
+    __syncthreads();
+    return t;
+}
+
+__device__ int block_max_i(int v, Shared& sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, d));
+    if (lane == 0) sh.warp_i[warp] = v;
+    __syncthreads();
+    int t = INT_MIN;
+    for (int w = 0; w < kAWarps; ++w) t = max(t, sh.warp_i[w]);
+    __syncthreads();
+    return t;
+}
+
 __device__ long long block_sum_l(long long v, Shared& sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -359,6 +444,23 @@ __device__ int block_scan_i(int v, int* total, Shared& sh) {
     }
     __syncthreads();
     *total = all;
+    return before + inc - v;
+}
+
+// Exclusive scan of an unsigned 64-bit value over threads (values small enough not to wrap).
+__device__ unsigned long long block_scan_u64(unsigned long long v, Shared& sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long inc = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long o = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += o;
+    }
+    if (lane == 31) sh.warp_l[warp] = (long long)inc;
+    __syncthreads();
+    unsigned long long before = 0;
+    for (int w = 0; w < warp; ++w) before += (unsigned long long)sh.warp_l[w];
+    __syncthreads();
     return before + inc - v;
 }
 
@@ -435,13 +537,31 @@ struct Src {
 
 // Chunk actions for up to two candidate exponents; writes them to the record.
 __device__ void chunk_actions(const float (&x)[kAV], int E0, int E1, int sign, ChunkRec* r, Shared& sh) {
+    if (E1 == kNoExp) {  // one candidate: one scan
+        EF tf[1], ex[1], tot[1];
+        tf[0] = ef_identity();
+        if (E0 != kNoExp)
+#pragma unroll
+            for (int e = 0; e < kAV; ++e) tf[0] = ef_compose(tf[0], ef_make(x[e], E0, sign));
+        block_scan_ef<1>(tf, ex, tot, sh);
+        if (threadIdx.x == 0) {
+            r->i0[0] = tot[0].i0;
+            r->i1[0] = tot[0].i1;
+            r->o[0] = E0 == kNoExp ? 6u : tot[0].o;
+            r->E[0] = E0;
+            r->i0[1] = r->i1[1] = 0;
+            r->o[1] = 6u;
+            r->E[1] = kNoExp;
+        }
+        return;
+    }
     EF tf[2], ex[2], tot[2];
     tf[0] = ef_identity();
     tf[1] = ef_identity();
 #pragma unroll
     for (int e = 0; e < kAV; ++e) {
         if (E0 != kNoExp) tf[0] = ef_compose(tf[0], ef_make(x[e], E0, sign));
-        if (E1 != kNoExp) tf[1] = ef_compose(tf[1], ef_make(x[e], E1, sign));
+        tf[1] = ef_compose(tf[1], ef_make(x[e], E1, sign));
     }
     block_scan_ef<2>(tf, ex, tot, sh);
     if (threadIdx.x == 0) {
@@ -456,13 +576,27 @@ __device__ void chunk_actions(const float (&x)[kAV], int E0, int E1, int sign, C
 }
 
 // The exact chain values (inclusive) of this thread's pixels in chunk c after the walk, and
-// the value before the thread's first pixel.
-__device__ void chain_values(const CoopArgs& a, int c, const float (&x)[kAV], int sign, double (&v)[kAV],
+// the value before the thread's first pixel. F is the chain's exact-region unit (kNoRegion: none).
+__device__ void chain_values(const CoopArgs& a, int c, const float (&x)[kAV], int sign, int F, double (&v)[kAV],
                              double* before, Shared& sh) {
     const int mode = __ldcg(&a.rec[c].mode);
     const double start = __ldcg(&a.rec[c].start);
     const int base = threadIdx.x * kAV;
-    if (mode < 2) {
+    if (mode == 3) {
+        unsigned long long u[kAV], t = 0;
+#pragma unroll
+        for (int e = 0; e < kAV; ++e) {
+            u[e] = int_units(x[e], F);
+            t += u[e];
+        }
+        unsigned long long P = __ldcg(&a.rec[c].pstart) + block_scan_u64(t, sh);
+        *before = units_to_double(P, F);
+#pragma unroll
+        for (int e = 0; e < kAV; ++e) {
+            P += u[e];
+            v[e] = units_to_double(P, F);
+        }
+    } else if (mode < 2) {
         const int E = __ldcg(&a.rec[c].E[mode]);
         EF tf[1], ex[1], tot[1];
         EF f[kAV];
@@ -595,9 +729,12 @@ __device__ double walk_exact(const CoopArgs& a, const Src& src, int c, double s,
 
 // Walks every chunk in order from s0. Block 0 only; writes start/mode/slot/nb of each chunk
 // and the final value and clip count to the scalars.
-__device__ void walk(const CoopArgs& a, const Src& src, double s0, int sign, bool keep_values, Shared& sh) {
+__device__ void walk(const CoopArgs& a, const Src& src, double s0, int sign, bool keep_values, int F, Shared& sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double s = s0;
+    // the exact region of a sum from zero (warp 0's state only)
+    bool region = F != kNoRegion && sign > 0 && s0 == 0.0;
+    unsigned long long P = 0;
     int clips = 0;
     int pool_used = 0;
     int exact = 0;
@@ -615,31 +752,89 @@ __device__ void walk(const CoopArgs& a, const Src& src, double s0, int sign, boo
         int c = 0;
         while (c < tn) {
             if (warp == 0) {
+                // 32 chunks per step: every lane takes the next chunk, the lanes' chunk maps are
+                // composed by a warp scan, and the chunks before the first one that does not fit
+                // (a missed binade, a crossing) are committed together
                 while (c < tn) {
-                    const ChunkRec& r = sh.tile[c];
-                    bool fast = false;
-                    if (binade_ok(s)) {
-                        const int E = exponent_of(s);
-                        const int q = (r.E[0] == E && !(r.o[0] & 4u)) ? 0 : ((r.E[1] == E && !(r.o[1] & 4u)) ? 1 : -1);
-                        if (q >= 0) {
-                            const long long S = scaled(s, E);
-                            const long long Se = S + ((S & 1) ? r.i1[q] : r.i0[q]);
-                            if (stays_in_binade(Se, sign)) {
-                                fast = true;
-                                if (lane == 0) {
-                                    ChunkRec* g = a.rec + t0 + c;
-                                    g->start = s;
-                                    g->mode = q;
-                                    g->slot = -1;
-                                    g->nb = clips;
-                                }
-                                s = unscaled(Se, E);
-                                clips += r.clips;
-                            }
-                        }
+                    const int cl = c + lane;
+                    const bool have = cl < tn;
+                    const ChunkRec* r = &sh.tile[have ? cl : c];
+                    int cinc = have ? r->clips : 0;  // inclusive clip count over the lanes
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const int o = __shfl_up_sync(0xffffffffu, cinc, d);
+                        if (lane >= d) cinc += o;
                     }
-                    if (!fast) break;
-                    ++c;
+                    const int cexc = cinc - (have ? r->clips : 0);
+                    int k;
+                    if (region) {
+                        unsigned long long u = have ? r->isum : kSat;
+#pragma unroll
+                        for (int d = 1; d < 32; d <<= 1) {
+                            const unsigned long long o = __shfl_up_sync(0xffffffffu, u, d);
+                            if (lane >= d) u = sat_add(u, o);
+                        }
+                        const unsigned long long uexc = sat_add(u, 0) - (have && r->isum < kSat ? r->isum : 0);
+                        const bool fits = have && u < kSat && P + u < (unsigned long long)kTwo53;
+                        const unsigned bad = __ballot_sync(0xffffffffu, !fits);
+                        k = bad ? __ffs(bad) - 1 : 32;
+                        if (lane < k) {
+                            ChunkRec* g = a.rec + t0 + cl;
+                            g->start = units_to_double(P + uexc, F);
+                            g->mode = 3;
+                            g->slot = -1;
+                            g->nb = clips + cexc;
+                            g->pstart = P + uexc;
+                        }
+                        if (k > 0) {
+                            P += __shfl_sync(0xffffffffu, u, k - 1);
+                            s = units_to_double(P, F);
+                            clips += __shfl_sync(0xffffffffu, cinc, k - 1);
+                            c += k;
+                        }
+                        // a chunk that does not fit ends the region (not the end of the tile); s holds
+                        // the exact sum so far and the binade walk goes on from it
+                        if (k < 32 && c < tn) region = false;
+                        continue;
+                    } else {
+                        if (!binade_ok(s)) break;
+                        const int E = exponent_of(s);
+                        const long long S = scaled(s, E);
+                        const unsigned p0 = unsigned(S & 1);
+                        int q = -1;
+                        if (have) q = (r->E[0] == E && !(r->o[0] & 4u)) ? 0 : ((r->E[1] == E && !(r->o[1] & 4u)) ? 1 : -1);
+                        EF f;
+                        if (q >= 0) {
+                            f.i0 = r->i0[q];
+                            f.i1 = r->i1[q];
+                            f.o = r->o[q];
+                        } else {
+                            f.i0 = f.i1 = 0;
+                            f.o = 6u;
+                        }
+#pragma unroll
+                        for (int d = 1; d < 32; d <<= 1) {
+                            const EF o = shfl_up_ef(f, d);
+                            if (lane >= d) f = ef_compose(o, f);
+                        }
+                        const long long Se = S + (p0 ? f.i1 : f.i0);
+                        const bool ok = have && !(f.o & 4u) && stays_in_binade(Se, sign);
+                        const unsigned bad = __ballot_sync(0xffffffffu, !ok);
+                        k = bad ? __ffs(bad) - 1 : 32;
+                        long long Sx = __shfl_up_sync(0xffffffffu, Se, 1);
+                        if (lane == 0) Sx = S;
+                        if (lane < k) {
+                            ChunkRec* g = a.rec + t0 + cl;
+                            g->start = unscaled(Sx, E);
+                            g->mode = q;
+                            g->slot = -1;
+                            g->nb = clips + cexc;
+                        }
+                        if (k > 0) s = unscaled(__shfl_sync(0xffffffffu, Se, k - 1), E);
+                    }
+                    if (k > 0) clips += __shfl_sync(0xffffffffu, cinc, k - 1);
+                    c += k;
+                    if (k == 0) break;  // chunk c is walked exactly
                 }
                 if (lane == 0) {
                     sh.bcast_d = s;
@@ -691,7 +886,23 @@ __device__ void walk(const CoopArgs& a, const Src& src, double s0, int sign, boo
 // Approximate prefix of the chunks' addend sums from s0 for this block's chunks, then the chunk
 // actions for the predicted binade (and the neighbouring one when the prediction is close to a
 // binade edge).
-__device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, double s0, int sign, Shared& sh) {
+// Saturating sum of unsigned values over the block (at most 2^62 each).
+__device__ unsigned long long block_sum_sat(unsigned long long v, Shared& sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = sat_add(v, __shfl_down_sync(0xffffffffu, v, d));
+    if (lane == 0) sh.warp_l[warp] = (long long)v;
+    __syncthreads();
+    unsigned long long t = 0;
+    for (int w = 0; w < kAWarps; ++w) t = sat_add(t, (unsigned long long)sh.warp_l[w]);
+    __syncthreads();
+    return t;
+}
+
+// ... and, for a sum from zero with an exact region (F != kNoRegion), each chunk's exact sum in
+// units of 2^-F; chunks predicted to end well inside the region get no binade actions (the walk
+// takes them whole).
+__device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, double s0, int sign, int F, Shared& sh) {
     const int G = gridDim.x;
     double carry = s0;
     for (int t0 = 0; t0 < a.nch; t0 += kAT) {
@@ -720,8 +931,28 @@ __device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, doubl
         carry = sign > 0 ? carry + all : carry - all;
     }
     __syncthreads();
+    const bool region = F != kNoRegion && sign > 0 && s0 == 0.0;
+    const double region_end = region && 53 - F > -1000 && 53 - F < 1000 ? pow2d(53 - F) * (1.0 - 1.0 / 1048576.0) : 0.0;
     for (int c = blockIdx.x; c < a.nch; c += G) {
         const double pred = sh.own_pred[c / G];
+        float x[kAV];
+        src.load(a, int64_t(c) * kAL + threadIdx.x * kAV, x);
+        if (region) {
+            unsigned long long u = 0;
+#pragma unroll
+            for (int e = 0; e < kAV; ++e) u = sat_add(u, int_units(x[e], F));
+            const unsigned long long t = block_sum_sat(u, sh);
+            if (threadIdx.x == 0) a.rec[c].isum = t;
+            if (pred + __ldcg(&a.rec[c].approx) < region_end) {
+                if (threadIdx.x == 0) {  // the walk takes this chunk whole from the exact sum
+                    a.rec[c].o[0] = a.rec[c].o[1] = 6u;
+                    a.rec[c].E[0] = a.rec[c].E[1] = kNoExp;
+                }
+                continue;
+            }
+        } else if (threadIdx.x == 0) {
+            a.rec[c].isum = kSat;
+        }
         int E0 = kNoExp, E1 = kNoExp;
         if (binade_ok(pred)) {
             E0 = exponent_of(pred);
@@ -729,17 +960,28 @@ __device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, doubl
             if (mant < 1.0 + 1.0 / 1024.0) E1 = E0 - 1;
             else if (mant > 2.0 - 1.0 / 1024.0) E1 = E0 + 1;
         }
-        float x[kAV];
-        src.load(a, int64_t(c) * kAL + threadIdx.x * kAV, x);
         chunk_actions(x, E0, E1, sign, a.rec + c, sh);
     }
+}
+
+// float(double(I) / R * double(Rs)) (main.cpp:1405-1406) with the quotient taken through the
+// reciprocal of R, computed once: the two agree to a few double ulps, so wherever the product is not
+// within 64 double ulps of a midpoint between two floats both round to the same float; otherwise the
+// reference's division decides.
+__device__ __forceinline__ float share_of(float I, double R, double rcp, double Rsd) {
+    const double t = (double(I) * rcp) * Rsd;
+    const long long b = __double_as_longlong(t);
+    const long long low = b & ((1ll << 29) - 1);  // the bits below a float's mantissa
+    const int e = int((b >> 52) & 0x7ff) - 1023;
+    if (b > 0 && e > -120 && e < 120 && llabs(low - (1ll << 28)) > 64) return __double2float_rn(t);
+    return float(double(I) / R * Rsd);
 }
 
 // remaining_importance clip test of the water-filling loop (main.cpp:1391-1393), with a
 // single-precision screen that leaves every undecided case to the reference's expression.
 __device__ __forceinline__ bool clip_test(float I, double R, int Rs, int m) {
     if (Rs > 0 && R > 1e-30 && R < 1e30) {
-        const float r = float(Rs) / float(R);
+        const float r = float(Rs) / float_trunc(R);
         const float d = I * r;
         const float fm = float(m);
         if (d > fm * 1.0001f) return true;
@@ -761,21 +1003,21 @@ __device__ void phase_decide_start(const CoopArgs& a, double R, int Rs, int fb, 
         load_f8(a.importance, k0, a.np, I);
         load_u8(a.state, k0, a.np, st);
         int n = 0;
-        double acc = 0.0;
+        float acc = 0.0f;
 #pragma unroll
         for (int e = 0; e < kAV; ++e) {
             const bool clip = (st[e] & 1u) && clip_test(I[e], R, Rs, a.max_extra);
             st[e] = uint8_t((st[e] & ~fbit) | (clip ? fbit : 0u));
-            if (clip) acc += double(I[e]);
+            if (clip) acc += I[e];
             n += clip;
         }
         store_u8(a.state, k0, a.np, st);
         int total;
         block_scan_i(n, &total, sh);
-        const double t = block_sum_d(acc, sh);
+        const float t = block_sum_f(acc, sh);
         if (threadIdx.x == 0) {
             a.rec[c].clips = total;
-            a.rec[c].approx = t;
+            a.rec[c].approx = double(t);
         }
     }
 }
@@ -801,7 +1043,7 @@ __device__ void phase_decide_round(const CoopArgs& a, double R0, int Rs0, int fb
         int total;
         const int nb_thread = block_scan_i(n, &total, sh);
         double v[kAV], before;
-        chain_values(a, c, x, -1, v, &before, sh);
+        chain_values(a, c, x, -1, kNoRegion, v, &before, sh);
         const int nb_chunk = __ldcg(&a.rec[c].nb);
         const double start = __ldcg(&a.rec[c].start);
         __syncthreads();  // the record is rewritten below
@@ -823,8 +1065,12 @@ __device__ void phase_decide_round(const CoopArgs& a, double R0, int Rs0, int fb
         store_u8(a.state, k0, a.np, st);
         int total_new;
         block_scan_i(n_new, &total_new, sh);
-        const int E0 = binade_ok(start) ? exponent_of(start) : (binade_ok(R0) ? exponent_of(R0) : kNoExp);
-        chunk_actions(x, E0, E0 == kNoExp ? kNoExp : E0 - 1, -1, a.rec + c, sh);
+        const double ref = binade_ok(start) ? start : R0;
+        const int E0 = binade_ok(ref) ? exponent_of(ref) : kNoExp;
+        // the clip set grows by little between rounds: the start stays in its binade unless it
+        // sits just above the binade's floor
+        const bool low = E0 != kNoExp && ((__double_as_longlong(ref) & (kTwo52 - 1)) >> 42) == 0;
+        chunk_actions(x, E0, low ? E0 - 1 : kNoExp, -1, a.rec + c, sh);
         if (threadIdx.x == 0) a.rec[c].clips = total_new;
     }
     const long long ch = block_sum_l((long long)changed, sh);
@@ -848,23 +1094,25 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
     // importance checks, desired_add = 0, every pixel alive, approximate chunk sums
     {
         int bad = 0;
+        int code = 0;  // largest 1000 - e over the nonzero importances (the exact region's unit)
         for (int c = blockIdx.x; c < a.nch; c += G) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
             float I[kAV];
             load_f8(a.importance, k0, a.np, I);
-            double acc = 0.0;
+            float acc = 0.0f;
             uint8_t st[kAV];
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
                 if (!(I[e] >= 0.0f && I[e] <= FLT_MAX)) bad = 1;
-                acc += double(I[e]);
+                if (I[e] > 0.0f) code = max(code, 1000 - float_exp(I[e]));
+                acc += I[e];
                 st[e] = 1u;
                 if (k0 + e < a.np) a.desired_add[k0 + e] = 0.0f;
             }
             store_u8(a.state, k0, a.np, st);
-            const double t = block_sum_d(acc, sh);
+            const float t = block_sum_f(acc, sh);
             if (threadIdx.x == 0) {
-                a.rec[c].approx = t;
+                a.rec[c].approx = double(t);
                 a.rec[c].len = int(min((long long)kAL, (long long)(a.np - int64_t(c) * kAL)));
                 a.rec[c].clips = 0;
             }
@@ -873,14 +1121,17 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
             atomicExch(&sc->reason, 1);
             atomicExch(&sc->fallback, 1);
         }
+        code = block_max_i(code, sh);
+        if (threadIdx.x == 0 && code > 0) atomicMax(&sc->region_code[0], code);
     }
     if (!grid_sync(sc) || fell_back(sc)) return;
+    const int F_imp = region_f(__ldcg(&sc->region_code[0]));
 
     // sum_importance (main.cpp:1370)
     const Src imp{0, 0u};
-    phase_predicted_actions(a, imp, 0.0, 1, sh);
+    phase_predicted_actions(a, imp, 0.0, 1, F_imp, sh);
     if (!grid_sync(sc)) return;
-    if (blockIdx.x == 0) walk(a, imp, 0.0, 1, false, sh);
+    if (blockIdx.x == 0) walk(a, imp, 0.0, 1, false, F_imp, sh);
     if (!grid_sync(sc) || fell_back(sc)) return;
     const double sum_importance = __ldcg(&sc->walk_final);
     const int remaining_samples0 = max(0, a.extra_sample_total - a.reserved_samples);
@@ -904,9 +1155,9 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
         }
         phase_decide_start(a, R, Rs, fb, sh);
         if (!grid_sync(sc)) return;
-        phase_predicted_actions(a, Src{1, 2u << fb}, R, -1, sh);
+        phase_predicted_actions(a, Src{1, 2u << fb}, R, -1, kNoRegion, sh);
         if (!grid_sync(sc)) return;
-        if (blockIdx.x == 0) walk(a, Src{1, 2u << fb}, R, -1, true, sh);
+        if (blockIdx.x == 0) walk(a, Src{1, 2u << fb}, R, -1, true, kNoRegion, sh);
         if (!grid_sync(sc) || fell_back(sc)) return;
         for (int round = 0;; ++round) {
             phase_decide_round(a, R, Rs, fb, sh);
@@ -923,7 +1174,7 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
                 }
                 return;
             }
-            if (blockIdx.x == 0) walk(a, Src{1, 2u << fb}, R, -1, true, sh);
+            if (blockIdx.x == 0) walk(a, Src{1, 2u << fb}, R, -1, true, kNoRegion, sh);
             if (!grid_sync(sc) || fell_back(sc)) return;
         }
         const int nc = __ldcg(&sc->walk_clips);
@@ -931,6 +1182,8 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
         const unsigned fbit = 2u << fb;
         if (nc == 0) {
             // no pixel clipped: the rest share the remaining samples (main.cpp:1403-1408)
+            const double rcp = 1.0 / R;
+            const double Rsd = double(Rs);
             for (int c = blockIdx.x; c < a.nch; c += G) {
                 const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
                 float I[kAV];
@@ -940,7 +1193,7 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
 #pragma unroll
                 for (int e = 0; e < kAV; ++e)
                     if ((st[e] & 1u) && k0 + e < a.np)
-                        a.desired_add[k0 + e] = float(double(I[e]) / R * double(Rs));
+                        a.desired_add[k0 + e] = share_of(I[e], R, rcp, Rsd);
             }
             break;
         }
@@ -966,9 +1219,10 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
     // floors and residual weights (main.cpp:1411-1420), approximate chunk sums of the weights
     {
         long long assigned = 0;
+        int code = 0;
         for (int c = blockIdx.x; c < a.nch; c += G) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
-            double acc = 0.0;
+            float acc = 0.0f;
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
                 if (k0 + e >= a.np) continue;
@@ -978,27 +1232,31 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
                 assigned += add;
                 const float r = fmaxs(0.0f, d - float(add));
                 a.residual[k0 + e] = r;
-                acc += double(r);
+                if (r > 0.0f) code = max(code, 1000 - float_exp(r));
+                acc += r;
             }
-            const double t = block_sum_d(acc, sh);
+            const float t = block_sum_f(acc, sh);
             if (threadIdx.x == 0) {
-                a.rec[c].approx = t;
+                a.rec[c].approx = double(t);
                 a.rec[c].clips = 0;
             }
         }
         const long long tot = block_sum_l(assigned, sh);
         if (threadIdx.x == 0 && tot) atomicAdd(reinterpret_cast<unsigned long long*>(&sc->assigned),
                                                (unsigned long long)tot);
+        code = block_max_i(code, sh);
+        if (threadIdx.x == 0 && code > 0) atomicMax(&sc->region_code[1], code);
     }
     if (!grid_sync(sc)) return;
+    const int F_res = region_f(__ldcg(&sc->region_code[1]));
     const int assigned = int(__ldcg(&sc->assigned));
     const int remaining = max(0, a.extra_sample_total - a.reserved_samples - assigned);
 
     // the cumulative chain of the residual weights (main.cpp:1417-1437)
     const Src res{2, 0u};
-    phase_predicted_actions(a, res, 0.0, 1, sh);
+    phase_predicted_actions(a, res, 0.0, 1, F_res, sh);
     if (!grid_sync(sc)) return;
-    if (blockIdx.x == 0) walk(a, res, 0.0, 1, true, sh);
+    if (blockIdx.x == 0) walk(a, res, 0.0, 1, true, F_res, sh);
     if (!grid_sync(sc) || fell_back(sc)) return;
     const double residual_sum = __ldcg(&sc->walk_final);
     if (remaining > 0 && residual_sum > double(1e-8f)) {
@@ -1021,21 +1279,22 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
             if (est < c - tol) return false;
             return (kk / rem_d) * residual_sum > c;
         };
-        // N(c): the number of targets t_k <= c, k < remaining
+        // N(c): the number of targets t_k <= c, k < remaining; from the estimate c / step - offset,
+        // stepped to the exact boundary t_{k-1} <= c < t_k
+        const double per_unit = rem_d / residual_sum;
         auto first_above = [&](double c) -> long long {
-            long long lo = 0, hi = remaining;  // answer in [lo, hi]
-            while (lo < hi) {
-                const long long mid = (lo + hi) >> 1;
-                if (above(mid, c)) hi = mid; else lo = mid + 1;
-            }
-            return lo;
+            const double e = c * per_unit - offset;
+            long long k = e <= 0.0 ? 0 : (e >= rem_d ? remaining : (long long)e);
+            while (k > 0 && above(k - 1, c)) --k;
+            while (k < remaining && !above(k, c)) ++k;
+            return k;
         };
         for (int c = blockIdx.x; c < a.nch; c += G) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
             float x[kAV];
             load_f8(a.residual, k0, a.np, x);
             double v[kAV], before;
-            chain_values(a, c, x, 1, v, &before, sh);
+            chain_values(a, c, x, 1, F_res, v, &before, sh);
             long long n_prev = k0 == 0 ? 0 : first_above(before);
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
@@ -1110,8 +1369,12 @@ cudaError_t launch_allocate_parallel(Job& j, const float* importance, int extra_
         }
         shape = g_coop_shape;
     }
+    // one block per SM (256 threads: a block leaves room on its SM for other kernels), or the cap
+    // of RPD_TUNE_ALLOCATOR; more when the frame has more chunks than the blocks can own
     const int resident = shape.sms * std::max(shape.per_sm, 0);
-    const int G = std::min(nch, std::min(resident, shape.sms));
+    int want = j.allocator_blocks >= 2 ? j.allocator_blocks : kDefaultBlocks;
+    want = std::max(want, int((int64_t(nch) + kMaxOwned - 1) / kMaxOwned));
+    const int G = std::min(nch, std::min(std::min(resident, shape.sms), want));
     if (G < 1 || int64_t(nch) > int64_t(kMaxOwned) * G) {
         // no cooperative launch possible here: leave it to the serial kernel
         e = cudaMemsetAsync(&sc->fallback, 1, sizeof(int), as);

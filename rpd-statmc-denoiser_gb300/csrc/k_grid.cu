@@ -680,6 +680,7 @@ struct WalkCtx {
     RowTable* rt;
     const float* xf;
     int lane;
+    int xlo;          // image column of xf[0]
     float wscale;
 };
 
@@ -795,6 +796,11 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
             const int64_t k = rt->k0[r] + kk;
             key = gp.key[k];
             y = gp.lum[k];
+            if (gp.col) {  // per-pixel counts: the statistics pass stored each sample's column
+                const int ci = int(gp.col[k]) - c.xlo;
+                w = unsigned(ci) < unsigned(rp.cols) ? c.xf[ci] * rt->ay[r] : 0.0f;
+                return;
+            }
             int pl;
             if (rp.spp_shift >= 0) {
                 pl = kk >> rp.spp_shift;
@@ -882,6 +888,7 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
     }
     const int xlo = imaxs(0, (nx - 1) * g.step - 1), xhi = imins(g.w - 1, (nx + 1) * g.step + 1);
     const int ylo = imaxs(0, (ny - 1) * g.step - 1), yhi = imins(g.h - 1, (ny + 1) * g.step + 1);
+    c.xlo = xlo;
     for (int col = threadIdx.x; col < rp.cols; col += NW * 32)
         xf[col] = (xlo + col <= xhi) ? axis_factor(gpar, xlo + col, nx, g.nodes_x) : 0.0f;
     for (int k = 0; k < L::kSlots; ++k) {

@@ -474,13 +474,15 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
             acc_lo[k] += err;
         }
     }
-    const double cs0 = double(acc_hi[0]) + double(acc_lo[0]);
-    const double cs1 = double(acc_hi[1]) + double(acc_lo[1]);
-    const double cs2 = double(acc_hi[2]) + double(acc_lo[2]);
-    const double weight_sum = double(acc_hi[3]) + double(acc_lo[3]);
-    const double weight_square_sum = double(acc_hi[4]) + double(acc_lo[4]);
-    const double weighted_variance_sum = double(acc_hi[5]) + double(acc_lo[5]);
-    if (accepted >= 2 && fabs(weight_sum - 1.1) <= 1.1 * kWsBand) {
+    // the blend in single precision from the double-float sums (their relative error, ~1e-7,
+    // is far inside the plain-form bar; the weight_sum >= 1.1 test keeps its guard band)
+    const float cs0 = acc_hi[0] + acc_lo[0];
+    const float cs1 = acc_hi[1] + acc_lo[1];
+    const float cs2 = acc_hi[2] + acc_lo[2];
+    const float weight_sum = acc_hi[3] + acc_lo[3];
+    const float weight_square_sum = acc_hi[4] + acc_lo[4];
+    const float weighted_variance_sum = acc_hi[5] + acc_lo[5];
+    if (accepted >= 2 && fabsf(weight_sum - 1.1f) <= 1.1f * float(kWsBand)) {
         exact_pixel(p, prm, idx);
         return;
     }
@@ -488,21 +490,21 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
     const float4 cmi4 = T[P_CM * tn + ei];
     const float cmi[3] = {cmi4.x, cmi4.y, cmi4.z};
     float mean_nb[3] = {cmi[0], cmi[1], cmi[2]};
-    double var_neighbors = double(var_mean_i);
-    if (weight_sum > double(1e-8f)) {
-        mean_nb[0] = float(cs0 / weight_sum);
-        mean_nb[1] = float(cs1 / weight_sum);
-        mean_nb[2] = float(cs2 / weight_sum);
-        var_neighbors = weighted_variance_sum / (weight_sum * weight_sum);
+    float var_neighbors = var_mean_i;
+    if (weight_sum > 1e-8f) {
+        const float inv = 1.0f / weight_sum;
+        mean_nb[0] = cs0 * inv;
+        mean_nb[1] = cs1 * inv;
+        mean_nb[2] = cs2 * inv;
+        var_neighbors = weighted_variance_sum * inv * inv;
     }
-    const double effective = weight_sum * weight_sum / dmaxs(double(1e-8f), weight_square_sum);
-    const double blend = (accepted >= 2 && weight_sum >= 1.1) ? dclamps(1.0 - 1.0 / sqrt(effective), 0.0, 0.8) : 0.0;
-    const float alpha = float(1.0 - blend);
-    const float fb = float(blend);
-    for (int c = 0; c < 3; ++c) p.denoised[c][idx] = lerpf(cmi[c], mean_nb[c], fb);
-    const float uncertainty = float(double(alpha) * double(alpha) * double(var_mean_i) + blend * blend * var_neighbors +
-                                    2.0 * double(alpha) * blend * (1.0 / dmaxs(weight_sum, double(1e-8f))) *
-                                        double(var_mean_i));
+    const float effective = weight_sum * weight_sum / fmaxf(1e-8f, weight_square_sum);
+    const float blend = (accepted >= 2 && weight_sum >= 1.1f) ? fminf(fmaxf(1.0f - rsqrtf(effective), 0.0f), 0.8f)
+                                                               : 0.0f;
+    const float alpha = 1.0f - blend;
+    for (int c = 0; c < 3; ++c) p.denoised[c][idx] = lerpf(cmi[c], mean_nb[c], blend);
+    const float uncertainty = alpha * alpha * var_mean_i + blend * blend * var_neighbors +
+                              2.0f * alpha * blend * (1.0f / fmaxf(weight_sum, 1e-8f)) * var_mean_i;
     p.alpha[idx] = alpha;
     p.uncertainty[idx] = uncertainty;
 }

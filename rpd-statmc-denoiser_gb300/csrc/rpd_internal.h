@@ -158,6 +158,7 @@ struct Job {
     int grid_shape = 6;          // launch shape of the random-dimension grid pass (row groups x dimension sets)
     int statmc_by = 0;           // StatMC tile height (0: the largest that fits)
     bool serial_allocator = false;  // RPD_TUNE_ALLOCATOR = 1: the one-thread allocation kernel only
+    int allocator_blocks = 0;       // RPD_TUNE_ALLOCATOR >= 2: blocks of the parallel allocation
     bool pass_open = false;
     bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)
     bool features_valid = false;
@@ -267,6 +268,8 @@ struct GridPrep {
     float2* pat2;             // W*H
     float* lum;               // per sample of the push (NaN when the radiance is not finite)
     uint32_t* key;            // per sample of the push: packed random-dimension bins + validity
+    uint16_t* col;            // per sample of a push with per-pixel counts: the pixel's column
+                              // (null for uniform pushes, where the column follows from the index)
     int width;
 };
 // Sample key: bits 0-3 lens bin, 4-7 brdf bin, 8-11 light_uv bin, 12-15 environment bin,

@@ -8,17 +8,18 @@
 // Per request the pipeline is the reference's render() (path_tracer/main.cpp:1543-1564) with
 // the tracer replaced by the seeded per-sample generator (include/rpd_synth.h) evaluated on the
 // device:
-//   first pass        spp samples per pixel, pushed, merged, recompute_sensitivity
-//                     (render_image_statmc, main.cpp:649-737)
-//   adaptive passes   statmc_denoise, variance_denoise, compute_adaptive_sample_counts, the
-//                     extra samples generated from the counts on the device, pushed, merged,
-//                     recompute_sensitivity (main.cpp:1547-1552, 1451-1538)
-//   final             statmc_denoise, variance_denoise, finalize (main.cpp:1554-1559); the
-//                     second recompute_sensitivity of main.cpp:1554 is skipped: nothing changed
-//                     since the last one, so it would recompute the same values
-// and the denoised image is copied to host memory. Nothing in it waits on the host: the counts,
-// their offsets and the extra samples stay in HBM, a push with device counts sizes its scratch
-// from the bound adaptive_spp * W * H, and every buffer comes from a stream-ordered pool.
+//   first pass        spp samples per pixel, pushed, merged (render_image_statmc,
+//                     main.cpp:649-737)
+//   adaptive passes   variance_denoise, compute_adaptive_sample_counts, the extra samples
+//                     generated from the counts on the device, pushed, merged (main.cpp:1547-1552,
+//                     1451-1538)
+//   final             recompute_sensitivity, statmc_denoise, variance_denoise, finalize
+//                     (main.cpp:1554-1559)
+// and the denoised image is copied to host memory. The adaptive passes' statmc_denoise and
+// recompute_sensitivity calls are dead work (see enqueue_request) and are not run. Nothing in
+// the pipeline waits on the host: the counts, their offsets and the extra samples stay in HBM,
+// a push with device counts sizes its scratch from the bound adaptive_spp * W * H, and every
+// buffer comes from a stream-ordered pool.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -279,7 +280,7 @@ rpd_config request_config(const Server& s, const rpd_request& r) {
 uint64_t job_bytes(const rpd_config& c, int64_t span_samples) {
     // the arena plus the offsets (8 B per pixel) and the per-sample scratch of the largest push
     const int64_t np = int64_t(c.image_width) * c.image_height;
-    return rpd_job_footprint(&c) + uint64_t(np + np / 512 + 64) * 9 + uint64_t(span_samples) * 9 + 512;
+    return rpd_job_footprint(&c) + uint64_t(np + np / 512 + 64) * 9 + uint64_t(span_samples + 64) * 12 + 512;
 }
 
 int64_t span_samples(const rpd_config& c, int32_t spp) {
@@ -413,11 +414,17 @@ int enqueue_request(Server& s, Request& r) {
         }
     }
     SRV_TRY(rpd_job_end_pass(jh));
-    SRV_TRY(rpd_recompute_sensitivity(jh));
+    // render() runs statmc_denoise and recompute_sensitivity in every adaptive pass
+    // (main.cpp:1547-1552) and again after the loop (1554-1556). Before that final
+    // statmc_denoise nothing reads what they write: variance_denoise and
+    // compute_adaptive_sample_counts read the per-pixel statistics, the feature cache and the hit
+    // counts only (main.cpp:1166-1446), recompute_sensitivity starts over from the grid on every
+    // call (741-953), and the final statmc_denoise overwrites every plane the earlier ones wrote.
+    // So the loop runs them once, after the last pass, and the result is the same bits (the
+    // tests compare it with the full sequence).
     int64_t* totals = s.slots[size_t(r.slot)].totals;
     const int passes = c.adaptive_spp > 0 ? std::max(0, c.adaptive_passes) : 0;
     for (int p = 1; p <= passes; ++p) {
-        SRV_TRY(rpd_statmc_denoise(jh));
         SRV_TRY(rpd_variance_denoise(jh));
         SRV_TRY(rpd_compute_adaptive_sample_counts(jh, nullptr, RPD_MEM_DEVICE));
         RPD_CUDA(launch_offsets_scan(j, j.p.counts, np));
@@ -427,8 +434,8 @@ int enqueue_request(Server& s, Request& r) {
         j.launches += 1;
         SRV_TRY(push_device_async(j, push_planes(0), 0, np, 0, j.p.counts, int64_t(c.adaptive_spp) * np));
         SRV_TRY(rpd_job_end_pass(jh));
-        SRV_TRY(rpd_recompute_sensitivity(jh));
     }
+    SRV_TRY(rpd_recompute_sensitivity(jh));
     SRV_TRY(rpd_statmc_denoise(jh));
     SRV_TRY(rpd_variance_denoise(jh));
     SRV_TRY(rpd_finalize(jh));
@@ -599,6 +606,23 @@ void worker_loop(Server* sp) {
             progress = true;
         }
         if (s.stop && s.queue.empty() && s.running.empty() && s.admitting == 0) break;
+        if (!progress) {
+            // a stream that stopped on a device error never reaches its completion callback:
+            // fail its request instead of waiting for it
+            for (size_t i = 0; i < s.running.size();) {
+                Request* r = s.running[i];
+                const cudaError_t e = r->gpu_done.load() ? cudaSuccess : cudaStreamQuery(r->job->stream);
+                if (e != cudaSuccess && e != cudaErrorNotReady) {
+                    r->status = cuda_fail(e, "request stream");
+                    s.fatal = rpd_last_error();
+                    s.running.erase(s.running.begin() + long(i));
+                    retire(s, r);
+                    progress = true;
+                } else {
+                    ++i;
+                }
+            }
+        }
         if (!progress) s.cv.wait_for(lk, std::chrono::microseconds(200));
     }
 }
@@ -733,6 +757,7 @@ int rpd_server_drain(rpd_server* srv, int32_t timeout_ms) {
             return fail(RPD_ERR_TIMEOUT, "requests still queued or running");
         s->cv.wait_for(lk, std::chrono::milliseconds(1));
     }
+    if (!s->fatal.empty()) return fail(RPD_ERR_CUDA, s->fatal);
     return RPD_OK;
 }
 

@@ -153,3 +153,20 @@ def test_pipeline_counts_match_the_oracle_with_both_allocators(gpu_ctx):
             np.testing.assert_array_equal(job.compute_adaptive_sample_counts(), want)
         finally:
             job.close()
+
+
+@pytest.mark.parametrize("blocks", [2, 7, 152])
+@pytest.mark.parametrize("w,h,kind", [(300, 200, "ties"), (1000, 700, "fireflies"), (640, 360, "binades")])
+def test_allocation_does_not_depend_on_the_launch_shape(gpu_ctx, blocks, w, h, kind):
+    rng = np.random.default_rng(blocks * 1000 + w)
+    imp = importance_map(kind, w * h, rng)
+    cfg = small_config(w, h, adaptive_spp=4, adaptive_base_samples=1, seed=blocks)
+    job = R.Job(gpu_ctx, cfg)
+    try:
+        job.set_tuning("allocator", blocks)
+        got = job.adaptive_allocate(imp)
+        st = job.allocator_stats()
+        assert st["parallel_done"] == 1 and st["fallback"] == 0, st
+        np.testing.assert_array_equal(got, B.port_allocate(imp, cfg))
+    finally:
+        job.close()

@@ -74,12 +74,21 @@ def test_compact_adaptive_pass(gpu_ctx):
     ex = R.DeviceSamples(gpu_ctx, extra_n, w * h)
     gpu_ctx.synth_fill(p, 0, w * h, 0, ex, counts=cb, start_n=np.full(w * h, spp, np.int32))
     ex16 = R.DeviceSamples16.encode(gpu_ctx, ex)
+    # the same extra samples into both jobs: compact planes with per-pixel counts (b) against FP32
+    # planes with the same counts (a)
+    counts_dev = R.DeviceBuffer(gpu_ctx, cb.nbytes)
+    counts_dev.upload(cb)
+    a.push(ex, 0, w * h, 0, counts=counts_dev)
     b.push(ex16, 0, w * h, 0, counts=cb)
-    b.end_pass()
-    b.recompute_sensitivity()
-    b.statmc_denoise()
+    for j in (a, b):
+        j.end_pass()
+        j.recompute_sensitivity()
+        j.statmc_denoise()
     assert np.all(np.isfinite(b.read("DENOISED")))
     assert int(b.read("SAMPLE_COUNT").sum()) == w * h * spp + extra_n
+    assert_bitwise(a.read("SAMPLE_COUNT"), b.read("SAMPLE_COUNT"), "SAMPLE_COUNT")
+    assert rel_mse(b.read("DENOISED"), a.read("DENOISED")) <= REL_MSE_BAR
+    counts_dev.free()
     for j in (a, b):
         j.close()
     for d in (dev, dev16, ex, ex16):
