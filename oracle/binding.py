@@ -77,6 +77,64 @@ def port() -> C.CDLL:
     return L
 
 
+_port64 = None
+PORT64_LIB = HERE / "_build" / "librpd_oracle64.so"
+
+
+def port64() -> C.CDLL:
+    """The double-precision form of the restatement (oracle/rpd_oracle64.c)."""
+    global _port64
+    if _port64 is not None:
+        return _port64
+    if not PORT64_LIB.exists():
+        build_port()
+    L = C.CDLL(str(PORT64_LIB))
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    sig = {
+        "orc_job_create": (vp, [C.POINTER(R.Config)]),
+        "orc_job_destroy": (None, [vp]),
+        "orc_set_threads": (None, [vp, C.c_int]),
+        "orc_job_begin_frame": (C.c_int, [vp]),
+        "orc_job_push_samples": (C.c_int, [vp, C.POINTER(R.SampleSoA), i64, i64, i32, vp]),
+        "orc_job_end_pass": (C.c_int, [vp]),
+        "orc_recompute_sensitivity": (C.c_int, [vp]),
+        "orc_statmc_denoise": (C.c_int, [vp]),
+        "orc_variance_denoise": (C.c_int, [vp]),
+        "orc_finalize": (C.c_int, [vp]),
+        "orc64_read": (C.c_int, [vp, C.c_int, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _port64 = L
+    return L
+
+
+def fp64_denoise(cfg: R.Config, samples: "R.HostSamples", spp: int, threads: int = 0) -> np.ndarray:
+    """The plain method (accumulate, sensitivity, StatMC, variance) on one frame in the
+    double-precision restatement; returns DENOISED (H, W, 3) as float."""
+    L = port64()
+    h = L.orc_job_create(C.byref(cfg))
+    if not h:
+        raise ValueError("invalid config")
+    try:
+        L.orc_set_threads(h, threads)
+        L.orc_job_begin_frame(h)
+        soa = samples.soa()
+        n = cfg.image_width * cfg.image_height
+        assert L.orc_job_push_samples(h, C.byref(soa), 0, n, spp, None) == 0
+        L.orc_job_end_pass(h)
+        L.orc_recompute_sensitivity(h)
+        L.orc_statmc_denoise(h)
+        L.orc_variance_denoise(h)
+        out = np.empty((cfg.image_height, cfg.image_width, 3), dtype=np.float32)
+        assert L.orc64_read(h, R.FIELD["DENOISED"], out.ctypes.data) == 0
+        return out
+    finally:
+        L.orc_job_destroy(h)
+
+
 def have_ref() -> bool:
     return REF_LIB.exists()
 

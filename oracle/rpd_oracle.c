@@ -260,26 +260,26 @@ orc_job* orc_job_create(const rpd_config* cfg) {
     j->stats = (pstats*)zalloc(np * sizeof(pstats));
     j->hit_count = (int32_t*)zalloc(np * 4);
     j->sample_count = (int32_t*)zalloc(np * 4);
-    j->radiance = (float*)zalloc(np * 12);
-    j->normal = (float*)zalloc(np * 12);
-    j->albedo = (float*)zalloc(np * 12);
-    j->depth = (float*)zalloc(np * 4);
+    j->radiance = (float*)zalloc(np * 3 * sizeof(float));
+    j->normal = (float*)zalloc(np * 3 * sizeof(float));
+    j->albedo = (float*)zalloc(np * 3 * sizeof(float));
+    j->depth = (float*)zalloc(np * sizeof(float));
     j->grid = (double*)zalloc(nn * NDEP * DSTRIDE * sizeof(double));
-    for (int f = 0; f < N_FIELDS; ++f) j->node[f] = (float*)zalloc(nn * 4);
-    j->sens_confidence = (float*)zalloc(np * 4);
-    j->sens_gradient = (float*)zalloc(np * 4);
-    j->f_normal = (float*)zalloc(np * 12);
-    j->f_depth = (float*)zalloc(np * 4);
-    j->f_albedo = (float*)zalloc(np * 12);
-    for (int f = 0; f < C_FIELDS; ++f) j->cache[f] = (float*)zalloc(np * 4);
-    j->denoised = (float*)zalloc(np * 12);
-    j->uncertainty = (float*)zalloc(np * 4);
-    j->alpha = (float*)zalloc(np * 4);
-    j->var_total = (float*)zalloc(np * 4);
-    j->var_eff = (float*)zalloc(np * 4);
-    j->var_ratio = (float*)zalloc(np * 4);
-    j->variance_denoised = (float*)zalloc(np * 4);
-    j->adaptive_importance = (float*)zalloc(np * 4);
+    for (int f = 0; f < N_FIELDS; ++f) j->node[f] = (float*)zalloc(nn * sizeof(float));
+    j->sens_confidence = (float*)zalloc(np * sizeof(float));
+    j->sens_gradient = (float*)zalloc(np * sizeof(float));
+    j->f_normal = (float*)zalloc(np * 3 * sizeof(float));
+    j->f_depth = (float*)zalloc(np * sizeof(float));
+    j->f_albedo = (float*)zalloc(np * 3 * sizeof(float));
+    for (int f = 0; f < C_FIELDS; ++f) j->cache[f] = (float*)zalloc(np * sizeof(float));
+    j->denoised = (float*)zalloc(np * 3 * sizeof(float));
+    j->uncertainty = (float*)zalloc(np * sizeof(float));
+    j->alpha = (float*)zalloc(np * sizeof(float));
+    j->var_total = (float*)zalloc(np * sizeof(float));
+    j->var_eff = (float*)zalloc(np * sizeof(float));
+    j->var_ratio = (float*)zalloc(np * sizeof(float));
+    j->variance_denoised = (float*)zalloc(np * sizeof(float));
+    j->adaptive_importance = (float*)zalloc(np * sizeof(float));
     j->last_counts = (int32_t*)zalloc(np * 4);
     return j;
 }
@@ -322,22 +322,22 @@ int orc_job_begin_frame(orc_job* j) {
     memset(j->stats, 0, np * sizeof(pstats));
     memset(j->hit_count, 0, np * 4);
     memset(j->sample_count, 0, np * 4);
-    memset(j->radiance, 0, np * 12);
-    memset(j->normal, 0, np * 12);
-    memset(j->albedo, 0, np * 12);
-    memset(j->depth, 0, np * 4);
+    memset(j->radiance, 0, np * 3 * sizeof(float));
+    memset(j->normal, 0, np * 3 * sizeof(float));
+    memset(j->albedo, 0, np * 3 * sizeof(float));
+    memset(j->depth, 0, np * sizeof(float));
     memset(j->grid, 0, nn * NDEP * DSTRIDE * sizeof(double));
-    for (int f = 0; f < N_FIELDS; ++f) memset(j->node[f], 0, nn * 4);
-    memset(j->sens_confidence, 0, np * 4);
-    memset(j->sens_gradient, 0, np * 4);
-    memset(j->uncertainty, 0, np * 4);
-    memset(j->alpha, 0, np * 4);
-    memset(j->var_total, 0, np * 4);
-    memset(j->var_eff, 0, np * 4);
-    memset(j->var_ratio, 0, np * 4);
-    memset(j->variance_denoised, 0, np * 4);
-    memset(j->adaptive_importance, 0, np * 4);
-    memset(j->denoised, 0, np * 12);
+    for (int f = 0; f < N_FIELDS; ++f) memset(j->node[f], 0, nn * sizeof(float));
+    memset(j->sens_confidence, 0, np * sizeof(float));
+    memset(j->sens_gradient, 0, np * sizeof(float));
+    memset(j->uncertainty, 0, np * sizeof(float));
+    memset(j->alpha, 0, np * sizeof(float));
+    memset(j->var_total, 0, np * sizeof(float));
+    memset(j->var_eff, 0, np * sizeof(float));
+    memset(j->var_ratio, 0, np * sizeof(float));
+    memset(j->variance_denoised, 0, np * sizeof(float));
+    memset(j->adaptive_importance, 0, np * sizeof(float));
+    memset(j->denoised, 0, np * 3 * sizeof(float));
     free_pass_grids(j);
     j->features_valid = 0;
     j->cache_valid = 0;
@@ -635,7 +635,7 @@ static void expand_values(const orc_job* j, const float* tiles, float* out) {
 static void ensure_sensitivity_cache(orc_job* j) {
     if (j->cache_valid) return;
     for (int f = 0; f < C_GRADIENT; ++f) expand_values(j, j->node[cache_from_node[f]], j->cache[f]);
-    memcpy(j->cache[C_GRADIENT], j->sens_gradient, j->np * 4);
+    memcpy(j->cache[C_GRADIENT], j->sens_gradient, j->np * sizeof(float));
     j->cache_valid = 1;
 }
 
@@ -718,8 +718,8 @@ int orc_recompute_sensitivity(orc_job* j) {
     const int64_t nn = (int64_t)j->nn, np = (int64_t)j->np;
     j->cache_valid = 0;
     if (j->cfg.rpf_shrinkage_scale <= 0.0f) {
-        memset(j->sens_confidence, 0, j->np * 4);
-        memset(j->sens_gradient, 0, j->np * 4);
+        memset(j->sens_confidence, 0, j->np * sizeof(float));
+        memset(j->sens_gradient, 0, j->np * sizeof(float));
         ensure_sensitivity_cache(j);
         j->stage_ms[RPD_STAGE_SENSITIVITY] = now_ms() - t0;
         return RPD_OK;
@@ -729,13 +729,13 @@ int orc_recompute_sensitivity(orc_job* j) {
     float* conf[R_FIELDS];
     float* prior[R_FIELDS];
     for (int f = 0; f < R_FIELDS; ++f) {
-        raw[f] = (float*)zalloc((size_t)nn * 4);
-        conf[f] = (float*)zalloc((size_t)nn * 4);
-        prior[f] = (float*)zalloc((size_t)nn * 4);
+        raw[f] = (float*)zalloc((size_t)nn * sizeof(float));
+        conf[f] = (float*)zalloc((size_t)nn * sizeof(float));
+        prior[f] = (float*)zalloc((size_t)nn * sizeof(float));
     }
-    float* nnorm = (float*)zalloc((size_t)nn * 12);
-    float* ndepth = (float*)zalloc((size_t)nn * 4);
-    float* nalb = (float*)zalloc((size_t)nn * 12);
+    float* nnorm = (float*)zalloc((size_t)nn * 3 * sizeof(float));
+    float* ndepth = (float*)zalloc((size_t)nn * sizeof(float));
+    float* nalb = (float*)zalloc((size_t)nn * 3 * sizeof(float));
     const double n0d = (double)j->cfg.rpf_confidence_samples;
 
     /* main.cpp:773-815 */
@@ -842,7 +842,7 @@ int orc_recompute_sensitivity(orc_job* j) {
     }
 
     /* main.cpp:930-947 */
-    float* expanded = (float*)zalloc((size_t)np * 4);
+    float* expanded = (float*)zalloc((size_t)np * sizeof(float));
     expand_values(j, T[N_ALL], expanded);
     expand_values(j, T[N_ALL_CONF], j->sens_confidence);
 #ifdef _OPENMP
@@ -931,8 +931,8 @@ int orc_statmc_denoise(orc_job* j) {
     const int64_t np = (int64_t)j->np;
     ensure_feature_cache(j);
     ensure_sensitivity_cache(j);
-    float* svm = (float*)zalloc((size_t)np * 12);  /* sqrt_variance_mean */
-    float* svs = (float*)zalloc((size_t)np * 12);  /* sqrt_variance_stable */
+    float* svm = (float*)zalloc((size_t)np * 3 * sizeof(float));  /* sqrt_variance_mean */
+    float* svs = (float*)zalloc((size_t)np * 3 * sizeof(float));  /* sqrt_variance_stable */
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -1087,8 +1087,8 @@ int orc_variance_denoise(orc_job* j) {
     const int iterations = j->cfg.var_iterations;
     const float max_variance = j->cfg.adaptive_sigma_max * j->cfg.adaptive_sigma_max;
     const int64_t np = (int64_t)j->np;
-    float* curr = (float*)zalloc((size_t)np * 4);
-    float* next = (float*)zalloc((size_t)np * 4);
+    float* curr = (float*)zalloc((size_t)np * sizeof(float));
+    float* next = (float*)zalloc((size_t)np * sizeof(float));
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -1152,6 +1152,7 @@ int orc_variance_denoise(orc_job* j) {
 }
 
 /* ---- compute_adaptive_sample_counts (main.cpp:1273-1446) ------------------------------ */
+#ifndef ORC_F64
 
 /* The budget-preserving allocation of compute_adaptive_sample_counts (main.cpp:1372-1438) on a
  * final importance map: counts holds the floor per pixel on entry and the counts on return.
@@ -1167,7 +1168,7 @@ void orc_allocate_counts(const float* importance, int64_t np, const rpd_config* 
         if (sum_importance <= 0.0 || remaining_samples <= 0) {
             return;
         }
-        float* desired_add = (float*)zalloc((size_t)np * 4);
+        float* desired_add = (float*)zalloc((size_t)np * sizeof(float));
         int32_t* active = (int32_t*)malloc((size_t)np * 4);
         int32_t* next_active = (int32_t*)malloc((size_t)np * 4);
         int64_t n_active = np;
@@ -1201,7 +1202,7 @@ void orc_allocate_counts(const float* importance, int64_t np, const rpd_config* 
             n_active = n_next;
         }
         int assigned = 0;
-        float* residual = (float*)zalloc((size_t)np * 4);
+        float* residual = (float*)zalloc((size_t)np * sizeof(float));
         double residual_sum = 0.0;
         for (int64_t i = 0; i < np; ++i) {
             const int add = (int)floorf(desired_add[i]);
@@ -1250,9 +1251,9 @@ int orc_compute_adaptive_sample_counts(orc_job* j, int32_t* counts_out) {
     {
         const float SIGMA_MAX = j->cfg.adaptive_sigma_max;
         ensure_feature_cache(j);
-        float* importance = (float*)zalloc((size_t)np * 4);
-        float* vs = (float*)zalloc((size_t)np * 4);
-        memcpy(vs, j->variance_denoised, (size_t)np * 4);
+        float* importance = (float*)zalloc((size_t)np * sizeof(float));
+        float* vs = (float*)zalloc((size_t)np * sizeof(float));
+        memcpy(vs, j->variance_denoised, (size_t)np * sizeof(float));
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -1273,7 +1274,7 @@ int orc_compute_adaptive_sample_counts(orc_job* j, int32_t* counts_out) {
 
         const int radius = j->cfg.adaptive_importance_smoothing_radius;
         if (radius > 0) {
-            float* smoothed = (float*)zalloc((size_t)np * 4);
+            float* smoothed = (float*)zalloc((size_t)np * sizeof(float));
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -1305,7 +1306,7 @@ int orc_compute_adaptive_sample_counts(orc_job* j, int32_t* counts_out) {
             sum_importance = 0.0;
             for (int64_t i = 0; i < np; ++i) sum_importance = sum_importance + (double)importance[i];
         }
-        memcpy(j->adaptive_importance, importance, (size_t)np * 4);
+        memcpy(j->adaptive_importance, importance, (size_t)np * sizeof(float));
 
         orc_allocate_counts(importance, np, &j->cfg, sum_importance, sc);
         free(importance); free(vs);
@@ -1315,6 +1316,8 @@ done:
     j->stage_ms[RPD_STAGE_ADAPTIVE] = now_ms() - t0;
     return RPD_OK;
 }
+
+#endif /* ORC_F64 */
 
 /* ---- FrameBuffers::finalize (core/buffers.h:152-167) --------------------------------- */
 
@@ -1359,6 +1362,7 @@ static int put(void* dst, size_t bytes, const void* src, uint64_t need) {
     return RPD_OK;
 }
 
+#ifndef ORC_F64
 int orc_job_read(orc_job* j, int field, void* dst, size_t bytes) {
     const uint64_t need = orc_field_bytes(j, field);
     const int64_t np = (int64_t)j->np;
@@ -1410,6 +1414,8 @@ int orc_job_read(orc_job* j, int field, void* dst, size_t bytes) {
     return RPD_ERR_INVALID_ARGUMENT;
 }
 
+#endif /* ORC_F64 */
+
 double orc_stage_ms(const orc_job* j, int stage) {
     return (stage >= 0 && stage < RPD_STAGE_COUNT_) ? j->stage_ms[stage] : -1.0;
 }
@@ -1420,6 +1426,7 @@ int orc_nodes(const orc_job* j, int32_t* nodes_x, int32_t* nodes_y) {
     return RPD_OK;
 }
 
+#ifndef ORC_F64
 /* ---- standalone filters ------------------------------------------------------------- */
 
 /* normalize + luminance helpers (denoising/atrous_wavelet.cpp:37-52) */
@@ -1583,3 +1590,4 @@ int orc_joint_bilateral(const float* raw, const float* normal, const float* albe
     }
     return RPD_OK;
 }
+#endif /* ORC_F64 */

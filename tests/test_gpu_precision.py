@@ -109,3 +109,30 @@ def test_compact_rejects_exact_grid(gpu_ctx):
     job.close()
     dev.free()
     dev16.free()
+
+
+@pytest.mark.parametrize("w,h,spp", [(256, 256, 4), (320, 180, 16)])
+def test_forms_against_the_fp64_oracle(gpu_ctx, w, h, spp):
+    """The plain FP32 path and the compact form against the double-precision restatement
+    (oracle/rpd_oracle64.c): relMSE with epsilon 1e-2."""
+    from conftest import B
+
+    cfg = small_config(w, h)
+    p = R.synth_params(w, h, 1234)
+    host = B.synth_fill(p, 0, w * h, spp, threads=8)
+    ref = B.fp64_denoise(cfg, host, spp, threads=8)
+    dev = R.DeviceSamples.from_host(gpu_ctx, host)
+    dev16 = R.DeviceSamples16.encode(gpu_ctx, dev)
+    a, b = R.Job(gpu_ctx, cfg), R.Job(gpu_ctx, cfg)
+    try:
+        run(a, dev, w, h, spp)
+        run(b, dev16, w, h, spp)
+        e32 = rel_mse(a.read("DENOISED"), ref)
+        e16 = rel_mse(b.read("DENOISED"), ref)
+        assert e32 <= 1e-6, e32
+        assert e16 <= REL_MSE_BAR, e16
+    finally:
+        a.close()
+        b.close()
+        dev.free()
+        dev16.free()

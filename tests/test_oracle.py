@@ -216,3 +216,25 @@ def test_port_filters_match_live_reference():
     for x, y in zip(B.port_joint_bilateral(raw, normal, albedo, 0.4, 0.3, 1.0, 0.2),
                     B.ref_joint_bilateral(raw, normal, albedo, 0.4, 0.3, 1.0, 0.2)):
         assert_bitwise(x, y, "joint")
+
+
+def test_fp64_restatement_stays_close_to_the_float_one():
+    """oracle/rpd_oracle64.c (the stage's single-precision quantities in double) against the
+    float restatement on a synthetic frame: the same method, so the two agree to rounding."""
+    w, h, spp = 64, 48, 8
+    cfg = R.default_config(image_width=w, image_height=h, rpf_tile_size=16, color_window_radius=5,
+                           var_window_radius=3, var_iterations=2, seed=1234)
+    s = B.synth_fill(R.synth_params(w, h, 77), 0, w * h, spp, threads=2)
+    d64 = B.fp64_denoise(cfg, s, spp, threads=2).astype(np.float64)
+    j = B.OracleJob(cfg, threads=2)
+    j.begin_frame()
+    j.push(s, 0, w * h, spp)
+    j.end_pass()
+    j.recompute_sensitivity()
+    j.statmc_denoise()
+    j.variance_denoise()
+    d32 = j.read("DENOISED").astype(np.float64)
+    j.close()
+    assert np.all(np.isfinite(d64))
+    assert float(np.mean((d32 - d64) ** 2 / (d64 ** 2 + 1e-2))) <= 1e-9
+
