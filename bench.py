@@ -675,6 +675,20 @@ def run_serving(args):
         print(json.dumps(out))
 
 
+def run_request(args):
+    """One request of the serving workload through the plain drop-in sequence at --width x
+    --height x --spp with --passes adaptive passes (a small case for profiling captures); prints
+    the samples it denoised."""
+    import rpd_gb300 as R
+
+    ctx = R.Context(0, 0)
+    knobs = serving_knobs(R).replace(adaptive_passes=args.passes)
+    _, samples = R.plain_request(ctx, knobs, args.width, args.height, args.spp, SEED)
+    ctx.close()
+    print(json.dumps({"form": "request", "width": args.width, "height": args.height, "spp": args.spp,
+                      "adaptive_passes": args.passes, "samples": samples}))
+
+
 def run_reference(args):
     world, rank, _, dist = dist_setup()
     if rank != 0:
@@ -707,7 +721,7 @@ def main():
     ap.add_argument("--grid-shape", type=int, default=0, help="random-dimension grid launch shape 1..6 (0: default)")
     ap.add_argument("--precision", choices=["fp32", "fp16"], default="fp32",
                     help="fp16: the precision form (compact per-sample storage, single-precision accumulation)")
-    ap.add_argument("--form", choices=["plain", "batched", "serving"], default="plain",
+    ap.add_argument("--form", choices=["plain", "batched", "serving", "request"], default="plain",
                     help="batched: uneven frames in one graph-captured launch (fp16 storage, autotuned shapes); "
                          "serving: a Poisson stream of requests through rpd_server (--steps requests)")
     ap.add_argument("--frames", type=int, default=48, help="frames of the batched form")
@@ -717,6 +731,7 @@ def main():
     ap.add_argument("--inflight", type=int, default=32, help="serving: requests on the GPU at once")
     ap.add_argument("--storage", choices=["fp16", "fp32"], default="fp16", help="serving: sample storage")
     ap.add_argument("--plain-requests", type=int, default=200, help="serving: stream prefix run through the plain drop-in")
+    ap.add_argument("--passes", type=int, default=1, help="request: adaptive passes of the profiled request")
     args = ap.parse_args()
     if (args.width, args.height, args.spp) != (W, H, SPP):
         W, H, SPP = args.width, args.height, args.spp
@@ -729,6 +744,8 @@ def main():
         run_batched(args)
     elif args.form == "serving":
         run_serving(args)
+    elif args.form == "request":
+        run_request(args)
     else:
         run_gpu(args)
 

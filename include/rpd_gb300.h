@@ -219,6 +219,7 @@ typedef enum rpd_kernel {
     RPD_KERNEL_VARIANCE,            /* variance stabilisation iterations */
     RPD_KERNEL_ADAPTIVE,            /* importance + allocation */
     RPD_KERNEL_OTHER,               /* finalize, reads, fills */
+    RPD_KERNEL_SYNTH,               /* the serving loop's sample generation */
     RPD_KERNEL_COUNT_
 } rpd_kernel;
 
@@ -490,6 +491,7 @@ typedef struct rpd_server_config {
     uint64_t hbm_budget_bytes;   /* admission budget for request state and buffers (0: the context's) */
     int32_t max_inflight;        /* requests on the GPU at once, 1..256 */
     int32_t storage;             /* rpd_storage of the sample buffers */
+    int32_t profile;             /* nonzero: time every kernel family of every request (CUDA events) */
 } rpd_server_config;
 
 typedef struct rpd_request {
@@ -532,6 +534,10 @@ int rpd_server_drain(rpd_server* srv, int32_t timeout_ms);
  * runs to the end (RPD_ERR_STATE). */
 int rpd_server_cancel(rpd_server* srv, uint64_t id);
 int rpd_server_get_stats(rpd_server* srv, rpd_server_stats* out);
+/* With profile set: the summed device time and launches of each kernel family (RPD_KERNEL_COUNT_
+ * entries each) over the requests finished so far. The times include waits behind other requests'
+ * work on a busy GPU. */
+int rpd_server_kernel_times(rpd_server* srv, double* ms_out, uint64_t* launches_out);
 /* Finishes every submitted request, then releases the server. */
 void rpd_server_destroy(rpd_server* srv);
 

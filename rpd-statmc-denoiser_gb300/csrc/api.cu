@@ -940,9 +940,9 @@ static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int
     GridPrep gp{};
     gp.width = j->g.w;
     const bool fast_grid = rpd && !j->exact_grid;
+    int64_t nsamp = total;
     if (fast_grid) {
         // the per-sample total (or a bound on it) is needed on the host to size the luminance plane
-        int64_t nsamp = total;
         if (counts && where != RPD_MEM_HOST && total <= 0) {
             RPD_CUDA(cudaMemcpyAsync(&nsamp, j->offsets + count, 8, cudaMemcpyDeviceToHost, j->stream));
             RPD_CUDA(cudaStreamSynchronize(j->stream));
@@ -970,9 +970,9 @@ static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int
             if (where == RPD_MEM_HOST)
                 for (int64_t i = 0; i < count; ++i) max_count = std::max(max_count, counts[i]);
             else
-                max_count = INT32_MAX;  // unknown on the host: keep the double-float weights
+                max_count = INT32_MAX;  // unknown on the host: the push's total bounds the weights
         }
-        RPD_CUDA(launch_grid_fast(*j, d, first, count, gp, counts ? 0 : spp, max_count));
+        RPD_CUDA(launch_grid_fast(*j, d, first, count, gp, counts ? 0 : spp, max_count, nsamp));
     }
     else if (rpd) RPD_CUDA(launch_accumulate_grid(*j, d, first, count));
     j->pass_open = true;
@@ -1277,7 +1277,7 @@ int rpd_job_mark_elapsed(rpd_job* job, int a, int b, float* ms) {
 const char* rpd_kernel_name(rpd_kernel k) {
     static const char* names[RPD_KERNEL_COUNT_] = {
         "offsets", "accumulate_pixels", "grid", "grid_random", "merge", "features", "node_stats", "node_combine",
-        "sens_pixels", "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other"};
+        "sens_pixels", "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other", "synth"};
     return (k >= 0 && k < RPD_KERNEL_COUNT_) ? names[k] : "unknown";
 }
 

@@ -1063,7 +1063,7 @@ cudaError_t launch_random_shape(Job& j, const RandParams& rp, const GridPrep& gp
 }  // namespace
 
 cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int64_t count, const GridPrep& gp,
-                             int32_t spp, int32_t max_count) {
+                             int32_t spp, int32_t max_count, int64_t total_samples) {
     const int step = j.g.step;
     const bool pow2 = (step & (step - 1)) == 0;
     GridParams gpar{j.g, first, count, 0, 0, 0, pow2 ? 1 : 0, 1.0f / float(step), spp, spp > 0 ? 1.0f / float(spp) : 0.0f};
@@ -1080,7 +1080,9 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
     // exact integer bin weights need a power-of-two step and a per-bin total below 2^32:
     // at most support^2 pixels * max_count samples * step^2
     const double bound = double(sup + 3) * double(sup + 3) * double(std::max(max_count, 1)) * double(step) * double(step);
-    const bool int_w = pow2 && bound < 4.0e9;
+    // a bin's weight sum is at most the push's samples times step^2 units as well
+    const double total_bound = double(std::max<int64_t>(total_samples, 1)) * double(step) * double(step);
+    const bool int_w = pow2 && (bound < 4.0e9 || total_bound < 4.0e9);
     cudaError_t e;
     {
         KernelScope ks(j, RPD_KERNEL_GRID);

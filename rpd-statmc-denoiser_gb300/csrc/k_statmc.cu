@@ -386,6 +386,7 @@ __global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcPar
         float row[6] = {0, 0, 0, 0, 0, 0};
         const int erow = (threadIdx.y + r + dy) * tw + threadIdx.x + r;
         const float* srow = spatial_tab + (dy + r) * side + r;
+#pragma unroll 2
         for (int dx = -r; dx <= r; ++dx) {
             const int e = erow + dx;
             const float4 gj = T[P_GATE * tn + e];

@@ -292,8 +292,10 @@ cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count);
 cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,
                                      const GridPrep& gp, int32_t spp);
 cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first, int64_t count);
+// max_count bounds the samples of one pixel; total_samples bounds the samples of the push. Either
+// bound can make the bin weights exact integers (no bin of a node can then pass 2^32 units).
 cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int64_t count, const GridPrep& gp,
-                             int32_t spp, int32_t max_count);
+                             int32_t spp, int32_t max_count, int64_t total_samples);
 cudaError_t launch_merge_grid(Job& j);
 cudaError_t launch_feature_cache(Job& j);
 cudaError_t launch_sensitivity(Job& j);

@@ -243,6 +243,8 @@ struct Server {
     uint64_t next_id = 1;
     int64_t submitted = 0, completed = 0, rejected = 0;
     uint64_t launches = 0;              // kernels enqueued for requests
+    double kernel_ms[RPD_KERNEL_COUNT_] = {};  // profile: per kernel family over finished requests
+    uint64_t kernel_n[RPD_KERNEL_COUNT_] = {};
     uint64_t reserved = 0, peak = 0;    // request buffers + cached jobs
     std::multimap<std::pair<int, int>, CachedJob> idle_jobs;
     std::map<Job*, uint64_t> busy_jobs;
@@ -396,15 +398,21 @@ int enqueue_request(Server& s, Request& r) {
         rc = (x);                     \
         if (rc != RPD_OK) return rc;  \
     } while (0)
-    k_srv_regions<<<1, RPD_SYNTH_MAX_REGIONS, 0, st>>>(prm, table);
-    k_srv_region_map<<<grid_for(np, 256), 256, 0, st>>>(prm, table, np, region, o);
-    j.launches += 2;
+    {
+        KernelScope ks(j, RPD_KERNEL_SYNTH);
+        k_srv_regions<<<1, RPD_SYNTH_MAX_REGIONS, 0, st>>>(prm, table);
+        k_srv_region_map<<<grid_for(np, 256), 256, 0, st>>>(prm, table, np, region, o);
+        j.launches += 2;
+    }
     SRV_TRY(rpd_job_begin_frame(jh));
     // the first pass: generated at once, pushed in spans of whole rows that bound the scratch
     const int32_t spp = r.req.spp;
     if (spp > 0) {
-        k_srv_synth_uniform<<<grid_for(np * spp, 256), 256, 0, st>>>(prm, table, region, np, spp, 0u, o);
-        j.launches += 1;
+        {
+            KernelScope ks(j, RPD_KERNEL_SYNTH);
+            k_srv_synth_uniform<<<grid_for(np * spp, 256), 256, 0, st>>>(prm, table, region, np, spp, 0u, o);
+            j.launches += 1;
+        }
         const int64_t rows_per_span =
             std::max<int64_t>(1, (kSpanSamples / std::max<int64_t>(1, int64_t(spp) * c.image_width)) & ~int64_t(7));
         for (int64_t y0 = 0; y0 < c.image_height; y0 += rows_per_span) {
@@ -429,9 +437,12 @@ int enqueue_request(Server& s, Request& r) {
         SRV_TRY(rpd_compute_adaptive_sample_counts(jh, nullptr, RPD_MEM_DEVICE));
         RPD_CUDA(launch_offsets_scan(j, j.p.counts, np));
         RPD_CUDA(cudaMemcpyAsync(totals + p, j.offsets + np, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        k_srv_synth_counts<<<grid_for(np, kSynthPix), 256, 0, st>>>(prm, table, region, j.offsets, np,
-                                                                      L.max_samples, uint32_t(p) * kPassOrdinalStride, o);
-        j.launches += 1;
+        {
+            KernelScope ks(j, RPD_KERNEL_SYNTH);
+            k_srv_synth_counts<<<grid_for(np, kSynthPix), 256, 0, st>>>(prm, table, region, j.offsets, np,
+                                                                          L.max_samples, uint32_t(p) * kPassOrdinalStride, o);
+            j.launches += 1;
+        }
         SRV_TRY(push_device_async(j, push_planes(0), 0, np, 0, j.p.counts, int64_t(c.adaptive_spp) * np));
         SRV_TRY(rpd_job_end_pass(jh));
     }
@@ -480,6 +491,7 @@ int acquire_job(Server& s, Request& r, Job** out) {
     int st = rpd_job_create(reinterpret_cast<rpd_ctx*>(s.ctx), &c, &h);
     if (st != RPD_OK) return st;
     Job* j = reinterpret_cast<Job*>(h);
+    if (s.cfg.profile) rpd_job_set_profiling(h, 1);
     st = job_reserve(*j, need_span);
     if (st != RPD_OK) {
         rpd_job_destroy(h);
@@ -519,6 +531,18 @@ void finish(Server& s, Request* r) {  // caller holds mu
 
 void retire(Server& s, Request* r) {  // caller holds mu; r's GPU work has finished
     r->t_done = s.now_ms();
+    if (r->job && s.cfg.profile) {
+        rpd_job* jh = reinterpret_cast<rpd_job*>(r->job);
+        for (int k = 0; k < RPD_KERNEL_COUNT_; ++k) {
+            double ms = 0.0;
+            uint64_t n = 0;
+            if (rpd_job_kernel_time(jh, rpd_kernel(k), &ms, &n) == RPD_OK) {
+                s.kernel_ms[k] += ms;
+                s.kernel_n[k] += n;
+            }
+        }
+        rpd_job_reset_kernel_times(jh);
+    }
     if (r->job) {
         auto it = s.busy_jobs.find(r->job);
         const uint64_t bytes = it != s.busy_jobs.end() ? it->second : 0;
@@ -794,6 +818,17 @@ int rpd_server_get_stats(rpd_server* srv, rpd_server_stats* out) {
     out->jobs_cached = int64_t(s->idle_jobs.size() + s->busy_jobs.size());
     out->now_ms = s->now_ms();
     out->launches = int64_t(s->launches);
+    return RPD_OK;
+}
+
+int rpd_server_kernel_times(rpd_server* srv, double* ms_out, uint64_t* launches_out) {
+    Server* s = reinterpret_cast<Server*>(srv);
+    if (!s || !ms_out || !launches_out) return fail(RPD_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (int k = 0; k < RPD_KERNEL_COUNT_; ++k) {
+        ms_out[k] = s->kernel_ms[k];
+        launches_out[k] = s->kernel_n[k];
+    }
     return RPD_OK;
 }
 

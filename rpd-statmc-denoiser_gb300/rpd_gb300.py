@@ -42,7 +42,7 @@ RGB_FIELDS = {"DENOISED", "RADIANCE_SUM", "NORMAL_SUM", "ALBEDO_SUM", "STATS_COL
 INT_FIELDS = {"HIT_COUNT", "SAMPLE_COUNT", "STATS_N", "ADAPTIVE_COUNTS"}
 STAGES = ["ACCUMULATE", "SENSITIVITY", "STATMC", "VARIANCE", "ADAPTIVE"]
 KERNELS = ["offsets", "accumulate_pixels", "grid", "grid_random", "merge", "features", "node_stats", "node_combine", "sens_pixels",
-           "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other"]
+           "rpd_cache", "sqrt_variance", "statmc_window", "variance", "adaptive", "other", "synth"]
 STAGE = {name: i for i, name in enumerate(STAGES)}
 
 HIT, PIXEL_VALID, LENS_VALID, BRDF_VALID, LIGHT_VALID, LIGHT_SELECT_VALID, ENV_VALID, RR_VALID = (
@@ -140,7 +140,7 @@ class SynthParams(C.Structure):
 class ServerConfig(C.Structure):
     """rpd_server_config."""
     _fields_ = [("knobs", Config), ("hbm_budget_bytes", C.c_uint64), ("max_inflight", C.c_int32),
-                ("storage", C.c_int32)]
+                ("storage", C.c_int32), ("profile", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -318,6 +318,7 @@ def lib() -> C.CDLL:
         "rpd_server_drain": (C.c_int, [vp, i32]),
         "rpd_server_cancel": (C.c_int, [vp, u64]),
         "rpd_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStats)]),
+        "rpd_server_kernel_times": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
         "rpd_server_destroy": (None, [vp]),
         "rpd_last_error": (C.c_char_p, []),
         "rpd_status_string": (C.c_char_p, [C.c_int]),
@@ -336,7 +337,8 @@ def exported_symbols() -> list[str]:
             "rpd_ctx_bytes_in_use", "rpd_job_create", "rpd_job_destroy", "rpd_job_set_config", "rpd_job_set_exact",
             "rpd_job_set_tuning", "rpd_job_get_tuning", "rpd_job_allocator_stats", "rpd_adaptive_allocate", "rpd_job_allocator_timeline",
             "rpd_server_config_defaults", "rpd_server_create", "rpd_server_submit", "rpd_server_poll",
-            "rpd_server_drain", "rpd_server_cancel", "rpd_server_get_stats", "rpd_server_destroy",
+            "rpd_server_drain", "rpd_server_cancel", "rpd_server_get_stats", "rpd_server_kernel_times",
+            "rpd_server_destroy",
             "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_push_samples16", "rpd_encode_samples16",
             "rpd_job_autotune", "rpd_batch_create", "rpd_batch_add", "rpd_batch_run", "rpd_batch_sync",
             "rpd_batch_last_ms", "rpd_batch_kernel_count", "rpd_batch_set_lanes", "rpd_batch_destroy", "rpd_job_end_pass", "rpd_recompute_sensitivity",
@@ -783,13 +785,14 @@ class Server:
     """rpd_server: the serving loop (continuous batching of denoise requests)."""
 
     def __init__(self, ctx: Context, knobs: Config, budget_bytes: int = 0, max_inflight: int = 16,
-                 storage: str = "fp16"):
+                 storage: str = "fp16", profile: bool = False):
         cfg = ServerConfig()
         lib().rpd_server_config_defaults(C.byref(cfg))
         cfg.knobs = knobs
         cfg.hbm_budget_bytes = budget_bytes
         cfg.max_inflight = max_inflight
         cfg.storage = STORAGE[storage]
+        cfg.profile = 1 if profile else 0
         h = C.c_void_p()
         check(lib().rpd_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
         self.handle = h.value
@@ -824,6 +827,13 @@ class Server:
         st = ServerStats()
         check(lib().rpd_server_get_stats(self.handle, C.byref(st)))
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def kernel_times(self) -> dict[str, tuple[float, int]]:
+        """{kernel family: (summed ms, launches)} over finished requests (profile=True)."""
+        ms = (C.c_double * len(KERNELS))()
+        n = (C.c_uint64 * len(KERNELS))()
+        check(lib().rpd_server_kernel_times(self.handle, ms, n))
+        return {name: (ms[i], int(n[i])) for i, name in enumerate(KERNELS)}
 
     def close(self) -> None:
         if self.handle:
