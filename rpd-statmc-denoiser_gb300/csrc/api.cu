@@ -1509,12 +1509,14 @@ int job_reserve(Job& j, int64_t max_push_samples) {
 }
 
 int push_device_async(Job& j, const DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
-                      int64_t total_bound) {
+                      int64_t total_bound, bool offsets_ready) {
     int st = ensure_offsets(j, count);
     if (st != RPD_OK) return st;
     StageTimer timer(j, RPD_STAGE_ACCUMULATE);
-    if (counts) RPD_CUDA(launch_offsets_scan(j, counts, count));
-    else RPD_CUDA(launch_offsets_uniform(j, count, spp));
+    if (!offsets_ready) {
+        if (counts) RPD_CUDA(launch_offsets_scan(j, counts, count));
+        else RPD_CUDA(launch_offsets_uniform(j, count, spp));
+    }
     DeviceSamples dd = d;
     return push_tail(&j, dd, first, count, spp, counts, RPD_MEM_DEVICE,
                      counts ? std::max<int64_t>(total_bound, 1) : int64_t(count) * spp);

@@ -227,11 +227,15 @@ struct __align__(16) ChunkRec {
     // written by the walk
     double start;      // exact chain value before the chunk
     int mode;          // 0/1: walked with candidate mode; 2: walked exactly, values in the pool;
-                       // 3: inside the exact region
+                       // 3: inside the exact region; 4: split at a binade crossing
     int slot;          // pool slot of an exactly walked chunk
     int nb;            // clipped pixels before the chunk
     int pad;
     unsigned long long pstart;  // units before the chunk (mode 3)
+    int split;         // >= 0: the chunk crosses into the next binade at this pixel; action 0 covers
+                       // the pixels before it (binade E[0]) and action 1 the pixels after (E[1])
+    float xval;        // the addend at the split pixel
+    double xstart;     // written by the walk: the chain value after the split pixel (mode 4)
 };
 
 static_assert(sizeof(ChunkRec) % 16 == 0, "the walk copies records as 16-byte words");
@@ -464,6 +468,27 @@ __device__ unsigned long long block_scan_u64(unsigned long long v, Shared& sh) {
     return before + inc - v;
 }
 
+// Exclusive scan of a double over threads; *total gets the block's sum.
+__device__ double block_exscan_d(double v, double* total, Shared& sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double inc = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const double o = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += o;
+    }
+    if (lane == 31) sh.warp_d[warp] = inc;
+    __syncthreads();
+    double before = 0.0, all = 0.0;
+    for (int w = 0; w < kAWarps; ++w) {
+        if (w < warp) before += sh.warp_d[w];
+        all += sh.warp_d[w];
+    }
+    __syncthreads();
+    *total = all;
+    return before + inc - v;
+}
+
 __device__ int block_min_i(int v, Shared& sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -552,6 +577,7 @@ __device__ void chunk_actions(const float (&x)[kAV], int E0, int E1, int sign, C
             r->i0[1] = r->i1[1] = 0;
             r->o[1] = 6u;
             r->E[1] = kNoExp;
+            r->split = -1;
         }
         return;
     }
@@ -572,6 +598,7 @@ __device__ void chunk_actions(const float (&x)[kAV], int E0, int E1, int sign, C
             r->o[n] = En == kNoExp ? 6u : tot[n].o;
             r->E[n] = En;
         }
+        r->split = -1;
     }
 }
 
@@ -595,6 +622,46 @@ __device__ void chain_values(const CoopArgs& a, int c, const float (&x)[kAV], in
         for (int e = 0; e < kAV; ++e) {
             P += u[e];
             v[e] = units_to_double(P, F);
+        }
+    } else if (mode == 4) {
+        // before the split pixel kx in binade E[0] from the start, kx itself, after it in E[1]
+        const int kx = __ldcg(&a.rec[c].split);
+        const int EA = __ldcg(&a.rec[c].E[0]), EB = __ldcg(&a.rec[c].E[1]);
+        const double sx = __ldcg(&a.rec[c].xstart);
+        EF fa[kAV], fb[kAV], tf[2], ex[2], tot[2];
+        tf[0] = ef_identity();
+        tf[1] = ef_identity();
+#pragma unroll
+        for (int e = 0; e < kAV; ++e) {
+            fa[e] = base + e < kx ? ef_make(x[e], EA, sign) : ef_identity();
+            fb[e] = base + e > kx ? ef_make(x[e], EB, sign) : ef_identity();
+            tf[0] = ef_compose(tf[0], fa[e]);
+            tf[1] = ef_compose(tf[1], fb[e]);
+        }
+        block_scan_ef<2>(tf, ex, tot, sh);
+        long long SA = scaled(start, EA);
+        const unsigned pa0 = unsigned(SA & 1);
+        SA += pa0 ? ex[0].i1 : ex[0].i0;
+        unsigned pa = (ex[0].o >> pa0) & 1u;
+        long long SB = scaled(sx, EB);
+        const unsigned pb0 = unsigned(SB & 1);
+        SB += pb0 ? ex[1].i1 : ex[1].i0;
+        unsigned pb = (ex[1].o >> pb0) & 1u;
+        *before = base <= kx ? unscaled(SA, EA) : unscaled(SB, EB);
+#pragma unroll
+        for (int e = 0; e < kAV; ++e) {
+            const int idx = base + e;
+            if (idx < kx) {
+                SA += pa ? fa[e].i1 : fa[e].i0;
+                pa = (fa[e].o >> pa) & 1u;
+                v[e] = unscaled(SA, EA);
+            } else if (idx == kx) {
+                v[e] = sx;
+            } else {
+                SB += pb ? fb[e].i1 : fb[e].i0;
+                pb = (fb[e].o >> pb) & 1u;
+                v[e] = unscaled(SB, EB);
+            }
         }
     } else if (mode < 2) {
         const int E = __ldcg(&a.rec[c].E[mode]);
@@ -802,7 +869,8 @@ __device__ void walk(const CoopArgs& a, const Src& src, double s0, int sign, boo
                         const long long S = scaled(s, E);
                         const unsigned p0 = unsigned(S & 1);
                         int q = -1;
-                        if (have) q = (r->E[0] == E && !(r->o[0] & 4u)) ? 0 : ((r->E[1] == E && !(r->o[1] & 4u)) ? 1 : -1);
+                        if (have && r->split < 0)
+                            q = (r->E[0] == E && !(r->o[0] & 4u)) ? 0 : ((r->E[1] == E && !(r->o[1] & 4u)) ? 1 : -1);
                         EF f;
                         if (q >= 0) {
                             f.i0 = r->i0[q];
@@ -834,7 +902,40 @@ __device__ void walk(const CoopArgs& a, const Src& src, double s0, int sign, boo
                     }
                     if (k > 0) clips += __shfl_sync(0xffffffffu, cinc, k - 1);
                     c += k;
-                    if (k == 0) break;  // chunk c is walked exactly
+                    if (k == 0) {
+                        // a split chunk: the pixels before the predicted crossing in binade E, the
+                        // crossing pixel added as the reference adds it, the rest in binade E + 1
+                        const ChunkRec& r0 = sh.tile[c];
+                        bool ok = false;
+                        if (r0.split >= 0 && sign > 0 && binade_ok(s) && exponent_of(s) == r0.E[0] &&
+                            !((r0.o[0] | r0.o[1]) & 4u)) {
+                            const int E = r0.E[0];
+                            const long long S = scaled(s, E);
+                            const long long SA = S + ((S & 1) ? r0.i1[0] : r0.i0[0]);
+                            if (stays_in_binade(SA, 1)) {
+                                const double sx = unscaled(SA, E) + double(r0.xval);
+                                if (binade_ok(sx) && exponent_of(sx) == E + 1) {
+                                    const long long Sx = scaled(sx, E + 1);
+                                    const long long SB = Sx + ((Sx & 1) ? r0.i1[1] : r0.i0[1]);
+                                    if (stays_in_binade(SB, 1)) {
+                                        ok = true;
+                                        if (lane == 0) {
+                                            ChunkRec* g = a.rec + t0 + c;
+                                            g->start = s;
+                                            g->mode = 4;
+                                            g->slot = -1;
+                                            g->nb = clips;
+                                            g->xstart = sx;
+                                        }
+                                        s = unscaled(SB, E + 1);
+                                        clips += r0.clips;
+                                        ++c;
+                                    }
+                                }
+                            }
+                        }
+                        if (!ok) break;  // chunk c is walked exactly
+                    }
                 }
                 if (lane == 0) {
                     sh.bcast_d = s;
@@ -947,6 +1048,7 @@ __device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, doubl
                 if (threadIdx.x == 0) {  // the walk takes this chunk whole from the exact sum
                     a.rec[c].o[0] = a.rec[c].o[1] = 6u;
                     a.rec[c].E[0] = a.rec[c].E[1] = kNoExp;
+                    a.rec[c].split = -1;
                 }
                 continue;
             }
@@ -959,6 +1061,52 @@ __device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, doubl
             const double mant = pred * pow2d(-E0);  // in [1, 2)
             if (mant < 1.0 + 1.0 / 1024.0) E1 = E0 - 1;
             else if (mant > 2.0 - 1.0 / 1024.0) E1 = E0 + 1;
+            // a sum that leaves its binade once inside the chunk: split the chunk at the predicted
+            // crossing pixel (the walk checks the prediction and walks the chunk exactly if it missed)
+            const double pend = pred + __ldcg(&a.rec[c].approx);
+            if (sign > 0 && E0 < 898 && pend >= pow2d(E0 + 1) && pend < pow2d(E0 + 2)) {
+                const int base = threadIdx.x * kAV;
+                const int len = __ldcg(&a.rec[c].len);
+                double loc = 0.0;
+#pragma unroll
+                for (int e = 0; e < kAV; ++e) loc += double(x[e]);
+                double tot;
+                const double ex = block_exscan_d(loc, &tot, sh);
+                const double edge = pow2d(E0 + 1);
+                double run = pred + ex;
+                int first = INT_MAX;
+#pragma unroll
+                for (int e = 0; e < kAV; ++e) {
+                    run += double(x[e]);
+                    if (first == INT_MAX && base + e < len && run >= edge) first = base + e;
+                }
+                const int kx = block_min_i(first, sh);
+                if (kx < len) {
+                    EF tf[2], exf[2], totf[2];
+                    tf[0] = ef_identity();
+                    tf[1] = ef_identity();
+#pragma unroll
+                    for (int e = 0; e < kAV; ++e) {
+                        if (base + e < kx) tf[0] = ef_compose(tf[0], ef_make(x[e], E0, sign));
+                        if (base + e > kx) tf[1] = ef_compose(tf[1], ef_make(x[e], E0 + 1, sign));
+                    }
+                    block_scan_ef<2>(tf, exf, totf, sh);
+                    ChunkRec* r = a.rec + c;
+                    if (threadIdx.x == 0) {
+                        r->i0[0] = totf[0].i0;
+                        r->i1[0] = totf[0].i1;
+                        r->o[0] = totf[0].o;
+                        r->E[0] = E0;
+                        r->i0[1] = totf[1].i0;
+                        r->i1[1] = totf[1].i1;
+                        r->o[1] = totf[1].o;
+                        r->E[1] = E0 + 1;
+                        r->split = kx;
+                    }
+                    if (kx / kAV == int(threadIdx.x)) r->xval = x[kx % kAV];
+                    continue;
+                }
+            }
         }
         chunk_actions(x, E0, E1, sign, a.rec + c, sh);
     }
@@ -1099,20 +1247,20 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
             float I[kAV];
             load_f8(a.importance, k0, a.np, I);
-            float acc = 0.0f;
+            double acc = 0.0;  // double: the split prediction needs chunk starts to ~1e-12
             uint8_t st[kAV];
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
                 if (!(I[e] >= 0.0f && I[e] <= FLT_MAX)) bad = 1;
                 if (I[e] > 0.0f) code = max(code, 1000 - float_exp(I[e]));
-                acc += I[e];
+                acc += double(I[e]);
                 st[e] = 1u;
                 if (k0 + e < a.np) a.desired_add[k0 + e] = 0.0f;
             }
             store_u8(a.state, k0, a.np, st);
-            const float t = block_sum_f(acc, sh);
+            const double t = block_sum_d(acc, sh);
             if (threadIdx.x == 0) {
-                a.rec[c].approx = double(t);
+                a.rec[c].approx = t;
                 a.rec[c].len = int(min((long long)kAL, (long long)(a.np - int64_t(c) * kAL)));
                 a.rec[c].clips = 0;
             }
@@ -1222,7 +1370,7 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
         int code = 0;
         for (int c = blockIdx.x; c < a.nch; c += G) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
-            float acc = 0.0f;
+            double acc = 0.0;
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
                 if (k0 + e >= a.np) continue;
@@ -1233,11 +1381,11 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
                 const float r = fmaxs(0.0f, d - float(add));
                 a.residual[k0 + e] = r;
                 if (r > 0.0f) code = max(code, 1000 - float_exp(r));
-                acc += r;
+                acc += double(r);
             }
-            const float t = block_sum_f(acc, sh);
+            const double t = block_sum_d(acc, sh);
             if (threadIdx.x == 0) {
-                a.rec[c].approx = double(t);
+                a.rec[c].approx = t;
                 a.rec[c].clips = 0;
             }
         }

@@ -329,8 +329,9 @@ cudaError_t launch_joint_bilateral(const float* raw, const float* normal, const 
 // that later pushes allocate nothing; push_device_async takes device planes and, with device
 // counts, a bound on the push's sample total instead of reading the total back.
 int job_reserve(Job& j, int64_t max_push_samples);
+// offsets_ready: j.offsets already holds the push's offsets (a scan of the same counts).
 int push_device_async(Job& j, const DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
-                      int64_t total_bound);
+                      int64_t total_bound, bool offsets_ready = false);
 
 inline unsigned grid_for(int64_t n, int block) {
     return static_cast<unsigned>((n + block - 1) / block);

@@ -443,7 +443,8 @@ int enqueue_request(Server& s, Request& r) {
                                                                           L.max_samples, uint32_t(p) * kPassOrdinalStride, o);
             j.launches += 1;
         }
-        SRV_TRY(push_device_async(j, push_planes(0), 0, np, 0, j.p.counts, int64_t(c.adaptive_spp) * np));
+        // the offsets of these counts are in j.offsets already (the scan above)
+        SRV_TRY(push_device_async(j, push_planes(0), 0, np, 0, j.p.counts, int64_t(c.adaptive_spp) * np, true));
         SRV_TRY(rpd_job_end_pass(jh));
     }
     SRV_TRY(rpd_recompute_sensitivity(jh));
