@@ -785,20 +785,24 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
             }
         }
     } else {
+        // A fetch returns the sample's column-factor index and row factor, not its weight: with
+        // per-pixel counts the index comes from a load, and looking the factor up at fetch time
+        // would wait for that load before the samples already fetched are processed.
         constexpr int U = 4;  // samples per lane in flight
-        auto fetch = [&](int t, uint32_t& key, float& y, float& w) {
+        auto fetch = [&](int t, uint32_t& key, float& y, int& ci, float& ay) {
             key = 0u;
             y = 0.0f;
-            w = 0.0f;
+            ci = -1;
+            ay = 0.0f;
             if (t >= total) return;
             while (t >= rt->base[r + 1]) ++r;
             const int kk = t - rt->base[r];
             const int64_t k = rt->k0[r] + kk;
             key = gp.key[k];
             y = gp.lum[k];
+            ay = rt->ay[r];
             if (gp.col) {  // per-pixel counts: the statistics pass stored each sample's column
-                const int ci = int(gp.col[k]) - c.xlo;
-                w = unsigned(ci) < unsigned(rp.cols) ? c.xf[ci] * rt->ay[r] : 0.0f;
+                ci = int(gp.col[k]) - c.xlo;
                 return;
             }
             int pl;
@@ -815,12 +819,13 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
                 }
                 pl = lo;
             }
-            w = c.xf[rt->col0[r] + pl] * rt->ay[r];
+            ci = rt->col0[r] + pl;
         };
         uint32_t nk[U];
-        float nyv[U], nw[U];
+        float nyv[U], nay[U];
+        int nci[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) fetch(lane + 32 * u, nk[u], nyv[u], nw[u]);
+        for (int u = 0; u < U; ++u) fetch(lane + 32 * u, nk[u], nyv[u], nci[u], nay[u]);
         for (int t0 = 0; t0 < total; t0 += 32 * U) {
             uint32_t ck[U];
             float cy[U], cw[U];
@@ -828,11 +833,11 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
             for (int u = 0; u < U; ++u) {
                 ck[u] = nk[u];
                 cy[u] = nyv[u];
-                cw[u] = nw[u];
+                cw[u] = unsigned(nci[u]) < unsigned(rp.cols) ? c.xf[nci[u]] * nay[u] : 0.0f;
             }
             if (t0 + 32 * U < total) {
 #pragma unroll
-                for (int u = 0; u < U; ++u) fetch(t0 + 32 * U + lane + 32 * u, nk[u], nyv[u], nw[u]);
+                for (int u = 0; u < U; ++u) fetch(t0 + 32 * U + lane + 32 * u, nk[u], nyv[u], nci[u], nay[u]);
             }
 #pragma unroll
             for (int u = 0; u < U; ++u)

@@ -118,6 +118,95 @@ __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth(PixelPlanes p, V
     dst[idx] = conservative_variance_update(var_i, neighbor_mean, prm.shrinkage_k);
 }
 
+// The same iteration with the radius fixed at compile time: the window is unrolled, every
+// gate of a neighbour is evaluated as a predicate (the lanes of a warp stay converged; the
+// quotient gates branch only for the rare values within the band of their thresholds), and
+// the accepted neighbours are added in the reference's order. A rejected neighbour adds
+// nothing, exactly as the reference's `continue` does.
+template <int R>
+__global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth_r(PixelPlanes p, VarParams prm, const float* src,
+                                                                  float* dst) {
+    constexpr int tw = kVarTx + 2 * R, th = kVarTy + 2 * R, tn = tw * th;
+    __shared__ float4 G[tn];  // (normal, depth)
+    __shared__ float V[tn];   // max(EPS_SMALL, src), -1 outside the image or without a hit
+    const int x0 = blockIdx.x * kVarTx, y0 = blockIdx.y * kVarTy;
+    const int tid = threadIdx.y * kVarTx + threadIdx.x;
+    for (int e = tid; e < tn; e += kVarTx * kVarTy) {
+        const int gx = x0 - R + e % tw, gy = y0 - R + e / tw;
+        const bool inside = gx >= 0 && gx < prm.w && gy >= 0 && gy < prm.h;
+        const int64_t q = inside ? int64_t(gy) * prm.w + gx : 0;
+        const bool hit = inside && p.hit_count[q] > 0;
+        G[e] = hit ? make_float4(p.f_normal[0][q], p.f_normal[1][q], p.f_normal[2][q], p.f_depth[q])
+                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        V[e] = hit ? fmaxs(1e-8f, src[q]) : -1.0f;
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= prm.w || y >= prm.h) return;
+    const int64_t idx = int64_t(y) * prm.w + x;
+    const int ei = (threadIdx.y + R) * tw + threadIdx.x + R;
+    const float var_i = V[ei];
+    if (var_i < 0.0f) {  // no primary hit (hit_count == 0)
+        dst[idx] = src[idx];
+        return;
+    }
+    const float4 gi = G[ei];
+    const float dabs_i = fabsf(gi.w);
+    const float dthr = prm.depth_threshold;
+    const float nthr = prm.normal_threshold;
+    const float sigma = prm.compat_sigma;
+    const float sigma_band = sigma * kGateBand;
+    float weight_sum = 0.0f, weighted_sum = 0.0f;
+#pragma unroll
+    for (int dy = -R; dy <= R; ++dy) {
+#pragma unroll
+        for (int dx = -R; dx <= R; ++dx) {
+            if (dx == 0 && dy == 0) continue;
+            const int e = ei + dy * tw + dx;
+            const float var_j = V[e];
+            const float4 gj = G[e];
+            bool ok = var_j >= 0.0f && !(dot3(gi.x, gi.y, gi.z, gj.x, gj.y, gj.z) < nthr);
+            // relative_depth_delta(depth_i, depth_j) > threshold (main.cpp:266-268)
+            float m = dabs_i;
+            if (m < fabsf(gj.w)) m = fabsf(gj.w);
+            if (m < 1e-8f) m = 1e-8f;
+            const float num = fabsf(gi.w - gj.w);
+            const float tm = dthr * m;
+            const bool d_hi = num > tm * (1.0f + kGateBand), d_lo = num < tm * (1.0f - kGateBand);
+            bool far = d_hi;
+            if (ok && !(tm >= 1e-30f && (d_hi || d_lo))) far = num / m > dthr;
+            ok = ok && !far;
+            // |var_i - var_j| / max(EPS_SMALL, sqrt(var_i * var_j)) > compat_sigma
+            const float diff = fabsf(var_i - var_j);
+            const float prod = var_i * var_j;
+            const float approx = diff * rsqrtf(prod);
+            bool incompatible = approx > sigma;
+            if (ok && !(fabsf(approx - sigma) > sigma_band && prod >= 1e-16f && prod < 1e36f))
+                incompatible = diff / fmaxs(1e-8f, sqrtf(prod)) > sigma;
+            ok = ok && !incompatible;
+            const float w_j = 1.0f / (1.0f + float(dx * dx + dy * dy));
+            if (ok) {
+                weighted_sum += w_j * var_j;
+                weight_sum += w_j;
+            }
+        }
+    }
+    float neighbor_mean = var_i;
+    if (weight_sum > 1e-8f) neighbor_mean = weighted_sum / weight_sum;
+    dst[idx] = conservative_variance_update(var_i, neighbor_mean, prm.shrinkage_k);
+}
+
+template <int R>
+cudaError_t launch_smooth_r(Job& j, const VarParams& prm, float*& curr, float*& next, dim3 vgrid) {
+    for (int it = 0; it < j.cfg.var_iterations; ++it) {
+        k_var_smooth_r<R><<<vgrid, dim3(kVarTx, kVarTy), 0, j.stream>>>(j.p, prm, curr, next);
+        float* t = curr;
+        curr = next;
+        next = t;
+    }
+    return cudaGetLastError();
+}
+
 __global__ void k_var_final(PixelPlanes p, int64_t np, float max_variance, const float* curr) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= np) return;
@@ -139,12 +228,22 @@ cudaError_t launch_variance(Job& j) {
     VarParams prm{j.g.w, j.g.h, j.cfg.var_window_radius, j.cfg.var_normal_threshold, j.cfg.var_depth_threshold,
                   j.cfg.var_compat_sigma, j.cfg.var_shrinkage_k};
     const int r = prm.radius;
+    const dim3 vgrid((j.g.w + kVarTx - 1) / kVarTx, (j.g.h + kVarTy - 1) / kVarTy);
+    if (r >= 1 && r <= 4) {
+        cudaError_t e = r == 1 ? launch_smooth_r<1>(j, prm, curr, next, vgrid)
+                      : r == 2 ? launch_smooth_r<2>(j, prm, curr, next, vgrid)
+                      : r == 3 ? launch_smooth_r<3>(j, prm, curr, next, vgrid)
+                               : launch_smooth_r<4>(j, prm, curr, next, vgrid);
+        if (e != cudaSuccess) return e;
+        k_var_final<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np, max_variance, curr);
+        j.launches += 2 + j.cfg.var_iterations;
+        return cudaGetLastError();
+    }
     const size_t smem = size_t(kVarTx + 2 * r) * size_t(kVarTy + 2 * r) * (sizeof(float4) + sizeof(float)) +
                         size_t(2 * r + 1) * size_t(2 * r + 1) * sizeof(float);
     if (smem > size_t(200) * 1024) return cudaErrorInvalidValue;  // radius beyond the shared-memory tile
     cudaError_t e = cudaFuncSetAttribute(k_var_smooth, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    const dim3 vgrid((j.g.w + kVarTx - 1) / kVarTx, (j.g.h + kVarTy - 1) / kVarTy);
     for (int it = 0; it < j.cfg.var_iterations; ++it) {
         k_var_smooth<<<vgrid, dim3(kVarTx, kVarTy), smem, j.stream>>>(j.p, prm, curr, next);
         float* t = curr;

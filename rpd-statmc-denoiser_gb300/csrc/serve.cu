@@ -16,7 +16,8 @@
 //   final             recompute_sensitivity, statmc_denoise, variance_denoise, finalize
 //                     (main.cpp:1554-1559)
 // and the denoised image is copied to host memory. The adaptive passes' statmc_denoise and
-// recompute_sensitivity calls are dead work (see enqueue_request) and are not run. Nothing in
+// recompute_sensitivity calls and the final variance_denoise are dead work for the denoised
+// image (see enqueue_request) and are not run. Nothing in
 // the pipeline waits on the host: the counts, their offsets and the extra samples stay in HBM,
 // a push with device counts sizes its scratch from the bound adaptive_spp * W * H, and every
 // buffer comes from a stream-ordered pool.
@@ -429,7 +430,9 @@ int enqueue_request(Server& s, Request& r) {
     // counts only (main.cpp:1166-1446), recompute_sensitivity starts over from the grid on every
     // call (741-953), and the final statmc_denoise overwrites every plane the earlier ones wrote.
     // So the loop runs them once, after the last pass, and the result is the same bits (the
-    // tests compare it with the full sequence).
+    // tests compare it with the full sequence). The variance_denoise after the loop (1556) writes
+    // only the denoised variance, which finalize does not read and the request does not return:
+    // it is not run either.
     int64_t* totals = s.slots[size_t(r.slot)].totals;
     const int passes = c.adaptive_spp > 0 ? std::max(0, c.adaptive_passes) : 0;
     for (int p = 1; p <= passes; ++p) {
@@ -449,7 +452,6 @@ int enqueue_request(Server& s, Request& r) {
     }
     SRV_TRY(rpd_recompute_sensitivity(jh));
     SRV_TRY(rpd_statmc_denoise(jh));
-    SRV_TRY(rpd_variance_denoise(jh));
     SRV_TRY(rpd_finalize(jh));
     k_srv_pack<<<grid_for(np, 256), 256, 0, st>>>(j.p.denoised[0], j.p.denoised[1], j.p.denoised[2], out, np);
     j.launches += 1;
