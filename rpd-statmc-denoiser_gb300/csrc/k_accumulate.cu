@@ -28,45 +28,66 @@ __global__ void k_offsets_uniform(int64_t* offsets, int64_t count, int32_t spp) 
     if (i <= count) offsets[i] = i * int64_t(spp);
 }
 
-// Three-phase exclusive scan of int32 counts into int64 offsets[0..count].
-__global__ void k_scan_block_sums(const int32_t* counts, int64_t count, int64_t* block_sums) {
-    __shared__ int64_t s[kScanBlock];
-    const int64_t i = int64_t(blockIdx.x) * kScanBlock + threadIdx.x;
-    s[threadIdx.x] = (i < count) ? int64_t(counts[i]) : 0;
+// Three-phase exclusive scan of int32 counts into int64 offsets[0..count]: per-block sums, a
+// scan of the block sums by one block, and the per-block scans shifted by them. Warp-shuffle
+// scans, so each phase is a few steps per element.
+__device__ __forceinline__ int64_t warp_incl_scan(int64_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int64_t t = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += t;
+    }
+    return v;
+}
+
+// inclusive scan over the block (blockDim.x == kScanBlock); `total` gets the block's sum
+__device__ __forceinline__ int64_t block_incl_scan(int64_t v, int64_t* total) {
+    __shared__ int64_t warp_tot[kScanBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = warp_incl_scan(v);
+    if (lane == 31) warp_tot[warp] = v;
     __syncthreads();
-    for (int stride = kScanBlock / 2; stride > 0; stride >>= 1) {
-        if (threadIdx.x < stride) s[threadIdx.x] += s[threadIdx.x + stride];
-        __syncthreads();
+    if (warp == 0) {
+        const int64_t t = warp_incl_scan(warp_tot[lane]);
+        warp_tot[lane] = t;
     }
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = s[0];
+    __syncthreads();
+    if (warp > 0) v += warp_tot[warp - 1];
+    if (total) *total = warp_tot[kScanBlock / 32 - 1];
+    __syncthreads();
+    return v;
 }
 
-__global__ void k_scan_block_offsets(int64_t* block_sums, int64_t nblocks) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int64_t run = 0;
-    for (int64_t b = 0; b < nblocks; ++b) {
-        const int64_t v = block_sums[b];
-        block_sums[b] = run;
-        run += v;
-    }
-    block_sums[nblocks] = run;
+__global__ void __launch_bounds__(kScanBlock) k_scan_block_sums(const int32_t* counts, int64_t count, int64_t* block_sums) {
+    const int64_t i = int64_t(blockIdx.x) * kScanBlock + threadIdx.x;
+    int64_t total;
+    block_incl_scan((i < count) ? int64_t(counts[i]) : 0, &total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
 }
 
-__global__ void k_scan_finish(const int32_t* counts, int64_t count, const int64_t* block_sums, int64_t* offsets) {
-    __shared__ int64_t s[kScanBlock];
+// one block: block_sums[0..nblocks) -> exclusive offsets, block_sums[nblocks] = the total
+__global__ void __launch_bounds__(kScanBlock) k_scan_block_offsets(int64_t* block_sums, int64_t nblocks) {
+    int64_t carry = 0;
+    for (int64_t b0 = 0; b0 < nblocks; b0 += kScanBlock) {
+        const int64_t b = b0 + threadIdx.x;
+        const int64_t v = b < nblocks ? block_sums[b] : 0;
+        int64_t total;
+        const int64_t incl = block_incl_scan(v, &total);
+        if (b < nblocks) block_sums[b] = carry + incl - v;
+        carry += total;
+    }
+    if (threadIdx.x == 0) block_sums[nblocks] = carry;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_finish(const int32_t* counts, int64_t count, const int64_t* block_sums,
+                                                           int64_t* offsets) {
     const int64_t i = int64_t(blockIdx.x) * kScanBlock + threadIdx.x;
     const int64_t v = (i < count) ? int64_t(counts[i]) : 0;
-    s[threadIdx.x] = v;
-    __syncthreads();
-    // Hillis-Steele inclusive scan
-    for (int off = 1; off < kScanBlock; off <<= 1) {
-        int64_t t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
-        __syncthreads();
-        s[threadIdx.x] += t;
-        __syncthreads();
-    }
-    if (i < count) offsets[i] = block_sums[blockIdx.x] + s[threadIdx.x] - v;
-    if (i == count - 1) offsets[count] = block_sums[blockIdx.x] + s[threadIdx.x];
+    const int64_t incl = block_incl_scan(v, nullptr);
+    const int64_t base = block_sums[blockIdx.x];
+    if (i < count) offsets[i] = base + incl - v;
+    if (i == count - 1) offsets[count] = base + incl;
 }
 
 // Dependency2D::add bin (core/stats.h:166-168)
@@ -711,10 +732,11 @@ cudaError_t launch_offsets_uniform(Job& j, int64_t count, int32_t spp) {
 
 cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count) {
     KernelScope ks(j, RPD_KERNEL_OFFSETS);
+    if (count <= 0) return cudaMemsetAsync(j.offsets, 0, sizeof(int64_t), j.stream);
     const int64_t nblocks = (count + kScanBlock - 1) / kScanBlock;
     int64_t* block_sums = j.offsets + (count + 1);  // the offsets buffer reserves room for these
     k_scan_block_sums<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums);
-    k_scan_block_offsets<<<1, 1, 0, j.stream>>>(block_sums, nblocks);
+    k_scan_block_offsets<<<1, kScanBlock, 0, j.stream>>>(block_sums, nblocks);
     k_scan_finish<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums, j.offsets);
     j.launches += 3;
     return cudaGetLastError();

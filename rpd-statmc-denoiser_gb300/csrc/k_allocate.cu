@@ -246,6 +246,7 @@ struct AllocScalars {
     int error;
     int fallback;
     unsigned long long changed;  // running count of decisions that changed between rounds
+    unsigned long long start_clips;  // running count of the clips decided at the passes' start states
     double walk_final;
     long long assigned;
     int walk_clips;
@@ -325,6 +326,7 @@ struct Shared {
     int warp_i[kAWarps];
     double own_pred[kMaxOwned];
     ChunkRec tile[kTile];
+    float xs[kAL];  // the addends of the chunk an exact walk is on
     double bcast_d;
     int bcast_i;
     int bcast_j;
@@ -697,15 +699,43 @@ __device__ void chain_values(const CoopArgs& a, int c, const float (&x)[kAV], in
 // ---- the walk (block 0) -----------------------------------------------------------------------
 // Chunk c walked exactly from value s: block scans within the binade, the crossing addend in
 // double precision. Stores every inclusive value in the pool slot when `slot` >= 0.
+// After a binade crossing that came within kDenseGap addends of the previous position, the next
+// kBurst addends are added one at a time by one thread (a sum from near zero crosses a binade
+// every few addends, and a block scan per crossing costs more than the additions).
+constexpr int kDenseGap = 64;
+constexpr int kBurst = 128;
+
 __device__ double walk_exact(const CoopArgs& a, const Src& src, int c, double s, int sign, int slot, Shared& sh) {
     const int len = __ldcg(&a.rec[c].len);
     const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
     const int base = threadIdx.x * kAV;
     float x[kAV];
     src.load(a, k0, x);
+#pragma unroll
+    for (int e = 0; e < kAV; ++e) sh.xs[base + e] = x[e];
+    __syncthreads();
     double* pv = slot >= 0 ? a.pool + int64_t(slot) * kAL : nullptr;
     int pos = 0;  // first pixel not yet walked
+    bool dense = false;
     while (pos < len) {
+        if (dense && binade_ok(s)) {
+            const int end = min(pos + kBurst, len);
+            if (threadIdx.x == 0) {
+                double t = s;
+                for (int k = pos; k < end; ++k) {
+                    const double xe = double(sh.xs[k]);
+                    t = sign > 0 ? t + xe : t - xe;
+                    if (pv) pv[k] = t;
+                }
+                sh.bcast_d = t;
+            }
+            __syncthreads();
+            s = sh.bcast_d;
+            __syncthreads();
+            pos = end;
+            dense = false;
+            continue;
+        }
         if (!binade_ok(s)) {
             // s is zero, negative or extreme: walk to the next nonzero addend one at a time
             int first = INT_MAX;
@@ -785,12 +815,14 @@ __device__ double walk_exact(const CoopArgs& a, const Src& src, int c, double s,
             __syncthreads();
             s = sh.bcast_d;
             __syncthreads();
+            dense = kb - pos < kDenseGap;
             pos = kb + 1;
         } else {
             s = prev;
             pos = len;
         }
     }
+    __syncthreads();  // sh.xs is rewritten by the next exact walk
     return s;
 }
 
@@ -1144,6 +1176,7 @@ __device__ __forceinline__ bool clip_test(float I, double R, int Rs, int m) {
 // chunk's clip count and approximate clipped importance (the binade predictions of the walk).
 __device__ void phase_decide_start(const CoopArgs& a, double R, int Rs, int fb, Shared& sh) {
     const unsigned fbit = 2u << fb;
+    unsigned long long block_clips = 0;
     for (int c = blockIdx.x; c < a.nch; c += gridDim.x) {
         const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
         float I[kAV];
@@ -1166,8 +1199,10 @@ __device__ void phase_decide_start(const CoopArgs& a, double R, int Rs, int fb, 
         if (threadIdx.x == 0) {
             a.rec[c].clips = total;
             a.rec[c].approx = double(t);
+            block_clips += (unsigned long long)total;
         }
     }
+    if (threadIdx.x == 0 && block_clips) atomicAdd(&a.sc->start_clips, block_clips);
 }
 
 // One fixed-point round: the chain values of clip set fb (walked), every alive pixel decided
@@ -1293,8 +1328,9 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
     int Rs = remaining_samples0;
     int64_t active = a.np;
     int fb = 0;
-    unsigned long long changed_seen = 0;
+    unsigned long long changed_seen = 0, start_clips_seen = 0;
     int passes = 0, rounds = 0;
+    bool shares = false;  // the alive pixels take share_of(I, R, Rs) as their desired_add
     while (active > 0 && Rs > 0 && R > double(1e-8f)) {
         ++passes;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1303,46 +1339,45 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
         }
         phase_decide_start(a, R, Rs, fb, sh);
         if (!grid_sync(sc)) return;
-        phase_predicted_actions(a, Src{1, 2u << fb}, R, -1, kNoRegion, sh);
-        if (!grid_sync(sc)) return;
-        if (blockIdx.x == 0) walk(a, Src{1, 2u << fb}, R, -1, true, kNoRegion, sh);
-        if (!grid_sync(sc) || fell_back(sc)) return;
-        for (int round = 0;; ++round) {
-            phase_decide_round(a, R, Rs, fb, sh);
+        // No pixel clips at the pass's start state: then none clips in the reference's order
+        // either (the state it tests against never leaves the start state), and the pass ends
+        // with the shares of the start state.
+        const unsigned long long sc_now = __ldcg(&sc->start_clips);
+        const bool none_at_start = sc_now == start_clips_seen;
+        start_clips_seen = sc_now;
+        int nc = 0;
+        double R_after = R;
+        if (!none_at_start) {
+            phase_predicted_actions(a, Src{1, 2u << fb}, R, -1, kNoRegion, sh);
             if (!grid_sync(sc)) return;
-            const unsigned long long ch = __ldcg(&sc->changed);
-            if (ch == changed_seen) break;  // buffer fb is the pass's clip set; its walk is current
-            changed_seen = ch;
-            ++rounds;
-            fb ^= 1;
-            if (round + 1 >= kMaxRounds) {
-                if (threadIdx.x == 0) {
-                    atomicExch(&sc->reason, 3);
-                    atomicExch(&sc->fallback, 1);
-                }
-                return;
-            }
             if (blockIdx.x == 0) walk(a, Src{1, 2u << fb}, R, -1, true, kNoRegion, sh);
             if (!grid_sync(sc) || fell_back(sc)) return;
+            for (int round = 0;; ++round) {
+                phase_decide_round(a, R, Rs, fb, sh);
+                if (!grid_sync(sc)) return;
+                const unsigned long long ch = __ldcg(&sc->changed);
+                if (ch == changed_seen) break;  // buffer fb is the pass's clip set; its walk is current
+                changed_seen = ch;
+                ++rounds;
+                fb ^= 1;
+                if (round + 1 >= kMaxRounds) {
+                    if (threadIdx.x == 0) {
+                        atomicExch(&sc->reason, 3);
+                        atomicExch(&sc->fallback, 1);
+                    }
+                    return;
+                }
+                if (blockIdx.x == 0) walk(a, Src{1, 2u << fb}, R, -1, true, kNoRegion, sh);
+                if (!grid_sync(sc) || fell_back(sc)) return;
+            }
+            nc = __ldcg(&sc->walk_clips);
+            R_after = __ldcg(&sc->walk_final);
         }
-        const int nc = __ldcg(&sc->walk_clips);
-        const double R_after = __ldcg(&sc->walk_final);
         const unsigned fbit = 2u << fb;
         if (nc == 0) {
-            // no pixel clipped: the rest share the remaining samples (main.cpp:1403-1408)
-            const double rcp = 1.0 / R;
-            const double Rsd = double(Rs);
-            for (int c = blockIdx.x; c < a.nch; c += G) {
-                const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
-                float I[kAV];
-                uint8_t st[kAV];
-                load_f8(a.importance, k0, a.np, I);
-                load_u8(a.state, k0, a.np, st);
-#pragma unroll
-                for (int e = 0; e < kAV; ++e)
-                    if ((st[e] & 1u) && k0 + e < a.np)
-                        a.desired_add[k0 + e] = share_of(I[e], R, rcp, Rsd);
-            }
+            // no pixel clipped: the rest share the remaining samples (main.cpp:1403-1408); the
+            // shares are taken where the residual weights are formed, below
+            shares = true;
             break;
         }
         // clipped pixels get the cap and leave the active list
@@ -1368,13 +1403,21 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
     {
         long long assigned = 0;
         int code = 0;
+        const double rcp = 1.0 / R;
+        const double Rsd = double(Rs);
         for (int c = blockIdx.x; c < a.nch; c += G) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
             double acc = 0.0;
+            float I[kAV];
+            uint8_t st[kAV];
+            if (shares) {
+                load_f8(a.importance, k0, a.np, I);
+                load_u8(a.state, k0, a.np, st);
+            }
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
                 if (k0 + e >= a.np) continue;
-                const float d = __ldcg(a.desired_add + k0 + e);
+                const float d = (shares && (st[e] & 1u)) ? share_of(I[e], R, rcp, Rsd) : __ldcg(a.desired_add + k0 + e);
                 const int add = int(floorf(d));
                 a.counts[k0 + e] += add;
                 assigned += add;
@@ -1437,18 +1480,37 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
             while (k < remaining && !above(k, c)) ++k;
             return k;
         };
+        // A single-precision screen decides t_k > c from values relative to the thread's first
+        // chain value `before`: tau_i = t_(n0+i) - before (its estimate for i = 0 in double, then
+        // steps of `step`) against d = c - before. Its error is below 2^-22 of the magnitudes
+        // involved plus 2^-48 of |before| (the double steps); a gap within the margin goes to
+        // above(), so the screen never decides what the estimate or the reference's expression
+        // would decide otherwise.
+        const float stepf = float(step);
         for (int c = blockIdx.x; c < a.nch; c += G) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
             float x[kAV];
             load_f8(a.residual, k0, a.np, x);
             double v[kAV], before;
             chain_values(a, c, x, 1, F_res, v, &before, sh);
-            long long n_prev = k0 == 0 ? 0 : first_above(before);
+            const long long n0 = k0 == 0 ? 0 : first_above(before);
+            const float tau0 = float((double(n0) + offset) * step - before);
+            const float mfix = float(fabs(before)) * (1.0f / 35184372088832.0f) + fabsf(tau0) * (1.0f / 1048576.0f);
+            long long n_prev = n0;
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
                 if (k0 + e >= a.np) break;
+                const float d = float(v[e] - before);
+                const float md = mfix + fabsf(d) * (1.0f / 1048576.0f);
                 long long n = n_prev;
-                while (n < remaining && !above(n, v[e])) ++n;
+                while (n < remaining) {
+                    const float i = float(n - n0);
+                    const float gap = (tau0 + i * stepf) - d;
+                    const float m = md + (i + 1.0f) * stepf * (1.0f / 1048576.0f);
+                    const bool ab = gap > m ? true : (gap < -m ? false : above(n, v[e]));
+                    if (ab) break;
+                    ++n;
+                }
                 if (n != n_prev) a.counts[k0 + e] += int(n - n_prev);
                 n_prev = n;
             }
