@@ -273,10 +273,14 @@ int rpd_job_set_exact(rpd_job* job, int flags);
 /* RPD_TUNE_STATMC_ROWS: pixel rows per block of the StatMC window kernel: 2, 4 or 8 (0, the
  * default: the tallest whose halo tile fits in shared memory). */
 #define RPD_TUNE_STATMC_ROWS 2
-/* RPD_TUNE_ALLOCATOR: 0 (default) the parallel allocation of the adaptive counts on a few dozen
- * blocks, N >= 2 the same on at most N blocks, 1 the one-thread kernel in the reference's order.
+/* RPD_TUNE_ALLOCATOR: 0 (default) the parallel allocation of the adaptive counts on one block
+ * per SM, N >= 2 the same on at most N blocks, 1 the one-thread kernel in the reference's order.
  * All give the same counts. */
 #define RPD_TUNE_ALLOCATOR 3
+/* RPD_TUNE_SMOOTHING: 0 (default) the adaptive importance smoothing's double-precision sums
+ * carried out exactly in integer instructions, 1 in double-precision instructions. Both give
+ * the same bits. */
+#define RPD_TUNE_SMOOTHING 4
 int rpd_job_set_tuning(rpd_job* job, int knob, int value);
 int rpd_job_get_tuning(rpd_job* job, int knob, int* value);
 /* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */

@@ -572,6 +572,11 @@ int rpd_job_set_tuning(rpd_job* job, int knob, int value) {
         j->allocator_blocks = value >= 2 ? value : 0;
         return RPD_OK;
     }
+    if (knob == RPD_TUNE_SMOOTHING) {
+        if (value != 0 && value != 1) return fail(RPD_ERR_INVALID_ARGUMENT, "smoothing must be 0 or 1");
+        j->smooth_fp64 = value == 1;
+        return RPD_OK;
+    }
     return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
@@ -583,6 +588,7 @@ int rpd_job_get_tuning(rpd_job* job, int knob, int* value) {
     else if (knob == RPD_TUNE_HOST_BAND_MB) *value = int(j->band_bytes >> 20);
     else if (knob == RPD_TUNE_STATMC_ROWS) *value = j->statmc_by;
     else if (knob == RPD_TUNE_ALLOCATOR) *value = j->serial_allocator ? 1 : j->allocator_blocks;
+    else if (knob == RPD_TUNE_SMOOTHING) *value = j->smooth_fp64 ? 1 : 0;
     else return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
     return RPD_OK;
 }

@@ -1,13 +1,15 @@
 // compute_adaptive_sample_counts (main.cpp:1273-1446).
 //
 //   k_importance        variance source and importance = sqrt (1303-1327)
-//   k_smooth_importance edge-aware smoothing (1331-1368)
+//   k_smooth_importance edge-aware smoothing (1331-1368), its double-precision sums carried
+//                       out exactly in integer instructions
 //   k_allocate_coop     the budget-preserving allocation (1329-1438) in parallel, with the
 //                       reference's integers bit for bit (k_allocate.cu)
 //   k_allocate_serial   the same allocation as one device thread in the reference's order. It
 //                       runs behind the parallel kernel and returns at once unless that kernel
 //                       flagged a case outside its method (or RPD_TUNE_ALLOCATOR selects it).
 #include <algorithm>
+#include <cfloat>
 
 #include "rpd_internal.h"
 #include "device_math.cuh"
@@ -30,17 +32,88 @@ __global__ void k_importance(PixelPlanes p, int64_t np, float sigma_max) {
     p.importance[i] = sqrtf(vs);
 }
 
-__global__ void k_smooth_importance(PixelPlanes p, int w, int h, int radius, const float* in, float* out) {
-    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= int64_t(w) * h) return;
-    if (p.hit_count[idx] == 0) {
-        out[idx] = in[idx];
-        return;
+// ---- exact double-precision arithmetic on nonnegative values, in integer instructions ------
+// The smoothing sums (main.cpp:1346-1360) are double-precision products and sums of floats.
+// GB300 issues double-precision instructions at 2 per SM per clock, so they are carried out on
+// the bits instead: a nonnegative double is m * 2^e with m = 0 or m in [2^52, 2^53), and each
+// product and sum is formed exactly and rounded to nearest-even as IEEE 754 rounds it. The
+// values here are never subnormal or infinite as doubles (they come from floats of at most
+// 2^128 and products of at most three of them); non-finite or negative inputs take the
+// double-precision operations instead.
+struct XD {
+    uint64_t m;
+    int e;
+};
+
+__device__ __forceinline__ XD xd_from_float(float f) {  // f >= 0, finite
+    const uint32_t b = __float_as_uint(f);
+    if (b == 0u) return XD{0ull, 0};
+    const uint32_t eb = b >> 23;
+    if (eb) return XD{uint64_t((b & 0x7fffffu) | 0x800000u) << 29, int(eb) - 179};
+    const int sh = __clzll((long long)b) - 11;  // a subnormal float: b * 2^-149
+    return XD{uint64_t(b) << sh, -149 - sh};
+}
+
+__device__ __forceinline__ XD xd_round(uint64_t r, uint64_t rem, uint64_t half, int e) {
+    if (rem > half || (rem == half && (r & 1ull))) {
+        ++r;
+        if (r == (1ull << 53)) {
+            r >>= 1;
+            ++e;
+        }
     }
-    const int y = int(idx / w), x = int(idx % w);
+    return XD{r, e};
+}
+
+__device__ __forceinline__ XD xd_mul(XD a, XD b) {
+    if (a.m == 0ull || b.m == 0ull) return XD{0ull, 0};
+    const uint64_t lo = a.m * b.m, hi = __umul64hi(a.m, b.m);  // product in [2^104, 2^106)
+    const int s = (hi >> 41) ? 53 : 52;
+    const uint64_t r = (hi << (64 - s)) | (lo >> s);
+    return xd_round(r, lo & ((1ull << s) - 1ull), 1ull << (s - 1), a.e + b.e + s);
+}
+
+__device__ __forceinline__ XD xd_add(XD a, XD b) {
+    if (b.m == 0ull) return a;
+    if (a.m == 0ull) return b;
+    if (a.e < b.e) {
+        const XD t = a;
+        a = b;
+        b = t;
+    }
+    const int d = a.e - b.e;
+    if (d >= 54) return a;  // b is below half an ulp of a
+    const uint64_t A = a.m << 10;
+    uint64_t B = b.m << 10;
+    if (d) B = (B >> d) | ((B & ((1ull << d) - 1ull)) ? 1ull : 0ull);  // bits shifted out: sticky
+    const uint64_t S = A + B;                                        // below 2^64
+    const int k = (S >> 63) ? 11 : 10;
+    return xd_round(S >> k, S & ((1ull << k) - 1ull), 1ull << (k - 1), a.e - 10 + k);
+}
+
+__device__ __forceinline__ double xd_to_double(XD a) {
+    if (a.m == 0ull) return 0.0;
+    return __longlong_as_double((static_cast<long long>(a.e + 1075) << 52) | static_cast<long long>(a.m - (1ull << 52)));
+}
+
+__device__ __forceinline__ bool xd_greater(XD a, XD b) {  // a > b, both normalised
+    if (a.m == 0ull) return false;
+    if (b.m == 0ull) return true;
+    return a.e > b.e || (a.e == b.e && a.m > b.m);
+}
+
+__device__ __forceinline__ bool finite_nonneg(float v) { return v >= 0.0f && v <= FLT_MAX; }
+
+// The edge-aware smoothing of one pixel (main.cpp:1339-1366). FP64 selects the reference's
+// double-precision instructions; otherwise the same operations run on the integer form above and
+// give the same bits.
+template <bool FP64>
+__device__ float smooth_pixel(const PixelPlanes& p, int w, int h, int radius, const float* in, int x, int y,
+                              int64_t idx, bool* bad) {
     const float ni0 = p.f_normal[0][idx], ni1 = p.f_normal[1][idx], ni2 = p.f_normal[2][idx];
     const float di = p.f_depth[idx];
     double accum = 0.0, weight_sum = 0.0;
+    XD xa{0ull, 0}, xw{0ull, 0};
     for (int dy = -radius; dy <= radius; ++dy) {
         const int yy = y + dy;
         if (yy < 0 || yy >= h) continue;
@@ -54,12 +127,43 @@ __global__ void k_smooth_importance(PixelPlanes p, int w, int h, int radius, con
                 (dot3(ni0, ni1, ni2, p.f_normal[0][nidx], p.f_normal[1][nidx], p.f_normal[2][nidx]) + 1.0f) * 0.5f,
                 0.0f, 1.0f);
             const float depth_w = expf(-4.0f * relative_depth_delta(di, p.f_depth[nidx]));
-            const double w_neighbor = double(spatial_w) * double(normal_w) * double(depth_w);
-            accum += w_neighbor * double(in[nidx]);
-            weight_sum += w_neighbor;
+            const float imp = in[nidx];
+            if (FP64) {
+                const double w_neighbor = double(spatial_w) * double(normal_w) * double(depth_w);
+                accum += w_neighbor * double(imp);
+                weight_sum += w_neighbor;
+            } else {
+                if (!(finite_nonneg(normal_w) && finite_nonneg(depth_w) && finite_nonneg(imp))) {
+                    *bad = true;
+                    return 0.0f;
+                }
+                const XD wn = xd_mul(xd_mul(xd_from_float(spatial_w), xd_from_float(normal_w)), xd_from_float(depth_w));
+                xa = xd_add(xa, xd_mul(wn, xd_from_float(imp)));
+                xw = xd_add(xw, wn);
+            }
         }
     }
-    out[idx] = (weight_sum > double(1e-8f)) ? float(accum / weight_sum) : in[idx];
+    if (!FP64) {
+        if (!xd_greater(xw, xd_from_float(1e-8f))) return in[idx];
+        return float(xd_to_double(xa) / xd_to_double(xw));
+    }
+    return (weight_sum > double(1e-8f)) ? float(accum / weight_sum) : in[idx];
+}
+
+__global__ void k_smooth_importance(PixelPlanes p, int w, int h, int radius, const float* in, float* out,
+                                    int fp64) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= int64_t(w) * h) return;
+    if (p.hit_count[idx] == 0) {
+        out[idx] = in[idx];
+        return;
+    }
+    const int y = int(idx / w), x = int(idx % w);
+    bool bad = false;
+    float v = 0.0f;
+    if (!fp64) v = smooth_pixel<false>(p, w, h, radius, in, x, y, idx, &bad);
+    if (fp64 || bad) v = smooth_pixel<true>(p, w, h, radius, in, x, y, idx, &bad);
+    out[idx] = v;
 }
 
 // hash_u32 / hash_to_unit_float (main.cpp:270-281)
@@ -200,7 +304,7 @@ cudaError_t launch_adaptive(Job& j) {
     const int radius = j.cfg.adaptive_importance_smoothing_radius;
     if (radius > 0) {
         k_smooth_importance<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, w, h, radius, j.p.importance,
-                                                                     j.p.importance_tmp);
+                                                                     j.p.importance_tmp, j.smooth_fp64 ? 1 : 0);
         k_copy<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p.importance_tmp, j.p.importance, np);
         j.launches += 2;
     }

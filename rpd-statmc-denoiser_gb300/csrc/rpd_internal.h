@@ -158,6 +158,7 @@ struct Job {
     int grid_shape = 6;          // launch shape of the random-dimension grid pass (row groups x dimension sets)
     int statmc_by = 0;           // StatMC tile height (0: the largest that fits)
     bool serial_allocator = false;  // RPD_TUNE_ALLOCATOR = 1: the one-thread allocation kernel only
+    bool smooth_fp64 = false;       // RPD_TUNE_SMOOTHING = 1: the importance smoothing in double-precision instructions
     int allocator_blocks = 0;       // RPD_TUNE_ALLOCATOR >= 2: blocks of the parallel allocation
     bool pass_open = false;
     bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)

@@ -640,7 +640,7 @@ class Job:
     def set_exact(self, grid: bool = False, window: bool = False) -> None:
         check(lib().rpd_job_set_exact(self.handle, (1 if grid else 0) | (2 if window else 0)))
 
-    TUNING = {"grid_shape": 0, "host_band_mb": 1, "statmc_rows": 2, "allocator": 3}
+    TUNING = {"grid_shape": 0, "host_band_mb": 1, "statmc_rows": 2, "allocator": 3, "smoothing": 4}
 
     def autotune(self, samples, spp: int) -> None:
         """rpd_job_autotune on device-resident planes (leaves the frame denoised)."""
