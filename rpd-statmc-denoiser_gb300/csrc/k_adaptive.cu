@@ -45,15 +45,6 @@ struct XD {
     int e;
 };
 
-__device__ __forceinline__ XD xd_from_float(float f) {  // f >= 0, finite
-    const uint32_t b = __float_as_uint(f);
-    if (b == 0u) return XD{0ull, 0};
-    const uint32_t eb = b >> 23;
-    if (eb) return XD{uint64_t((b & 0x7fffffu) | 0x800000u) << 29, int(eb) - 179};
-    const int sh = __clzll((long long)b) - 11;  // a subnormal float: b * 2^-149
-    return XD{uint64_t(b) << sh, -149 - sh};
-}
-
 __device__ __forceinline__ XD xd_round(uint64_t r, uint64_t rem, uint64_t half, int e) {
     if (rem > half || (rem == half && (r & 1ull))) {
         ++r;
@@ -65,12 +56,31 @@ __device__ __forceinline__ XD xd_round(uint64_t r, uint64_t rem, uint64_t half, 
     return XD{r, e};
 }
 
-__device__ __forceinline__ XD xd_mul(XD a, XD b) {
-    if (a.m == 0ull || b.m == 0ull) return XD{0ull, 0};
-    const uint64_t lo = a.m * b.m, hi = __umul64hi(a.m, b.m);  // product in [2^104, 2^106)
-    const int s = (hi >> 41) ? 53 : 52;
+// A positive normal float as m * 2^e with m in [2^23, 2^24); false for zero, subnormals,
+// negative values, infinities and NaN.
+__device__ __forceinline__ bool float_parts(float f, uint32_t& m, int& e) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t eb = b >> 23;  // the sign bit makes a negative value's eb >= 256
+    m = (b & 0x7fffffu) | 0x800000u;
+    e = int(eb) - 150;
+    return eb != 0u && eb < 255u;
+}
+
+// a * b * 2^e rounded to 53 bits, for a product a * b in [2^69, 2^77) (a < 2^53, b < 2^24)
+__device__ __forceinline__ XD xd_mul24(uint64_t a, uint32_t b, int e) {
+    const uint64_t lo1 = (a & 0xffffffffull) * b;
+    const uint64_t mid = (a >> 32) * b;
+    const uint64_t lo = lo1 + (mid << 32);
+    const uint64_t hi = (mid >> 32) + (lo < lo1 ? 1ull : 0ull);  // in [2^5, 2^13)
+    const int s = 75 - __clzll(static_cast<long long>(hi));      // top bit - 52, 17..24
     const uint64_t r = (hi << (64 - s)) | (lo >> s);
-    return xd_round(r, lo & ((1ull << s) - 1ull), 1ull << (s - 1), a.e + b.e + s);
+    return xd_round(r, lo & ((1ull << s) - 1ull), 1ull << (s - 1), e + s);
+}
+
+// an exact product a * 2^e of at most 53 bits (a in [2^46, 2^48)) in normal form
+__device__ __forceinline__ XD xd_exact48(uint64_t a, int e) {
+    const int sh = __clzll(static_cast<long long>(a)) - 11;
+    return XD{a << sh, e - sh};
 }
 
 __device__ __forceinline__ XD xd_add(XD a, XD b) {
@@ -96,24 +106,35 @@ __device__ __forceinline__ double xd_to_double(XD a) {
     return __longlong_as_double((static_cast<long long>(a.e + 1075) << 52) | static_cast<long long>(a.m - (1ull << 52)));
 }
 
-__device__ __forceinline__ bool xd_greater(XD a, XD b) {  // a > b, both normalised
-    if (a.m == 0ull) return false;
-    if (b.m == 0ull) return true;
-    return a.e > b.e || (a.e == b.e && a.m > b.m);
+// float(a / w) with the quotient rounded to double first, a = am * 2^ae and w = wm * 2^we
+// (am, wm in [2^52, 2^53)). A single-precision quotient q0 = qm * 2^qe is within a few ulps of
+// t = am / wm; the remainder am * 2^-qe - qm * wm is exact in 64-bit integers, and its ratio to
+// wm places t between the float grid points. Where t lies within 2^-8 of an ulp of a midpoint,
+// or the result leaves q0's binade or the normal range, it returns false.
+__device__ __forceinline__ bool quotient_to_float(uint64_t am, int ae, uint64_t wm, int we, float& out) {
+    const float q0 = float(uint32_t(am >> 29)) / float(uint32_t(wm >> 29));
+    const uint32_t qb = __float_as_uint(q0);
+    const uint32_t qm = (qb & 0x7fffffu) | 0x800000u;
+    const int qe = int(qb >> 23) - 150;                                     // -25 .. -22
+    const long long r = static_cast<long long>((am << (-qe)) - uint64_t(qm) * wm);  // |r| < 8 wm
+    const float u = float(r) / float(wm);
+    const float n = rintf(u);
+    if (fabsf(fabsf(u - n) - 0.5f) < 1.0f / 256.0f) return false;
+    const long long M = static_cast<long long>(qm) + static_cast<long long>(n);
+    if (M < (1ll << 23) || M >= (1ll << 24)) return false;
+    const int be = qe + ae - we + 150;
+    if (be < 1 || be > 254) return false;
+    out = __uint_as_float((uint32_t(be) << 23) | (uint32_t(M) & 0x7fffffu));
+    return true;
 }
 
-__device__ __forceinline__ bool finite_nonneg(float v) { return v >= 0.0f && v <= FLT_MAX; }
-
-// The edge-aware smoothing of one pixel (main.cpp:1339-1366). FP64 selects the reference's
-// double-precision instructions; otherwise the same operations run on the integer form above and
-// give the same bits.
-template <bool FP64>
-__device__ float smooth_pixel(const PixelPlanes& p, int w, int h, int radius, const float* in, int x, int y,
-                              int64_t idx, bool* bad) {
+// The edge-aware smoothing of one pixel (main.cpp:1339-1366) in the reference's double-precision
+// instructions.
+__device__ float smooth_pixel_fp64(const PixelPlanes& p, int w, int h, int radius, const float* in, int x, int y,
+                                   int64_t idx) {
     const float ni0 = p.f_normal[0][idx], ni1 = p.f_normal[1][idx], ni2 = p.f_normal[2][idx];
     const float di = p.f_depth[idx];
     double accum = 0.0, weight_sum = 0.0;
-    XD xa{0ull, 0}, xw{0ull, 0};
     for (int dy = -radius; dy <= radius; ++dy) {
         const int yy = y + dy;
         if (yy < 0 || yy >= h) continue;
@@ -127,27 +148,80 @@ __device__ float smooth_pixel(const PixelPlanes& p, int w, int h, int radius, co
                 (dot3(ni0, ni1, ni2, p.f_normal[0][nidx], p.f_normal[1][nidx], p.f_normal[2][nidx]) + 1.0f) * 0.5f,
                 0.0f, 1.0f);
             const float depth_w = expf(-4.0f * relative_depth_delta(di, p.f_depth[nidx]));
-            const float imp = in[nidx];
-            if (FP64) {
-                const double w_neighbor = double(spatial_w) * double(normal_w) * double(depth_w);
-                accum += w_neighbor * double(imp);
-                weight_sum += w_neighbor;
-            } else {
-                if (!(finite_nonneg(normal_w) && finite_nonneg(depth_w) && finite_nonneg(imp))) {
-                    *bad = true;
-                    return 0.0f;
-                }
-                const XD wn = xd_mul(xd_mul(xd_from_float(spatial_w), xd_from_float(normal_w)), xd_from_float(depth_w));
-                xa = xd_add(xa, xd_mul(wn, xd_from_float(imp)));
-                xw = xd_add(xw, wn);
-            }
+            const double w_neighbor = double(spatial_w) * double(normal_w) * double(depth_w);
+            accum += w_neighbor * double(in[nidx]);
+            weight_sum += w_neighbor;
         }
     }
-    if (!FP64) {
-        if (!xd_greater(xw, xd_from_float(1e-8f))) return in[idx];
-        return float(xd_to_double(xa) / xd_to_double(xw));
-    }
     return (weight_sum > double(1e-8f)) ? float(accum / weight_sum) : in[idx];
+}
+
+// The same pixel with the products and the weight sum in integer instructions (XD) and the
+// importance sum in double precision from the products' bits: the same bits as
+// smooth_pixel_fp64. R > 0 fixes the radius at compile time (R = 0: `radius`). Returns false for
+// inputs outside the integer form (negative, subnormal or non-finite weights or importances).
+template <int R>
+__device__ bool smooth_pixel_int(const PixelPlanes& p, int w, int h, int radius, const float* in, int x, int y,
+                                 int64_t idx, float& out) {
+    const int rad = R > 0 ? R : radius;
+    const float ni0 = p.f_normal[0][idx], ni1 = p.f_normal[1][idx], ni2 = p.f_normal[2][idx];
+    const float di = p.f_depth[idx];
+    double accum = 0.0;
+    XD xw{0ull, 0};
+    bool ok = true;
+#pragma unroll
+    for (int dy = -rad; dy <= rad; ++dy) {
+        const int yy = y + dy;
+        if (yy < 0 || yy >= h) continue;
+#pragma unroll
+        for (int dx = -rad; dx <= rad; ++dx) {
+            const int xx = x + dx;
+            if (xx < 0 || xx >= w) continue;
+            const int64_t nidx = int64_t(yy) * w + xx;
+            if (p.hit_count[nidx] == 0) continue;
+            const float spatial_w = 1.0f / (1.0f + float(dx * dx + dy * dy));
+            const float normal_w = fclamps(
+                (dot3(ni0, ni1, ni2, p.f_normal[0][nidx], p.f_normal[1][nidx], p.f_normal[2][nidx]) + 1.0f) * 0.5f,
+                0.0f, 1.0f);
+            const float depth_w = expf(-4.0f * relative_depth_delta(di, p.f_depth[nidx]));
+            const float imp = in[nidx];
+            uint32_t sm, nm, dm, im;
+            int se, ne, de, ie;
+            float_parts(spatial_w, sm, se);
+            const bool nok = float_parts(normal_w, nm, ne), dok = float_parts(depth_w, dm, de);
+            const bool iok = float_parts(imp, im, ie);
+            if (!(nok && dok)) {
+                // a zero normal weight (opposite normals) adds exact zeros to both sums
+                if (normal_w == 0.0f && dok && (iok || imp == 0.0f)) continue;
+                ok = false;
+                continue;
+            }
+            // (spatial * normal) * depth: the first product is exact; the second is exact too
+            // when the spatial weight is a power of two (then it is normal * depth scaled), else
+            // rounded
+            const XD wn = sm == 0x800000u ? xd_exact48(uint64_t(nm) * dm, ne + de + se + 23)
+                                          : xd_mul24(uint64_t(sm) * nm, dm, se + ne + de);
+            if (iok) accum += xd_to_double(xd_mul24(wn.m, im, wn.e + ie));
+            else if (imp != 0.0f) ok = false;
+            xw = xd_add(xw, wn);
+        }
+    }
+    if (!ok) return false;
+    // weight_sum > double(1e-8f): 1e-8f = 11258999 * 2^-50 exactly
+    const XD eps{uint64_t(11258999u) << 29, -79};
+    if (!(xw.m != 0ull && (xw.e > eps.e || (xw.e == eps.e && xw.m > eps.m)))) {
+        out = in[idx];
+        return true;
+    }
+    if (accum == 0.0) {
+        out = 0.0f;
+        return true;
+    }
+    const long long ab = __double_as_longlong(accum);
+    const uint64_t am = (uint64_t(ab) & ((1ull << 52) - 1ull)) | (1ull << 52);
+    const int ae = int((ab >> 52) & 0x7ff) - 1075;
+    if (!quotient_to_float(am, ae, xw.m, xw.e, out)) out = float(accum / xd_to_double(xw));
+    return true;
 }
 
 __global__ void k_smooth_importance(PixelPlanes p, int w, int h, int radius, const float* in, float* out,
@@ -159,10 +233,13 @@ __global__ void k_smooth_importance(PixelPlanes p, int w, int h, int radius, con
         return;
     }
     const int y = int(idx / w), x = int(idx % w);
-    bool bad = false;
     float v = 0.0f;
-    if (!fp64) v = smooth_pixel<false>(p, w, h, radius, in, x, y, idx, &bad);
-    if (fp64 || bad) v = smooth_pixel<true>(p, w, h, radius, in, x, y, idx, &bad);
+    bool done = false;
+    if (!fp64) {
+        done = radius == 1 ? smooth_pixel_int<1>(p, w, h, radius, in, x, y, idx, v)
+                           : smooth_pixel_int<0>(p, w, h, radius, in, x, y, idx, v);
+    }
+    if (!done) v = smooth_pixel_fp64(p, w, h, radius, in, x, y, idx);
     out[idx] = v;
 }
 
