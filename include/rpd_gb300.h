@@ -277,9 +277,9 @@ int rpd_job_set_exact(rpd_job* job, int flags);
  * per SM, N >= 2 the same on at most N blocks, 1 the one-thread kernel in the reference's order.
  * All give the same counts. */
 #define RPD_TUNE_ALLOCATOR 3
-/* RPD_TUNE_SMOOTHING: 0 (default) the adaptive importance smoothing's double-precision sums
- * carried out exactly in integer instructions, 1 in double-precision instructions. Both give
- * the same bits. */
+/* RPD_TUNE_SMOOTHING: 0 (default) the adaptive importance smoothing's double-precision products
+ * carried out exactly in integer instructions, 1 all of it in double-precision instructions. Both
+ * give the same bits. */
 #define RPD_TUNE_SMOOTHING 4
 int rpd_job_set_tuning(rpd_job* job, int knob, int value);
 int rpd_job_get_tuning(rpd_job* job, int knob, int* value);

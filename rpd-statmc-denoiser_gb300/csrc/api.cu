@@ -83,6 +83,7 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5]
     L.add(p.variance_denoised, np);
     L.add(p.var_ping, np);
     L.add(p.var_pong, np);
+    L.add(p.var_mask, np);
     L.add(p.importance, np);
     L.add(p.importance_tmp, np);
     L.add(p.desired_add, np);
@@ -146,6 +147,7 @@ void rebase_all(PixelPlanes& p, NodePlanes& n, char* base) {
     rebase(p.variance_denoised, base);
     rebase(p.var_ping, base);
     rebase(p.var_pong, base);
+    rebase(p.var_mask, base);
     rebase(p.importance, base);
     rebase(p.importance_tmp, base);
     rebase(p.desired_add, base);

@@ -1,7 +1,7 @@
 // compute_adaptive_sample_counts (main.cpp:1273-1446).
 //
 //   k_importance        variance source and importance = sqrt (1303-1327)
-//   k_smooth_importance edge-aware smoothing (1331-1368), its double-precision sums carried
+//   k_smooth_importance edge-aware smoothing (1331-1368), its double-precision products carried
 //                       out exactly in integer instructions
 //   k_allocate_coop     the budget-preserving allocation (1329-1438) in parallel, with the
 //                       reference's integers bit for bit (k_allocate.cu)
@@ -32,14 +32,15 @@ __global__ void k_importance(PixelPlanes p, int64_t np, float sigma_max) {
     p.importance[i] = sqrtf(vs);
 }
 
-// ---- exact double-precision arithmetic on nonnegative values, in integer instructions ------
-// The smoothing sums (main.cpp:1346-1360) are double-precision products and sums of floats.
-// GB300 issues double-precision instructions at 2 per SM per clock, so they are carried out on
-// the bits instead: a nonnegative double is m * 2^e with m = 0 or m in [2^52, 2^53), and each
-// product and sum is formed exactly and rounded to nearest-even as IEEE 754 rounds it. The
-// values here are never subnormal or infinite as doubles (they come from floats of at most
-// 2^128 and products of at most three of them); non-finite or negative inputs take the
-// double-precision operations instead.
+// ---- exact double-precision products in integer instructions ---------------------------------
+// The smoothing sums (main.cpp:1346-1360) are double-precision products of three floats, a product
+// with the importance and two running sums. GB300 issues double-precision instructions at 2 per SM
+// per clock, so the products and the float-to-double conversions are carried out on the bits: a
+// positive double is m * 2^e with m in [2^52, 2^53), each product is formed exactly from 24-bit
+// mantissas and rounded to nearest-even as IEEE 754 rounds it, and only the two additions per
+// neighbour run as double-precision instructions. The values are never subnormal or infinite as
+// doubles (they come from positive normal floats); any other input takes the double-precision
+// operations throughout.
 struct XD {
     uint64_t m;
     int e;
@@ -81,24 +82,6 @@ __device__ __forceinline__ XD xd_mul24(uint64_t a, uint32_t b, int e) {
 __device__ __forceinline__ XD xd_exact48(uint64_t a, int e) {
     const int sh = __clzll(static_cast<long long>(a)) - 11;
     return XD{a << sh, e - sh};
-}
-
-__device__ __forceinline__ XD xd_add(XD a, XD b) {
-    if (b.m == 0ull) return a;
-    if (a.m == 0ull) return b;
-    if (a.e < b.e) {
-        const XD t = a;
-        a = b;
-        b = t;
-    }
-    const int d = a.e - b.e;
-    if (d >= 54) return a;  // b is below half an ulp of a
-    const uint64_t A = a.m << 10;
-    uint64_t B = b.m << 10;
-    if (d) B = (B >> d) | ((B & ((1ull << d) - 1ull)) ? 1ull : 0ull);  // bits shifted out: sticky
-    const uint64_t S = A + B;                                        // below 2^64
-    const int k = (S >> 63) ? 11 : 10;
-    return xd_round(S >> k, S & ((1ull << k) - 1ull), 1ull << (k - 1), a.e - 10 + k);
 }
 
 __device__ __forceinline__ double xd_to_double(XD a) {
@@ -156,28 +139,29 @@ __device__ float smooth_pixel_fp64(const PixelPlanes& p, int w, int h, int radiu
     return (weight_sum > double(1e-8f)) ? float(accum / weight_sum) : in[idx];
 }
 
-// The same pixel with the products and the weight sum in integer instructions (XD) and the
-// importance sum in double precision from the products' bits: the same bits as
-// smooth_pixel_fp64. R > 0 fixes the radius at compile time (R = 0: `radius`). Returns false for
-// inputs outside the integer form (negative, subnormal or non-finite weights or importances).
+// The same pixel with the products in integer instructions (XD) and the two sums as double
+// additions of the products' bits: the same bits as smooth_pixel_fp64 with three of its five
+// double-precision operations per neighbour, and none of its conversions, left out. R > 0 fixes
+// the radius at compile time (R = 0: `radius`). Returns false for inputs outside the integer
+// form (negative, subnormal or non-finite weights or importances).
 template <int R>
 __device__ bool smooth_pixel_int(const PixelPlanes& p, int w, int h, int radius, const float* in, int x, int y,
                                  int64_t idx, float& out) {
     const int rad = R > 0 ? R : radius;
     const float ni0 = p.f_normal[0][idx], ni1 = p.f_normal[1][idx], ni2 = p.f_normal[2][idx];
     const float di = p.f_depth[idx];
-    double accum = 0.0;
-    XD xw{0ull, 0};
+    double accum = 0.0, weight_sum = 0.0;
     bool ok = true;
 #pragma unroll
     for (int dy = -rad; dy <= rad; ++dy) {
         const int yy = y + dy;
         if (yy < 0 || yy >= h) continue;
+        const int64_t row = idx + int64_t(dy) * w;
 #pragma unroll
         for (int dx = -rad; dx <= rad; ++dx) {
             const int xx = x + dx;
             if (xx < 0 || xx >= w) continue;
-            const int64_t nidx = int64_t(yy) * w + xx;
+            const int64_t nidx = row + dx;
             if (p.hit_count[nidx] == 0) continue;
             const float spatial_w = 1.0f / (1.0f + float(dx * dx + dy * dy));
             const float normal_w = fclamps(
@@ -203,13 +187,11 @@ __device__ bool smooth_pixel_int(const PixelPlanes& p, int w, int h, int radius,
                                           : xd_mul24(uint64_t(sm) * nm, dm, se + ne + de);
             if (iok) accum += xd_to_double(xd_mul24(wn.m, im, wn.e + ie));
             else if (imp != 0.0f) ok = false;
-            xw = xd_add(xw, wn);
+            weight_sum += xd_to_double(wn);
         }
     }
     if (!ok) return false;
-    // weight_sum > double(1e-8f): 1e-8f = 11258999 * 2^-50 exactly
-    const XD eps{uint64_t(11258999u) << 29, -79};
-    if (!(xw.m != 0ull && (xw.e > eps.e || (xw.e == eps.e && xw.m > eps.m)))) {
+    if (!(weight_sum > double(1e-8f))) {
         out = in[idx];
         return true;
     }
@@ -217,10 +199,11 @@ __device__ bool smooth_pixel_int(const PixelPlanes& p, int w, int h, int radius,
         out = 0.0f;
         return true;
     }
-    const long long ab = __double_as_longlong(accum);
+    const long long ab = __double_as_longlong(accum), wb = __double_as_longlong(weight_sum);
     const uint64_t am = (uint64_t(ab) & ((1ull << 52) - 1ull)) | (1ull << 52);
-    const int ae = int((ab >> 52) & 0x7ff) - 1075;
-    if (!quotient_to_float(am, ae, xw.m, xw.e, out)) out = float(accum / xd_to_double(xw));
+    const uint64_t wm = (uint64_t(wb) & ((1ull << 52) - 1ull)) | (1ull << 52);
+    const int ae = int((ab >> 52) & 0x7ff) - 1075, we = int((wb >> 52) & 0x7ff) - 1075;
+    if (!quotient_to_float(am, ae, wm, we, out)) out = float(accum / weight_sum);
     return true;
 }
 

@@ -123,12 +123,18 @@ __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth(PixelPlanes p, V
 // quotient gates branch only for the rare values within the band of their thresholds), and
 // the accepted neighbours are added in the reference's order. A rejected neighbour adds
 // nothing, exactly as the reference's `continue` does.
-template <int R>
+//
+// The hit, normal and depth gates depend on the features only, which the iterations do not
+// change. MODE 0 evaluates every gate; MODE 1 also writes each pixel's geometric-gate bits (one
+// per neighbour, in window order) to var_mask; MODE 2 reads them and evaluates only the
+// variance-compatibility gate of the neighbours they pass.
+template <int R, int MODE>
 __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth_r(PixelPlanes p, VarParams prm, const float* src,
                                                                   float* dst) {
+    static_assert(MODE == 0 || (2 * R + 1) * (2 * R + 1) - 1 <= 64, "the gate bits fit one word");
     constexpr int tw = kVarTx + 2 * R, th = kVarTy + 2 * R, tn = tw * th;
-    __shared__ float4 G[tn];  // (normal, depth)
-    __shared__ float V[tn];   // max(EPS_SMALL, src), -1 outside the image or without a hit
+    __shared__ float4 G[MODE == 2 ? 1 : tn];  // (normal, depth)
+    __shared__ float V[tn];                   // max(EPS_SMALL, src), -1 outside the image or without a hit
     const int x0 = blockIdx.x * kVarTx, y0 = blockIdx.y * kVarTy;
     const int tid = threadIdx.y * kVarTx + threadIdx.x;
     for (int e = tid; e < tn; e += kVarTx * kVarTy) {
@@ -136,8 +142,9 @@ __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth_r(PixelPlanes p,
         const bool inside = gx >= 0 && gx < prm.w && gy >= 0 && gy < prm.h;
         const int64_t q = inside ? int64_t(gy) * prm.w + gx : 0;
         const bool hit = inside && p.hit_count[q] > 0;
-        G[e] = hit ? make_float4(p.f_normal[0][q], p.f_normal[1][q], p.f_normal[2][q], p.f_depth[q])
-                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (MODE != 2)
+            G[e] = hit ? make_float4(p.f_normal[0][q], p.f_normal[1][q], p.f_normal[2][q], p.f_depth[q])
+                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         V[e] = hit ? fmaxs(1e-8f, src[q]) : -1.0f;
     }
     __syncthreads();
@@ -150,13 +157,16 @@ __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth_r(PixelPlanes p,
         dst[idx] = src[idx];
         return;
     }
-    const float4 gi = G[ei];
-    const float dabs_i = fabsf(gi.w);
-    const float dthr = prm.depth_threshold;
-    const float nthr = prm.normal_threshold;
     const float sigma = prm.compat_sigma;
     const float sigma_band = sigma * kGateBand;
     float weight_sum = 0.0f, weighted_sum = 0.0f;
+    uint64_t gates = MODE == 2 ? p.var_mask[idx] : 0ull;
+    float4 gi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (MODE != 2) gi = G[ei];
+    const float dabs_i = fabsf(gi.w);
+    const float dthr = prm.depth_threshold;
+    const float nthr = prm.normal_threshold;
+    int bit = 0;
 #pragma unroll
     for (int dy = -R; dy <= R; ++dy) {
 #pragma unroll
@@ -164,18 +174,25 @@ __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth_r(PixelPlanes p,
             if (dx == 0 && dy == 0) continue;
             const int e = ei + dy * tw + dx;
             const float var_j = V[e];
-            const float4 gj = G[e];
-            bool ok = var_j >= 0.0f && !(dot3(gi.x, gi.y, gi.z, gj.x, gj.y, gj.z) < nthr);
-            // relative_depth_delta(depth_i, depth_j) > threshold (main.cpp:266-268)
-            float m = dabs_i;
-            if (m < fabsf(gj.w)) m = fabsf(gj.w);
-            if (m < 1e-8f) m = 1e-8f;
-            const float num = fabsf(gi.w - gj.w);
-            const float tm = dthr * m;
-            const bool d_hi = num > tm * (1.0f + kGateBand), d_lo = num < tm * (1.0f - kGateBand);
-            bool far = d_hi;
-            if (ok && !(tm >= 1e-30f && (d_hi || d_lo))) far = num / m > dthr;
-            ok = ok && !far;
+            bool ok;
+            if (MODE == 2) {
+                ok = (gates >> bit) & 1ull;
+            } else {
+                const float4 gj = G[e];
+                ok = var_j >= 0.0f && !(dot3(gi.x, gi.y, gi.z, gj.x, gj.y, gj.z) < nthr);
+                // relative_depth_delta(depth_i, depth_j) > threshold (main.cpp:266-268)
+                float m = dabs_i;
+                if (m < fabsf(gj.w)) m = fabsf(gj.w);
+                if (m < 1e-8f) m = 1e-8f;
+                const float num = fabsf(gi.w - gj.w);
+                const float tm = dthr * m;
+                const bool d_hi = num > tm * (1.0f + kGateBand), d_lo = num < tm * (1.0f - kGateBand);
+                bool far = d_hi;
+                if (ok && !(tm >= 1e-30f && (d_hi || d_lo))) far = num / m > dthr;
+                ok = ok && !far;
+                if (MODE == 1 && ok) gates |= 1ull << bit;
+            }
+            ++bit;
             // |var_i - var_j| / max(EPS_SMALL, sqrt(var_i * var_j)) > compat_sigma
             const float diff = fabsf(var_i - var_j);
             const float prod = var_i * var_j;
@@ -191,6 +208,7 @@ __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth_r(PixelPlanes p,
             }
         }
     }
+    if (MODE == 1) p.var_mask[idx] = gates;
     float neighbor_mean = var_i;
     if (weight_sum > 1e-8f) neighbor_mean = weighted_sum / weight_sum;
     dst[idx] = conservative_variance_update(var_i, neighbor_mean, prm.shrinkage_k);
@@ -198,8 +216,15 @@ __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth_r(PixelPlanes p,
 
 template <int R>
 cudaError_t launch_smooth_r(Job& j, const VarParams& prm, float*& curr, float*& next, dim3 vgrid) {
-    for (int it = 0; it < j.cfg.var_iterations; ++it) {
-        k_var_smooth_r<R><<<vgrid, dim3(kVarTx, kVarTy), 0, j.stream>>>(j.p, prm, curr, next);
+    const int iters = j.cfg.var_iterations;
+    constexpr bool kMask = (2 * R + 1) * (2 * R + 1) - 1 <= 64;
+    for (int it = 0; it < iters; ++it) {
+        if (!kMask || iters == 1)
+            k_var_smooth_r<R, 0><<<vgrid, dim3(kVarTx, kVarTy), 0, j.stream>>>(j.p, prm, curr, next);
+        else if (it == 0)
+            k_var_smooth_r<R, kMask ? 1 : 0><<<vgrid, dim3(kVarTx, kVarTy), 0, j.stream>>>(j.p, prm, curr, next);
+        else
+            k_var_smooth_r<R, kMask ? 2 : 0><<<vgrid, dim3(kVarTx, kVarTy), 0, j.stream>>>(j.p, prm, curr, next);
         float* t = curr;
         curr = next;
         next = t;

@@ -79,6 +79,7 @@ struct PixelPlanes {
     float* variance_denoised;
     float* var_ping;
     float* var_pong;
+    uint64_t* var_mask;  // variance_denoise: per pixel, the neighbours that pass the geometric gates
     // compute_adaptive_sample_counts (main.cpp:1300-1438)
     float* importance;
     float* importance_tmp;

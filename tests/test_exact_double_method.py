@@ -1,9 +1,9 @@
 """The method of the importance smoothing's integer arithmetic (csrc/k_adaptive.cu: float_parts,
-xd_mul24, xd_exact48, xd_add, quotient_to_float), restated in Python integers and checked
-against IEEE 754 arithmetic (numpy float64 and float32): the weight products of three floats,
-the products with the importance, sums of nonnegative doubles rounded to nearest-even, and the
-final float(accum / weight_sum), on random operands across wide exponent ranges and on
-constructed ties. The CUDA kernel itself is compared with the double-precision instructions in
+xd_mul24, xd_exact48, quotient_to_float), restated in Python integers and checked against IEEE
+754 arithmetic (numpy float64 and float32): the weight products of three floats, the products
+with the importance (summed as doubles, as the kernel sums them), and the final
+float(accum / weight_sum), on random operands across wide exponent ranges and on quotients at
+float midpoints. The CUDA kernel itself is compared with the double-precision instructions in
 tests/test_gpu_smoothing.py."""
 from __future__ import annotations
 
@@ -49,25 +49,6 @@ def xd_exact48(a: int, e: int):
     return (a << sh, e - sh)
 
 
-def xd_add(a, b):
-    if b[0] == 0:
-        return a
-    if a[0] == 0:
-        return b
-    if a[1] < b[1]:
-        a, b = b, a
-    d = a[1] - b[1]
-    if d >= 54:
-        return a
-    A, B = a[0] << 10, b[0] << 10
-    if d:
-        B = (B >> d) | (1 if B & ((1 << d) - 1) else 0)
-    S = A + B
-    assert S < 1 << 64
-    k = 11 if (S >> 63) else 10
-    return xd_round(S >> k, S & ((1 << k) - 1), 1 << (k - 1), a[1] - 10 + k)
-
-
 def quotient_to_float(am: int, ae: int, wm: int, we: int):
     q0 = np.float32(np.float32(am >> 29) / np.float32(wm >> 29))
     qb = struct.unpack("<I", struct.pack("<f", float(q0)))[0]
@@ -110,11 +91,11 @@ def rnd(rng, lo, hi):
     return float(np.float32(rng.uniform(lo, hi)))
 
 
-def test_weights_products_and_sums_match_ieee_double():
+def test_weights_and_products_match_ieee_double():
     rng = np.random.default_rng(7)
     spatial = [float(np.float32(1.0) / np.float32(1.0 + d2)) for d2 in (0, 1, 2, 4, 5, 8, 9, 10, 13, 18)]
     for _ in range(5000):
-        acc, xacc, wsum, ws_ref = np.float64(0.0), np.float64(0.0), (0, 0), np.float64(0.0)
+        acc, xacc = np.float64(0.0), np.float64(0.0)
         for _ in range(int(rng.integers(1, 10))):
             sw = spatial[int(rng.integers(len(spatial)))]
             nw = rnd(rng, 2.0**-25, 1.0) if rng.random() < 0.9 else float(np.float32(rng.integers(1, 64) / 64.0))
@@ -128,22 +109,7 @@ def test_weights_products_and_sums_match_ieee_double():
             assert value(pv) == want_w * np.float64(imp)
             acc = acc + want_w * np.float64(imp)
             xacc = xacc + np.float64(value(pv))
-            wsum = xd_add(wsum, wn)
-            ws_ref = ws_ref + want_w
-            assert value(wsum) == ws_ref
             assert xacc == acc
-
-
-def test_sums_match_ieee_double_and_ties_round_to_even():
-    rng = np.random.default_rng(11)
-    for _ in range(20000):
-        e = int(rng.integers(-60, 10))
-        a = np.float64(int(rng.integers(1 << 52, 1 << 53))) * 2.0**e
-        b = np.float64(int(rng.integers(1 << 52, 1 << 53))) * 2.0 ** (e - int(rng.integers(1, 60)))
-        half = np.float64(2.0 ** (e - 1))
-        for bb in (b, half, 3 * half, half * (1 + 2.0**-52), half * (1 - 2.0**-53)):
-            got = value(xd_add(parts_of_double(float(a)), parts_of_double(float(bb))))
-            assert got == a + bb, (a, bb)
 
 
 def test_quotient_matches_double_then_float_rounding():
