@@ -232,9 +232,11 @@ __device__ __forceinline__ uint16_t lane4h(const uint2& v, int i) {
 
 // VEC4: every present plane is 16-byte aligned at the pixel's first sample and the pixel's
 // sample count is a multiple of 4, so each plane is read four samples per load. COMPACT: the
-// planes are rpd_sample_soa16's (s.c16), decoded to float here.
-template <bool VEC4, bool COMPACT, bool WIDE>
-__global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets,
+// planes are rpd_sample_soa16's (s.c16), decoded to float here. MINB: resident blocks per SM
+// the register allocation must allow (the pass is latency-bound; more resident pixels beat
+// the few spills that buys).
+template <bool VEC4, bool COMPACT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets,
                                                            int32_t spp, int64_t first, int64_t count, GridPrep gp) {
     const int64_t local = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (local >= count) return;
@@ -295,20 +297,15 @@ __global__ void __launch_bounds__(128) k_accumulate_pixels(PixelPlanes p, Device
         const DeviceSamples16& h = s.c16;
         const float dscale = h.depth_scale;
         if (VEC4) {
-            // V samples per plane load: 8 (16-byte loads) when WIDE, else 4 (8-byte loads)
-            constexpr int V = WIDE ? 8 : 4;
+            // 4 samples per plane load (8-byte loads)
+            constexpr int V = 4;
             constexpr int NW = V / 2;  // 32-bit words per load
             struct Wv { uint32_t w[NW]; };
             auto ldv = [](const void* ptr, int64_t k) {
                 Wv r;
-                if (WIDE) {
-                    const uint4 v = *reinterpret_cast<const uint4*>(static_cast<const uint16_t*>(ptr) + k);
-                    r.w[0] = v.x; r.w[NW > 1 ? 1 : 0] = v.y;
-                    if (NW > 2) { r.w[NW > 2 ? 2 : 0] = v.z; r.w[NW > 3 ? 3 : 0] = v.w; }
-                } else {
-                    const uint2 v = *reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(ptr) + k);
-                    r.w[0] = v.x; r.w[NW > 1 ? 1 : 0] = v.y;
-                }
+                const uint2 v = *reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(ptr) + k);
+                r.w[0] = v.x;
+                r.w[1] = v.y;
                 return r;
             };
             auto lane16 = [](const Wv& v, int i) { return uint16_t(v.w[i >> 1] >> (16 * (i & 1))); };
@@ -766,27 +763,18 @@ cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t fir
     }
     vec4 = vec4 && (!gp.lum || (aligned(gp.lum, 16) && aligned(gp.key, 16)));
     const unsigned blocks = grid_for(count, 128);
+    // resident blocks per SM, measured on GB300: compact planes 4 (vector loads) and 5; FP32
+    // planes 3 (vector loads) and 5
     if (s.compact) {
-        // 16-byte loads of 8 samples when every present plane allows them
-        bool wide = vec4 && spp % 8 == 0;
-        const DeviceSamples16& h = s.c16;
-        for (int c = 0; c < 3; ++c) wide = wide && aligned(h.sqrt_radiance[c], 16) && aligned(h.normal[c], 16);
-        wide = wide && aligned(h.depth, 16);
-        for (int c = 0; c < 2; ++c)
-            wide = wide && (!h.pixel_u[0] || aligned(h.pixel_u[c], 16)) && (!h.lens_u[0] || aligned(h.lens_u[c], 16)) &&
-                   (!h.brdf_u[0] || aligned(h.brdf_u[c], 16)) && (!h.light_u[0] || aligned(h.light_u[c], 16)) &&
-                   (!h.env_u[0] || aligned(h.env_u[c], 16));
-        if (wide)
-            k_accumulate_pixels<true, true, true><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
-        else if (vec4)
-            k_accumulate_pixels<true, true, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        if (vec4)
+            k_accumulate_pixels<true, true, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
         else
-            k_accumulate_pixels<false, true, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<false, true, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     } else {
         if (vec4)
-            k_accumulate_pixels<true, false, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<true, false, 3><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
         else
-            k_accumulate_pixels<false, false, false><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<false, false, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     }
     j.launches += 1;
     return cudaGetLastError();

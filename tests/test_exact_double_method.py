@@ -1,10 +1,9 @@
-"""The method of the importance smoothing's integer arithmetic (csrc/k_adaptive.cu: float_parts,
-xd_mul24, xd_exact48, quotient_to_float), restated in Python integers and checked against IEEE
-754 arithmetic (numpy float64 and float32): the weight products of three floats, the products
-with the importance (summed as doubles, as the kernel sums them), and the final
-float(accum / weight_sum), on random operands across wide exponent ranges and on quotients at
-float midpoints. The CUDA kernel itself is compared with the double-precision instructions in
-tests/test_gpu_smoothing.py."""
+"""The importance smoothing's integer arithmetic (csrc/k_adaptive.cu: float_parts, xd_mul24,
+xd_exact48, quotient_to_float) restated in Python integers and checked against IEEE 754
+arithmetic (numpy float64 and float32): the weight products of three floats, the products with
+the importance (summed as doubles, as the kernel sums them) and the final float(accum /
+weight_sum), on operands across wide exponent ranges and on quotients at float midpoints. The
+kernel itself is compared with the double-precision path in tests/test_gpu_smoothing.py."""
 from __future__ import annotations
 
 import struct
@@ -132,3 +131,4 @@ def test_quotient_matches_double_then_float_rounding():
         else:
             assert np.float32(got) == want, (a, w, got, want)
     assert fallbacks < trials // 4 + trials // 50  # the constructed midpoints and about 1/128 of the rest
+
