@@ -653,6 +653,17 @@ __global__ void __launch_bounds__(128) k_grid_ordered(Geometry g, double* pass_g
     acc[35] = y2_sum;
 }
 
+// float -> double from the bits (the conversion instruction runs on the double-precision pipe,
+// 2 per SM per clock); zeros keep their sign, subnormals, infinities and NaN convert as usual.
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t b = __float_as_uint(f);
+    if ((b & 0x7fffffffu) == 0u) return __longlong_as_double(static_cast<long long>(uint64_t(b) << 32));
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return double(f);
+    return __longlong_as_double(static_cast<long long>((uint64_t(b >> 31) << 63) | (uint64_t(e + 896u) << 52) |
+                                                       (uint64_t(b & 0x7fffffu) << 29)));
+}
+
 // grid += pass (the first pass of a frame: grid = 0 + pass), then clear the pass grid. The
 // fast path's pass grid holds double-float pairs (hi, lo) in the bytes of each double.
 template <bool DF, bool FRESH>
@@ -662,7 +673,7 @@ __global__ void k_merge_grid(double* grid, double* pass_grid, int64_t n) {
     double v;
     if (DF) {
         const float2 p = reinterpret_cast<const float2*>(pass_grid)[i];
-        v = double(p.x) + double(p.y);
+        v = widen(p.x) + widen(p.y);
     } else {
         v = pass_grid[i];
     }

@@ -321,7 +321,7 @@ __device__ __forceinline__ bool fell_back(AllocScalars* sc) { return *(volatile 
 // ---- block-level helpers --------------------------------------------------------------------
 struct Shared {
     EF warp_ef[2][kAWarps];
-    double warp_d[kAWarps];
+    float2 warp_f2[kAWarps];
     long long warp_l[kAWarps];
     int warp_i[kAWarps];
     double own_pred[kMaxOwned];
@@ -384,16 +384,76 @@ __device__ void block_scan_ef(EF (&tf)[N], EF (&ex)[N], EF (&total)[N], Shared& 
     __syncthreads();
 }
 
-__device__ double block_sum_d(double v, Shared& sh) {
+// Double-float (h + l) sums for the approximate chain values: the chunk sums, their prefix and the
+// split prediction need about 2^-40 relative accuracy, which pairs of floats give on the FP32 pipes
+// (a chain of double-precision additions waits on each one at 2 per SM per clock).
+struct DF {
+    float h, l;
+};
+
+__device__ __forceinline__ void df_acc(DF& a, float x) {  // a += x, the rounding error kept in l
+    const float s = a.h + x;
+    const float bb = s - a.h;
+    a.l += (a.h - (s - bb)) + (x - bb);
+    a.h = s;
+}
+
+__device__ __forceinline__ DF df_sum(DF a, DF b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb);
+    const float l = e + (a.l + b.l);
+    const float h = s + l;
+    return DF{h, l - (h - s)};
+}
+
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ double df_value(DF a) { return double(a.h) + double(a.l); }
+__device__ __forceinline__ DF df_of(double v) {
+    const float h = __double2float_rn(v);
+    return DF{h, __double2float_rn(v - double(h))};
+}
+__device__ __forceinline__ DF shfl_down_df(DF a, int d) {
+    return DF{__shfl_down_sync(0xffffffffu, a.h, d), __shfl_down_sync(0xffffffffu, a.l, d)};
+}
+__device__ __forceinline__ DF shfl_up_df(DF a, int d) {
+    return DF{__shfl_up_sync(0xffffffffu, a.h, d), __shfl_up_sync(0xffffffffu, a.l, d)};
+}
+
+__device__ DF block_sum_df(DF v, Shared& sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
-    if (lane == 0) sh.warp_d[warp] = v;
+    for (int d = 16; d > 0; d >>= 1) v = df_sum(v, shfl_down_df(v, d));
+    if (lane == 0) sh.warp_f2[warp] = make_float2(v.h, v.l);
     __syncthreads();
-    double t = 0.0;
-    for (int w = 0; w < kAWarps; ++w) t += sh.warp_d[w];
+    DF t{0.0f, 0.0f};
+    for (int w = 0; w < kAWarps; ++w) t = df_sum(t, DF{sh.warp_f2[w].x, sh.warp_f2[w].y});
     __syncthreads();
     return t;
+}
+
+// Exclusive scan of double-floats over the block's threads; *total gets the block's sum.
+__device__ DF block_exscan_df(DF v, DF* total, Shared& sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    DF inc = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const DF o = shfl_up_df(inc, d);
+        if (lane >= d) inc = df_sum(o, inc);
+    }
+    DF ex = shfl_up_df(inc, 1);
+    if (lane == 0) ex = DF{0.0f, 0.0f};
+    if (lane == 31) sh.warp_f2[warp] = make_float2(inc.h, inc.l);
+    __syncthreads();
+    DF before{0.0f, 0.0f}, all{0.0f, 0.0f};
+    for (int w = 0; w < kAWarps; ++w) {
+        const DF t{sh.warp_f2[w].x, sh.warp_f2[w].y};
+        if (w < warp) before = df_sum(before, t);
+        all = df_sum(all, t);
+    }
+    __syncthreads();
+    *total = all;
+    return df_sum(before, ex);
 }
 
 __device__ float block_sum_f(float v, Shared& sh) {
@@ -467,27 +527,6 @@ __device__ unsigned long long block_scan_u64(unsigned long long v, Shared& sh) {
     unsigned long long before = 0;
     for (int w = 0; w < warp; ++w) before += (unsigned long long)sh.warp_l[w];
     __syncthreads();
-    return before + inc - v;
-}
-
-// Exclusive scan of a double over threads; *total gets the block's sum.
-__device__ double block_exscan_d(double v, double* total, Shared& sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double inc = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const double o = __shfl_up_sync(0xffffffffu, inc, d);
-        if (lane >= d) inc += o;
-    }
-    if (lane == 31) sh.warp_d[warp] = inc;
-    __syncthreads();
-    double before = 0.0, all = 0.0;
-    for (int w = 0; w < kAWarps; ++w) {
-        if (w < warp) before += sh.warp_d[w];
-        all += sh.warp_d[w];
-    }
-    __syncthreads();
-    *total = all;
     return before + inc - v;
 }
 
@@ -1037,31 +1076,15 @@ __device__ unsigned long long block_sum_sat(unsigned long long v, Shared& sh) {
 // takes them whole).
 __device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, double s0, int sign, int F, Shared& sh) {
     const int G = gridDim.x;
-    double carry = s0;
+    DF carry = df_of(s0);
     for (int t0 = 0; t0 < a.nch; t0 += kAT) {
         const int c = t0 + threadIdx.x;
-        const double v = c < a.nch ? __ldcg(&a.rec[c].approx) : 0.0;
-        // inclusive warp scan, then warps in order
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        double inc = v;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const double o = __shfl_up_sync(0xffffffffu, inc, d);
-            if (lane >= d) inc += o;
-        }
-        if (lane == 31) sh.warp_d[warp] = inc;
-        __syncthreads();
-        double before = 0.0, all = 0.0;
-        for (int w = 0; w < kAWarps; ++w) {
-            if (w < warp) before += sh.warp_d[w];
-            all += sh.warp_d[w];
-        }
-        if (c < a.nch && c % G == int(blockIdx.x)) {
-            const double pred = sign > 0 ? carry + (before + inc - v) : carry - (before + inc - v);
-            sh.own_pred[c / G] = pred;
-        }
-        __syncthreads();
-        carry = sign > 0 ? carry + all : carry - all;
+        const DF v = c < a.nch ? df_of(__ldcg(&a.rec[c].approx)) : DF{0.0f, 0.0f};
+        DF all;
+        const DF ex = block_exscan_df(v, &all, sh);
+        if (c < a.nch && c % G == int(blockIdx.x))
+            sh.own_pred[c / G] = df_value(df_sum(carry, sign > 0 ? ex : df_neg(ex)));
+        carry = df_sum(carry, sign > 0 ? all : df_neg(all));
     }
     __syncthreads();
     const bool region = F != kNoRegion && sign > 0 && s0 == 0.0;
@@ -1099,18 +1122,22 @@ __device__ void phase_predicted_actions(const CoopArgs& a, const Src& src, doubl
             if (sign > 0 && E0 < 898 && pend >= pow2d(E0 + 1) && pend < pow2d(E0 + 2)) {
                 const int base = threadIdx.x * kAV;
                 const int len = __ldcg(&a.rec[c].len);
-                double loc = 0.0;
+                DF loc{0.0f, 0.0f};
 #pragma unroll
-                for (int e = 0; e < kAV; ++e) loc += double(x[e]);
-                double tot;
-                const double ex = block_exscan_d(loc, &tot, sh);
-                const double edge = pow2d(E0 + 1);
-                double run = pred + ex;
+                for (int e = 0; e < kAV; ++e) df_acc(loc, x[e]);
+                DF tot;
+                const DF ex = block_exscan_df(loc, &tot, sh);
+                // the running sum against 2^(E0+1) (a float when E0 + 1 is within the float range)
+                const bool fits = E0 + 1 >= -125 && E0 + 1 <= 126;
+                const float edgef = fits ? __int_as_float((E0 + 1 + 127) << 23) : 0.0f;
+                DF run = df_sum(df_of(pred), ex);
                 int first = INT_MAX;
 #pragma unroll
                 for (int e = 0; e < kAV; ++e) {
-                    run += double(x[e]);
-                    if (first == INT_MAX && base + e < len && run >= edge) first = base + e;
+                    df_acc(run, x[e]);
+                    const float h = run.h + run.l, l = run.l - (h - run.h);
+                    if (fits && first == INT_MAX && base + e < len && (h > edgef || (h == edgef && l >= 0.0f)))
+                        first = base + e;
                 }
                 const int kx = block_min_i(first, sh);
                 if (kx < len) {
@@ -1282,18 +1309,18 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
             float I[kAV];
             load_f8(a.importance, k0, a.np, I);
-            double acc = 0.0;  // double: the split prediction needs chunk starts to ~1e-12
+            DF acc{0.0f, 0.0f};  // the split prediction needs chunk starts to ~2^-40
             uint8_t st[kAV];
 #pragma unroll
             for (int e = 0; e < kAV; ++e) {
                 if (!(I[e] >= 0.0f && I[e] <= FLT_MAX)) bad = 1;
                 if (I[e] > 0.0f) code = max(code, 1000 - float_exp(I[e]));
-                acc += double(I[e]);
+                df_acc(acc, I[e]);
                 st[e] = 1u;
                 if (k0 + e < a.np) a.desired_add[k0 + e] = 0.0f;
             }
             store_u8(a.state, k0, a.np, st);
-            const double t = block_sum_d(acc, sh);
+            const double t = df_value(block_sum_df(acc, sh));
             if (threadIdx.x == 0) {
                 a.rec[c].approx = t;
                 a.rec[c].len = int(min((long long)kAL, (long long)(a.np - int64_t(c) * kAL)));
@@ -1407,7 +1434,7 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
         const double Rsd = double(Rs);
         for (int c = blockIdx.x; c < a.nch; c += G) {
             const int64_t k0 = int64_t(c) * kAL + threadIdx.x * kAV;
-            double acc = 0.0;
+            DF acc{0.0f, 0.0f};
             float I[kAV];
             uint8_t st[kAV];
             if (shares) {
@@ -1424,9 +1451,9 @@ __global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
                 const float r = fmaxs(0.0f, d - float(add));
                 a.residual[k0 + e] = r;
                 if (r > 0.0f) code = max(code, 1000 - float_exp(r));
-                acc += double(r);
+                df_acc(acc, r);
             }
-            const double t = block_sum_d(acc, sh);
+            const double t = df_value(block_sum_df(acc, sh));
             if (threadIdx.x == 0) {
                 a.rec[c].approx = t;
                 a.rec[c].clips = 0;

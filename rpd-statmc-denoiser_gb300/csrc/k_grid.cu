@@ -669,6 +669,7 @@ struct RowTable {
     float ay[32];      // the row's y factor
     int p0[32];        // first pixel of the segment, relative to the push (varying counts)
     int npx[32];       // pixels in the segment
+    int len[32];       // samples in the segment
 };
 
 // Everything a warp's walk needs.
@@ -730,14 +731,84 @@ __device__ __forceinline__ void rand_update(const WalkCtx<INT_W, DS>& c, uint32_
     }
 }
 
-// The flat walk of one row-segment chunk (total samples) for dimension set SET.
-template <bool INT_W, int DS, int SET, bool VEC>
+// Walk modes: samples one by one (0); quads of 4 samples of one pixel (1, uniform counts); aligned
+// quads of 4 consecutive samples of the push with each sample's column (2, per-pixel counts).
+constexpr int kWalkScalar = 0, kWalkPixelQuads = 1, kWalkColumnQuads = 2;
+
+// The flat walk of one row-segment chunk (total samples, or total quads in the quad modes) for
+// dimension set SET.
+template <bool INT_W, int DS, int SET, int MODE>
 __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const RandParams& rp, const GridPrep& gp,
                                           const int64_t* offsets, int total) {
     const RowTable* rt = c.rt;
     const int lane = c.lane;
     int r = 0;  // current segment of this lane (monotone along its walk)
-    if (VEC) {
+    if (MODE == kWalkColumnQuads) {
+        // Quads of the push's samples 4Q .. 4Q+3 (16-byte loads of keys and luminances, 8 bytes of
+        // columns; the sample planes are padded to a multiple of 64 samples). A quad may start
+        // before the segment or run past it: those samples weigh nothing (the trash slot). The
+        // weights are formed when the quad is processed, one batch after its loads were issued.
+        constexpr int U = 2;
+        const int nq = total;
+        auto fetchq = [&](int q, uint4& kq, float4& yq, uint2& cq, int64_t& k4, int& seg) {
+            kq = make_uint4(0u, 0u, 0u, 0u);
+            yq = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            cq = make_uint2(0u, 0u);
+            k4 = 0;
+            seg = -1;
+            if (q >= nq) return;
+            while (q >= rt->base[r + 1]) ++r;
+            k4 = ((rt->k0[r] >> 2) + (q - rt->base[r])) << 2;
+            kq = *reinterpret_cast<const uint4*>(gp.key + k4);
+            yq = *reinterpret_cast<const float4*>(gp.lum + k4);
+            cq = *reinterpret_cast<const uint2*>(gp.col + k4);
+            seg = r;
+        };
+        uint4 nk[U];
+        float4 nyv[U];
+        uint2 ncq[U];
+        int64_t nk4[U];
+        int nseg[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) fetchq(lane + 32 * u, nk[u], nyv[u], ncq[u], nk4[u], nseg[u]);
+        for (int q0 = 0; q0 < nq; q0 += 32 * U) {
+            uint4 ck[U];
+            float4 cy[U];
+            uint2 ccq[U];
+            int64_t ck4[U];
+            int cseg[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                ck[u] = nk[u];
+                cy[u] = nyv[u];
+                ccq[u] = ncq[u];
+                ck4[u] = nk4[u];
+                cseg[u] = nseg[u];
+            }
+            if (q0 + 32 * U < nq) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) fetchq(q0 + 32 * U + lane + 32 * u, nk[u], nyv[u], ncq[u], nk4[u], nseg[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                if (cseg[u] >= 0) {
+                    const int64_t ks = rt->k0[cseg[u]], ke = ks + rt->len[cseg[u]];
+                    const float ay = rt->ay[cseg[u]];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int64_t k = ck4[u] + i;
+                        const int ci = int(((i < 2 ? ccq[u].x : ccq[u].y) >> (16 * (i & 1))) & 0xffffu) - c.xlo;
+                        if (k >= ks && k < ke && unsigned(ci) < unsigned(rp.cols)) w[i] = c.xf[ci] * ay;
+                    }
+                }
+                rand_update<INT_W, DS, SET>(c, ck[u].x, w[0], INT_W ? uint32_t(w[0] * c.wscale) : 0u, cy[u].x);
+                rand_update<INT_W, DS, SET>(c, ck[u].y, w[1], INT_W ? uint32_t(w[1] * c.wscale) : 0u, cy[u].y);
+                rand_update<INT_W, DS, SET>(c, ck[u].z, w[2], INT_W ? uint32_t(w[2] * c.wscale) : 0u, cy[u].z);
+                rand_update<INT_W, DS, SET>(c, ck[u].w, w[3], INT_W ? uint32_t(w[3] * c.wscale) : 0u, cy[u].w);
+            }
+        }
+    } else if (MODE == kWalkPixelQuads) {
         // quads of 4 consecutive samples of one pixel (the samples per pixel are a power of two
         // >= 4 and every segment starts 16-byte aligned): one 16-byte load of keys and one of
         // luminances per quad, 2 quads per lane in flight
@@ -846,7 +917,7 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
     }
 }
 
-template <bool INT_W, int RW, int DS, bool VEC>
+template <bool INT_W, int RW, int DS, int MODE>
 __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, float2* pass_grid,
                                                               const int64_t* offsets, GridPrep gp) {
     constexpr int NW = RW * DS;
@@ -913,7 +984,7 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
     for (int c0 = 0; c0 < nrows; c0 += 32) {
         // ---- this chunk's row segments, one lane per row ----
         const int y = ylo + rgroup + RW * (c0 + lane);
-        int n = 0;
+        int n = 0;  // the walk's units in the segment: samples, or quads in the column-quad mode
         if (c0 + lane < nrows && y <= yhi && xa <= xb) {
             const float ay = axis_factor(gpar, y, ny, g.nodes_y);
             int64_t p0 = int64_t(y) * g.w + xa, p1 = int64_t(y) * g.w + xb + 1;
@@ -921,8 +992,10 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
             p1 = p1 > gpar.first + gpar.count ? gpar.first + gpar.count : p1;
             if (ay > 0.0f && p0 < p1) {
                 const int64_t k0 = offsets[p0 - gpar.first];
-                n = int(offsets[p1 - gpar.first] - k0);
+                const int len = int(offsets[p1 - gpar.first] - k0);
+                n = MODE == kWalkColumnQuads ? (len > 0 ? int(((k0 + len - 1) >> 2) - (k0 >> 2) + 1) : 0) : len;
                 rt->k0[lane] = k0;
+                rt->len[lane] = len;
                 rt->col0[lane] = int(p0 - int64_t(y) * g.w) - xlo;
                 rt->ay[lane] = ay;
                 rt->p0[lane] = int(p0 - gpar.first);
@@ -938,9 +1011,9 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
         if (lane == 0) rt->base[0] = 0;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
-        if (dset == 0) rand_walk<INT_W, DS, 0, VEC>(c, rp, gp, offsets, total);
-        if (DS > 1 && dset == 1) rand_walk<INT_W, DS, 1, VEC>(c, rp, gp, offsets, total);
-        if (DS > 2 && dset == 2) rand_walk<INT_W, DS, 2, VEC>(c, rp, gp, offsets, total);
+        if (dset == 0) rand_walk<INT_W, DS, 0, MODE>(c, rp, gp, offsets, total);
+        if (DS > 1 && dset == 1) rand_walk<INT_W, DS, 1, MODE>(c, rp, gp, offsets, total);
+        if (DS > 2 && dset == 2) rand_walk<INT_W, DS, 2, MODE>(c, rp, gp, offsets, total);
         __syncwarp();
     }
     __syncthreads();
@@ -1029,28 +1102,31 @@ uint32_t spp_magic_for(int spp, int max_k) {
     return uint32_t(m);
 }
 
-template <bool INT_W, int RW, int DS, bool VEC>
+template <bool INT_W, int RW, int DS, int MODE>
 cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) {
     constexpr int NW = RW * DS;
     const size_t smem = size_t(NW) * RandLayout<INT_W, DS>::kWarpBytes + size_t(NW) * sizeof(RowTable) +
                         size_t(rp.cols) * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, RW, DS, VEC>,
+    cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, RW, DS, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     const unsigned nblocks = unsigned(rp.gp.count_nodes);
-    k_grid_random<INT_W, RW, DS, VEC><<<nblocks, NW * 32, smem, j.stream>>>(
+    k_grid_random<INT_W, RW, DS, MODE><<<nblocks, NW * 32, smem, j.stream>>>(
         rp, reinterpret_cast<float2*>(j.n.pass_grid), j.offsets, gp);
     j.launches += 1;
     return cudaGetLastError();
 }
 
-// quads need samples per pixel a multiple of 4 (and a power of two, for the shift) with
-// 16-byte aligned key and luminance planes
+// Pixel quads need samples per pixel a multiple of 4 (and a power of two, for the shift) with
+// 16-byte aligned key and luminance planes; column quads need the per-sample columns (per-pixel
+// counts) with 16-byte aligned key and luminance planes and an 8-byte aligned column plane.
 template <bool INT_W, int RW, int DS>
 cudaError_t launch_random(Job& j, const RandParams& rp, const GridPrep& gp) {
-    const bool vec = rp.spp_shift >= 2 && (reinterpret_cast<uintptr_t>(gp.key) & 15u) == 0 &&
-                     (reinterpret_cast<uintptr_t>(gp.lum) & 15u) == 0;
-    return vec ? launch_random_vec<INT_W, RW, DS, true>(j, rp, gp) : launch_random_vec<INT_W, RW, DS, false>(j, rp, gp);
+    const bool aligned = (reinterpret_cast<uintptr_t>(gp.key) & 15u) == 0 && (reinterpret_cast<uintptr_t>(gp.lum) & 15u) == 0;
+    if (rp.spp_shift >= 2 && aligned) return launch_random_vec<INT_W, RW, DS, kWalkPixelQuads>(j, rp, gp);
+    if (gp.col && aligned && (reinterpret_cast<uintptr_t>(gp.col) & 7u) == 0)
+        return launch_random_vec<INT_W, RW, DS, kWalkColumnQuads>(j, rp, gp);
+    return launch_random_vec<INT_W, RW, DS, kWalkScalar>(j, rp, gp);
 }
 
 template <bool INT_W>
