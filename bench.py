@@ -556,7 +556,8 @@ def run_serving(args):
     knobs = serving_knobs(R)
     n_req = args.steps
     stream = request_stream(n_req, args.rate, SEED + 1000 * rank)
-    srv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=args.inflight, storage=args.storage)
+    srv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=args.inflight, storage=args.storage,
+                   allocator_blocks=args.alloc_blocks)
     # warm-up: a few requests of every size (creates the cached jobs, fills the buffer pool)
     for k in range(max(1, args.warmup)):
         for (w, h) in SIZES:
@@ -643,6 +644,7 @@ def run_serving(args):
                                   f"from {SPPS}, adaptive_passes 3, adaptive_spp 4, base samples 1; samples of every "
                                   f"pass generated on the device (seed {SEED})",
                       "step": "one request", "hbm_budget_gb": args.budget_gb, "max_inflight": args.inflight,
+                      "allocator_blocks": args.alloc_blocks,
                       "storage": args.storage, "samples": samples, "wall_s": round(wall_s, 4),
                       "l2": "sample planes of every request larger than L2 except the 256x256 ones",
                       "parallelism": "replicas"},
@@ -730,6 +732,8 @@ def main():
     ap.add_argument("--budget-gb", type=int, default=120, help="serving: HBM admission budget")
     ap.add_argument("--inflight", type=int, default=32, help="serving: requests on the GPU at once")
     ap.add_argument("--storage", choices=["fp16", "fp32"], default="fp16", help="serving: sample storage")
+    ap.add_argument("--alloc-blocks", type=int, default=0,
+                    help="serving: blocks of each request's parallel adaptive allocation (0: one per SM)")
     ap.add_argument("--plain-requests", type=int, default=200, help="serving: stream prefix run through the plain drop-in")
     ap.add_argument("--passes", type=int, default=1, help="request: adaptive passes of the profiled request")
     args = ap.parse_args()

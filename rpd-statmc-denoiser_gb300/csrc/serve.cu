@@ -495,6 +495,7 @@ int acquire_job(Server& s, Request& r, Job** out) {
     if (st != RPD_OK) return st;
     Job* j = reinterpret_cast<Job*>(h);
     if (s.cfg.profile) rpd_job_set_profiling(h, 1);
+    if (s.cfg.allocator_blocks >= 2) rpd_job_set_tuning(h, RPD_TUNE_ALLOCATOR, s.cfg.allocator_blocks);
     st = job_reserve(*j, need_span);
     if (st != RPD_OK) {
         rpd_job_destroy(h);
@@ -681,6 +682,8 @@ int rpd_server_create(rpd_ctx* ctx, const rpd_server_config* cfg, rpd_server** o
         return fail(RPD_ERR_INVALID_ARGUMENT, "max_inflight must be 1..256");
     if (cfg->storage != RPD_STORAGE_FP32 && cfg->storage != RPD_STORAGE_FP16)
         return fail(RPD_ERR_INVALID_ARGUMENT, "unknown sample storage");
+    if (cfg->allocator_blocks < 0 || cfg->allocator_blocks == 1 || cfg->allocator_blocks > 4096)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "allocator_blocks must be 0 or 2..4096");
     {
         rpd_config probe = cfg->knobs;
         probe.image_width = std::max(probe.image_width, 1);

@@ -140,7 +140,7 @@ class SynthParams(C.Structure):
 class ServerConfig(C.Structure):
     """rpd_server_config."""
     _fields_ = [("knobs", Config), ("hbm_budget_bytes", C.c_uint64), ("max_inflight", C.c_int32),
-                ("storage", C.c_int32), ("profile", C.c_int32)]
+                ("storage", C.c_int32), ("profile", C.c_int32), ("allocator_blocks", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -785,7 +785,7 @@ class Server:
     """rpd_server: the serving loop (continuous batching of denoise requests)."""
 
     def __init__(self, ctx: Context, knobs: Config, budget_bytes: int = 0, max_inflight: int = 16,
-                 storage: str = "fp16", profile: bool = False):
+                 storage: str = "fp16", profile: bool = False, allocator_blocks: int = 0):
         cfg = ServerConfig()
         lib().rpd_server_config_defaults(C.byref(cfg))
         cfg.knobs = knobs
@@ -793,6 +793,7 @@ class Server:
         cfg.max_inflight = max_inflight
         cfg.storage = STORAGE[storage]
         cfg.profile = 1 if profile else 0
+        cfg.allocator_blocks = allocator_blocks
         h = C.c_void_p()
         check(lib().rpd_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
         self.handle = h.value
