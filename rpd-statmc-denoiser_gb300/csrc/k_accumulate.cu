@@ -232,10 +232,9 @@ __device__ __forceinline__ uint16_t lane4h(const uint2& v, int i) {
 
 // VEC4: every present plane is 16-byte aligned at the pixel's first sample and the pixel's
 // sample count is a multiple of 4, so each plane is read four samples per load. COMPACT: the
-// planes are rpd_sample_soa16's (s.c16), decoded to float here. MINB: resident blocks per SM
-// the register allocation must allow (the pass is latency-bound; more resident pixels beat
-// the few spills that buys).
-template <bool VEC4, bool COMPACT, int MINB>
+// planes are rpd_sample_soa16's (s.c16), decoded to float here; WIDE reads them 8 samples (16
+// bytes) per load. MINB: resident blocks per SM the register allocation must allow.
+template <bool VEC4, bool COMPACT, bool WIDE, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets,
                                                            int32_t spp, int64_t first, int64_t count, GridPrep gp) {
     const int64_t local = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -297,15 +296,23 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
         const DeviceSamples16& h = s.c16;
         const float dscale = h.depth_scale;
         if (VEC4) {
-            // 4 samples per plane load (8-byte loads)
-            constexpr int V = 4;
+            // V samples per plane load: 8 (16-byte loads) when WIDE, else 4 (8-byte loads)
+            constexpr int V = WIDE ? 8 : 4;
             constexpr int NW = V / 2;  // 32-bit words per load
             struct Wv { uint32_t w[NW]; };
             auto ldv = [](const void* ptr, int64_t k) {
                 Wv r;
-                const uint2 v = *reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(ptr) + k);
-                r.w[0] = v.x;
-                r.w[1] = v.y;
+                if constexpr (WIDE) {
+                    const uint4 v = *reinterpret_cast<const uint4*>(static_cast<const uint16_t*>(ptr) + k);
+                    r.w[0] = v.x;
+                    r.w[1] = v.y;
+                    r.w[2] = v.z;
+                    r.w[3] = v.w;
+                } else {
+                    const uint2 v = *reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(ptr) + k);
+                    r.w[0] = v.x;
+                    r.w[1] = v.y;
+                }
                 return r;
             };
             auto lane16 = [](const Wv& v, int i) { return uint16_t(v.w[i >> 1] >> (16 * (i & 1))); };
@@ -776,16 +783,36 @@ cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t fir
     const unsigned blocks = grid_for(count, 128);
     // resident blocks per SM, measured on GB300: compact planes 4 (vector loads) and 5; FP32
     // planes 3 (vector loads) and 5
+    // Shapes measured on GB300 at 1920x1080. Up to 16 samples per pixel, more resident pixels
+    // hide the per-pixel latency (compact planes 4 blocks per SM, FP32 planes 3, per-pixel counts
+    // 5). From 32 on, a thread's sample run spans more bytes per plane than L1 keeps between its
+    // loads, and a block's registers are not capped; from 64 on, compact planes are read 16 bytes
+    // (8 samples) per load.
+    const bool many = spp > 16;
     if (s.compact) {
-        if (vec4)
-            k_accumulate_pixels<true, true, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        bool wide = vec4 && spp >= 64 && spp % 8 == 0;
+        const DeviceSamples16& h = s.c16;
+        for (int c = 0; c < 3; ++c) wide = wide && aligned(h.sqrt_radiance[c], 16) && aligned(h.normal[c], 16);
+        wide = wide && aligned(h.depth, 16);
+        for (int c = 0; c < 2; ++c)
+            wide = wide && (!h.pixel_u[0] || aligned(h.pixel_u[c], 16)) && (!h.lens_u[0] || aligned(h.lens_u[c], 16)) &&
+                   (!h.brdf_u[0] || aligned(h.brdf_u[c], 16)) && (!h.light_u[0] || aligned(h.light_u[c], 16)) &&
+                   (!h.env_u[0] || aligned(h.env_u[c], 16));
+        if (wide)
+            k_accumulate_pixels<true, true, true, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else if (vec4 && many)
+            k_accumulate_pixels<true, true, false, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else if (vec4)
+            k_accumulate_pixels<true, true, false, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
         else
-            k_accumulate_pixels<false, true, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<false, true, false, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     } else {
-        if (vec4)
-            k_accumulate_pixels<true, false, 3><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        if (vec4 && many)
+            k_accumulate_pixels<true, false, false, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+        else if (vec4)
+            k_accumulate_pixels<true, false, false, 3><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
         else
-            k_accumulate_pixels<false, false, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<false, false, false, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     }
     j.launches += 1;
     return cudaGetLastError();
