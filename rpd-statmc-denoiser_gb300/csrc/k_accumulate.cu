@@ -109,7 +109,12 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
 struct SampleIn {
     float L[3], n[3], d, alb[3], pu[2], lu[2], bu[2], liu[2], eu[2];
     uint8_t f, cat;
+    uint32_t bins;  // RAW_BINS: the lens, BRDF, light and environment bins, 4 bits each
 };
+
+// Dependency2D::add's bin of a compact (unorm16) pair: u = q / 65536 exactly, so
+// int(u * 4) = q >> 14, already within 0..3 (core/stats.h:166-168)
+__device__ __forceinline__ uint32_t bin2d_q(uint16_t qu, uint16_t qv) { return uint32_t(qv >> 14) * 4u + uint32_t(qu >> 14); }
 
 // Per-pixel running state of the statistics pass.
 struct PixelAcc {
@@ -127,6 +132,7 @@ struct PixelAcc {
     uint8_t pflags;
 };
 
+template <bool RAW_BINS = false>
 __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, bool per_sample_albedo,
                                                const float* palb, bool prep, uint8_t plane_mask, float fx,
                                                float fy, float& lum_out, uint32_t& key_out) {
@@ -166,10 +172,15 @@ __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, 
     const uint8_t fm = in.f & plane_mask;
     // packed random-dimension bins (Dependency2D::add, core/stats.h:166-168)
     uint32_t key = 0;
-    if (fm & RPD_SAMPLE_LENS_VALID) key |= uint32_t(bin2d_k(in.lu[0], in.lu[1]));
-    if (fm & RPD_SAMPLE_BRDF_VALID) key |= uint32_t(bin2d_k(in.bu[0], in.bu[1])) << 4;
-    if (fm & RPD_SAMPLE_LIGHT_VALID) key |= uint32_t(bin2d_k(in.liu[0], in.liu[1])) << 8;
-    if (fm & RPD_SAMPLE_ENV_VALID) key |= uint32_t(bin2d_k(in.eu[0], in.eu[1])) << 12;
+    if (RAW_BINS) {
+        key = in.bins & ((fm & RPD_SAMPLE_LENS_VALID ? 0x000fu : 0u) | (fm & RPD_SAMPLE_BRDF_VALID ? 0x00f0u : 0u) |
+                         (fm & RPD_SAMPLE_LIGHT_VALID ? 0x0f00u : 0u) | (fm & RPD_SAMPLE_ENV_VALID ? 0xf000u : 0u));
+    } else {
+        if (fm & RPD_SAMPLE_LENS_VALID) key |= uint32_t(bin2d_k(in.lu[0], in.lu[1]));
+        if (fm & RPD_SAMPLE_BRDF_VALID) key |= uint32_t(bin2d_k(in.bu[0], in.bu[1])) << 4;
+        if (fm & RPD_SAMPLE_LIGHT_VALID) key |= uint32_t(bin2d_k(in.liu[0], in.liu[1])) << 8;
+        if (fm & RPD_SAMPLE_ENV_VALID) key |= uint32_t(bin2d_k(in.eu[0], in.eu[1])) << 12;
+    }
     key |= uint32_t(in.cat & RPD_CATEGORY_LIGHT_INDEX_MASK) << 16;
     key |= (in.cat & RPD_CATEGORY_RR_SURVIVED) ? (1u << 20) : 0u;
     key |= uint32_t(fm & 0xfe) << (kKeyValidShift - 1);
@@ -348,16 +359,14 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
                         in.alb[c] = 0.0f;
                     }
                     in.d = h2f(lane16(D, i)) * dscale;
-                    for (int c = 0; c < 2; ++c) {
-                        in.pu[c] = unorm16(lane16(PU[c], i));
-                        in.lu[c] = unorm16(lane16(LU[c], i));
-                        in.bu[c] = unorm16(lane16(BU[c], i));
-                        in.liu[c] = unorm16(lane16(LI[c], i));
-                        in.eu[c] = unorm16(lane16(EU[c], i));
-                    }
+                    for (int c = 0; c < 2; ++c) in.pu[c] = unorm16(lane16(PU[c], i));
+                    in.bins = bin2d_q(lane16(LU[0], i), lane16(LU[1], i)) |
+                              (bin2d_q(lane16(BU[0], i), lane16(BU[1], i)) << 4) |
+                              (bin2d_q(lane16(LI[0], i), lane16(LI[1], i)) << 8) |
+                              (bin2d_q(lane16(EU[0], i), lane16(EU[1], i)) << 12);
                     in.f = uint8_t(F[i >> 2] >> (8 * (i & 3)));
                     in.cat = uint8_t(Cg[i >> 2] >> (8 * (i & 3)));
-                    process_sample(a, in, false, palb, prep, plane_mask, fx, fy, lumv[i], keyv[i]);
+                    process_sample<true>(a, in, false, palb, prep, plane_mask, fx, fy, lumv[i], keyv[i]);
                 }
                 if (prep) {
                     for (int q = 0; q < V / 4; ++q) {
@@ -377,18 +386,21 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
                     in.alb[c] = 0.0f;
                 }
                 in.d = h2f(h.depth[k]) * dscale;
+                uint16_t q[4][2];
                 for (int c = 0; c < 2; ++c) {
                     in.pu[c] = (dims && has_pu) ? unorm16(h.pixel_u[c][k]) : 0.0f;
-                    in.lu[c] = (dims && has_lu) ? unorm16(h.lens_u[c][k]) : 0.0f;
-                    in.bu[c] = (dims && has_bu) ? unorm16(h.brdf_u[c][k]) : 0.0f;
-                    in.liu[c] = (dims && has_li) ? unorm16(h.light_u[c][k]) : 0.0f;
-                    in.eu[c] = (dims && has_eu) ? unorm16(h.env_u[c][k]) : 0.0f;
+                    q[0][c] = (dims && has_lu) ? h.lens_u[c][k] : uint16_t(0);
+                    q[1][c] = (dims && has_bu) ? h.brdf_u[c][k] : uint16_t(0);
+                    q[2][c] = (dims && has_li) ? h.light_u[c][k] : uint16_t(0);
+                    q[3][c] = (dims && has_eu) ? h.env_u[c][k] : uint16_t(0);
                 }
+                in.bins = bin2d_q(q[0][0], q[0][1]) | (bin2d_q(q[1][0], q[1][1]) << 4) |
+                          (bin2d_q(q[2][0], q[2][1]) << 8) | (bin2d_q(q[3][0], q[3][1]) << 12);
                 in.f = s.flags[k];
                 in.cat = (dims && s.category) ? s.category[k] : 0;
                 float lum;
                 uint32_t key;
-                process_sample(a, in, false, palb, prep, plane_mask, fx, fy, lum, key);
+                process_sample<true>(a, in, false, palb, prep, plane_mask, fx, fy, lum, key);
                 if (prep) {
                     gp.lum[k] = lum;
                     gp.key[k] = key;
