@@ -118,16 +118,20 @@ __device__ __forceinline__ void srv_write(const SynthOut& o, int64_t k, const rp
 }
 
 // spp samples for every pixel, sample q of pixel i at index i * spp + q, ordinals start + q.
+// One block row per image row (blockIdx.y): the row-local sample index splits into the column
+// and q with a shift when spp is a power of two (spp_shift >= 0), else a 32-bit division.
 __global__ void k_srv_synth_uniform(rpd_synth_params prm, const rpd_synth_region* table, const uint8_t* region,
-                                    int64_t np, int32_t spp, uint32_t start, SynthOut o) {
-    const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (k >= np * spp) return;
-    const int64_t i = k / spp;
-    const int q = int(k - i * spp);
-    const int x = int(i % prm.width), y = int(i / prm.width);
+                                    int32_t spp, int spp_shift, int y0, uint32_t start, SynthOut o) {
+    const uint32_t rk = blockIdx.x * blockDim.x + threadIdx.x;  // sample within the row
+    const uint32_t row_samples = uint32_t(prm.width) * uint32_t(spp);
+    if (rk >= row_samples) return;
+    const int y = y0 + int(blockIdx.y);
+    const uint32_t x = spp_shift >= 0 ? rk >> spp_shift : rk / uint32_t(spp);
+    const uint32_t q = rk - x * uint32_t(spp);
+    const int64_t i = int64_t(y) * prm.width + x;
     rpd_synth_sample s;
-    rpd_synth_sample_make(&prm, &table[region[i]], x, y, start + uint32_t(q), &s);
-    srv_write(o, k, s);
+    rpd_synth_sample_make(&prm, &table[region[i]], int(x), y, start + q, &s);
+    srv_write(o, int64_t(y) * row_samples + rk, s);
 }
 
 // counts[i] samples for pixel i at offsets[i] + q, ordinals start + q. One block per 256
@@ -136,9 +140,17 @@ constexpr int kSynthPix = 256;
 __global__ void k_srv_synth_counts(rpd_synth_params prm, const rpd_synth_region* table, const uint8_t* region,
                                    const int64_t* offsets, int64_t np, int64_t capacity, uint32_t start, SynthOut o) {
     __shared__ int64_t off[kSynthPix + 1];
+    __shared__ int xy[kSynthPix][2];
     const int64_t p0 = int64_t(blockIdx.x) * kSynthPix;
     const int np_block = int(min((long long)kSynthPix, (long long)(np - p0)));
-    for (int t = threadIdx.x; t <= np_block; t += blockDim.x) off[t] = offsets[p0 + t];
+    for (int t = threadIdx.x; t <= np_block; t += blockDim.x) {
+        off[t] = offsets[p0 + t];
+        if (t < np_block) {
+            const int64_t i = p0 + t;
+            xy[t][0] = int(i % prm.width);
+            xy[t][1] = int(i / prm.width);
+        }
+    }
     __syncthreads();
     // the counts of a pass never exceed adaptive_spp * W * H (the capacity); the bound only keeps
     // the writes inside the buffer
@@ -150,9 +162,8 @@ __global__ void k_srv_synth_counts(rpd_synth_params prm, const rpd_synth_region*
             if (off[mid] <= k) lo = mid; else hi = mid - 1;
         }
         const int64_t i = p0 + lo;
-        const int x = int(i % prm.width), y = int(i / prm.width);
         rpd_synth_sample s;
-        rpd_synth_sample_make(&prm, &table[region[i]], x, y, start + uint32_t(k - off[lo]), &s);
+        rpd_synth_sample_make(&prm, &table[region[i]], xy[lo][0], xy[lo][1], start + uint32_t(k - off[lo]), &s);
         srv_write(o, k, s);
     }
 }
@@ -411,7 +422,14 @@ int enqueue_request(Server& s, Request& r) {
     if (spp > 0) {
         {
             KernelScope ks(j, RPD_KERNEL_SYNTH);
-            k_srv_synth_uniform<<<grid_for(np * spp, 256), 256, 0, st>>>(prm, table, region, np, spp, 0u, o);
+            int spp_shift = -1;
+            if ((spp & (spp - 1)) == 0)
+                for (spp_shift = 0; (1 << spp_shift) < spp; ++spp_shift) {}
+            for (int y0 = 0; y0 < c.image_height; y0 += 65535) {  // grid rows per launch
+                const dim3 sgrid(unsigned((int64_t(c.image_width) * spp + 255) / 256),
+                                 unsigned(std::min(65535, c.image_height - y0)));
+                k_srv_synth_uniform<<<sgrid, 256, 0, st>>>(prm, table, region, spp, spp_shift, y0, 0u, o);
+            }
             j.launches += 1;
         }
         const int64_t rows_per_span =
