@@ -109,8 +109,21 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
 struct SampleIn {
     float L[3], n[3], d, alb[3], pu[2], lu[2], bu[2], liu[2], eu[2];
     uint8_t f, cat;
-    uint32_t bins;  // RAW_BINS: the lens, BRDF, light and environment bins, 4 bits each
+    uint32_t bins;  // COMPACT_IN: the lens, BRDF, light and environment bins, 4 bits each
+    float root[3];  // COMPACT_IN: sqrt(max(0, L)), known exactly (L is the square of a half)
 };
+
+// x / d correctly rounded from rd = 1/d (itself correctly rounded) by Markstein's correction
+// (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000 processor",
+// IBM J. Res. Dev. 34(1), 1990): q = RN(x rd), the remainder x - d q is exact in a fused
+// multiply-add, and RN(q + (x - d q) rd) is the correctly rounded x / d. It holds for a
+// positive normal d whose mantissa is not all ones and a quotient, remainder and x in the
+// normal range (or x = +0).
+__device__ __forceinline__ float div_markstein(float x, float d, float rd) {
+    const float q = __fmul_rn(x, rd);
+    return __fmaf_rn(__fmaf_rn(-d, q, x), rd, q);
+}
+__device__ __forceinline__ bool markstein_ok(float x) { return x == 0.0f || fabsf(x) >= 5.42101086e-20f; }  // 2^-64
 
 // Dependency2D::add's bin of a compact (unorm16) pair: u = q / 65536 exactly, so
 // int(u * 4) = q >> 14, already within 0..3 (core/stats.h:166-168)
@@ -132,7 +145,10 @@ struct PixelAcc {
     uint8_t pflags;
 };
 
-template <bool RAW_BINS = false>
+// COMPACT_IN: a sample decoded from the compact planes. Its radiance is the square of a
+// non-negative half, so sqrt(max(0, L)) is exactly that half (in.root), no quotient's dividend is
+// -0, and the random-dimension bins come with it (in.bins).
+template <bool COMPACT_IN = false>
 __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, bool per_sample_albedo,
                                                const float* palb, bool prep, uint8_t plane_mask, float fx,
                                                float fy, float& lum_out, uint32_t& key_out) {
@@ -151,18 +167,44 @@ __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, 
     const float lum = luminance(in.L[0], in.L[1], in.L[2]);
     const float delta = lum - a.mean;
     ++a.n;
-    a.mean += delta / float(a.n);
-    const float delta2 = lum - a.mean;
-    a.m2 += delta * delta2;
-    for (int c = 0; c < 3; ++c) {
-        const float cd = in.L[c] - a.cm[c];
-        a.cm[c] += cd / float(a.n);
-    }
-    for (int c = 0; c < 3; ++c) {
-        const float sc = sqrtf(fmaxs(0.0f, in.L[c]));
-        const float sd = sc - a.sm[c];
-        a.sm[c] += sd / float(a.n);
-        a.sq[c] += sd * (sc - a.sm[c]);
+    if (COMPACT_IN) {
+        // the seven quotients by n from one reciprocal, each still the IEEE quotient (the
+        // dividends are known before any of the updates)
+        const float fn = float(a.n);
+        float cd[3], sd[3];
+        bool fast = a.n < (1 << 23) && markstein_ok(delta);
+        for (int c = 0; c < 3; ++c) {
+            cd[c] = in.L[c] - a.cm[c];
+            sd[c] = in.root[c] - a.sm[c];
+            fast = fast && markstein_ok(cd[c]) && markstein_ok(sd[c]);
+        }
+        if (fast) {
+            const float rn = 1.0f / fn;
+            a.mean += div_markstein(delta, fn, rn);
+            for (int c = 0; c < 3; ++c) a.cm[c] += div_markstein(cd[c], fn, rn);
+            for (int c = 0; c < 3; ++c) a.sm[c] += div_markstein(sd[c], fn, rn);
+        } else {
+            a.mean += delta / fn;
+            for (int c = 0; c < 3; ++c) a.cm[c] += cd[c] / fn;
+            for (int c = 0; c < 3; ++c) a.sm[c] += sd[c] / fn;
+        }
+        const float delta2 = lum - a.mean;
+        a.m2 += delta * delta2;
+        for (int c = 0; c < 3; ++c) a.sq[c] += sd[c] * (in.root[c] - a.sm[c]);
+    } else {
+        a.mean += delta / float(a.n);
+        const float delta2 = lum - a.mean;
+        a.m2 += delta * delta2;
+        for (int c = 0; c < 3; ++c) {
+            const float cd = in.L[c] - a.cm[c];
+            a.cm[c] += cd / float(a.n);
+        }
+        for (int c = 0; c < 3; ++c) {
+            const float sc = sqrtf(fmaxs(0.0f, in.L[c]));
+            const float sd = sc - a.sm[c];
+            a.sm[c] += sd / float(a.n);
+            a.sq[c] += sd * (sc - a.sm[c]);
+        }
     }
     for (int c = 0; c < 3; ++c) a.rad[c] += in.L[c];
     ++a.nsamples;
@@ -172,7 +214,7 @@ __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, 
     const uint8_t fm = in.f & plane_mask;
     // packed random-dimension bins (Dependency2D::add, core/stats.h:166-168)
     uint32_t key = 0;
-    if (RAW_BINS) {
+    if (COMPACT_IN) {
         key = in.bins & ((fm & RPD_SAMPLE_LENS_VALID ? 0x000fu : 0u) | (fm & RPD_SAMPLE_BRDF_VALID ? 0x00f0u : 0u) |
                          (fm & RPD_SAMPLE_LIGHT_VALID ? 0x0f00u : 0u) | (fm & RPD_SAMPLE_ENV_VALID ? 0xf000u : 0u));
     } else {
@@ -354,7 +396,8 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
                 for (int i = 0; i < V; ++i) {
                     SampleIn in;
                     for (int c = 0; c < 3; ++c) {
-                        in.L[c] = sq(h2f(lane16(L[c], i)));
+                        in.root[c] = fabsf(h2f(lane16(L[c], i)));
+                        in.L[c] = sq(in.root[c]);
                         in.n[c] = snorm16(int16_t(lane16(N[c], i)));
                         in.alb[c] = 0.0f;
                     }
@@ -381,7 +424,8 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
             for (int64_t k = k0; k < k1; ++k) {
                 SampleIn in;
                 for (int c = 0; c < 3; ++c) {
-                    in.L[c] = sq(h2f(h.sqrt_radiance[c][k]));
+                    in.root[c] = fabsf(h2f(h.sqrt_radiance[c][k]));
+                    in.L[c] = sq(in.root[c]);
                     in.n[c] = snorm16(h.normal[c][k]);
                     in.alb[c] = 0.0f;
                 }
