@@ -280,11 +280,20 @@ def run_gpu(args):
     alg = algorithmic_bytes(dominant, np_, nn, n) / launches_per_frame
     peaks = measured_peaks()
     achieved = alg / (per_launch_ms * 1e-3) / 1e9 if alg else None
+    # DRAM bytes per launch of the dominant kernel from one ncu --set full capture of this bench
+    # at 960x540 (dram__bytes_read.sum + dram__bytes_write.sum: 51.9 + 3.2 MB), scaled by the pixel
+    # count: the window's traffic grows with the pixels it filters
+    ncu_traffic = {"statmc_window": (55.08e6 * (np_ / (960 * 540)), "ncu at 960x540, scaled by the pixel count")}
+    traffic = ncu_traffic.get(dominant) if (W, H, SPP) == (1920, 1080, 16) else None
     roofline = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                 "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4) if achieved else None,
-                "traffic": None, "peak_source": peaks["source"], "ms_per_launch": round(per_launch_ms, 4),
-                "algorithmic_bytes_per_launch": alg}
+                "traffic": round(traffic[0]) if traffic else None,
+                "traffic_source": traffic[1] if traffic else None,
+                "peak_source": peaks["source"], "ms_per_launch": round(per_launch_ms, 4),
+                "algorithmic_bytes_per_launch": alg,
+                "note": "the StatMC window is bound by instruction issue (window decisions per neighbour), "
+                        "not by HBM; no dense contraction exists on this path"}
     kernels_ms = {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]}
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -678,17 +687,27 @@ def run_serving(args):
 
 
 def run_request(args):
-    """One request of the serving workload through the plain drop-in sequence at --width x
-    --height x --spp with --passes adaptive passes (a small case for profiling captures); prints
-    the samples it denoised."""
+    """One request of the serving workload at --width x --height x --spp with --passes adaptive
+    passes (a small case for profiling captures): through the plain drop-in sequence, or with
+    --served through rpd_server (compact storage, --storage) alone on the GPU; prints the samples
+    it denoised."""
     import rpd_gb300 as R
 
     ctx = R.Context(0, 0)
     knobs = serving_knobs(R).replace(adaptive_passes=args.passes)
-    _, samples = R.plain_request(ctx, knobs, args.width, args.height, args.spp, SEED)
+    if args.served:
+        srv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=1, storage=args.storage)
+        srv.submit(args.width, args.height, args.spp, SEED)
+        srv.drain(600000)
+        done = srv.poll(4)
+        srv.close()
+        assert len(done) == 1 and done[0]["status"] == 0, done
+        samples = done[0]["samples"]
+    else:
+        _, samples = R.plain_request(ctx, knobs, args.width, args.height, args.spp, SEED)
     ctx.close()
-    print(json.dumps({"form": "request", "width": args.width, "height": args.height, "spp": args.spp,
-                      "adaptive_passes": args.passes, "samples": samples}))
+    print(json.dumps({"form": "request", "served": bool(args.served), "width": args.width, "height": args.height,
+                      "spp": args.spp, "adaptive_passes": args.passes, "samples": samples}))
 
 
 def run_reference(args):
@@ -732,6 +751,7 @@ def main():
     ap.add_argument("--budget-gb", type=int, default=120, help="serving: HBM admission budget")
     ap.add_argument("--inflight", type=int, default=32, help="serving: requests on the GPU at once")
     ap.add_argument("--storage", choices=["fp16", "fp32"], default="fp16", help="serving: sample storage")
+    ap.add_argument("--served", action="store_true", help="request form: through rpd_server instead of the plain drop-in")
     ap.add_argument("--alloc-blocks", type=int, default=0,
                     help="serving: blocks of each request's parallel adaptive allocation (0: one per SM)")
     ap.add_argument("--plain-requests", type=int, default=200, help="serving: stream prefix run through the plain drop-in")
