@@ -185,6 +185,8 @@ typedef enum rpd_field {
     RPD_FIELD_EXPANDED_ENVIRONMENT,
     RPD_FIELD_EXPANDED_RR,
     RPD_FIELD_ADAPTIVE_COUNTS,       /* int32 last compute_adaptive_sample_counts result */
+    RPD_FIELD_SQRT_VARIANCE_STABLE,  /* rgb: the StatMC window's sqrt-variance, max of the pixel's and its
+                                      * 3x3 average (main.cpp:972-990), of the last statmc_denoise */
     RPD_FIELD_COUNT_
 } rpd_field;
 

@@ -157,6 +157,7 @@ struct orc_job {
     float* var_eff;
     float* var_ratio;
     float* variance_denoised;
+    float* sqrt_var_stable;  /* rgb interleaved, the last statmc_denoise's */
     float* adaptive_importance;
     int32_t* last_counts;
     double stage_ms[RPD_STAGE_COUNT_];
@@ -279,6 +280,7 @@ orc_job* orc_job_create(const rpd_config* cfg) {
     j->var_eff = (float*)zalloc(np * sizeof(float));
     j->var_ratio = (float*)zalloc(np * sizeof(float));
     j->variance_denoised = (float*)zalloc(np * sizeof(float));
+    j->sqrt_var_stable = (float*)zalloc(np * 3 * sizeof(float));
     j->adaptive_importance = (float*)zalloc(np * sizeof(float));
     j->last_counts = (int32_t*)zalloc(np * 4);
     return j;
@@ -300,7 +302,7 @@ void orc_job_destroy(orc_job* j) {
     free(j->sens_confidence); free(j->sens_gradient); free(j->f_normal); free(j->f_depth); free(j->f_albedo);
     for (int f = 0; f < C_FIELDS; ++f) free(j->cache[f]);
     free(j->denoised); free(j->uncertainty); free(j->alpha); free(j->var_total); free(j->var_eff);
-    free(j->var_ratio); free(j->variance_denoised); free(j->adaptive_importance); free(j->last_counts);
+    free(j->var_ratio); free(j->variance_denoised); free(j->sqrt_var_stable); free(j->adaptive_importance); free(j->last_counts);
     free(j);
 }
 
@@ -932,7 +934,7 @@ int orc_statmc_denoise(orc_job* j) {
     ensure_feature_cache(j);
     ensure_sensitivity_cache(j);
     float* svm = (float*)zalloc((size_t)np * 3 * sizeof(float));  /* sqrt_variance_mean */
-    float* svs = (float*)zalloc((size_t)np * 3 * sizeof(float));  /* sqrt_variance_stable */
+    float* svs = j->sqrt_var_stable;  /* sqrt_variance_stable, kept for reads */
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -1062,7 +1064,7 @@ int orc_statmc_denoise(orc_job* j) {
         j->uncertainty[idx] = uncertainty;
     }
     free(svm);
-    free(svs);
+
     j->stage_ms[RPD_STAGE_STATMC] = now_ms() - t0;
     return RPD_OK;
 }
@@ -1347,6 +1349,7 @@ uint64_t orc_field_bytes(const orc_job* j, int field) {
     switch (field) {
     case RPD_FIELD_DENOISED: case RPD_FIELD_RADIANCE_SUM: case RPD_FIELD_NORMAL_SUM: case RPD_FIELD_ALBEDO_SUM:
     case RPD_FIELD_STATS_COLOR_MEAN: case RPD_FIELD_STATS_SQRT_MEAN: case RPD_FIELD_STATS_SQRT_SQUARE_DIFF:
+    case RPD_FIELD_SQRT_VARIANCE_STABLE:
         return np * 12;
     case RPD_FIELD_GRID: return nn * NDEP * DSTRIDE * 8;
     default:
@@ -1401,6 +1404,7 @@ int orc_job_read(orc_job* j, int field, void* dst, size_t bytes) {
         return RPD_OK;
     case RPD_FIELD_GRID: return put(dst, bytes, j->grid, need);
     case RPD_FIELD_ADAPTIVE_COUNTS: return put(dst, bytes, j->last_counts, need);
+    case RPD_FIELD_SQRT_VARIANCE_STABLE: return put(dst, bytes, j->sqrt_var_stable, need);
     default:
         break;
     }

@@ -1119,6 +1119,7 @@ uint64_t rpd_field_bytes(const rpd_job* job, rpd_field f) {
     switch (f) {
     case RPD_FIELD_DENOISED: case RPD_FIELD_RADIANCE_SUM: case RPD_FIELD_NORMAL_SUM: case RPD_FIELD_ALBEDO_SUM:
     case RPD_FIELD_STATS_COLOR_MEAN: case RPD_FIELD_STATS_SQRT_MEAN: case RPD_FIELD_STATS_SQRT_SQUARE_DIFF:
+    case RPD_FIELD_SQRT_VARIANCE_STABLE:
         return np * 12;
     case RPD_FIELD_GRID: return nn * kDeps * kDepStride * 8;
     default:
@@ -1148,6 +1149,7 @@ int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory 
     case RPD_FIELD_STATS_COLOR_MEAN: rgb = j->p.color_mean; break;
     case RPD_FIELD_STATS_SQRT_MEAN: rgb = j->p.sqrt_mean; break;
     case RPD_FIELD_STATS_SQRT_SQUARE_DIFF: rgb = j->p.sqrt_sq; break;
+    case RPD_FIELD_SQRT_VARIANCE_STABLE: rgb = j->p.sqrt_var_stable; break;
     case RPD_FIELD_UNCERTAINTY: src = j->p.uncertainty; break;
     case RPD_FIELD_ALPHA: src = j->p.alpha; break;
     case RPD_FIELD_VAR_TOTAL_DEBUG: src = j->p.var_total; break;

@@ -30,6 +30,7 @@
 
 #include "rpd_internal.h"
 #include "device_math.cuh"
+#include "exact_arith.cuh"
 
 namespace rpd {
 
@@ -90,8 +91,12 @@ __global__ void k_sqrt_var_mean(PixelPlanes p, int64_t np) {
 // component max (981-990). The reference accumulates in double: v * weight with weights 1/3
 // (corners, 1.0 / 3.0 rounded), 1/2 and 1 (both exact), nine additions in (dy, dx) order, one
 // division by the summed weights. A 32 x 8 block stages, per pixel of its (clamped) 34 x 10 halo,
-// the three products each channel can need (v, v * 0.5, v * (1.0 / 3.0)) in double once, so a
-// pixel pays only its nine additions and the division on GB300's slow double pipe.
+// the three products each channel can need (v, v * 0.5, v * (1.0 / 3.0)) in double once. Of a
+// pixel's three channels, the first's nine additions run exactly in integer instructions
+// (exact_arith.cuh) and the others' as double additions, so the integer and double pipes share
+// the work; each quotient is rounded to float through a single-precision estimate and an exact
+// integer remainder (the double division only where that cannot decide). The values are
+// positive: sqrt_var_mean is floored at 1e-8.
 constexpr int kSvTx = 32, kSvTy = 8;
 __global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p, int w, int h, double weight_sum) {
     __shared__ double tile[3][3][(kSvTy + 2) * (kSvTx + 2)];  // [channel][v, v/2, v/3][pixel]
@@ -114,21 +119,39 @@ __global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p
     if (x >= w || y >= h) return;
     const int64_t i = int64_t(y) * w + x;
     const int e = (threadIdx.y + 1) * tw + threadIdx.x + 1;
+    const XD wsum = xd_of_double(weight_sum);
     for (int c = 0; c < 3; ++c) {
         const double* t1 = tile[c][0];
         const double* th = tile[c][1];
         const double* tt = tile[c][2];
-        double a = 0.0;
-        a += tt[e - tw - 1];
-        a += th[e - tw];
-        a += tt[e - tw + 1];
-        a += th[e - 1];
-        a += t1[e];
-        a += th[e + 1];
-        a += tt[e + tw - 1];
-        a += th[e + tw];
-        a += tt[e + tw + 1];
-        p.sqrt_var_stable[c][i] = fmaxs(p.sqrt_var_mean[c][i], float(a / weight_sum));
+        double a;
+        if (c == 0) {
+            XD x = xd_of_double(tt[e - tw - 1]);
+            x = xd_add(x, xd_of_double(th[e - tw]));
+            x = xd_add(x, xd_of_double(tt[e - tw + 1]));
+            x = xd_add(x, xd_of_double(th[e - 1]));
+            x = xd_add(x, xd_of_double(t1[e]));
+            x = xd_add(x, xd_of_double(th[e + 1]));
+            x = xd_add(x, xd_of_double(tt[e + tw - 1]));
+            x = xd_add(x, xd_of_double(th[e + tw]));
+            x = xd_add(x, xd_of_double(tt[e + tw + 1]));
+            a = xd_to_double(x);
+        } else {
+            a = 0.0;
+            a += tt[e - tw - 1];
+            a += th[e - tw];
+            a += tt[e - tw + 1];
+            a += th[e - 1];
+            a += t1[e];
+            a += th[e + 1];
+            a += tt[e + tw - 1];
+            a += th[e + tw];
+            a += tt[e + tw + 1];
+        }
+        const XD ax = xd_of_double(a);
+        float q;
+        if (!quotient_to_float(ax.m, ax.e, wsum.m, wsum.e, q)) q = float(a / weight_sum);
+        p.sqrt_var_stable[c][i] = fmaxs(p.sqrt_var_mean[c][i], q);
     }
 }
 

@@ -34,11 +34,11 @@ FIELDS = [
     "GRID",
     "EXPANDED_ALL", "EXPANDED_PIXEL", "EXPANDED_BRDF", "EXPANDED_LENS", "EXPANDED_LIGHT",
     "EXPANDED_LIGHT_UV", "EXPANDED_LIGHT_SELECT", "EXPANDED_ENVIRONMENT", "EXPANDED_RR",
-    "ADAPTIVE_COUNTS",
+    "ADAPTIVE_COUNTS", "SQRT_VARIANCE_STABLE",
 ]
 FIELD = {name: i for i, name in enumerate(FIELDS)}
 RGB_FIELDS = {"DENOISED", "RADIANCE_SUM", "NORMAL_SUM", "ALBEDO_SUM", "STATS_COLOR_MEAN", "STATS_SQRT_MEAN",
-              "STATS_SQRT_SQUARE_DIFF"}
+              "STATS_SQRT_SQUARE_DIFF", "SQRT_VARIANCE_STABLE"}
 INT_FIELDS = {"HIT_COUNT", "SAMPLE_COUNT", "STATS_N", "ADAPTIVE_COUNTS"}
 STAGES = ["ACCUMULATE", "SENSITIVITY", "STATMC", "VARIANCE", "ADAPTIVE"]
 KERNELS = ["offsets", "accumulate_pixels", "grid", "grid_random", "merge", "features", "node_stats", "node_combine", "sens_pixels",

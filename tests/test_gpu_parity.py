@@ -62,6 +62,8 @@ def check_pipeline(g, o, exact_grid=True):
         assert err <= TOL, (f, err)
     # the variance stabilisation is single precision without exp: bit-exact
     assert_bitwise(g.read("VARIANCE_DENOISED"), o.read("VARIANCE_DENOISED"), "VARIANCE_DENOISED")
+    # the window's sqrt variance: the reference's double 3x3 average, bit-exact
+    assert_bitwise(g.read("SQRT_VARIANCE_STABLE"), o.read("SQRT_VARIANCE_STABLE"), "SQRT_VARIANCE_STABLE")
 
 
 @pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
