@@ -579,8 +579,10 @@ __global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pas
             bl += va.y;
         }
         if (bh != 0.0f || bl != 0.0f) df_accum(base + dep_s * kDepStride + lane, bh, bl);
-        float2 t4[4];
-        reduce_totals(ts, t4);
+        // no listed pixel: this class's totals are all zeros on every lane (nothing to reduce)
+        float2 t4[4] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f),
+                        make_float2(0.0f, 0.0f)};
+        if (nlist > 0) reduce_totals(ts, t4);
         if (lane == 0) {
             for (int k = 0; k < 4; ++k) {
                 float h = t4[k].x, l = t4[k].y;
@@ -592,7 +594,7 @@ __global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pas
             }
         }
         if (cl > 0) {
-            reduce_totals(tx, t4);
+            if (nlist > 0) reduce_totals(tx, t4);
             if (lane == 0) {
                 for (int k = 0; k < 4; ++k) {
                     float h = t4[k].x, l = t4[k].y;
