@@ -87,19 +87,22 @@ __device__ void local_avg3(float* const* v, int w, int h, int cx, int cy, float 
     out[2] = float(a2 / weight_sum);
 }
 
+// One thread per (node, task): tasks 0 .. R_FIELDS-1 are the dependencies' sensitivity and
+// confidence, task R_FIELDS the node's features (blockIdx.y). The tasks are independent, so the
+// double-precision chains of a node run side by side instead of one after another.
 __global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= g.nn) return;
-    const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
-    const double* tile = n.grid + idx * kDeps * kDepStride;
-    const double n0d = double(n0);
-    for (int f = 0; f < R_FIELDS; ++f) {
+    const int f = int(blockIdx.y);
+    if (f < R_FIELDS) {
         const int d = c_raw_dep[f];
-        const double* dep = tile + d * kDepStride;
+        const double* dep = n.grid + idx * kDeps * kDepStride + d * kDepStride;
         n.raw[f][idx] = compute_sensitivity(dep, d == D_RR ? 2 : 16);
         const double mass = sample_mass(dep);
-        n.conf[f][idx] = float(mass / (mass + n0d));
+        n.conf[f][idx] = float(mass / (mass + double(n0)));
+        return;
     }
+    const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
     const int px = iclamps(ix * g.step, 0, g.w - 1);
     const int py = iclamps(iy * g.step, 0, g.h - 1);
     float nn3[3], na3[3];
@@ -258,7 +261,8 @@ __global__ void k_expand(Geometry g, const float* tiles, float* out) {
 cudaError_t launch_sensitivity(Job& j) {
     {
         KernelScope ks(j, RPD_KERNEL_NODE_STATS);
-        k_node_stats<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n, j.p, j.cfg.rpf_confidence_samples);
+        k_node_stats<<<dim3(grid_for(j.g.nn, 128), R_FIELDS + 1), 128, 0, j.stream>>>(j.g, j.n, j.p,
+                                                                                    j.cfg.rpf_confidence_samples);
     }
     {
         KernelScope ks(j, RPD_KERNEL_NODE_COMBINE);
