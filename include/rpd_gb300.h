@@ -270,7 +270,8 @@ int rpd_job_set_exact(rpd_job* job, int flags);
  * keep fewer bins per warp (more resident warps) but walk the samples once per set. */
 #define RPD_TUNE_GRID_SHAPE 0
 /* RPD_TUNE_HOST_BAND_MB: a host-memory push is copied to HBM in row bands of about this many
- * megabytes (default 96), each band's copy overlapping the previous band's passes. */
+ * megabytes (default 768, measured: fewer, larger copies keep the host link busier), each band's copy
+ * overlapping the previous band's passes. */
 #define RPD_TUNE_HOST_BAND_MB 1
 /* RPD_TUNE_STATMC_ROWS: pixel rows per block of the StatMC window kernel: 2, 4 or 8 (0, the
  * default: the tallest whose halo tile fits in shared memory). */
@@ -368,6 +369,10 @@ int rpd_finalize(rpd_job* job);
 
 /* Copy a field to `where` memory. bytes must equal the field's size. */
 int rpd_job_read(rpd_job* job, rpd_field field, void* dst, size_t bytes, rpd_memory where);
+/* rpd_job_read enqueued on the job's stream without waiting: dst (page-locked host memory from
+ * rpd_host_alloc, or device memory) holds the field once rpd_job_sync returns or the job's later
+ * work has run. The copy overlaps the caller's next push into another job. */
+int rpd_job_read_async(rpd_job* job, rpd_field field, void* dst, size_t bytes, rpd_memory where);
 uint64_t rpd_field_bytes(const rpd_job* job, rpd_field field);
 int rpd_job_sync(rpd_job* job);
 /* Device milliseconds of the last run of a stage on this job. */

@@ -1129,7 +1129,7 @@ uint64_t rpd_field_bytes(const rpd_job* job, rpd_field f) {
     }
 }
 
-int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory where) {
+static int job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory where, bool sync) {
     Job* j = reinterpret_cast<Job*>(job);
     CHECK_JOB(j);
     const uint64_t need = rpd_field_bytes(job, f);
@@ -1178,7 +1178,7 @@ int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory 
     }
     if (src) {
         RPD_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, j->stream));
-        RPD_CUDA(cudaStreamSynchronize(j->stream));
+        if (sync) RPD_CUDA(cudaStreamSynchronize(j->stream));
         return RPD_OK;
     }
     // fields computed on read go through the staging buffer
@@ -1196,8 +1196,20 @@ int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory 
         return fail(RPD_ERR_INVALID_ARGUMENT, "unknown field");
     }
     RPD_CUDA(cudaMemcpyAsync(dst, tmp, bytes, kind, j->stream));
-    RPD_CUDA(cudaStreamSynchronize(j->stream));
+    if (sync) {
+        RPD_CUDA(cudaStreamSynchronize(j->stream));
+    } else {
+        RPD_CUDA(cudaEventRecord(j->staging_free, j->stream));  // the next host push waits for this copy
+    }
     return RPD_OK;
+}
+
+int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory where) {
+    return job_read(job, f, dst, bytes, where, true);
+}
+
+int rpd_job_read_async(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory where) {
+    return job_read(job, f, dst, bytes, where, false);
 }
 
 int rpd_job_sync(rpd_job* job) {

@@ -146,7 +146,7 @@ struct Job {
     cudaEvent_t staging_free = nullptr;
     cudaEvent_t alloc_ready = nullptr;  // the job's stream reached the allocation
     cudaEvent_t alloc_done = nullptr;   // the allocation stream finished it
-    int64_t band_bytes = int64_t(96) << 20;  // target size of a band (RPD_TUNE_HOST_BAND_MB)
+    int64_t band_bytes = int64_t(768) << 20;  // target size of a band (RPD_TUNE_HOST_BAND_MB)
     float* lum = nullptr;        // per-sample luminance of the current push (fast grid pass)
     uint64_t lum_cap = 0;
     float* cls[kClasses][5]{};   // per-pixel validity-class sums of deviant pixels (arena)

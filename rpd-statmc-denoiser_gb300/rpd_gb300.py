@@ -291,6 +291,7 @@ def lib() -> C.CDLL:
         "rpd_compute_adaptive_sample_counts": (C.c_int, [vp, vp, C.c_int]),
         "rpd_finalize": (C.c_int, [vp]),
         "rpd_job_read": (C.c_int, [vp, C.c_int, vp, C.c_size_t, C.c_int]),
+        "rpd_job_read_async": (C.c_int, [vp, C.c_int, vp, C.c_size_t, C.c_int]),
         "rpd_field_bytes": (u64, [vp, C.c_int]),
         "rpd_job_sync": (C.c_int, [vp]),
         "rpd_job_stage_ms": (f32, [vp, C.c_int]),
@@ -343,7 +344,7 @@ def exported_symbols() -> list[str]:
             "rpd_job_autotune", "rpd_batch_create", "rpd_batch_add", "rpd_batch_run", "rpd_batch_sync",
             "rpd_batch_last_ms", "rpd_batch_kernel_count", "rpd_batch_set_lanes", "rpd_batch_destroy", "rpd_job_end_pass", "rpd_recompute_sensitivity",
             "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
-            "rpd_job_read", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
+            "rpd_job_read", "rpd_job_read_async", "rpd_field_bytes", "rpd_job_sync", "rpd_job_stage_ms", "rpd_job_launch_count",
             "rpd_job_set_profiling", "rpd_job_kernel_time", "rpd_job_reset_kernel_times", "rpd_kernel_name",
             "rpd_job_mark", "rpd_job_mark_elapsed",
             "rpd_atrous_wavelet", "rpd_joint_bilateral", "rpd_atrous_wavelet_noalloc", "rpd_device_alloc", "rpd_device_free", "rpd_host_alloc",
