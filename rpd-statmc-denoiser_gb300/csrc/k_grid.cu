@@ -21,6 +21,8 @@
 // products via FMA; about 2^-44 relative — GB300 executes double precision at 1/55 of its
 // single-precision rate). With a power-of-two node step every weight is an exact multiple
 // of 1/step^2, so the bin weights are accumulated as exact integers.
+#include <type_traits>
+
 #include "rpd_internal.h"
 #include "device_math.cuh"
 
@@ -653,13 +655,14 @@ struct RandParams {
     int cols;            // support columns of a node, 2 * step + 3 (shared-memory tables)
 };
 
-template <bool INT_W, int DS>
+template <int WB, int DS>
 struct RandLayout {
-    // per warp: weights [slots][32] (u32 exact integers or float2 double-float), then
-    // sums [slots][32] float2; slot kTrash absorbs the updates of absent dimensions
+    // per warp: weights [slots][32] (WB bytes each: u16 or u32 exact integers, or float2
+    // double-float), then sums [slots][32] float2; slot kTrash absorbs the updates of absent
+    // dimensions
     static constexpr int kTrash = set_slots<DS>();
     static constexpr int kSlots = kTrash + 1;
-    static constexpr int kWeightBytes = kSlots * 32 * (INT_W ? 4 : 8);
+    static constexpr int kWeightBytes = kSlots * 32 * WB;
     static constexpr int kWarpBytes = kWeightBytes + kSlots * 32 * 8;
 };
 
@@ -675,9 +678,9 @@ struct RowTable {
 };
 
 // Everything a warp's walk needs.
-template <bool INT_W, int DS>
+template <int WB, int DS>
 struct WalkCtx {
-    uint32_t* wint;
+    std::conditional_t<WB == 2, uint16_t, uint32_t>* wint;
     float2* wdf;
     float2* sums;
     RowTable* rt;
@@ -690,10 +693,11 @@ struct WalkCtx {
 // One sample: add w (weights) and w*y (sums) to the bin of every dimension of set SET the
 // sample carries. Absent dimensions (and w <= 1e-8, which BinnedDependency::add skips,
 // core/stats.h:103) go to the trash slot with the same arithmetic.
-template <bool INT_W, int DS, int SET>
-__device__ __forceinline__ void rand_update(const WalkCtx<INT_W, DS>& c, uint32_t key, float w, uint32_t iw,
+template <int WB, int DS, int SET>
+__device__ __forceinline__ void rand_update(const WalkCtx<WB, DS>& c, uint32_t key, float w, uint32_t iw,
                                             float y) {
-    using L = RandLayout<INT_W, DS>;
+    constexpr bool INT_W = WB != 8;
+    using L = RandLayout<WB, DS>;
     const bool wok = w > 1e-8f;
     const float wy = w * y;
     const float wye = __fmaf_rn(w, y, -wy);
@@ -739,9 +743,10 @@ constexpr int kWalkScalar = 0, kWalkPixelQuads = 1, kWalkColumnQuads = 2;
 
 // The flat walk of one row-segment chunk (total samples, or total quads in the quad modes) for
 // dimension set SET.
-template <bool INT_W, int DS, int SET, int MODE>
-__device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const RandParams& rp, const GridPrep& gp,
+template <int WB, int DS, int SET, int MODE>
+__device__ __forceinline__ void rand_walk(const WalkCtx<WB, DS>& c, const RandParams& rp, const GridPrep& gp,
                                           const int64_t* offsets, int total) {
+    constexpr bool INT_W = WB != 8;
     const RowTable* rt = c.rt;
     const int lane = c.lane;
     int r = 0;  // current segment of this lane (monotone along its walk)
@@ -804,10 +809,10 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
                         if (k >= ks && k < ke && unsigned(ci) < unsigned(rp.cols)) w[i] = c.xf[ci] * ay;
                     }
                 }
-                rand_update<INT_W, DS, SET>(c, ck[u].x, w[0], INT_W ? uint32_t(w[0] * c.wscale) : 0u, cy[u].x);
-                rand_update<INT_W, DS, SET>(c, ck[u].y, w[1], INT_W ? uint32_t(w[1] * c.wscale) : 0u, cy[u].y);
-                rand_update<INT_W, DS, SET>(c, ck[u].z, w[2], INT_W ? uint32_t(w[2] * c.wscale) : 0u, cy[u].z);
-                rand_update<INT_W, DS, SET>(c, ck[u].w, w[3], INT_W ? uint32_t(w[3] * c.wscale) : 0u, cy[u].w);
+                rand_update<WB, DS, SET>(c, ck[u].x, w[0], INT_W ? uint32_t(w[0] * c.wscale) : 0u, cy[u].x);
+                rand_update<WB, DS, SET>(c, ck[u].y, w[1], INT_W ? uint32_t(w[1] * c.wscale) : 0u, cy[u].y);
+                rand_update<WB, DS, SET>(c, ck[u].z, w[2], INT_W ? uint32_t(w[2] * c.wscale) : 0u, cy[u].z);
+                rand_update<WB, DS, SET>(c, ck[u].w, w[3], INT_W ? uint32_t(w[3] * c.wscale) : 0u, cy[u].w);
             }
         }
     } else if (MODE == kWalkPixelQuads) {
@@ -851,10 +856,10 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const uint32_t iw = INT_W ? uint32_t(cw[u] * c.wscale) : 0u;
-                rand_update<INT_W, DS, SET>(c, ck[u].x, cw[u], iw, cy[u].x);
-                rand_update<INT_W, DS, SET>(c, ck[u].y, cw[u], iw, cy[u].y);
-                rand_update<INT_W, DS, SET>(c, ck[u].z, cw[u], iw, cy[u].z);
-                rand_update<INT_W, DS, SET>(c, ck[u].w, cw[u], iw, cy[u].w);
+                rand_update<WB, DS, SET>(c, ck[u].x, cw[u], iw, cy[u].x);
+                rand_update<WB, DS, SET>(c, ck[u].y, cw[u], iw, cy[u].y);
+                rand_update<WB, DS, SET>(c, ck[u].z, cw[u], iw, cy[u].z);
+                rand_update<WB, DS, SET>(c, ck[u].w, cw[u], iw, cy[u].w);
             }
         }
     } else {
@@ -914,18 +919,20 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<INT_W, DS>& c, const Ran
             }
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                rand_update<INT_W, DS, SET>(c, ck[u], cw[u], INT_W ? uint32_t(cw[u] * c.wscale) : 0u, cy[u]);
+                rand_update<WB, DS, SET>(c, ck[u], cw[u], INT_W ? uint32_t(cw[u] * c.wscale) : 0u, cy[u]);
         }
     }
 }
 
-template <bool INT_W, int RW, int DS, int MODE>
+template <int WB, int RW, int DS, int MODE>
 __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, float2* pass_grid,
                                                               const int64_t* offsets, GridPrep gp) {
+    constexpr bool INT_W = WB != 8;
+    using WT = std::conditional_t<WB == 2, uint16_t, uint32_t>;
     constexpr int NW = RW * DS;
     constexpr int VPT = (2 * kRandSlots + NW * 32 - 1) / (NW * 32);  // combined values per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using L = RandLayout<INT_W, DS>;
+    using L = RandLayout<WB, DS>;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int dset = warp % DS;     // the dimension set of this warp
@@ -935,8 +942,8 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
     const int64_t node = rp.gp.node0 + blockIdx.x;
     const int nx = int(node % g.nodes_x), ny = int(node / g.nodes_x);
     unsigned char* wbase = smem_raw + warp * L::kWarpBytes;
-    WalkCtx<INT_W, DS> c;
-    c.wint = reinterpret_cast<uint32_t*>(wbase);
+    WalkCtx<WB, DS> c;
+    c.wint = reinterpret_cast<WT*>(wbase);
     c.wdf = reinterpret_cast<float2*>(wbase);
     c.sums = reinterpret_cast<float2*>(wbase + L::kWeightBytes);
     c.rt = reinterpret_cast<RowTable*>(smem_raw + NW * L::kWarpBytes) + warp;
@@ -1013,9 +1020,9 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
         if (lane == 0) rt->base[0] = 0;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
-        if (dset == 0) rand_walk<INT_W, DS, 0, MODE>(c, rp, gp, offsets, total);
-        if (DS > 1 && dset == 1) rand_walk<INT_W, DS, 1, MODE>(c, rp, gp, offsets, total);
-        if (DS > 2 && dset == 2) rand_walk<INT_W, DS, 2, MODE>(c, rp, gp, offsets, total);
+        if (dset == 0) rand_walk<WB, DS, 0, MODE>(c, rp, gp, offsets, total);
+        if (DS > 1 && dset == 1) rand_walk<WB, DS, 1, MODE>(c, rp, gp, offsets, total);
+        if (DS > 2 && dset == 2) rand_walk<WB, DS, 2, MODE>(c, rp, gp, offsets, total);
         __syncwarp();
     }
     __syncthreads();
@@ -1051,7 +1058,7 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
                 const unsigned char* b = smem_raw + (rg * DS + vset[vi]) * L::kWarpBytes;
                 const int v = threadIdx.x + vi * NW * 32;
                 if (vw[vi] && INT_W) {
-                    const uint32_t* src = reinterpret_cast<const uint32_t*>(b) + vslot[vi] * 32;
+                    const WT* src = reinterpret_cast<const WT*>(b) + vslot[vi] * 32;
                     itot[vi] += uint64_t(src[(i + v) & 31]) + uint64_t(src[(i + 1 + v) & 31]);
                 } else {
                     const float2* src =
@@ -1104,16 +1111,16 @@ uint32_t spp_magic_for(int spp, int max_k) {
     return uint32_t(m);
 }
 
-template <bool INT_W, int RW, int DS, int MODE>
+template <int WB, int RW, int DS, int MODE>
 cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) {
     constexpr int NW = RW * DS;
-    const size_t smem = size_t(NW) * RandLayout<INT_W, DS>::kWarpBytes + size_t(NW) * sizeof(RowTable) +
+    const size_t smem = size_t(NW) * RandLayout<WB, DS>::kWarpBytes + size_t(NW) * sizeof(RowTable) +
                         size_t(rp.cols) * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(k_grid_random<INT_W, RW, DS, MODE>,
+    cudaError_t e = cudaFuncSetAttribute(k_grid_random<WB, RW, DS, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     const unsigned nblocks = unsigned(rp.gp.count_nodes);
-    k_grid_random<INT_W, RW, DS, MODE><<<nblocks, NW * 32, smem, j.stream>>>(
+    k_grid_random<WB, RW, DS, MODE><<<nblocks, NW * 32, smem, j.stream>>>(
         rp, reinterpret_cast<float2*>(j.n.pass_grid), j.offsets, gp);
     j.launches += 1;
     return cudaGetLastError();
@@ -1122,24 +1129,30 @@ cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) 
 // Pixel quads need samples per pixel a multiple of 4 (and a power of two, for the shift) with
 // 16-byte aligned key and luminance planes; column quads need the per-sample columns (per-pixel
 // counts) with 16-byte aligned key and luminance planes and an 8-byte aligned column plane.
-template <bool INT_W, int RW, int DS>
+template <int WB, int RW, int DS>
 cudaError_t launch_random(Job& j, const RandParams& rp, const GridPrep& gp) {
     const bool aligned = (reinterpret_cast<uintptr_t>(gp.key) & 15u) == 0 && (reinterpret_cast<uintptr_t>(gp.lum) & 15u) == 0;
-    if (rp.spp_shift >= 2 && aligned) return launch_random_vec<INT_W, RW, DS, kWalkPixelQuads>(j, rp, gp);
+    if (rp.spp_shift >= 2 && aligned) return launch_random_vec<WB, RW, DS, kWalkPixelQuads>(j, rp, gp);
     if (gp.col && aligned && (reinterpret_cast<uintptr_t>(gp.col) & 7u) == 0)
-        return launch_random_vec<INT_W, RW, DS, kWalkColumnQuads>(j, rp, gp);
-    return launch_random_vec<INT_W, RW, DS, kWalkScalar>(j, rp, gp);
+        return launch_random_vec<WB, RW, DS, kWalkColumnQuads>(j, rp, gp);
+    return launch_random_vec<WB, RW, DS, kWalkScalar>(j, rp, gp);
 }
 
-template <bool INT_W>
+// WB: bytes of a lane-private bin weight (8 double-float, 4 or 2 exact integers); the 2-byte
+// form is built for the default shape only (the caller checks that the lane sums fit)
+template <int WB>
 cudaError_t launch_random_shape(Job& j, const RandParams& rp, const GridPrep& gp, int shape) {
-    switch (shape) {
-    case 1: return launch_random<INT_W, 2, 1>(j, rp, gp);
-    case 2: return launch_random<INT_W, 2, 2>(j, rp, gp);
-    case 3: return launch_random<INT_W, 2, 3>(j, rp, gp);
-    case 4: return launch_random<INT_W, 1, 2>(j, rp, gp);
-    case 5: return launch_random<INT_W, 1, 3>(j, rp, gp);
-    default: return launch_random<INT_W, 1, 1>(j, rp, gp);
+    if constexpr (WB == 2) {
+        return launch_random<2, 1, 1>(j, rp, gp);
+    } else {
+        switch (shape) {
+        case 1: return launch_random<WB, 2, 1>(j, rp, gp);
+        case 2: return launch_random<WB, 2, 2>(j, rp, gp);
+        case 3: return launch_random<WB, 2, 3>(j, rp, gp);
+        case 4: return launch_random<WB, 1, 2>(j, rp, gp);
+        case 5: return launch_random<WB, 1, 3>(j, rp, gp);
+        default: return launch_random<WB, 1, 1>(j, rp, gp);
+        }
     }
 }
 
@@ -1209,7 +1222,14 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
             rp.spp_magic = spp_magic_for(spp, (2 * step + 3) * spp);
         }
     }
-    return int_w ? launch_random_shape<true>(j, rp, gp, j.grid_shape) : launch_random_shape<false>(j, rp, gp, j.grid_shape);
+    // 16-bit lane sums (smaller bins, more resident warps) when no lane's sum can reach 2^16: a
+    // lane takes at most 1/32 of a node's quads of a uniform push (plus two partial quads per row
+    // segment) and each sample adds at most step^2 units
+    const bool default_shape = j.grid_shape == 0 || j.grid_shape == 6;
+    const bool w16 = int_w && default_shape && spp > 0 &&
+                     (double(sup + 3) * double(sup + 3) * double(spp) / 32.0 + 8.0) * double(step) * double(step) < 65536.0;
+    if (w16) return launch_random_shape<2>(j, rp, gp, j.grid_shape);
+    return int_w ? launch_random_shape<4>(j, rp, gp, j.grid_shape) : launch_random_shape<8>(j, rp, gp, j.grid_shape);
 }
 
 }  // namespace rpd
