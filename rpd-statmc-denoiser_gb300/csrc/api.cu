@@ -230,8 +230,8 @@ int grow_device(Job& j, void** buf, uint64_t* cap, uint64_t need) {
 }
 
 int ensure_offsets(Job& j, int64_t count) {
-    // count+1 offsets plus room for the scan's block sums
-    const int64_t need = count + 1 + (count + 1023) / 1024 + 2;
+    // count+1 offsets plus room for the scan's block sums and block maxima
+    const int64_t need = count + 1 + 2 * ((count + 1023) / 1024) + 4;
     if (j.offsets_cap >= need) return RPD_OK;
     if (j.offsets) {
         cudaStreamSynchronize(j.stream);
@@ -980,7 +980,9 @@ static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int
             else
                 max_count = INT32_MAX;  // unknown on the host: the push's total bounds the weights
         }
-        RPD_CUDA(launch_grid_fast(*j, d, first, count, gp, counts ? 0 : spp, max_count, nsamp));
+        // every push with per-pixel counts scanned them into j->offsets first
+        const int64_t* d_max = (counts && max_count == INT32_MAX) ? offsets_count_max(*j, count) : nullptr;
+        RPD_CUDA(launch_grid_fast(*j, d, first, count, gp, counts ? 0 : spp, max_count, nsamp, d_max));
     }
     else if (rpd) RPD_CUDA(launch_accumulate_grid(*j, d, first, count));
     j->pass_open = true;
@@ -1423,10 +1425,10 @@ int rpd_synth_fill(rpd_ctx* ctx, const rpd_synth_params* prm, int64_t first, int
         tmp.stream = st;
         tmp.offsets = d_offsets;
         if (counts) {
-            // launch_offsets_scan writes its block sums after offsets[count]; use a
-            // dedicated buffer large enough for both
+            // launch_offsets_scan writes its block sums and maxima after offsets[count]; use a
+            // dedicated buffer large enough for all of them
             int64_t* both = nullptr;
-            RPD_CUDA(cudaMallocAsync(&both, uint64_t(count + 1 + nblocks + 2) * 8, st));
+            RPD_CUDA(cudaMallocAsync(&both, uint64_t(count + 1 + 2 * nblocks + 4) * 8, st));
             tmp.offsets = both;
             RPD_CUDA(launch_offsets_scan(tmp, counts, count));
             RPD_CUDA(cudaMemcpyAsync(d_offsets, both, uint64_t(count + 1) * 8, cudaMemcpyDeviceToDevice, st));

@@ -59,16 +59,38 @@ __device__ __forceinline__ int64_t block_incl_scan(int64_t v, int64_t* total) {
     return v;
 }
 
-__global__ void __launch_bounds__(kScanBlock) k_scan_block_sums(const int32_t* counts, int64_t count, int64_t* block_sums) {
-    const int64_t i = int64_t(blockIdx.x) * kScanBlock + threadIdx.x;
-    int64_t total;
-    block_incl_scan((i < count) ? int64_t(counts[i]) : 0, &total);
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+// largest count of the block (counts are >= 0; 0 for an empty block)
+__device__ __forceinline__ int32_t block_max(int32_t v) {
+    __shared__ int32_t warp_max[kScanBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = __reduce_max_sync(0xffffffffu, v);
+    if (lane == 0) warp_max[warp] = v;
+    __syncthreads();
+    if (warp == 0) v = __reduce_max_sync(0xffffffffu, warp_max[lane]);
+    __syncthreads();
+    return v;
 }
 
-// one block: block_sums[0..nblocks) -> exclusive offsets, block_sums[nblocks] = the total
-__global__ void __launch_bounds__(kScanBlock) k_scan_block_offsets(int64_t* block_sums, int64_t nblocks) {
+// per block: the sum of its counts (block_sums) and their maximum (block_max)
+__global__ void __launch_bounds__(kScanBlock) k_scan_block_sums(const int32_t* counts, int64_t count, int64_t* block_sums,
+                                                              int64_t* block_maxima) {
+    const int64_t i = int64_t(blockIdx.x) * kScanBlock + threadIdx.x;
+    const int32_t c = (i < count) ? counts[i] : 0;
+    int64_t total;
+    block_incl_scan(int64_t(c), &total);
+    const int32_t m = block_max(c < 0 ? 0 : c);
+    if (threadIdx.x == 0) {
+        block_sums[blockIdx.x] = total;
+        block_maxima[blockIdx.x] = m;
+    }
+}
+
+// one block: block_sums[0..nblocks) -> exclusive offsets, block_sums[nblocks] = the total;
+// block_maxima[nblocks] = the largest count
+__global__ void __launch_bounds__(kScanBlock) k_scan_block_offsets(int64_t* block_sums, int64_t* block_maxima,
+                                                                 int64_t nblocks) {
     int64_t carry = 0;
+    int32_t mx = 0;
     for (int64_t b0 = 0; b0 < nblocks; b0 += kScanBlock) {
         const int64_t b = b0 + threadIdx.x;
         const int64_t v = b < nblocks ? block_sums[b] : 0;
@@ -76,8 +98,12 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_block_offsets(int64_t* bloc
         const int64_t incl = block_incl_scan(v, &total);
         if (b < nblocks) block_sums[b] = carry + incl - v;
         carry += total;
+        mx = max(mx, block_max(b < nblocks ? int32_t(block_maxima[b]) : 0));
     }
-    if (threadIdx.x == 0) block_sums[nblocks] = carry;
+    if (threadIdx.x == 0) {
+        block_sums[nblocks] = carry;
+        block_maxima[nblocks] = mx;
+    }
 }
 
 __global__ void __launch_bounds__(kScanBlock) k_scan_finish(const int32_t* counts, int64_t count, const int64_t* block_sums,
@@ -275,12 +301,82 @@ __device__ __forceinline__ float h2f(uint16_t h) { return __half2float(__ushort_
 __device__ __forceinline__ float snorm16(int16_t q) { return fmaxf(float(q) * (1.0f / 32767.0f), -1.0f); }
 __device__ __forceinline__ float unorm16(uint16_t q) { return float(q) * (1.0f / 65536.0f); }
 __device__ __forceinline__ float sq(float v) { return v * v; }
-// four consecutive 16-bit values (8-byte aligned) as sample i of the load
-__device__ __forceinline__ uint2 ld4h(const void* p, int64_t k) {
-    return *reinterpret_cast<const uint2*>(static_cast<const uint16_t*>(p) + k);
+
+// A pixel's running state before its first sample of the push (the class sums start empty).
+__device__ __forceinline__ void acc_init(PixelAcc& a) {
+    a.pflags = kPixUniform;
+    a.have_pat = false;
+    a.dev = false;
+    a.pat = 0;
+    a.pc = a.p1h = a.p1l = a.p2h = a.p2l = 0.0f;
+    for (int c = 0; c < kClasses; ++c) a.cc[c] = a.s1h[c] = a.s1l[c] = a.s2h[c] = a.s2l[c] = 0.0f;
 }
-__device__ __forceinline__ uint16_t lane4h(const uint2& v, int i) {
-    return uint16_t((i < 2 ? v.x : v.y) >> (16 * (i & 1)));
+
+// The grid-pass sums of a pixel without samples in the push.
+__device__ __forceinline__ void acc_store_empty(const GridPrep& gp, int64_t idx) {
+    gp.pat4[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    gp.pat2[idx] = make_float2(0.0f, __uint_as_float(uint32_t(kPixUniform) << 8));
+}
+
+__device__ __forceinline__ void acc_load(PixelAcc& a, const PixelPlanes& p, int64_t idx) {
+    a.mean = p.mean[idx];
+    a.m2 = p.square_diff[idx];
+    a.n = p.n[idx];
+    for (int c = 0; c < 3; ++c) {
+        a.cm[c] = p.color_mean[c][idx];
+        a.sm[c] = p.sqrt_mean[c][idx];
+        a.sq[c] = p.sqrt_sq[c][idx];
+        a.rad[c] = p.radiance[c][idx];
+        a.nor[c] = p.normal[c][idx];
+        a.alb[c] = p.albedo[c][idx];
+    }
+    a.dep = p.depth[idx];
+    a.hits = p.hit_count[idx];
+    a.nsamples = p.sample_count[idx];
+}
+
+// The pixel's statistics back to its planes, and its grid-pass sums: the pattern class's, and
+// for a deviant pixel the full per-class sums.
+__device__ __forceinline__ void acc_store(const PixelAcc& a, const PixelPlanes& p, const GridPrep& gp, int64_t idx,
+                                          bool prep) {
+    p.mean[idx] = a.mean;
+    p.square_diff[idx] = a.m2;
+    p.n[idx] = a.n;
+    for (int c = 0; c < 3; ++c) {
+        p.color_mean[c][idx] = a.cm[c];
+        p.sqrt_mean[c][idx] = a.sm[c];
+        p.sqrt_sq[c][idx] = a.sq[c];
+        p.radiance[c][idx] = a.rad[c];
+        p.normal[c][idx] = a.nor[c];
+        p.albedo[c][idx] = a.alb[c];
+    }
+    p.depth[idx] = a.dep;
+    p.hit_count[idx] = a.hits;
+    p.sample_count[idx] = a.nsamples;
+    if (prep) {
+        gp.pat4[idx] = make_float4(a.pc, a.p1h, a.p1l, a.p2h);
+        const uint32_t bits = uint32_t(a.have_pat ? a.pat : 0) |
+                              (uint32_t(a.pflags | (a.dev ? kPixDeviant : 0)) << 8);
+        gp.pat2[idx] = make_float2(a.p2l, __uint_as_float(bits));
+        if (a.dev) {
+            // full per-class sums: the deviating samples plus the pattern's
+            for (int c = 0; c < kClasses; ++c) {
+                float h1 = a.s1h[c], l1 = a.s1l[c], h2 = a.s2h[c], l2 = a.s2l[c], cnt = a.cc[c];
+                if (a.have_pat && (a.pat & class_bit(c))) {
+                    cnt += a.pc;
+                    df_add(h1, l1, a.p1h);
+                    l1 += a.p1l;
+                    df_add(h2, l2, a.p2h);
+                    l2 += a.p2l;
+                }
+                gp.cls[c][0][idx] = cnt;
+                gp.cls[c][1][idx] = h1;
+                gp.cls[c][2][idx] = l1;
+                gp.cls[c][3][idx] = h2;
+                gp.cls[c][4][idx] = l2;
+            }
+        }
+    }
 }
 
 // VEC4: every present plane is 16-byte aligned at the pixel's first sample and the pixel's
@@ -308,33 +404,12 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
                                                  (has_eu ? 0 : RPD_SAMPLE_ENV_VALID)));
     const float fx = float(idx % gp.width), fy = float(idx / gp.width);
     PixelAcc a;
-    a.pflags = kPixUniform;
-    a.have_pat = false;
-    a.dev = false;
-    a.pat = 0;
-    a.pc = a.p1h = a.p1l = a.p2h = a.p2l = 0.0f;
-    for (int c = 0; c < kClasses; ++c) a.cc[c] = a.s1h[c] = a.s1l[c] = a.s2h[c] = a.s2l[c] = 0.0f;
+    acc_init(a);
     if (k0 == k1) {
-        if (prep) {
-            gp.pat4[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            gp.pat2[idx] = make_float2(0.0f, __uint_as_float(uint32_t(a.pflags) << 8));
-        }
+        if (prep) acc_store_empty(gp, idx);
         return;
     }
-    a.mean = p.mean[idx];
-    a.m2 = p.square_diff[idx];
-    a.n = p.n[idx];
-    for (int c = 0; c < 3; ++c) {
-        a.cm[c] = p.color_mean[c][idx];
-        a.sm[c] = p.sqrt_mean[c][idx];
-        a.sq[c] = p.sqrt_sq[c][idx];
-        a.rad[c] = p.radiance[c][idx];
-        a.nor[c] = p.normal[c][idx];
-        a.alb[c] = p.albedo[c][idx];
-    }
-    a.dep = p.depth[idx];
-    a.hits = p.hit_count[idx];
-    a.nsamples = p.sample_count[idx];
+    acc_load(a, p, idx);
     const bool per_sample_albedo = !COMPACT && s.albedo[0] != nullptr;
     float palb[3] = {0.0f, 0.0f, 0.0f};
     if (COMPACT) {
@@ -527,44 +602,7 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
         }
     }
 
-    p.mean[idx] = a.mean;
-    p.square_diff[idx] = a.m2;
-    p.n[idx] = a.n;
-    for (int c = 0; c < 3; ++c) {
-        p.color_mean[c][idx] = a.cm[c];
-        p.sqrt_mean[c][idx] = a.sm[c];
-        p.sqrt_sq[c][idx] = a.sq[c];
-        p.radiance[c][idx] = a.rad[c];
-        p.normal[c][idx] = a.nor[c];
-        p.albedo[c][idx] = a.alb[c];
-    }
-    p.depth[idx] = a.dep;
-    p.hit_count[idx] = a.hits;
-    p.sample_count[idx] = a.nsamples;
-    if (prep) {
-        gp.pat4[idx] = make_float4(a.pc, a.p1h, a.p1l, a.p2h);
-        const uint32_t bits = uint32_t(a.have_pat ? a.pat : 0) |
-                              (uint32_t(a.pflags | (a.dev ? kPixDeviant : 0)) << 8);
-        gp.pat2[idx] = make_float2(a.p2l, __uint_as_float(bits));
-        if (a.dev) {
-            // full per-class sums: the deviating samples plus the pattern's
-            for (int c = 0; c < kClasses; ++c) {
-                float h1 = a.s1h[c], l1 = a.s1l[c], h2 = a.s2h[c], l2 = a.s2l[c], cnt = a.cc[c];
-                if (a.have_pat && (a.pat & class_bit(c))) {
-                    cnt += a.pc;
-                    df_add(h1, l1, a.p1h);
-                    l1 += a.p1l;
-                    df_add(h2, l2, a.p2h);
-                    l2 += a.p2l;
-                }
-                gp.cls[c][0][idx] = cnt;
-                gp.cls[c][1][idx] = h1;
-                gp.cls[c][2][idx] = l1;
-                gp.cls[c][3][idx] = h2;
-                gp.cls[c][4][idx] = l2;
-            }
-        }
-    }
+    acc_store(a, p, gp, idx, prep);
 }
 
 // Valid-flag bit each dependency needs, and whether it bins the screen position.
@@ -805,12 +843,19 @@ cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count) 
     KernelScope ks(j, RPD_KERNEL_OFFSETS);
     if (count <= 0) return cudaMemsetAsync(j.offsets, 0, sizeof(int64_t), j.stream);
     const int64_t nblocks = (count + kScanBlock - 1) / kScanBlock;
-    int64_t* block_sums = j.offsets + (count + 1);  // the offsets buffer reserves room for these
-    k_scan_block_sums<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums);
-    k_scan_block_offsets<<<1, kScanBlock, 0, j.stream>>>(block_sums, nblocks);
+    // the offsets buffer reserves room for these after offsets[count]
+    int64_t* block_sums = j.offsets + (count + 1);
+    int64_t* block_maxima = block_sums + (nblocks + 1);
+    k_scan_block_sums<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums, block_maxima);
+    k_scan_block_offsets<<<1, kScanBlock, 0, j.stream>>>(block_sums, block_maxima, nblocks);
     k_scan_finish<<<unsigned(nblocks), kScanBlock, 0, j.stream>>>(d_counts, count, block_sums, j.offsets);
     j.launches += 3;
     return cudaGetLastError();
+}
+
+const int64_t* offsets_count_max(const Job& j, int64_t count) {
+    const int64_t nblocks = (count + kScanBlock - 1) / kScanBlock;
+    return j.offsets + (count + 1) + (nblocks + 1) + nblocks;
 }
 
 cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,

@@ -21,6 +21,7 @@
 // products via FMA; about 2^-44 relative — GB300 executes double precision at 1/55 of its
 // single-precision rate). With a power-of-two node step every weight is an exact multiple
 // of 1/step^2, so the bin weights are accumulated as exact integers.
+#include <cmath>
 #include <type_traits>
 
 #include "rpd_internal.h"
@@ -653,6 +654,11 @@ struct RandParams {
     uint32_t spp_magic;  // floor(k / spp) == umulhi(k, magic) for every in-segment k (0: search)
     int spp_shift;       // spp is 2^shift (-1: not a power of two)
     int cols;            // support columns of a node, 2 * step + 3 (shared-memory tables)
+    // a launch that runs only when the push's largest per-pixel count (*max_count, in device
+    // memory) is at most (max_mode 1) or above (max_mode 2) max_limit; max_mode 0: always runs
+    const int64_t* max_count;
+    int64_t max_limit;
+    int max_mode;
 };
 
 template <int WB, int DS>
@@ -931,6 +937,7 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
     using WT = std::conditional_t<WB == 2, uint16_t, uint32_t>;
     constexpr int NW = RW * DS;
     constexpr int VPT = (2 * kRandSlots + NW * 32 - 1) / (NW * 32);  // combined values per thread
+    if (rp.max_mode != 0 && ((*rp.max_count <= rp.max_limit) != (rp.max_mode == 1))) return;  // the other form runs
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using L = RandLayout<WB, DS>;
     const int lane = threadIdx.x & 31;
@@ -1159,7 +1166,7 @@ cudaError_t launch_random_shape(Job& j, const RandParams& rp, const GridPrep& gp
 }  // namespace
 
 cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int64_t count, const GridPrep& gp,
-                             int32_t spp, int32_t max_count, int64_t total_samples) {
+                             int32_t spp, int32_t max_count, int64_t total_samples, const int64_t* d_max_count) {
     const int step = j.g.step;
     const bool pow2 = (step & (step - 1)) == 0;
     GridParams gpar{j.g, first, count, 0, 0, 0, pow2 ? 1 : 0, 1.0f / float(step), spp, spp > 0 ? 1.0f / float(spp) : 0.0f};
@@ -1212,7 +1219,7 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     KernelScope ks(j, RPD_KERNEL_GRID_RANDOM);
-    RandParams rp{gpar, 0u, -1, 2 * step + 3};
+    RandParams rp{gpar, 0u, -1, 2 * step + 3, nullptr, 0, 0};
     if (spp > 0) {
         if ((spp & (spp - 1)) == 0) {
             int sh = 0;
@@ -1222,13 +1229,39 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
             rp.spp_magic = spp_magic_for(spp, (2 * step + 3) * spp);
         }
     }
-    // 16-bit lane sums (smaller bins, more resident warps) when no lane's sum can reach 2^16: a
-    // lane takes at most 1/32 of a node's quads of a uniform push (plus two partial quads per row
-    // segment) and each sample adds at most step^2 units
+    // 16-bit lane sums (smaller bins, more resident warps) when no lane's sum can reach 2^16. Each
+    // sample adds at most step^2 units. Uniform push: a lane takes at most 1/32 of a node's quads
+    // (plus two partial quads per row segment). Per-pixel counts of at most M: a node's support
+    // holds at most side^2 M samples, a segment of len samples spans at most len/4 + 1.5 quads, and
+    // a lane takes at most 1/32 of a chunk's (up to 32 segments) quads plus one, so at most
+    // side^2 M / 32 + 10 samples per chunk of 32 support rows.
     const bool default_shape = j.grid_shape == 0 || j.grid_shape == 6;
-    const bool w16 = int_w && default_shape && spp > 0 &&
-                     (double(sup + 3) * double(sup + 3) * double(spp) / 32.0 + 8.0) * double(step) * double(step) < 65536.0;
-    if (w16) return launch_random_shape<2>(j, rp, gp, j.grid_shape);
+    const double side = double(2 * step + 3), units = double(step) * double(step);
+    const double chunks = std::ceil(side / 32.0);
+    auto counts_fit = [&](double m) { return (side * side * m / 32.0 + 10.0 * chunks) * units < 65536.0; };
+    if (int_w && default_shape) {
+        if (spp > 0) {
+            if ((double(sup + 3) * double(sup + 3) * double(spp) / 32.0 + 8.0) * units < 65536.0)
+                return launch_random_shape<2>(j, rp, gp, j.grid_shape);
+        } else if (max_count != INT32_MAX) {
+            if (counts_fit(double(std::max(max_count, 1)))) return launch_random_shape<2>(j, rp, gp, j.grid_shape);
+        } else if (d_max_count) {
+            // the largest count is known on the device only: launch both forms, each block of the
+            // one that does not apply returns at once
+            int64_t lim = int64_t(std::max(0.0, (65536.0 / units - 10.0 * chunks) * 32.0 / (side * side)));
+            while (lim > 0 && !counts_fit(double(lim))) --lim;
+            if (lim > 0) {
+                RandParams r16 = rp;
+                r16.max_count = d_max_count;
+                r16.max_limit = lim;
+                r16.max_mode = 1;
+                if ((e = launch_random_shape<2>(j, r16, gp, j.grid_shape)) != cudaSuccess) return e;
+                RandParams r32 = r16;
+                r32.max_mode = 2;
+                return launch_random_shape<4>(j, r32, gp, j.grid_shape);
+            }
+        }
+    }
     return int_w ? launch_random_shape<4>(j, rp, gp, j.grid_shape) : launch_random_shape<8>(j, rp, gp, j.grid_shape);
 }
 

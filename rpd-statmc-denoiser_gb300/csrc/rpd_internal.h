@@ -290,14 +290,20 @@ __host__ __device__ constexpr int key_bin_shift(int group) {
 cudaError_t launch_encode_samples16(const DeviceSamples& in, int64_t n_samples, int64_t n_pixels,
                                     const DeviceSamples16& out, cudaStream_t stream);
 cudaError_t launch_offsets_uniform(Job& j, int64_t count, int32_t spp);
+// The exclusive offsets of per-pixel counts into j.offsets[0..count]; the largest count goes to
+// offsets_count_max(j, count), which stays valid until the next scan.
 cudaError_t launch_offsets_scan(Job& j, const int32_t* d_counts, int64_t count);
+const int64_t* offsets_count_max(const Job& j, int64_t count);
 cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,
                                      const GridPrep& gp, int32_t spp);
 cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first, int64_t count);
 // max_count bounds the samples of one pixel; total_samples bounds the samples of the push. Either
 // bound can make the bin weights exact integers (no bin of a node can then pass 2^32 units).
+// d_max_count: the push's largest per-pixel count in device memory when the host does not know it
+// (max_count INT32_MAX), or nullptr.
 cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int64_t count, const GridPrep& gp,
-                             int32_t spp, int32_t max_count, int64_t total_samples);
+                             int32_t spp, int32_t max_count, int64_t total_samples,
+                             const int64_t* d_max_count = nullptr);
 cudaError_t launch_merge_grid(Job& j);
 cudaError_t launch_feature_cache(Job& j);
 cudaError_t launch_sensitivity(Job& j);
