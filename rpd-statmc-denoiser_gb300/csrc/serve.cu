@@ -134,13 +134,18 @@ __global__ void k_srv_synth_uniform(rpd_synth_params prm, const rpd_synth_region
     srv_write(o, int64_t(y) * row_samples + rk, s);
 }
 
-// counts[i] samples for pixel i at offsets[i] + q, ordinals start + q. One block per 256
-// pixels; the block's offsets are staged in shared memory for the owner search.
+// counts[i] samples for pixel i at offsets[i] + q, ordinals start + q. One block of 256
+// threads per 256 pixels: each thread marks its pixel's samples among the block's first
+// kSynthOwners in shared memory, and a sample past those finds its pixel by a search of the
+// block's offsets.
 constexpr int kSynthPix = 256;
-__global__ void k_srv_synth_counts(rpd_synth_params prm, const rpd_synth_region* table, const uint8_t* region,
-                                   const int64_t* offsets, int64_t np, int64_t capacity, uint32_t start, SynthOut o) {
+constexpr int kSynthOwners = 4096;
+__global__ void __launch_bounds__(kSynthPix) k_srv_synth_counts(rpd_synth_params prm, const rpd_synth_region* table,
+                                                                const uint8_t* region, const int64_t* offsets, int64_t np,
+                                                                int64_t capacity, uint32_t start, SynthOut o) {
     __shared__ int64_t off[kSynthPix + 1];
     __shared__ int xy[kSynthPix][2];
+    __shared__ uint8_t owner[kSynthOwners];
     const int64_t p0 = int64_t(blockIdx.x) * kSynthPix;
     const int np_block = int(min((long long)kSynthPix, (long long)(np - p0)));
     for (int t = threadIdx.x; t <= np_block; t += blockDim.x) {
@@ -155,11 +160,21 @@ __global__ void k_srv_synth_counts(rpd_synth_params prm, const rpd_synth_region*
     // the counts of a pass never exceed adaptive_spp * W * H (the capacity); the bound only keeps
     // the writes inside the buffer
     const int64_t k0 = off[0], k1 = min((long long)off[np_block], (long long)capacity);
+    const int64_t marked = min((long long)(k1 - k0), (long long)kSynthOwners);  // samples k0 .. k0 + marked - 1
+    if (threadIdx.x < np_block) {
+        const int64_t a = off[threadIdx.x] - k0, b = min((long long)(off[threadIdx.x + 1] - k0), (long long)marked);
+        for (int64_t u = a; u < b; ++u) owner[u] = uint8_t(threadIdx.x);
+    }
+    __syncthreads();
     for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         int lo = 0, hi = np_block - 1;  // last pixel whose offset <= k
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (off[mid] <= k) lo = mid; else hi = mid - 1;
+        if (k - k0 < marked) {
+            lo = owner[k - k0];
+        } else {
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (off[mid] <= k) lo = mid; else hi = mid - 1;
+            }
         }
         const int64_t i = p0 + lo;
         rpd_synth_sample s;
