@@ -882,11 +882,9 @@ cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t fir
     }
     vec4 = vec4 && (!gp.lum || (aligned(gp.lum, 16) && aligned(gp.key, 16)));
     const unsigned blocks = grid_for(count, 128);
-    // resident blocks per SM, measured on GB300: compact planes 4 (vector loads) and 5; FP32
-    // planes 3 (vector loads) and 5
     // Shapes measured on GB300 at 1920x1080. Up to 16 samples per pixel, more resident pixels
-    // hide the per-pixel latency (compact planes 4 blocks per SM, FP32 planes 3, per-pixel counts
-    // 5). From 32 on, a thread's sample run spans more bytes per plane than L1 keeps between its
+    // hide the per-pixel latency (compact planes 4 blocks per SM, FP32 planes 3; per-pixel counts
+    // 4 over compact planes, 5 over FP32 planes). From 32 on, a thread's sample run spans more bytes per plane than L1 keeps between its
     // loads, and a block's registers are not capped; from 64 on, compact planes are read 16 bytes
     // (8 samples) per load.
     const bool many = spp > 16;
@@ -906,7 +904,7 @@ cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t fir
         else if (vec4)
             k_accumulate_pixels<true, true, false, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
         else
-            k_accumulate_pixels<false, true, false, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<false, true, false, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
     } else {
         if (vec4 && many)
             k_accumulate_pixels<true, false, false, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
