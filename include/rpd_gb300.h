@@ -367,6 +367,16 @@ int rpd_adaptive_allocate(rpd_job* job, const float* importance, rpd_memory wher
 /* FrameBuffers::finalize (core/buffers.h:152-167) on the radiance/feature sums. */
 int rpd_finalize(rpd_job* job);
 
+/* rpd_job_push_samples / rpd_job_push_samples16 of host planes (RPD_MEM_HOST) that return once
+ * the copies are enqueued (no counterpart in the reference, whose push has read its input when it
+ * returns): the planes and counts must be page-locked (rpd_host_alloc) and stay unchanged until
+ * rpd_job_sync returns. The copies overlap whatever the caller does next, such as the stages of
+ * another job or the next frame's push into another job. */
+int rpd_job_push_samples_async(rpd_job* job, const rpd_sample_soa* s, int64_t first_pixel,
+                               int64_t pixel_count, int32_t spp, const int32_t* counts);
+int rpd_job_push_samples16_async(rpd_job* job, const rpd_sample_soa16* s, int64_t first_pixel,
+                                 int64_t pixel_count, int32_t spp, const int32_t* counts);
+
 /* Copy a field to `where` memory. bytes must equal the field's size. */
 int rpd_job_read(rpd_job* job, rpd_field field, void* dst, size_t bytes, rpd_memory where);
 /* rpd_job_read enqueued on the job's stream without waiting: dst (page-locked host memory from

@@ -633,7 +633,8 @@ struct HostPlane {
 // job stream as soon as its copy is done, overlapping the copies of the later bands (a pass
 // pushed in bands accumulates exactly as one push). The copies wait only for the previous host
 // push's passes to release the staging. Returns when every copy has completed, so the caller
-// may reuse its host planes.
+// may reuse its host planes; for the asynchronous pushes (j->host_async) it returns once the copies
+// are enqueued, and the job stream's passes wait for them.
 static int push_host_banded(Job* j, const std::vector<HostPlane>& planes, const DeviceSamples& proto, int64_t first,
                             int64_t count, int32_t spp, const int32_t* counts, int64_t total) {
     std::vector<int64_t> pre;
@@ -707,7 +708,7 @@ static int push_host_banded(Job* j, const std::vector<HostPlane>& planes, const 
         if (st != RPD_OK) return st;
     }
     RPD_CUDA(cudaEventRecord(j->staging_free, j->stream));
-    RPD_CUDA(cudaStreamSynchronize(j->copy_stream));
+    if (!j->host_async) RPD_CUDA(cudaStreamSynchronize(j->copy_stream));
     return RPD_OK;
 }
 
@@ -1212,6 +1213,26 @@ int rpd_job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory 
 
 int rpd_job_read_async(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memory where) {
     return job_read(job, f, dst, bytes, where, false);
+}
+
+int rpd_job_push_samples_async(rpd_job* job, const rpd_sample_soa* s, int64_t first, int64_t count, int32_t spp,
+                               const int32_t* counts) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    j->host_async = true;
+    const int st = rpd_job_push_samples(job, s, first, count, spp, counts, RPD_MEM_HOST);
+    j->host_async = false;
+    return st;
+}
+
+int rpd_job_push_samples16_async(rpd_job* job, const rpd_sample_soa16* s, int64_t first, int64_t count, int32_t spp,
+                                 const int32_t* counts) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    j->host_async = true;
+    const int st = rpd_job_push_samples16(job, s, first, count, spp, counts, RPD_MEM_HOST);
+    j->host_async = false;
+    return st;
 }
 
 int rpd_job_sync(rpd_job* job) {

@@ -274,6 +274,8 @@ def lib() -> C.CDLL:
         "rpd_job_begin_frame": (C.c_int, [vp]),
         "rpd_job_push_samples": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp, C.c_int]),
         "rpd_job_push_samples16": (C.c_int, [vp, C.POINTER(SampleSoA16), i64, i64, i32, vp, C.c_int]),
+        "rpd_job_push_samples_async": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, i32, vp]),
+        "rpd_job_push_samples16_async": (C.c_int, [vp, C.POINTER(SampleSoA16), i64, i64, i32, vp]),
         "rpd_encode_samples16": (C.c_int, [vp, C.POINTER(SampleSoA), i64, i64, C.POINTER(SampleSoA16)]),
         "rpd_job_autotune": (C.c_int, [vp, C.POINTER(SampleSoA), C.POINTER(SampleSoA16), i32]),
         "rpd_batch_create": (C.c_int, [vp, C.POINTER(vp)]),
@@ -340,7 +342,8 @@ def exported_symbols() -> list[str]:
             "rpd_server_config_defaults", "rpd_server_create", "rpd_server_submit", "rpd_server_poll",
             "rpd_server_drain", "rpd_server_cancel", "rpd_server_get_stats", "rpd_server_kernel_times",
             "rpd_server_destroy",
-            "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_push_samples16", "rpd_encode_samples16",
+            "rpd_job_begin_frame", "rpd_job_push_samples", "rpd_job_push_samples16", "rpd_job_push_samples_async",
+            "rpd_job_push_samples16_async", "rpd_encode_samples16",
             "rpd_job_autotune", "rpd_batch_create", "rpd_batch_add", "rpd_batch_run", "rpd_batch_sync",
             "rpd_batch_last_ms", "rpd_batch_kernel_count", "rpd_batch_set_lanes", "rpd_batch_destroy", "rpd_job_end_pass", "rpd_recompute_sensitivity",
             "rpd_statmc_denoise", "rpd_variance_denoise", "rpd_compute_adaptive_sample_counts", "rpd_finalize",
@@ -695,6 +698,16 @@ class Job:
         else:
             cp = counts.ptr
         check(lib().rpd_job_push_samples(self.handle, C.byref(s), first, count, spp, cp, where))
+
+    def push_async(self, samples, first: int, count: int, spp: int = 0, counts_ptr=None) -> None:
+        """rpd_job_push_samples_async (or its compact form, by the type of samples.soa()) of
+        page-locked host planes (rpd_host_alloc memory, as are the counts at counts_ptr if given):
+        the copies run after the call returns, so the planes must stay unchanged until sync()."""
+        s = samples.soa()
+        if isinstance(s, SampleSoA16):
+            check(lib().rpd_job_push_samples16_async(self.handle, C.byref(s), first, count, spp, counts_ptr))
+        else:
+            check(lib().rpd_job_push_samples_async(self.handle, C.byref(s), first, count, spp, counts_ptr))
 
     def push16(self, samples, first: int, count: int, spp: int = 0, counts=None, where: int = MEM_DEVICE) -> None:
         """rpd_job_push_samples16 of compact planes (device-resident unless `where` says host)."""
