@@ -36,7 +36,7 @@ __device__ __forceinline__ float conservative_variance_update(float value, float
 // float operations are the reference's, in its order; the two quotient gates are decided by a
 // product or a reciprocal square root away from their thresholds and by the IEEE quotient near
 // them, and the spatial weights 1 / (1 + d^2) come from a table.
-constexpr int kVarTx = 32, kVarTy = 8;
+constexpr int kVarTx = 32, kVarTy = 16;
 constexpr float kGateBand = 1.0f / 1048576.0f;  // 2^-20
 
 __global__ void __launch_bounds__(kVarTx * kVarTy) k_var_smooth(PixelPlanes p, VarParams prm, const float* src,
