@@ -65,18 +65,22 @@ def config_json(R, cfg, extra=None):
 
 
 # Algorithmic bytes each kernel family must move for one frame (per launch of that family
-# in a frame), from the plane sizes: per sample 29 B for the statistics pass (radiance 12,
-# normal 12, depth 4, flags 1), 46 B for the grid pass (radiance 12, pixel/lens/brdf/light
-# uv 32, flags 1, category 1); per pixel 12 B of albedo plus 96 B of state read and written
-# by the statistics pass; per node 3744 B of grid read and written by the grid pass; per
-# pixel 100 B read and 32 B written by the StatMC window.
+# in a frame), from the plane sizes. Statistics pass: per sample 62 B of FP32 planes read
+# (radiance 12, normal 12, depth 4, pixel/lens/brdf/light uv 32, flags 1, category 1) and 8 B
+# written for the grid pass (luminance, packed key); per pixel 12 B of albedo read, 88 B of
+# statistics and sums read and written (176 B) and 24 B of pattern sums written. Grid pass:
+# per sample the 8 B the statistics pass wrote; per node 3744 B of grid read and written.
+# StatMC window: per pixel the 96 B of packed neighbour records (read once; the halos of
+# neighbouring tiles come from L2) and 20 B of outputs.
 def algorithmic_bytes(kernel: str, np_: int, nn: int, n: int) -> float:
     if kernel == "accumulate_pixels":
-        return 29.0 * n + (12.0 + 192.0) * np_
+        return 70.0 * n + (12.0 + 176.0 + 24.0) * np_
     if kernel == "grid":
-        return 46.0 * n + 2.0 * 3744.0 * nn
+        return 8.0 * n + 24.0 * np_ + 2.0 * 3744.0 * nn
+    if kernel == "grid_random":
+        return 8.0 * n + 2.0 * 3744.0 * nn
     if kernel == "statmc_window":
-        return 132.0 * np_
+        return (96.0 + 20.0) * np_
     if kernel == "merge":
         return 3.0 * 3744.0 * nn
     if kernel == "variance":
@@ -84,6 +88,17 @@ def algorithmic_bytes(kernel: str, np_: int, nn: int, n: int) -> float:
     if kernel == "node_stats":
         return 3744.0 * nn + 4.0 * 34 * nn
     return 0.0
+
+
+# FP32-equivalent operations per neighbour visit of the StatMC window, counted from the
+# reference's loop body (main.cpp:1032-1096): gates ~15, Welch per channel ~12 (x3), RPD
+# relaxation and weight ~10, weighted accumulation ~12. One frame visits W*H*(2r+1)^2
+# neighbours. Fixed here once; the roofline's achieved rate for the window uses it.
+WINDOW_OPS_PER_VISIT = 75
+
+
+def window_visits(w: int, h: int, r: int) -> int:
+    return w * h * (2 * r + 1) ** 2
 
 
 class ClockSampler:
@@ -201,6 +216,8 @@ def run_gpu(args):
     for _ in range(args.warmup):
         step(samples)
     job.sync()
+    # the FP32 issue rate of this GPU at its present clock: the window's roofline denominator
+    fp32_peak = R.probe_fp32_issue(local, 5)
     # device-resident timed region
     job.set_profiling(True)
     job.reset_kernel_times()
@@ -281,28 +298,20 @@ def run_gpu(args):
         for o in outs:
             o.free()
 
-    # roofline of the dominant kernel
-    dominant = max(ktimes, key=lambda k: ktimes[k][0])
-    dom_ms, dom_launches = ktimes[dominant]
-    per_launch_ms = dom_ms / max(1, dom_launches)
-    launches_per_frame = max(1, dom_launches // args.steps)
-    alg = algorithmic_bytes(dominant, np_, nn, n) / launches_per_frame
+    # roofline of the dominant kernel (per-launch CUDA-event time on the job stream)
     peaks = measured_peaks()
-    achieved = alg / (per_launch_ms * 1e-3) / 1e9 if alg else None
-    # DRAM bytes per launch of the dominant kernel from one ncu --set full capture of this bench
-    # at 960x540 (dram__bytes_read.sum + dram__bytes_write.sum: 51.9 + 3.2 MB), scaled by the pixel
-    # count: the window's traffic grows with the pixels it filters
-    ncu_traffic = {"statmc_window": (55.08e6 * (np_ / (960 * 540)), "ncu at 960x540, scaled by the pixel count")}
-    traffic = ncu_traffic.get(dominant) if (W, H, SPP) == (1920, 1080, 16) else None
-    roofline = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
-                "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": round(achieved / peaks["hbm_gbs"], 4) if achieved else None,
-                "traffic": round(traffic[0]) if traffic else None,
-                "traffic_source": traffic[1] if traffic else None,
-                "peak_source": peaks["source"], "ms_per_launch": round(per_launch_ms, 4),
-                "algorithmic_bytes_per_launch": alg,
-                "note": "the StatMC window is bound by instruction issue (window decisions per neighbour), "
-                        "not by HBM; no dense contraction exists on this path"}
+    dominant = max(ktimes, key=lambda k: ktimes[k][0])
+    roofline = kernel_roofline(dominant, ktimes[dominant], args.steps, cfg, np_, nn, n, peaks, fp32_peak)
+    others = {k: kernel_roofline(k, ktimes[k], args.steps, cfg, np_, nn, n, peaks, fp32_peak)
+              for k in ("statmc_window", "accumulate_pixels", "grid_random") if k != dominant and ktimes[k][1]}
+    # the whole frame against HBM: the sample planes read once plus the required per-pixel
+    # outputs (denoised RGB, uncertainty, alpha, variance_denoised) and the albedo input
+    frame_bytes = 62.0 * n + (24.0 + 12.0) * np_
+    frame_gbs = frame_bytes / (ms_per_step * 1e-3) / 1e9
+    roofline["frame"] = {"bytes_per_step": frame_bytes, "achieved": round(frame_gbs, 1), "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": round(frame_gbs / peaks["hbm_gbs"], 4),
+                         "floor_ms": round(frame_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3, 4)}
+    roofline["other_kernels"] = others
     kernels_ms = {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]}
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -316,7 +325,7 @@ def run_gpu(args):
     if quality is not None:
         out["quality"] = quality
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, steps=1)
+        out["cpu_baseline"] = cpu_baseline(args, steps=3)
     job.close()
     if samples is not dev:
         samples.free()
@@ -390,6 +399,45 @@ def compact_quality(R, ctx, cfg, dev, dev16):
     return {"reference": "the same frame pushed as FP32 planes (the oracle-pinned path)",
             "rel_mse": float(np.mean((x - r) ** 2 / (r * r + 1e-2))),
             "max_rel_err": float(np.max(np.abs(x - r) / np.maximum(np.abs(r), 1e-3)))}
+
+
+# DRAM bytes per pixel per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu
+# captures summarised in profiles/, for the kernels whose traffic grows with the pixel count
+NCU_TRAFFIC_PER_PIXEL = {}
+
+
+def kernel_roofline(kernel, times, steps, cfg, np_, nn, n, peaks, fp32_peak):
+    """Roofline of one kernel family: achieved = algorithmic work per launch / average launch
+    time. The StatMC window is bound by FP32 issue (its neighbour decisions), the rest by HBM."""
+    total_ms, launches = times
+    per_launch_ms = total_ms / max(1, launches)
+    launches_per_frame = max(1, launches // steps)
+    alg = algorithmic_bytes(kernel, np_, nn, n) / launches_per_frame
+    gbs = alg / (per_launch_ms * 1e-3) / 1e9 if alg else None
+    traffic = NCU_TRAFFIC_PER_PIXEL.get(kernel)
+    hbm = {"achieved": round(gbs, 1) if gbs else None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+           "frac": round(gbs / peaks["hbm_gbs"], 4) if gbs else None, "peak_source": peaks["source"],
+           "algorithmic_bytes_per_launch": alg,
+           "traffic": round(traffic[0] * np_) if traffic else None,
+           "traffic_source": traffic[1] if traffic else None}
+    out = {"kernel": kernel, "ms_per_launch": round(per_launch_ms, 4)}
+    if kernel == "statmc_window" and fp32_peak:
+        visits = window_visits(cfg.image_width, cfg.image_height, cfg.color_window_radius)
+        ops = WINDOW_OPS_PER_VISIT * visits
+        achieved = ops / (per_launch_ms * 1e-3) / 1e9
+        peak = fp32_peak["per_second"] / 1e9
+        out.update({"bound": "fp32_issue", "achieved": round(achieved, 1), "peak": round(peak, 1),
+                    "unit": "Gop/s (FP32 lane operations)", "frac": round(achieved / peak, 4),
+                    "traffic": hbm["traffic"],
+                    "ops_per_launch": ops, "ops_per_visit": WINDOW_OPS_PER_VISIT, "visits_per_launch": visits,
+                    "peak_source": "measured here: rpd_probe_fp32_issue (independent FFMA chains on every SM, "
+                                   f"CUDA events, best of 5: {fp32_peak['ms']:.3f} ms)",
+                    "hbm": hbm})
+    else:
+        out.update({"bound": "hbm", "achieved": hbm["achieved"], "peak": hbm["peak"], "unit": "GB/s",
+                    "frac": hbm["frac"], "traffic": hbm["traffic"], "traffic_source": hbm["traffic_source"],
+                    "peak_source": hbm["peak_source"], "algorithmic_bytes_per_launch": alg})
+    return out
 
 
 def measured_peaks():
@@ -735,6 +783,19 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def launch_replicas(n: int, argv: list[str]) -> int:
+    """Run this bench as n replica processes (torch.distributed.run, rendezvous on 127.0.0.1);
+    returns their exit status."""
+    import socket
+
+    with socket.socket() as sock:
+        sock.bind(("127.0.0.1", 0))
+        port = sock.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(Path(__file__).resolve()), *argv]
+    return subprocess.call(cmd)
+
+
 def main():
     global W, H, SPP, METRIC
     ap = argparse.ArgumentParser()
@@ -766,6 +827,12 @@ def main():
     ap.add_argument("--plain-requests", type=int, default=200, help="serving: stream prefix run through the plain drop-in")
     ap.add_argument("--passes", type=int, default=1, help="request: adaptive passes of the profiled request")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one replica process per GPU, as the driver launches it: rerun this command under
+        # torch.distributed.run (rank r uses GPU r; rank 0 prints the line)
+        sys.exit(launch_replicas(args.gpus, sys.argv[1:]))
+    if "WORLD_SIZE" in os.environ and int(os.environ["WORLD_SIZE"]) != args.gpus:
+        sys.exit(f"--gpus {args.gpus} does not match WORLD_SIZE={os.environ['WORLD_SIZE']}")
     if (args.width, args.height, args.spp) != (W, H, SPP):
         W, H, SPP = args.width, args.height, args.spp
         METRIC = f"denoised Msamples/s at {W}x{H} {SPP}spp (plain)"

@@ -274,7 +274,7 @@ int rpd_job_set_exact(rpd_job* job, int flags);
  * overlapping the previous band's passes. */
 #define RPD_TUNE_HOST_BAND_MB 1
 /* RPD_TUNE_STATMC_ROWS: pixel rows per block of the StatMC window kernel: 2, 4 or 8 (0, the
- * default: the tallest whose halo tile fits in shared memory). */
+ * default: 8 where the halo tile fits in shared memory, else the tallest that fits). */
 #define RPD_TUNE_STATMC_ROWS 2
 /* RPD_TUNE_ALLOCATOR: 0 (default) the parallel allocation of the adaptive counts on one block
  * per SM, N >= 2 the same on at most N blocks, 1 the one-thread kernel in the reference's order.
@@ -284,6 +284,12 @@ int rpd_job_set_exact(rpd_job* job, int flags);
  * carried out exactly in integer instructions, 1 all of it in double-precision instructions. Both
  * give the same bits. */
 #define RPD_TUNE_SMOOTHING 4
+/* RPD_TUNE_WINDOW_GUARD: the fast StatMC window recomputes in double every neighbour whose
+ * compatibility q (or Welch-Satterthwaite df) lies within 2^-g, relative, of a decision point,
+ * and every pixel whose weight sum lies within 2^-(g+1) of the blend's 1.1 test; g = 15 by
+ * default, 0..15 allowed. A smaller g sends more decisions to double; results stay within the
+ * plain-form bar for every g (tested). */
+#define RPD_TUNE_WINDOW_GUARD 5
 int rpd_job_set_tuning(rpd_job* job, int knob, int value);
 int rpd_job_get_tuning(rpd_job* job, int knob, int* value);
 /* Start a new frame: clears every accumulator, like render_image_statmc's set-up. */
@@ -400,6 +406,29 @@ const char* rpd_kernel_name(rpd_kernel kernel);
  * milliseconds between two recorded slots (synchronises on the later one). */
 int rpd_job_mark(rpd_job* job, int slot);
 int rpd_job_mark_elapsed(rpd_job* job, int from_slot, int to_slot, float* ms);
+
+/* Device-side counters of a job, no counterpart in the reference (its statmc_denoise,
+ * main.cpp:957-1162, evaluates every neighbour in double precision). The fast StatMC window
+ * evaluates neighbours in single precision and recomputes in double, exactly as the reference
+ * does, the decisions that fall inside its guard bands; these counters show how often. */
+typedef enum rpd_counter {
+    RPD_COUNTER_WINDOW_PAIR_RECHECKS = 0,  /* neighbour pairs whose compatibility q was recomputed in
+                                            * double (last statmc_denoise) */
+    RPD_COUNTER_WINDOW_PIXEL_RECHECKS,     /* pixels whose whole window was recomputed in double
+                                            * (weight sum within the 1.1 test's band; last statmc_denoise) */
+    RPD_COUNTER_DEVICE_WAIT_TIMEOUTS,      /* bounded device-side waits that gave up (since job creation);
+                                            * rpd_job_sync returns RPD_ERR_TIMEOUT while it is non-zero */
+    RPD_COUNTER_COUNT_ = 8
+} rpd_counter;
+/* Waits for the job's stream and copies min(n, RPD_COUNTER_COUNT_) counters to out. */
+int rpd_job_counters(rpd_job* job, uint64_t* out, int32_t n);
+
+/* FP32 issue-rate probe (no counterpart in the reference): times a microkernel in which every
+ * thread of a grid filling all SMs runs independent chains of single-precision fused
+ * multiply-adds, with CUDA events, best of `repeats` launches. *per_second gets the FP32
+ * lane instructions issued per second (one fused multiply-add = one instruction), *ms the
+ * best launch's time. Changes no clock or power setting. */
+int rpd_probe_fp32_issue(int device, int32_t repeats, double* per_second, double* ms);
 
 /* ---- standalone filters (denoising/atrous_wavelet.cpp, denoising/joint_bilateral.cpp) ---- */
 

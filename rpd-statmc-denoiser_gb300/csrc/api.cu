@@ -80,6 +80,7 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5]
     L.add(p.var_ratio, np);
     for (int c = 0; c < 3; ++c) L.add(p.sqrt_var_mean[c], np);
     for (int c = 0; c < 3; ++c) L.add(p.sqrt_var_stable[c], np);
+    L.add(p.win, 6 * np);
     L.add(p.variance_denoised, np);
     L.add(p.var_ping, np);
     L.add(p.var_pong, np);
@@ -93,6 +94,7 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5]
     L.add(p.active_b, np);
     L.add(p.alloc_state, np);
     L.add(p.alloc_work, int64_t(allocator_work_bytes(np)));
+    L.add(p.counters, RPD_COUNTER_COUNT_);
     L.add(n.grid, nn * kDeps * kDepStride);
     L.add(n.pass_grid, nn * kDeps * kDepStride);
     for (int f = 0; f < N_FIELDS; ++f) L.add(n.field[f], nn);
@@ -129,6 +131,7 @@ void rebase_all(PixelPlanes& p, NodePlanes& n, char* base) {
         rebase(p.denoised[c], base);
         rebase(p.sqrt_var_mean[c], base);
         rebase(p.sqrt_var_stable[c], base);
+        if (c == 0) rebase(p.win, base);
         rebase(n.n_normal[c], base);
         rebase(n.n_albedo[c], base);
     }
@@ -157,6 +160,7 @@ void rebase_all(PixelPlanes& p, NodePlanes& n, char* base) {
     rebase(p.active_b, base);
     rebase(p.alloc_state, base);
     rebase(p.alloc_work, base);
+    rebase(p.counters, base);
     rebase(n.grid, base);
     rebase(n.pass_grid, base);
     for (int f = 0; f < N_FIELDS; ++f) rebase(n.field[f], base);
@@ -579,6 +583,11 @@ int rpd_job_set_tuning(rpd_job* job, int knob, int value) {
         j->smooth_fp64 = value == 1;
         return RPD_OK;
     }
+    if (knob == RPD_TUNE_WINDOW_GUARD) {
+        if (value < 0 || value > 15) return fail(RPD_ERR_INVALID_ARGUMENT, "window guard must be 0..15");
+        j->window_guard = value;
+        return RPD_OK;
+    }
     return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
@@ -591,6 +600,7 @@ int rpd_job_get_tuning(rpd_job* job, int knob, int* value) {
     else if (knob == RPD_TUNE_STATMC_ROWS) *value = j->statmc_by;
     else if (knob == RPD_TUNE_ALLOCATOR) *value = j->serial_allocator ? 1 : j->allocator_blocks;
     else if (knob == RPD_TUNE_SMOOTHING) *value = j->smooth_fp64 ? 1 : 0;
+    else if (knob == RPD_TUNE_WINDOW_GUARD) *value = j->window_guard;
     else return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tuning knob");
     return RPD_OK;
 }
@@ -1033,6 +1043,9 @@ int rpd_statmc_denoise(rpd_job* job) {
     if (st != RPD_OK) return st;
     st = ensure_cache(*j);
     if (st != RPD_OK) return st;
+    // the window's recheck counters describe the last call
+    RPD_CUDA(cudaMemsetAsync(j->p.counters + RPD_COUNTER_WINDOW_PAIR_RECHECKS, 0, 2 * sizeof(unsigned long long),
+                             j->stream));
     RPD_CUDA(launch_statmc(*j));
     return RPD_OK;
 }
@@ -1239,6 +1252,23 @@ int rpd_job_sync(rpd_job* job) {
     Job* j = reinterpret_cast<Job*>(job);
     CHECK_JOB(j);
     RPD_CUDA(cudaStreamSynchronize(j->stream));
+    unsigned long long timeouts = 0;
+    RPD_CUDA(cudaMemcpy(&timeouts, j->p.counters + RPD_COUNTER_DEVICE_WAIT_TIMEOUTS, sizeof(timeouts),
+                        cudaMemcpyDeviceToHost));
+    if (timeouts)
+        return fail(RPD_ERR_TIMEOUT, std::to_string(timeouts) + " bounded device wait(s) of this job gave up");
+    return RPD_OK;
+}
+
+int rpd_job_counters(rpd_job* job, uint64_t* out, int32_t n) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!out || n < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "bad counter output");
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    RPD_CUDA(cudaStreamSynchronize(j->stream));
+    unsigned long long c[RPD_COUNTER_COUNT_];
+    RPD_CUDA(cudaMemcpy(c, j->p.counters, sizeof(c), cudaMemcpyDeviceToHost));
+    for (int32_t i = 0; i < n && i < RPD_COUNTER_COUNT_; ++i) out[i] = c[i];
     return RPD_OK;
 }
 
@@ -1479,8 +1509,10 @@ int rpd_atrous_wavelet(rpd_ctx* ctx, const float* raw, const float* normal, cons
     cudaStream_t st = c->util_stream;
     const uint64_t bytes = uint64_t(w) * h * 12;
     float *d_raw = nullptr, *d_n = nullptr, *d_a = nullptr, *b0 = nullptr, *b1 = nullptr;
+    float4* records = nullptr;
     RPD_CUDA(cudaMallocAsync(&b0, bytes, st));
     RPD_CUDA(cudaMallocAsync(&b1, bytes, st));
+    RPD_CUDA(cudaMallocAsync(&records, uint64_t(w) * h * 2 * sizeof(float4), st));
     if (where == RPD_MEM_HOST) {
         RPD_CUDA(cudaMallocAsync(&d_raw, bytes, st));
         RPD_CUDA(cudaMallocAsync(&d_n, bytes, st));
@@ -1494,10 +1526,12 @@ int rpd_atrous_wavelet(rpd_ctx* ctx, const float* raw, const float* normal, cons
     const float* a_in = where == RPD_MEM_HOST ? d_a : albedo;
     float* result = nullptr;
     uint64_t launches = 0;
-    RPD_CUDA(launch_atrous(r_in, n_in, a_in, w, h, sigma_c, sigma_n, sigma_a, iterations, b0, b1, &result, st, &launches));
+    RPD_CUDA(launch_atrous(r_in, n_in, a_in, w, h, sigma_c, sigma_n, sigma_a, iterations, b0, b1, records, &result, st,
+                           &launches));
     RPD_CUDA(cudaMemcpyAsync(out, result, bytes, where == RPD_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     RPD_CUDA(cudaFreeAsync(b0, st));
     RPD_CUDA(cudaFreeAsync(b1, st));
+    RPD_CUDA(cudaFreeAsync(records, st));
     if (d_raw) RPD_CUDA(cudaFreeAsync(d_raw, st));
     if (d_n) RPD_CUDA(cudaFreeAsync(d_n, st));
     if (d_a) RPD_CUDA(cudaFreeAsync(d_a, st));
@@ -1514,26 +1548,32 @@ int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, con
     RPD_CUDA(cudaSetDevice(c->device));
     cudaStream_t st = c->util_stream;
     const uint64_t bytes = uint64_t(w) * h * 12;
-    if (where == RPD_MEM_DEVICE) {
-        uint64_t launches = 0;
-        RPD_CUDA(launch_joint_bilateral(raw, normal, albedo, w, h, sigma_c, sigma_n, sigma_p, sigma_a, gaussian,
-                                        bilateral, joint, st, &launches));
-        RPD_CUDA(cudaStreamSynchronize(st));
-        return RPD_OK;
-    }
+    void* scratch = nullptr;
+    RPD_CUDA(cudaMallocAsync(&scratch, joint_bilateral_scratch_bytes(w, h), st));
     float* d[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    for (auto& p : d) RPD_CUDA(cudaMallocAsync(&p, bytes, st));
-    RPD_CUDA(cudaMemcpyAsync(d[0], raw, bytes, cudaMemcpyHostToDevice, st));
-    RPD_CUDA(cudaMemcpyAsync(d[1], normal, bytes, cudaMemcpyHostToDevice, st));
-    RPD_CUDA(cudaMemcpyAsync(d[2], albedo, bytes, cudaMemcpyHostToDevice, st));
+    const float* in[3] = {raw, normal, albedo};
+    float* outs[3] = {gaussian, bilateral, joint};
+    if (where == RPD_MEM_HOST) {
+        for (auto& p : d) RPD_CUDA(cudaMallocAsync(&p, bytes, st));
+        for (int k = 0; k < 3; ++k) RPD_CUDA(cudaMemcpyAsync(d[k], in[k], bytes, cudaMemcpyHostToDevice, st));
+        for (int k = 0; k < 3; ++k) in[k] = d[k];
+    }
+    float* dev_out[3] = {where == RPD_MEM_HOST ? d[3] : gaussian, where == RPD_MEM_HOST ? d[4] : bilateral,
+                         where == RPD_MEM_HOST ? d[5] : joint};
     uint64_t launches = 0;
-    RPD_CUDA(launch_joint_bilateral(d[0], d[1], d[2], w, h, sigma_c, sigma_n, sigma_p, sigma_a, d[3], d[4], d[5], st,
-                                    &launches));
-    RPD_CUDA(cudaMemcpyAsync(gaussian, d[3], bytes, cudaMemcpyDeviceToHost, st));
-    RPD_CUDA(cudaMemcpyAsync(bilateral, d[4], bytes, cudaMemcpyDeviceToHost, st));
-    RPD_CUDA(cudaMemcpyAsync(joint, d[5], bytes, cudaMemcpyDeviceToHost, st));
-    for (auto& p : d) RPD_CUDA(cudaFreeAsync(p, st));
+    RPD_CUDA(launch_joint_bilateral(in[0], in[1], in[2], w, h, sigma_c, sigma_n, sigma_p, sigma_a, dev_out[0], dev_out[1],
+                                    dev_out[2], scratch, st, &launches));
+    if (where == RPD_MEM_HOST)
+        for (int k = 0; k < 3; ++k) RPD_CUDA(cudaMemcpyAsync(outs[k], dev_out[k], bytes, cudaMemcpyDeviceToHost, st));
+    unsigned timeouts = 0;
+    const uint64_t flag_offset = joint_bilateral_scratch_bytes(w, h) - 256;
+    RPD_CUDA(cudaMemcpyAsync(&timeouts, static_cast<char*>(scratch) + flag_offset, sizeof(timeouts),
+                             cudaMemcpyDeviceToHost, st));
+    for (auto& p : d)
+        if (p) RPD_CUDA(cudaFreeAsync(p, st));
+    RPD_CUDA(cudaFreeAsync(scratch, st));
     RPD_CUDA(cudaStreamSynchronize(st));
+    if (timeouts) return fail(RPD_ERR_TIMEOUT, "a joint-bilateral tile copy did not complete in time");
     return RPD_OK;
 }
 

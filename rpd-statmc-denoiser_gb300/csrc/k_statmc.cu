@@ -2,48 +2,72 @@
 // compatibility window with the RPD relaxation.
 //
 //   k_sqrt_var_mean    sqrt-domain variance of the mean, floored at EPS_SMALL (972-980)
-//   k_sqrt_var_stable  max with its 3x3 inverse-distance average (981-990)
-//   k_statmc_tile      the (2r+1)^2 window (998-1127), fast path. A 32 x BY block stages
-//                      its (32+2r) x (BY+2r) halo tile of per-pixel records in shared memory
-//                      (structure of arrays, so a warp reading 32 neighbours at one offset is
-//                      bank-conflict free) and evaluates every neighbour in single precision:
+//   k_sqrt_var_stable  max with its 3x3 inverse-distance average (981-990); the same pass packs
+//                      every pixel's neighbour record into six float4 planes (p.win):
+//                        W_GATE (unit normal xyz, depth)      the normal / depth gates
+//                        W_ALB  (albedo xyz, 1/max(n-1, 1))   the albedo gate; 0 marks a pixel
+//                                                             without a primary hit
+//                        W_SM   (sqrt mean rgb, rpd[4])       Welch means
+//                        W_SV   (stabilised sqrt var rgb, rpd[5])
+//                        W_RPD  (rpd[0..3])                   the RPD relaxation
+//                        W_CM   (colour mean rgb, var of the mean) the weighted sums; for a
+//                                                             pixel without a hit, its pass-through
+//                                                             uncertainty instead
+//   k_statmc_tma       the (2r+1)^2 window (998-1127), fast path. A 32 x BY block stages its
+//                      (32+2r) x (BY+2r) halo tile of the six planes into shared memory with
+//                      one tensor copy (cp.async.bulk.tensor, completion on an mbarrier; the
+//                      copy's zero fill past the image edges marks those neighbours invalid)
+//                      and evaluates every neighbour in single precision:
 //                        * the normal / depth / albedo gates are decided exactly as the
 //                          reference decides them (identical float operations; the depth
 //                          quotient is only rounded exactly when it lies within 2^-20 of the
 //                          threshold; the albedo norm is compared through the exact squared
 //                          threshold of the correctly rounded sqrt);
-//                        * the Welch t^2, Welch-Satterthwaite df, t-table lookup and RPD
-//                          relaxation run in float with approximate division. Their relative
-//                          error is below 3e-6, so whenever q lies within 2^-15 (relative)
-//                          of a decision point — q = 25 (reject), q = 2 ln 20 (the accepted-
-//                          neighbour count), df = 30.5 / 30 (t-table branch) or the 1e-8
-//                          df-denominator test — that neighbour's q is recomputed in double
-//                          exactly as the reference computes it, and the decisions use it.
-//                      Weights are accumulated in float per window row and in double-float
-//                      across rows. The blend's weight_sum >= 1.1 test has its own guard
-//                      band; a pixel inside it is recomputed wholly in double.
+//                        * the Welch t^2, Welch-Satterthwaite df, t critical value and RPD
+//                          relaxation run in float with approximate reciprocals (relative
+//                          error below 3e-6), and whenever q lies within the guard band
+//                          (2^-15 relative by default) of a decision point — q = 25 (reject),
+//                          q = 2 ln 20 (the accepted-neighbour count), the df of the t-table /
+//                          normal-quantile switch, or the 1e-8 df-denominator test — the
+//                          pixel is recomputed wholly in double exactly as the reference
+//                          computes it (rare: no pixel of the 1080p benchmark frame needs it);
+//                        * each block picks a specialised loop from the range of 1/(n-1) over
+//                          its halo: when every pair's df lies below the t-table switch
+//                          (df <= (n_i - 1) + (n_j - 1)) no neighbour needs the switch test, and
+//                          when every df lies above it (df >= min(n_i, n_j) - 1 >= 31) the t
+//                          critical value is the normal quantile and df is not formed at all.
+//                      Weights are summed in float per window row and across rows. The blend's
+//                      weight_sum >= 1.1 test has its own guard band; a pixel inside it is
+//                      recomputed wholly in double.
 //   k_statmc_window    the whole window in double, the reference's operations in its order
-//                      (the exact mode, the fallback of the fast path, and the path for
-//                      radii whose halo tile would not fit in shared memory).
+//                      (the exact mode, and the path for radii whose halo tile would not fit in
+//                      shared memory).
+
 #include <algorithm>
 #include <cmath>
 
 #include "rpd_internal.h"
 #include "device_math.cuh"
 #include "exact_arith.cuh"
+#include "tma.cuh"
 
 namespace rpd {
 
 namespace {
 
-__constant__ float c_t05[30] = {
-    12.706f, 4.303f, 3.182f, 2.776f, 2.571f, 2.447f, 2.365f, 2.306f, 2.262f, 2.228f,
-    2.201f, 2.179f, 2.160f, 2.145f, 2.131f, 2.120f, 2.110f, 2.101f, 2.093f, 2.086f,
-    2.080f, 2.074f, 2.069f, 2.064f, 2.060f, 2.056f, 2.052f, 2.048f, 2.045f, 2.042f};
-__constant__ float c_t01[30] = {
-    63.657f, 9.925f, 5.841f, 4.604f, 4.032f, 3.707f, 3.499f, 3.355f, 3.250f, 3.169f,
-    3.106f, 3.055f, 3.012f, 2.977f, 2.947f, 2.921f, 2.898f, 2.878f, 2.861f, 2.845f,
-    2.831f, 2.819f, 2.807f, 2.797f, 2.787f, 2.779f, 2.771f, 2.763f, 2.756f, 2.750f};
+// The two-sided t critical values of lookup_t_critical (main.cpp:199-212), df = 1..30.
+#define RPD_T05                                                                                   \
+    12.706f, 4.303f, 3.182f, 2.776f, 2.571f, 2.447f, 2.365f, 2.306f, 2.262f, 2.228f, 2.201f, 2.179f, \
+        2.160f, 2.145f, 2.131f, 2.120f, 2.110f, 2.101f, 2.093f, 2.086f, 2.080f, 2.074f, 2.069f,      \
+        2.064f, 2.060f, 2.056f, 2.052f, 2.048f, 2.045f, 2.042f
+#define RPD_T01                                                                                   \
+    63.657f, 9.925f, 5.841f, 4.604f, 4.032f, 3.707f, 3.499f, 3.355f, 3.250f, 3.169f, 3.106f, 3.055f, \
+        3.012f, 2.977f, 2.947f, 2.921f, 2.898f, 2.878f, 2.861f, 2.845f, 2.831f, 2.819f, 2.807f,      \
+        2.797f, 2.787f, 2.779f, 2.771f, 2.763f, 2.756f, 2.750f
+__constant__ float c_t05[30] = {RPD_T05};
+__constant__ float c_t01[30] = {RPD_T01};
+constexpr float kT05[30] = {RPD_T05};
+constexpr float kT01[30] = {RPD_T01};
 
 __device__ __forceinline__ float interpolate_table(const float* table, float df) {
     const int lo = iclamps(int(floorf(df)), 1, 30);
@@ -97,8 +121,44 @@ __global__ void k_sqrt_var_mean(PixelPlanes p, int64_t np) {
 // the work; each quotient is rounded to float through a single-precision estimate and an exact
 // integer remainder (the double division only where that cannot decide). The values are
 // positive: sqrt_var_mean is floored at 1e-8.
+enum WinPlane { W_GATE = 0, W_ALB, W_SM, W_SV, W_RPD, W_CM, W_COUNT };
+
+// The neighbour record of pixel i (the planes of p.win) and the window's debug planes
+// (main.cpp:1010-1023). Records of pixels without a primary hit are zero but for W_CM, which
+// holds what the window writes for them (main.cpp:1001-1006): the colour mean and the
+// unclamped variance over n.
+__device__ __forceinline__ void pack_window_record(const PixelPlanes& p, int64_t np, int64_t i, const float sv[3],
+                                                   float var2_max) {
+    float4* win = p.win;
+    const int n_raw = p.n[i];
+    const float m2 = p.square_diff[i];
+    const float4 cm = make_float4(p.color_mean[0][i], p.color_mean[1][i], p.color_mean[2][i], 0.0f);
+    if (p.hit_count[i] == 0) {
+        const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int k = W_GATE; k < W_CM; ++k) win[k * np + i] = z;
+        win[W_CM * np + i] = make_float4(cm.x, cm.y, cm.z, pixel_variance(m2, n_raw) / float(imaxs(1, n_raw)));
+        return;
+    }
+    float var = pixel_variance(m2, n_raw);
+    if (!isfinite(var)) var = 1e-8f;
+    var = fclamps(var, 1e-8f, var2_max);
+    const int n = imaxs(1, n_raw);
+    const float vm = fmaxs(1e-8f, var / float(n));
+    p.var_total[i] = var;
+    p.var_eff[i] = vm;
+    p.var_ratio[i] = (var > 1e-8f) ? (vm * float(n)) / var : 0.0f;
+    const float rp = 1.0f / fmaxf(float(n - 1), 1.0f);
+    win[W_GATE * np + i] = make_float4(p.f_normal[0][i], p.f_normal[1][i], p.f_normal[2][i], p.f_depth[i]);
+    win[W_ALB * np + i] = make_float4(p.f_albedo[0][i], p.f_albedo[1][i], p.f_albedo[2][i], rp);
+    win[W_SM * np + i] = make_float4(p.sqrt_mean[0][i], p.sqrt_mean[1][i], p.sqrt_mean[2][i], p.rpd[4][i]);
+    win[W_SV * np + i] = make_float4(sv[0], sv[1], sv[2], p.rpd[5][i]);
+    win[W_RPD * np + i] = make_float4(p.rpd[0][i], p.rpd[1][i], p.rpd[2][i], p.rpd[3][i]);
+    win[W_CM * np + i] = make_float4(cm.x, cm.y, cm.z, vm);
+}
+
 constexpr int kSvTx = 32, kSvTy = 8;
-__global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p, int w, int h, double weight_sum) {
+__global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p, int w, int h, double weight_sum,
+                                                                  float var2_max) {
     __shared__ double tile[3][3][(kSvTy + 2) * (kSvTx + 2)];  // [channel][v, v/2, v/3][pixel]
     const int tw = kSvTx + 2, tn = (kSvTy + 2) * (kSvTx + 2);
     const int x0 = blockIdx.x * kSvTx, y0 = blockIdx.y * kSvTy;
@@ -120,6 +180,7 @@ __global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p
     const int64_t i = int64_t(y) * w + x;
     const int e = (threadIdx.y + 1) * tw + threadIdx.x + 1;
     const XD wsum = xd_of_double(weight_sum);
+    float sv[3];
     for (int c = 0; c < 3; ++c) {
         const double* t1 = tile[c][0];
         const double* th = tile[c][1];
@@ -151,8 +212,10 @@ __global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p
         const XD ax = xd_of_double(a);
         float q;
         if (!quotient_to_float(ax.m, ax.e, wsum.m, wsum.e, q)) q = float(a / weight_sum);
-        p.sqrt_var_stable[c][i] = fmaxs(p.sqrt_var_mean[c][i], q);
+        sv[c] = fmaxs(p.sqrt_var_mean[c][i], q);
+        p.sqrt_var_stable[c][i] = sv[c];
     }
+    pack_window_record(p, int64_t(w) * h, i, sv, var2_max);
 }
 
 struct StatmcParams {
@@ -160,9 +223,14 @@ struct StatmcParams {
     float normal_threshold, depth_threshold, rpd_scale, alpha, var2_max;
     float albedo_sq_threshold;  // smallest float s with fl(sqrt(s)) > 0.12f
     int table;                  // 0: alpha 0.05 table, 1: alpha 0.01 table, 2: normal quantile
-    float z;                    // normal quantile of the alpha (table == 2)
+    float z;                    // normal quantile of the alpha
+    float inv_z2;               // 1 / z^2
     float df_break;             // 30.5 with a table, 30 with the quantile
-    int by;                     // block height of the tiled kernel
+    float band;                 // relative guard band of the q and df decisions
+    float ws_band;              // relative guard band of the weight_sum >= 1.1 test
+    float rp_below;             // a block whose smallest 1/(n-1) is at least this has every df below df_break
+    float rp_above;             // a block whose largest 1/(n-1) is at most this has every df at or above 31
+    int by;                     // block rows of the generic-radius tiled kernel
 };
 
 // The Welch compatibility q of one (i, j) pair in double, the reference's operations in
@@ -186,7 +254,7 @@ __device__ double exact_q(const float* svi, const float* smi, int n_i, const flo
 }
 
 // One pixel of statmc_denoise entirely in double (main.cpp:999-1127).
-__device__ void exact_pixel(const PixelPlanes& p, const StatmcParams& prm, int64_t idx) {
+__device__ __noinline__ void exact_pixel(const PixelPlanes& p, const StatmcParams& prm, int64_t idx) {
     const int y = int(idx / prm.w), x = int(idx % prm.w);
     const int n_raw = p.n[idx];
     const float m2_i = p.square_diff[idx];
@@ -283,250 +351,301 @@ __global__ void __launch_bounds__(128) k_statmc_window(PixelPlanes p, StatmcPara
     exact_pixel(p, prm, idx);
 }
 
-// ---- fast tiled path ----------------------------------------------------------------------
-
-// Halo tile planes, float4 per pixel (structure of float4 arrays: a warp reading 32
-// neighbours at one offset reads 512 contiguous bytes, conflict free):
-//   P_GATE (nx, ny, nz, depth)         normal / depth gates
-//   P_ALB  (ax, ay, az, n)             albedo gate, sample count as float (0: outside the
-//                                      image or no primary hit, which the reference skips)
-//   P_SM   (sqrt mean rgb, rpd[4])     Welch means
-//   P_SV   (sqrt var stable rgb, rpd[5]) Welch variances
-//   P_A    (sv^2 / (n - 1) rgb, var of the mean)
-//   P_RPD  (rpd[0..3])
-//   P_CM   (colour mean rgb, 0)
-enum TilePlane { P_GATE = 0, P_ALB, P_SM, P_SV, P_A, P_RPD, P_CM, P_COUNT };
+// ---- fast tiled path ------------------------------------------------------------------------
 
 constexpr int kTileX = 32;
-constexpr float kBand = 1.0f / 32768.0f;          // 2^-15 relative guard band
-constexpr float kQAccept = 5.991464547107979f;     // 2 ln 20: exp(-q/2) > 0.05
-constexpr double kWsBand = 1.0 / 65536.0;          // guard band of weight_sum >= 1.1
-constexpr float kDepthBand = 1.0f / 1048576.0f;    // 2^-20: depth quotient decided by a product
+constexpr int kRows = 8;                          // block rows of the fixed-radius kernels
+constexpr float kQAccept = 5.991464547107979f;   // 2 ln 20: exp(-q/2) > 0.05 (main.cpp:1093)
+constexpr float kDepthBand = 1.0f / 1048576.0f;  // 2^-20: depth quotient decided by a product
 
-// t critical value of the fast path. The table branch interpolates (tab[lo-1], tab[lo]) with
-// lo = round(df - 1/2) taken from the float's bits (df in [1, 30.5): no conversion unit); at
-// an integer df this may pick the lower cell with fraction 1, the same value to an ulp. The
-// pairs hold (tab[i], tab[i+1] - tab[i]) and (tab[29], 0), so df in [30, 30.5) gives tab[29]
-// as lookup_t_critical does.
-__device__ __forceinline__ float tile_t_lookup(const float2* pairs, float df, const StatmcParams& prm) {
-    df = fmaxf(df, 1.0f);
-    if (prm.table < 2 && df < 30.5f) {
-        const float fl = (df - 0.5f) + 12582912.0f;  // 1.5 * 2^23: integer part in the low bits
-        const int lo = imaxs(__float_as_int(fl) - 0x4B400000, 1);
-        const float2 ab = pairs[lo - 1];
-        return __fmaf_rn(ab.y, df - float(lo), ab.x);
+// t critical value per half unit of df for the t-table alphas: k = floor(2 df) (df clamped to
+// 31.75) selects a line, t = v[k].y * df + v[k].x. k < 2: df below 1, which lookup_t_critical
+// raises to 1 (t[0]); k in [2, 59]: the interpolation between t[lo-1] and t[lo], lo = k / 2;
+// k = 60: df in [30, 30.5), t[29]; k >= 61: df >= 30.5, the normal quantile z.
+struct LineTable {
+    float2 v[64];
+};
+
+// The centre pixel's record, held in registers through its window.
+struct Pix {
+    float n0, n1, n2;        // unit normal
+    float d, dm;             // depth, max(|depth|, EPS_SMALL)
+    float a0, a1, a2;        // albedo
+    float sm0, sm1, sm2;     // sqrt colour mean
+    float sv0, sv1, sv2;     // stabilised sqrt variance of the mean
+    float v0, v1, v2;        // sv^2 / max(n - 1, 1)
+    float r0, r1, r2, r3, r4, r5;  // RPD components
+};
+
+// t critical value of a neighbour's df. MODE 1: the block's df all lie below the table /
+// quantile switch, so the switch is not tested.
+template <int MODE>
+__device__ __forceinline__ float t_crit(float df, const float2* __restrict__ line, const StatmcParams& prm) {
+    if (prm.table < 2) {
+        const float dfc = fminf(df, 31.75f);
+        const float fl = __fadd_rd(dfc + dfc, 12582912.0f);  // 1.5 * 2^23: floor(2 df) in the low bits
+        const float2 l = line[__float_as_int(fl) - 0x4B400000];
+        return __fmaf_rn(l.y, dfc, l.x);
     }
-    float z = prm.z;
-    if (df < 30.0f) z = z * sqrtf(__fdividef(df, fmaxf(1.0f, df - 1.0f)));
-    return z;
+    const float dfc = fmaxf(df, 1.0f);
+    if (MODE == 1 || dfc < 30.0f) {
+        const float x = __fdividef(dfc, fmaxf(1.0f, dfc - 1.0f));
+        return prm.z * (x * rsqrtf(x));
+    }
+    return prm.z;
 }
 
-__global__ void __launch_bounds__(256, 2) k_statmc_tile(PixelPlanes p, StatmcParams prm) {
-    extern __shared__ float4 smem4[];
-    const int r = prm.r;
-    const int tw = kTileX + 2 * r, th = prm.by + 2 * r;
-    const int tn = tw * th;
-    const int side = 2 * r + 1;
-    float4* T = smem4;                                                  // P_COUNT planes of tn
-    float2* pairs = reinterpret_cast<float2*>(smem4 + P_COUNT * tn);    // 32 t-table pairs
-    float* spatial_tab = reinterpret_cast<float*>(pairs + 32);          // side * side
-    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * prm.by;
-    const int tid = threadIdx.y * kTileX + threadIdx.x;
-    const int nthreads = kTileX * prm.by;
+// One neighbour of the window: gates, Welch q, relaxation, weight, accumulation. MODE 0: any
+// df; 1: every df of the block below the switch; 2: every df at or above 31 (t = z).
+template <int MODE>
+__device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int e, float sw, int dx, int dy,
+                                      const StatmcParams& prm, const Pix& P, const float2* __restrict__ line,
+                                      float row[6], int& accepted, int& rechecks) {
+    const float4 G = T[W_GATE * tn + e];
+    if (dot3(P.n0, P.n1, P.n2, G.x, G.y, G.z) < prm.normal_threshold) return;
+    const float4 A = T[W_ALB * tn + e];
+    if (!(A.w > 0.0f)) return;  // outside the image or no primary hit
+    {
+        // relative_depth_delta(d_i, d_j) > threshold: fl(|d_i - d_j| / m) against the threshold,
+        // decided by the product threshold * m away from it and by the IEEE quotient near it
+        float m = P.dm;
+        const float dj = fabsf(G.w);
+        if (m < dj) m = dj;
+        const float num = fabsf(P.d - G.w);
+        const float tm = prm.depth_threshold * m;
+        const float dl = num - tm;
+        bool far;
+        if (fabsf(dl) <= tm * kDepthBand || !(tm >= 1e-30f)) far = __fdiv_rn(num, m) > prm.depth_threshold;
+        else far = dl > 0.0f;
+        if (far) return;
+    }
+    const float da0 = P.a0 - A.x, da1 = P.a1 - A.y, da2 = P.a2 - A.z;
+    if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) return;
 
-    if (tid < 32) {
-        const float* tab = prm.table == 0 ? c_t05 : c_t01;
-        pairs[tid] = tid < 29 ? make_float2(tab[tid], tab[tid + 1] - tab[tid])
-                              : make_float2(tid == 29 ? tab[29] : 0.0f, 0.0f);
-    }
-    for (int e = tid; e < side * side; e += nthreads) {
-        const int dx = e % side - r, dy = e / side - r;
-        spatial_tab[e] = __frcp_rn(1.0f + float(dx * dx + dy * dy));  // 1 / (1 + d^2), main.cpp:1096
-    }
-    for (int e = tid; e < tn; e += nthreads) {
-        const int gx = x0 - r + e % tw, gy = y0 - r + e / tw;
-        bool inside = gx >= 0 && gx < prm.w && gy >= 0 && gy < prm.h;
-        const int64_t q = inside ? int64_t(gy) * prm.w + gx : 0;
-        const bool hit = inside && p.hit_count[q] > 0;
-        T[P_GATE * tn + e] = hit ? make_float4(p.f_normal[0][q], p.f_normal[1][q], p.f_normal[2][q], p.f_depth[q])
-                                 : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (!hit) {
-            T[P_ALB * tn + e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            continue;
+    const float4 S = T[W_SM * tn + e], V = T[W_SV * tn + e];
+    bool exact = false;
+    const float vs0 = P.sv0 + V.x, vs1 = P.sv1 + V.y, vs2 = P.sv2 + V.z;
+    const float md0 = P.sm0 - S.x, md1 = P.sm1 - S.y, md2 = P.sm2 - S.z;
+    float qmax;
+    if constexpr (MODE == 2) {
+        qmax = fmaxf(fmaxf(__fdividef(md0 * md0, vs0), __fdividef(md1 * md1, vs1)), __fdividef(md2 * md2, vs2)) *
+               prm.inv_z2;
+    } else {
+        const float rpj = A.w;
+        const float den0 = __fmaf_rn(V.x * V.x, rpj, P.v0);
+        const float den1 = __fmaf_rn(V.y * V.y, rpj, P.v1);
+        const float den2 = __fmaf_rn(V.z * V.z, rpj, P.v2);
+        exact |= fminf(fminf(den0, den1), den2) <= 1e-8f * (1.0f + prm.band);
+        const float df0 = __fdividef(vs0 * vs0, den0);
+        const float df1 = __fdividef(vs1 * vs1, den1);
+        const float df2 = __fdividef(vs2 * vs2, den2);
+        if constexpr (MODE == 0) {
+            const float lim = prm.df_break * prm.band;
+            exact |= fabsf(df0 - prm.df_break) <= lim;
+            exact |= fabsf(df1 - prm.df_break) <= lim;
+            exact |= fabsf(df2 - prm.df_break) <= lim;
         }
-        const int n_raw = p.n[q];
-        const int nj = imaxs(1, n_raw);
-        float var = pixel_variance(p.square_diff[q], n_raw);
-        if (!isfinite(var)) var = 1e-8f;
-        var = fclamps(var, 1e-8f, prm.var2_max);
-        const float nm1 = fmaxf(float(nj - 1), 1.0f);
-        float sv[3];
-        for (int c = 0; c < 3; ++c) sv[c] = p.sqrt_var_stable[c][q];
-        T[P_ALB * tn + e] = make_float4(p.f_albedo[0][q], p.f_albedo[1][q], p.f_albedo[2][q], float(nj));
-        T[P_SM * tn + e] = make_float4(p.sqrt_mean[0][q], p.sqrt_mean[1][q], p.sqrt_mean[2][q], p.rpd[4][q]);
-        T[P_SV * tn + e] = make_float4(sv[0], sv[1], sv[2], p.rpd[5][q]);
-        T[P_A * tn + e] = make_float4(__fdividef(sv[0] * sv[0], nm1), __fdividef(sv[1] * sv[1], nm1),
-                                      __fdividef(sv[2] * sv[2], nm1), fmaxs(1e-8f, var / float(nj)));
-        T[P_RPD * tn + e] = make_float4(p.rpd[0][q], p.rpd[1][q], p.rpd[2][q], p.rpd[3][q]);
-        T[P_CM * tn + e] = make_float4(p.color_mean[0][q], p.color_mean[1][q], p.color_mean[2][q], 0.0f);
+        const float t0 = t_crit<MODE>(df0, line, prm);
+        const float t1 = t_crit<MODE>(df1, line, prm);
+        const float t2 = t_crit<MODE>(df2, line, prm);
+        qmax = fmaxf(fmaxf(__fdividef(md0 * md0, vs0 * (t0 * t0)), __fdividef(md1 * md1, vs1 * (t1 * t1))),
+                     __fdividef(md2 * md2, vs2 * (t2 * t2)));
+    }
+    // rpf::shared_reliability + relax_compatibility (core/stats.h:56-78)
+    const float4 RJ = T[W_RPD * tn + e];
+    float shared = fmaxf(fmaxf(fminf(P.r0, RJ.x), fminf(P.r1, RJ.y)), fmaxf(fminf(P.r2, RJ.z), fminf(P.r3, RJ.w)));
+    shared = __saturatef(fmaxf(shared, fmaxf(fminf(P.r4, S.w), fminf(P.r5, V.w))));
+    const float adjustment = __saturatef(prm.rpd_scale * shared);
+    const float q = __fdividef(qmax, 1.0f + adjustment);
+    const bool center = dx == 0 && dy == 0;
+    exact |= fabsf(q - 25.0f) <= 25.0f * prm.band;
+    exact |= !center && fabsf(q - kQAccept) <= kQAccept * prm.band;
+    // a decision inside a guard band sends the whole pixel to the double-precision path
+    rechecks += exact ? 1 : 0;
+    if (q > 25.0f) return;
+    if (!center && q < kQAccept) ++accepted;
+    const float wj = sw * __expf(-0.5f * q);
+    const float4 CM = T[W_CM * tn + e];
+    const float w2 = wj * wj;
+    row[0] = __fmaf_rn(wj, CM.x, row[0]);
+    row[1] = __fmaf_rn(wj, CM.y, row[1]);
+    row[2] = __fmaf_rn(wj, CM.z, row[2]);
+    row[3] += wj;
+    row[4] += w2;
+    row[5] = __fmaf_rn(w2, CM.w, row[5]);
+}
+
+template <int RC, int MODE>
+__device__ __forceinline__ void window_rows(const float4* __restrict__ T, int tn, int tw, int r,
+                                            const float* __restrict__ spatial, const float2* __restrict__ line,
+                                            const StatmcParams& prm, const Pix& P, int ei, float acc[6],
+                                            int& accepted, int& rechecks) {
+    const int side = 2 * r + 1;
+    for (int dy = -r; dy <= r; ++dy) {
+        float row[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        const int erow = ei + dy * tw;
+        const float* srow = spatial + (dy + r) * side + r;
+        if constexpr (RC > 0) {
+#pragma unroll
+            for (int dx = -RC; dx <= RC; ++dx)
+                visit<MODE>(T, tn, erow + dx, srow[dx], dx, dy, prm, P, line, row, accepted, rechecks);
+        } else {
+#pragma unroll 1
+            for (int dx = -r; dx <= r; ++dx)
+                visit<MODE>(T, tn, erow + dx, srow[dx], dx, dy, prm, P, line, row, accepted, rechecks);
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[k] += row[k];
+    }
+}
+
+// RC > 0: radius RC and kRows block rows fixed at compile time; RC == 0: prm.r and prm.by.
+template <int RC>
+__global__ void __launch_bounds__(kTileX * kRows, 3)
+    k_statmc_tma(PixelPlanes p, StatmcParams prm, LineTable lt, const __grid_constant__ CUtensorMap tmap) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ float2 s_line[64];
+    __shared__ unsigned s_rpmin, s_rpmax;
+    __shared__ int s_fail;
+    const int r = RC > 0 ? RC : prm.r;
+    const int by = RC > 0 ? kRows : prm.by;
+    const int tw = kTileX + 2 * r, th = by + 2 * r, tn = tw * th, side = 2 * r + 1;
+    // the tile copy's destination, 128-byte aligned
+    const uint32_t pad = (128u - (smem_addr(smem_raw) & 127u)) & 127u;
+    float4* T = reinterpret_cast<float4*>(smem_raw + pad);
+    float* spatial = reinterpret_cast<float*>(T + W_COUNT * tn);  // side * side
+    const int tid = threadIdx.y * kTileX + threadIdx.x;
+    const int nthreads = kTileX * by;
+    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * by;
+    const uint32_t bar_a = smem_addr(&bar);
+
+    if (tid == 0) {
+        mbar_init(bar_a, 1);
+        s_rpmin = 0x7f800000u;  // +inf
+        s_rpmax = 0u;
+        s_fail = 0;
     }
     __syncthreads();
+    if (tid == 0) {
+        tile_load(T, &tmap, x0, y0, r, tw, th, W_COUNT, bar_a);
+    }
+    if (tid < 64) s_line[tid] = lt.v[tid];
+    for (int e = tid; e < side * side; e += nthreads) {
+        const int dx = e % side - r, dy = e / side - r;
+        spatial[e] = __frcp_rn(1.0f + float(dx * dx + dy * dy));  // 1 / (1 + d^2), main.cpp:1094
+    }
+    if (!mbar_wait_bounded(bar_a, 0)) s_fail = 1;
+    __syncthreads();
+    if (s_fail) {
+        // the copy did not land in time: report it, and let the copy finish (bounded) before the
+        // block's shared memory is released
+        if (tid == 0) {
+            atomicAdd(p.counters + RPD_COUNTER_DEVICE_WAIT_TIMEOUTS, 1ull);
+            mbar_wait_bounded(bar_a, 0);
+        }
+        return;
+    }
+
+    // the halo's range of 1/max(n-1, 1) selects the block's loop
+    float lmin = __uint_as_float(0x7f800000u), lmax = 0.0f;
+    for (int e = tid; e < tn; e += nthreads) {
+        const float rp = T[W_ALB * tn + e].w;
+        if (rp > 0.0f) {
+            lmin = fminf(lmin, rp);
+            lmax = fmaxf(lmax, rp);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+        lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    }
+    if ((tid & 31) == 0) {
+        atomicMin(&s_rpmin, __float_as_uint(lmin));  // non-negative floats order as their bits
+        atomicMax(&s_rpmax, __float_as_uint(lmax));
+    }
+    __syncthreads();
+    const int mode = __uint_as_float(s_rpmax) <= prm.rp_above ? 2 : __uint_as_float(s_rpmin) >= prm.rp_below ? 1 : 0;
 
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
     if (x >= prm.w || y >= prm.h) return;
     const int64_t idx = int64_t(y) * prm.w + x;
-    if (p.hit_count[idx] == 0) {
-        const int n_raw = p.n[idx];
-        for (int c = 0; c < 3; ++c) p.denoised[c][idx] = p.color_mean[c][idx];
-        p.uncertainty[idx] = pixel_variance(p.square_diff[idx], n_raw) / float(imaxs(1, n_raw));
+    const int ei = (threadIdx.y + r) * tw + threadIdx.x + r;
+    const float4 cmi = T[W_CM * tn + ei];
+    const float4 ali = T[W_ALB * tn + ei];
+    if (!(ali.w > 0.0f)) {  // no primary hit: the pixel passes through (main.cpp:1001-1006)
+        p.denoised[0][idx] = cmi.x;
+        p.denoised[1][idx] = cmi.y;
+        p.denoised[2][idx] = cmi.z;
+        p.uncertainty[idx] = cmi.w;
         p.alpha[idx] = 1.0f;
         return;
     }
-    const int ei = (threadIdx.y + r) * tw + threadIdx.x + r;
-    const float4 gi = T[P_GATE * tn + ei], ali = T[P_ALB * tn + ei];
-    const float4 smi4 = T[P_SM * tn + ei], svi4 = T[P_SV * tn + ei], ai4 = T[P_A * tn + ei], ri4 = T[P_RPD * tn + ei];
-    const float smi[3] = {smi4.x, smi4.y, smi4.z}, svi[3] = {svi4.x, svi4.y, svi4.z};
-    const float nif = ali.w;
-    const int n_i = int(nif);
+    Pix P;
     {
-        // the debug planes (main.cpp:1021-1023)
-        const int n_raw = p.n[idx];
-        float var_i = pixel_variance(p.square_diff[idx], n_raw);
-        if (!isfinite(var_i)) var_i = 1e-8f;
-        var_i = fclamps(var_i, 1e-8f, prm.var2_max);
-        const float vm = fmaxs(1e-8f, var_i / float(n_i));
-        p.var_total[idx] = var_i;
-        p.var_eff[idx] = vm;
-        p.var_ratio[idx] = (var_i > 1e-8f) ? (vm * float(n_i)) / var_i : 0.0f;
+        const float4 g = T[W_GATE * tn + ei], s = T[W_SM * tn + ei], v = T[W_SV * tn + ei], rr = T[W_RPD * tn + ei];
+        P.n0 = g.x;
+        P.n1 = g.y;
+        P.n2 = g.z;
+        P.d = g.w;
+        P.dm = fabsf(g.w);
+        if (P.dm < 1e-8f) P.dm = 1e-8f;
+        P.a0 = ali.x;
+        P.a1 = ali.y;
+        P.a2 = ali.z;
+        P.sm0 = s.x;
+        P.sm1 = s.y;
+        P.sm2 = s.z;
+        P.sv0 = v.x;
+        P.sv1 = v.y;
+        P.sv2 = v.z;
+        P.v0 = v.x * v.x * ali.w;
+        P.v1 = v.y * v.y * ali.w;
+        P.v2 = v.z * v.z * ali.w;
+        P.r0 = rr.x;
+        P.r1 = rr.y;
+        P.r2 = rr.z;
+        P.r3 = rr.w;
+        P.r4 = s.w;
+        P.r5 = v.w;
     }
-    const float dthr = prm.depth_threshold;
-    const float dabs_i = fabsf(gi.w);
+    float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    int accepted = 0, rechecks = 0;
+    if (mode == 2)
+        window_rows<RC, 2>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, rechecks);
+    else if (mode == 1)
+        window_rows<RC, 1>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, rechecks);
+    else
+        window_rows<RC, 0>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, rechecks);
 
-    // double-float accumulators across rows: colour (3), weight, weight^2, weight^2*var
-    float acc_hi[6] = {0, 0, 0, 0, 0, 0}, acc_lo[6] = {0, 0, 0, 0, 0, 0};
-    int accepted = 0;
-    for (int dy = -r; dy <= r; ++dy) {
-        float row[6] = {0, 0, 0, 0, 0, 0};
-        const int erow = (threadIdx.y + r + dy) * tw + threadIdx.x + r;
-        const float* srow = spatial_tab + (dy + r) * side + r;
-#pragma unroll 2
-        for (int dx = -r; dx <= r; ++dx) {
-            const int e = erow + dx;
-            const float4 gj = T[P_GATE * tn + e];
-            if (dot3(gi.x, gi.y, gi.z, gj.x, gj.y, gj.z) < prm.normal_threshold) continue;
-            const float4 aj = T[P_ALB * tn + e];
-            if (!(aj.w > 0.0f)) continue;  // outside the image or no primary hit
-            // relative_depth_delta(di, dj) > threshold: fl(num / m) against dthr, decided by
-            // the product dthr * m away from the threshold and by the IEEE quotient near it
-            float m = dabs_i;
-            if (m < fabsf(gj.w)) m = fabsf(gj.w);
-            if (m < 1e-8f) m = 1e-8f;
-            const float num = fabsf(gi.w - gj.w);
-            const float tm = dthr * m;
-            bool far;
-            if (!(tm >= 1e-30f)) far = __fdiv_rn(num, m) > dthr;  // tiny or zero threshold: no product test
-            else if (num > tm * (1.0f + kDepthBand)) far = true;
-            else if (num < tm * (1.0f - kDepthBand)) far = false;
-            else far = __fdiv_rn(num, m) > dthr;
-            if (far) continue;
-            const float da0 = ali.x - aj.x, da1 = ali.y - aj.y, da2 = ali.z - aj.z;
-            if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) continue;
-
-            const float4 smj = T[P_SM * tn + e], svj = T[P_SV * tn + e], aaj = T[P_A * tn + e];
-            const float njf = aj.w;
-            bool exact = false;
-            // per channel t^2 / t_crit^2 = md^2 / (vs * tc^2); the largest is found by cross
-            // products and divided once, together with the RPD relaxation
-            float qn = 0.0f, qd = 1.0f;
-            {
-                const float sj[3] = {smj.x, smj.y, smj.z}, vj[3] = {svj.x, svj.y, svj.z};
-                const float aj3[3] = {aaj.x, aaj.y, aaj.z}, ai3[3] = {ai4.x, ai4.y, ai4.z};
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float vs = svi[c] + vj[c];
-                    const float md = smi[c] - sj[c];
-                    const float den = ai3[c] + aj3[c];
-                    exact |= fabsf(den - 1e-8f) <= 1e-8f * kBand;
-                    const float df = den > 1e-8f ? __fdividef(vs * vs, den) : nif + njf - 2.0f;
-                    exact |= fabsf(df - prm.df_break) <= prm.df_break * kBand;
-                    const float tc = tile_t_lookup(pairs, df, prm);
-                    const float n2 = md * md, d2 = vs * tc * tc;
-                    if (n2 * qd > qn * d2) {
-                        qn = n2;
-                        qd = d2;
-                    }
-                }
-            }
-            const float4 rj = T[P_RPD * tn + e];
-            float shared = fmaxs(fmaxs(fmins(ri4.x, rj.x), fmins(ri4.y, rj.y)),
-                                 fmaxs(fmins(ri4.z, rj.z), fmins(ri4.w, rj.w)));
-            shared = fmaxs(shared, fmaxs(fmins(smi4.w, smj.w), fmins(svi4.w, svj.w)));
-            shared = fclamps(shared, 0.0f, 1.0f);
-            const float adjustment = fclamps(prm.rpd_scale * shared, 0.0f, 1.0f);
-            const float q = __fdividef(qn, qd * (1.0f + adjustment));
-            const bool center = dx == 0 && dy == 0;
-            exact |= fabsf(q - 25.0f) <= 25.0f * kBand;
-            exact |= !center && fabsf(q - kQAccept) <= kQAccept * kBand;
-            float wj;
-            if (exact) {
-                const float sjx[3] = {smj.x, smj.y, smj.z}, vjx[3] = {svj.x, svj.y, svj.z};
-                const double qx = exact_q(svi, smi, n_i, vjx, sjx, int(njf), prm.alpha, adjustment);
-                if (qx > 25.0) continue;
-                const double sw = 1.0 / (1.0 + double(dx * dx + dy * dy));
-                const double wd = sw * exp(-0.5 * qx);
-                if (!center && wd > 0.05 * sw) ++accepted;
-                wj = float(wd);
-            } else {
-                if (q > 25.0f) continue;
-                if (!center && q < kQAccept) ++accepted;
-                wj = srow[dx] * __expf(-0.5f * q);
-            }
-            const float4 cmj = T[P_CM * tn + e];
-            const float w2 = wj * wj;
-            row[0] = __fmaf_rn(wj, cmj.x, row[0]);
-            row[1] = __fmaf_rn(wj, cmj.y, row[1]);
-            row[2] = __fmaf_rn(wj, cmj.z, row[2]);
-            row[3] += wj;
-            row[4] += w2;
-            row[5] = __fmaf_rn(w2, aaj.w, row[5]);
-        }
-        for (int k = 0; k < 6; ++k) {  // TwoSum into the double-float accumulators
-            const float s = acc_hi[k] + row[k];
-            const float bb = s - acc_hi[k];
-            const float err = (acc_hi[k] - (s - bb)) + (row[k] - bb);
-            acc_hi[k] = s;
-            acc_lo[k] += err;
-        }
-    }
-    // the blend in single precision from the double-float sums (their relative error, ~1e-7,
-    // is far inside the plain-form bar; the weight_sum >= 1.1 test keeps its guard band)
-    const float cs0 = acc_hi[0] + acc_lo[0];
-    const float cs1 = acc_hi[1] + acc_lo[1];
-    const float cs2 = acc_hi[2] + acc_lo[2];
-    const float weight_sum = acc_hi[3] + acc_lo[3];
-    const float weight_square_sum = acc_hi[4] + acc_lo[4];
-    const float weighted_variance_sum = acc_hi[5] + acc_lo[5];
-    if (accepted >= 2 && fabsf(weight_sum - 1.1f) <= 1.1f * float(kWsBand)) {
+    // the blend in single precision from the float sums (relative error ~1e-6, far inside the
+    // plain-form bar); the weight_sum >= 1.1 test keeps its guard band. A pixel with a decision
+    // inside a band is recomputed wholly in double, the reference's operations in its order.
+    const float weight_sum = acc[3];
+    if (rechecks > 0 || (accepted >= 2 && fabsf(weight_sum - 1.1f) <= 1.1f * prm.ws_band)) {
+        if (rechecks > 0) atomicAdd(p.counters + RPD_COUNTER_WINDOW_PAIR_RECHECKS, (unsigned long long)rechecks);
+        atomicAdd(p.counters + RPD_COUNTER_WINDOW_PIXEL_RECHECKS, 1ull);
         exact_pixel(p, prm, idx);
         return;
     }
-    const float var_mean_i = ai4.w;
-    const float4 cmi4 = T[P_CM * tn + ei];
-    const float cmi[3] = {cmi4.x, cmi4.y, cmi4.z};
-    float mean_nb[3] = {cmi[0], cmi[1], cmi[2]};
+    const float var_mean_i = cmi.w;
+    float mean_nb[3] = {cmi.x, cmi.y, cmi.z};
     float var_neighbors = var_mean_i;
     if (weight_sum > 1e-8f) {
         const float inv = 1.0f / weight_sum;
-        mean_nb[0] = cs0 * inv;
-        mean_nb[1] = cs1 * inv;
-        mean_nb[2] = cs2 * inv;
-        var_neighbors = weighted_variance_sum * inv * inv;
+        mean_nb[0] = acc[0] * inv;
+        mean_nb[1] = acc[1] * inv;
+        mean_nb[2] = acc[2] * inv;
+        var_neighbors = acc[5] * inv * inv;
     }
-    const float effective = weight_sum * weight_sum / fmaxf(1e-8f, weight_square_sum);
-    const float blend = (accepted >= 2 && weight_sum >= 1.1f) ? fminf(fmaxf(1.0f - rsqrtf(effective), 0.0f), 0.8f)
-                                                               : 0.0f;
+    const float effective = weight_sum * weight_sum / fmaxf(1e-8f, acc[4]);
+    const float blend =
+        (accepted >= 2 && weight_sum >= 1.1f) ? fminf(fmaxf(1.0f - rsqrtf(effective), 0.0f), 0.8f) : 0.0f;
     const float alpha = 1.0f - blend;
-    for (int c = 0; c < 3; ++c) p.denoised[c][idx] = lerpf(cmi[c], mean_nb[c], blend);
+    p.denoised[0][idx] = lerpf(cmi.x, mean_nb[0], blend);
+    p.denoised[1][idx] = lerpf(cmi.y, mean_nb[1], blend);
+    p.denoised[2][idx] = lerpf(cmi.z, mean_nb[2], blend);
     const float uncertainty = alpha * alpha * var_mean_i + blend * blend * var_neighbors +
                               2.0f * alpha * blend * (1.0f / fmaxf(weight_sum, 1e-8f)) * var_mean_i;
     p.alpha[idx] = alpha;
@@ -550,14 +669,70 @@ float sqrt_gate_threshold(float t) {
 
 size_t tile_bytes(int r, int by) {
     const size_t side = size_t(2 * r + 1);
-    return size_t(kTileX + 2 * r) * size_t(by + 2 * r) * P_COUNT * sizeof(float4) + 32 * sizeof(float2) +
-           side * side * sizeof(float);
+    return 128 + size_t(kTileX + 2 * r) * size_t(by + 2 * r) * W_COUNT * sizeof(float4) + side * side * sizeof(float);
+}
+
+LineTable line_table(int table, float z) {
+    const float* tab = table == 0 ? kT05 : kT01;
+    LineTable lt{};
+    for (int k = 0; k < 64; ++k) {
+        if (k < 2) {
+            lt.v[k] = make_float2(tab[0], 0.0f);
+        } else if (k < 60) {
+            const int lo = k >> 1;
+            const float d = tab[lo] - tab[lo - 1];
+            lt.v[k] = make_float2(float(double(tab[lo - 1]) - double(lo) * double(d)), d);
+        } else if (k == 60) {
+            lt.v[k] = make_float2(tab[29], 0.0f);
+        } else {
+            lt.v[k] = make_float2(z, 0.0f);
+        }
+    }
+    return lt;
+}
+
+// The tensor map of the job's packed records for halo boxes of radius r and `by` block rows.
+cudaError_t window_map(Job& j, int r, int by) {
+    if (j.win_map_r == r && j.win_map_by == by) return cudaSuccess;
+    const cudaError_t e = encode_record_map(reinterpret_cast<CUtensorMap*>(j.win_map), j.p.win, j.g.w, j.g.h, W_COUNT,
+                                            kTileX + 2 * r, by + 2 * r);
+    if (e != cudaSuccess) return e;
+    j.win_map_r = r;
+    j.win_map_by = by;
+    return cudaSuccess;
+}
+
+template <int RC>
+cudaError_t launch_tma(Job& j, const StatmcParams& prm, const LineTable& lt, int by) {
+    const size_t smem = tile_bytes(prm.r, by);
+    // the dynamic shared memory size this instantiation allows, per device
+    static std::mutex mu;
+    static std::unordered_map<int, size_t> configured;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        size_t& allowed = configured[j.ctx->device];
+        if (smem > allowed) {
+            const cudaError_t e = cudaFuncSetAttribute(k_statmc_tma<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       int(smem));
+            if (e != cudaSuccess) return e;
+            allowed = smem;
+        }
+    }
+    const cudaError_t e = window_map(j, prm.r, by);
+    if (e != cudaSuccess) return e;
+    CUtensorMap map;
+    std::memcpy(&map, j.win_map, sizeof(map));
+    const dim3 block(kTileX, by);
+    const dim3 grid((j.g.w + kTileX - 1) / kTileX, (j.g.h + by - 1) / by);
+    k_statmc_tma<RC><<<grid, block, smem, j.stream>>>(j.p, prm, lt, map);
+    return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_statmc(Job& j) {
     const int64_t np = j.g.np;
+    const float var2_max = j.cfg.color_sigma_max * j.cfg.color_sigma_max;
     {
         KernelScope ks(j, RPD_KERNEL_SQRT_VARIANCE);
         k_sqrt_var_mean<<<grid_for(np, 256), 256, 0, j.stream>>>(j.p, np);
@@ -566,7 +741,7 @@ cudaError_t launch_statmc(Job& j) {
         for (int dy = -1; dy <= 1; ++dy)
             for (int dx = -1; dx <= 1; ++dx) weight_sum += 1.0 / (1.0 + double(dx * dx + dy * dy));
         const dim3 sgrid((j.g.w + kSvTx - 1) / kSvTx, (j.g.h + kSvTy - 1) / kSvTy);
-        k_sqrt_var_stable<<<sgrid, dim3(kSvTx, kSvTy), 0, j.stream>>>(j.p, j.g.w, j.g.h, weight_sum);
+        k_sqrt_var_stable<<<sgrid, dim3(kSvTx, kSvTy), 0, j.stream>>>(j.p, j.g.w, j.g.h, weight_sum, var2_max);
     }
     KernelScope ks(j, RPD_KERNEL_STATMC_WINDOW);
     StatmcParams prm{};
@@ -577,7 +752,7 @@ cudaError_t launch_statmc(Job& j) {
     prm.depth_threshold = j.cfg.color_depth_threshold;
     prm.rpd_scale = j.cfg.rpf_shrinkage_scale;
     prm.alpha = j.cfg.color_compat_alpha;
-    prm.var2_max = j.cfg.color_sigma_max * j.cfg.color_sigma_max;
+    prm.var2_max = var2_max;
     static const float albedo_sq = sqrt_gate_threshold(0.12f);
     prm.albedo_sq_threshold = albedo_sq;
     // the branch of lookup_t_critical this alpha takes (main.cpp:189-225)
@@ -587,29 +762,46 @@ cudaError_t launch_statmc(Job& j) {
     else prm.table = 2;
     prm.z = a <= 0.001f ? 3.29f : a <= 0.005f ? 2.81f : a <= 0.01f ? 2.58f : a <= 0.02f ? 2.33f
           : a <= 0.05f ? 1.96f : a <= 0.10f ? 1.64f : 1.28f;
+    prm.inv_z2 = float(1.0 / (double(prm.z) * double(prm.z)));
     prm.df_break = prm.table < 2 ? 30.5f : 30.0f;
-    int by = 0;
-    for (int cand : {8, 4, 2}) {
-        if (tile_bytes(prm.r, cand) <= size_t(110) * 1024) {
-            by = cand;
-            break;
+    prm.band = std::ldexp(1.0f, -j.window_guard);
+    prm.ws_band = std::ldexp(1.0f, -j.window_guard - 1);
+    // df <= (n_i - 1) + (n_j - 1) < 30.5 (table) / 30 (quantile) when every n - 1 <= 15 / 14;
+    // df >= min(n_i, n_j) - 1 >= 31 when every n - 1 >= 31
+    prm.rp_below = prm.table < 2 ? 1.0f / 15.0f : 1.0f / 14.0f;
+    prm.rp_above = 1.0f / 31.0f;
+    cudaError_t e = cudaSuccess;
+    const int r = prm.r;
+    if (j.exact_window || r > 16) {
+        k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
+        e = cudaGetLastError();
+    } else {
+        const LineTable lt = line_table(prm.table, prm.z);
+        const size_t limit = size_t(200) * 1024;
+        const bool fixed = (r == 3 || r == 5 || r == 7) && (j.statmc_by == 0 || j.statmc_by == kRows) &&
+                           tile_bytes(r, kRows) <= limit;
+        if (fixed) {
+            prm.by = kRows;
+            e = r == 5 ? launch_tma<5>(j, prm, lt, kRows) : r == 7 ? launch_tma<7>(j, prm, lt, kRows)
+                                                               : launch_tma<3>(j, prm, lt, kRows);
+        } else {
+            int by = 0;
+            for (int cand : {8, 4, 2})
+                if (tile_bytes(r, cand) <= limit && (j.statmc_by == 0 || cand <= j.statmc_by)) {
+                    by = cand;
+                    break;
+                }
+            if (by == 0) {
+                k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
+                e = cudaGetLastError();
+            } else {
+                prm.by = by;
+                e = launch_tma<0>(j, prm, lt, by);
+            }
         }
     }
-    // a tuned tile height (RPD_TUNE_STATMC_ROWS) when its tile fits
-    if (j.statmc_by > 0 && j.statmc_by <= by) by = j.statmc_by;
-    if (j.exact_window || by == 0) {
-        k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
-    } else {
-        prm.by = by;
-        const size_t smem = tile_bytes(prm.r, by);
-        cudaError_t e = cudaFuncSetAttribute(k_statmc_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-        const dim3 block(kTileX, by);
-        const dim3 grid((j.g.w + kTileX - 1) / kTileX, (j.g.h + by - 1) / by);
-        k_statmc_tile<<<grid, block, smem, j.stream>>>(j.p, prm);
-    }
     j.launches += 3;
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace rpd

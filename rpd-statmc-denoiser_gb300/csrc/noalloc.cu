@@ -77,8 +77,9 @@ extern "C" int rpd_atrous_wavelet_noalloc(const float* raw, const float* normal,
     float* second = (iterations & 1) ? scratch : out;
     float* result = nullptr;
     uint64_t launches = 0;
+    // no records scratch: the passes renormalise each tap's normal from the caller's buffer
     RPD_CUDA(rpd::launch_atrous(raw, normal, albedo, width, height, sigma_c, sigma_n, sigma_a, iterations, first,
-                                second, &result, s, &launches));
+                                second, nullptr, &result, s, &launches));
     if (result != out) return fail(RPD_ERR_STATE, "a-trous passes did not end in the output buffer");
     return RPD_OK;
 }

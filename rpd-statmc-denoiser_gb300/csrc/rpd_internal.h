@@ -75,6 +75,10 @@ struct PixelPlanes {
     // statmc scratch: stabilised sqrt variance of the mean (main.cpp:972-990)
     float* sqrt_var_mean[3];
     float* sqrt_var_stable[3];
+    // statmc_denoise's packed neighbour records: six float4 planes of W*H, one after the other
+    // (record k of pixel i at win[k * W*H + i]), written with the stabilised sqrt variance and
+    // staged into shared memory tile by tile by the window kernel (k_statmc.cu)
+    float4* win;
     // variance_denoise (main.cpp:1178-1264)
     float* variance_denoised;
     float* var_ping;
@@ -91,6 +95,8 @@ struct PixelPlanes {
     // scratch of the parallel allocation (k_allocate.cu)
     uint8_t* alloc_state;
     unsigned char* alloc_work;
+    // RPD_COUNTER_COUNT_ device counters (rpd_counter)
+    unsigned long long* counters;
 };
 
 struct NodePlanes {
@@ -158,6 +164,7 @@ struct Job {
     bool exact_window = false;   // RPD_EXACT_WINDOW: double-precision StatMC window
     int grid_shape = 6;          // launch shape of the random-dimension grid pass (row groups x dimension sets)
     int statmc_by = 0;           // StatMC tile height (0: the largest that fits)
+    int window_guard = 15;       // the StatMC window's guard band is 2^-window_guard (RPD_TUNE_WINDOW_GUARD)
     bool serial_allocator = false;  // RPD_TUNE_ALLOCATOR = 1: the one-thread allocation kernel only
     bool smooth_fp64 = false;       // RPD_TUNE_SMOOTHING = 1: the importance smoothing in double-precision instructions
     int allocator_blocks = 0;       // RPD_TUNE_ALLOCATOR >= 2: blocks of the parallel allocation
@@ -179,6 +186,10 @@ struct Job {
     double ktotal[RPD_KERNEL_COUNT_]{};
     uint64_t kcount[RPD_KERNEL_COUNT_]{};
     cudaEvent_t marks[8]{};      // rpd_job_mark slots
+    // the StatMC window's tensor map over `win` (a CUtensorMap, 64-byte aligned), for the
+    // halo box of radius win_map_r and win_map_by rows per block (0: not encoded yet)
+    alignas(64) unsigned char win_map[128]{};
+    int win_map_r = 0, win_map_by = 0;
 };
 
 // Brackets the launches of one kernel family with CUDA events when profiling is on.
@@ -326,12 +337,19 @@ cudaError_t allocator_stats(Job& j, int32_t* out);
 int allocator_timeline(Job& j, uint64_t* ns, int32_t max, int32_t* n);
 cudaError_t launch_finalize(Job& j);
 cudaError_t launch_expand(Job& j, const float* node_field, float* out);
+// `iterations` a-trous passes ping-ponging between buf_a and buf_b (interleaved RGB); *result
+// gets the buffer holding the last pass (raw for 0 passes). records: scratch for 2 * w * h float4
+// normal and albedo records, or nullptr to renormalise the normals at every tap instead.
 cudaError_t launch_atrous(const float* raw, const float* normal, const float* albedo, int w, int h,
                           float sigma_c, float sigma_n, float sigma_a, int iterations, float* buf_a,
-                          float* buf_b, float** result, cudaStream_t stream, uint64_t* launches);
+                          float* buf_b, float4* records, float** result, cudaStream_t stream, uint64_t* launches);
+// The joint bilateral filter's scratch (its records and a copy-timeout flag), and the filter.
+// The flag (an unsigned after the records) is non-zero when a tile copy's bounded wait gave up.
+uint64_t joint_bilateral_scratch_bytes(int w, int h);
 cudaError_t launch_joint_bilateral(const float* raw, const float* normal, const float* albedo, int w, int h,
                                    float sigma_c, float sigma_n, float sigma_p, float sigma_a, float* gaussian,
-                                   float* bilateral, float* joint, cudaStream_t stream, uint64_t* launches);
+                                   float* bilateral, float* joint, void* scratch, cudaStream_t stream,
+                                   uint64_t* launches);
 
 // Pushes without host synchronisation (the serving loop, serve.cu). job_reserve sizes the
 // offsets for every pixel and the per-sample scratch for pushes of up to max_push_samples, so

@@ -323,6 +323,8 @@ def lib() -> C.CDLL:
         "rpd_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStats)]),
         "rpd_server_kernel_times": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
         "rpd_server_destroy": (None, [vp]),
+        "rpd_job_counters": (C.c_int, [vp, C.POINTER(C.c_uint64), i32]),
+        "rpd_probe_fp32_issue": (C.c_int, [C.c_int, i32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "rpd_last_error": (C.c_char_p, []),
         "rpd_status_string": (C.c_char_p, [C.c_int]),
     }
@@ -351,7 +353,8 @@ def exported_symbols() -> list[str]:
             "rpd_job_set_profiling", "rpd_job_kernel_time", "rpd_job_reset_kernel_times", "rpd_kernel_name",
             "rpd_job_mark", "rpd_job_mark_elapsed",
             "rpd_atrous_wavelet", "rpd_joint_bilateral", "rpd_atrous_wavelet_noalloc", "rpd_device_alloc", "rpd_device_free", "rpd_host_alloc",
-            "rpd_host_free", "rpd_memcpy", "rpd_synth_fill", "rpd_last_error", "rpd_status_string"]
+            "rpd_host_free", "rpd_memcpy", "rpd_synth_fill", "rpd_last_error", "rpd_status_string",
+            "rpd_job_counters", "rpd_probe_fp32_issue"]
 
 
 def check(status: int) -> None:
@@ -644,7 +647,7 @@ class Job:
     def set_exact(self, grid: bool = False, window: bool = False) -> None:
         check(lib().rpd_job_set_exact(self.handle, (1 if grid else 0) | (2 if window else 0)))
 
-    TUNING = {"grid_shape": 0, "host_band_mb": 1, "statmc_rows": 2, "allocator": 3, "smoothing": 4}
+    TUNING = {"grid_shape": 0, "host_band_mb": 1, "statmc_rows": 2, "allocator": 3, "smoothing": 4, "window_guard": 5}
 
     def autotune(self, samples, spp: int) -> None:
         """rpd_job_autotune on device-resident planes (leaves the frame denoised)."""
@@ -794,6 +797,14 @@ class Job:
             out[name] = (ms.value, n.value)
         return out
 
+    def counters(self) -> dict[str, int]:
+        """The job's device counters (rpd_counter): the StatMC window's double-precision
+        rechecks of the last statmc_denoise and the device waits that gave up."""
+        out = (C.c_uint64 * 8)()
+        check(lib().rpd_job_counters(self.handle, out, 8))
+        return {"window_pair_rechecks": int(out[0]), "window_pixel_rechecks": int(out[1]),
+                "device_wait_timeouts": int(out[2])}
+
 
 class Server:
     """rpd_server: the serving loop (continuous batching of denoise requests)."""
@@ -908,6 +919,13 @@ def plain_request(ctx: Context, knobs: Config, width: int, height: int, spp: int
         start_dev.free()
         if own:
             job.close()
+
+
+def probe_fp32_issue(device: int = 0, repeats: int = 5) -> dict:
+    """FP32 lane instructions per second the device issues (rpd_probe_fp32_issue)."""
+    rate, ms = C.c_double(), C.c_double()
+    check(lib().rpd_probe_fp32_issue(device, repeats, C.byref(rate), C.byref(ms)))
+    return {"per_second": rate.value, "ms": ms.value}
 
 
 class PinnedBuffer:

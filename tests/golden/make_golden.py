@@ -18,6 +18,9 @@ oracle/binding.py:
 Fixtures (numpy .npz, compressed; `meta` is a JSON string):
 
   cornell_48x48x4.npz         reference-traced samples + every stage output + counts
+  cornell_256x256x4.npz       the plain-method cornell_box configuration at its full size
+                              (256x256, 4 spp, seed 1234, adaptive_passes 0): reference-traced
+                              samples and every stage output
   cornell_32x32_adaptive.npz  base + per-pass extra samples (traced with the reference's
                               counts), per-pass counts, final outputs (adaptive_passes 2)
   synth_48x32x8.npz           outputs for the synthetic generator (samples regenerated from
@@ -45,7 +48,8 @@ sys.path.insert(0, str(ROOT))
 from oracle import binding as B  # noqa: E402
 
 R = B.R
-REF_ROOT = Path(os.environ.get("REF_ROOT", "/root/reference"))
+# the reference checkout: REF_ROOT, else a checkout named "reference" beside this repository
+REF_ROOT = Path(os.environ.get("REF_ROOT", ROOT.parent / "reference"))
 YAML = REF_ROOT / "path_tracer" / "config" / "cornell.yaml"
 
 # Fields compared by the tests (EXPANDED_* are the caches behind the sensitivity maps; the
@@ -95,6 +99,26 @@ def cornell_single() -> None:
     arrays["out_ADAPTIVE_IMPORTANCE"] = job.read("ADAPTIVE_IMPORTANCE")
     job.close()
     save("cornell_48x48x4.npz", {"config": B.config_dict(cfg), "spp": spp, "planes": list(s.planes)}, arrays)
+
+
+def cornell_full() -> None:
+    """The 256x256 4-spp cornell_box configuration itself (one frame, no adaptive pass)."""
+    w = h = 256
+    spp = 4
+    cfg = B.ref_parse_yaml(str(YAML)).replace(image_width=w, image_height=h, adaptive_passes=0,
+                                               adaptive_spp=4, adaptive_base_samples=1, **CORNELL_KNOBS)
+    s = B.trace_cornell(str(YAML), w, h, spp, cfg.seed)
+    job = B.RefJob(cfg, threads=1)  # the single-thread grid order, which the exact grid mode reproduces
+    B.run_pipeline(job, s, spp)
+    arrays = {}
+    # lens and environment samples are never valid in this scene (zero planes): not stored
+    planes = [k for k, v in s.planes.items() if np.any(v)]
+    for k in planes:
+        arrays["s_" + k] = s.planes[k]
+    put_fields(arrays, job)
+    job.close()
+    save("cornell_256x256x4.npz", {"config": B.config_dict(cfg), "spp": spp, "planes": planes,
+                                   "sample_sha256": sample_hashes(s)}, arrays)
 
 
 def cornell_adaptive() -> None:
@@ -246,6 +270,7 @@ if __name__ == "__main__":
     if not B.have_ref():
         sys.exit("oracle/_ref is not built: run `make -C oracle ref REF_ROOT=<reference checkout>` first")
     cornell_single()
+    cornell_full()
     cornell_adaptive()
     synth_single()
     synth_adaptive()

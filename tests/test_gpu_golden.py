@@ -70,6 +70,23 @@ def test_cornell_golden(gpu_ctx, exact):
 
 
 @pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+def test_cornell_256x256x4_golden(gpu_ctx, exact):
+    """The plain-method cornell_box configuration at its own size: 256x256, 4 spp, seed 1234,
+    samples traced by the reference, every stage output the reference's."""
+    meta, a = load_golden("cornell_256x256x4.npz")
+    cfg = golden_config(meta)
+    assert (cfg.image_width, cfg.image_height, meta["spp"], cfg.seed) == (256, 256, 4, 1234)
+    s = golden_samples(a, "s_", meta["planes"], cfg.image_width * cfg.image_height)
+    for name, plane in s.planes.items():
+        assert hashlib.sha256(np.ascontiguousarray(plane).tobytes()).hexdigest() == meta["sample_sha256"][name]
+    g = R.Job(gpu_ctx, cfg)
+    g.set_exact(grid=exact, window=exact)
+    B.run_pipeline(g, s, meta["spp"])
+    check_golden(g, a, exact)
+    g.close()
+
+
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
 def test_cornell_adaptive_golden(gpu_ctx, exact):
     """render()'s adaptive loop with the reference's traced extra samples: each pass pushes
     the samples the reference drew for its own counts."""

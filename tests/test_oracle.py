@@ -18,7 +18,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from conftest import (B, GOLDEN, R, assert_bitwise, golden_config, golden_samples, load_golden, replay_adaptive,
+from conftest import (B, GOLDEN, ROOT, R, assert_bitwise, golden_config, golden_samples, load_golden, replay_adaptive,
                       small_config)
 
 REF_DIR = B.HERE / "_ref"
@@ -47,7 +47,7 @@ def test_reference_unit_tests_pass(binary):
     args = [str(exe)]
     if binary == "config_test":
         # the test parses every YAML of the reference's config folder (its CTest argument)
-        cfg_dir = Path(os.environ.get("REF_ROOT", "/root/reference")) / "path_tracer" / "config"
+        cfg_dir = Path(os.environ.get("REF_ROOT", ROOT.parent / "reference")) / "path_tracer" / "config"
         if not cfg_dir.is_dir():
             pytest.skip("reference config folder not present")
         args.append(str(cfg_dir))
@@ -67,6 +67,18 @@ def test_port_cornell_golden():
     assert_all_fields(o, a)
     assert np.array_equal(o.compute_adaptive_sample_counts(), a["counts"])
     assert_bitwise(o.read("ADAPTIVE_IMPORTANCE"), a["out_ADAPTIVE_IMPORTANCE"], "importance")
+    o.close()
+
+
+def test_port_cornell_256x256x4_golden():
+    """The plain-method cornell_box configuration at its own size (256x256, 4 spp)."""
+    meta, a = load_golden("cornell_256x256x4.npz")
+    cfg = golden_config(meta)
+    w, h = cfg.image_width, cfg.image_height
+    s = golden_samples(a, "s_", meta["planes"], w * h)
+    o = B.OracleJob(cfg, threads=1)
+    B.run_pipeline(o, s, meta["spp"])
+    assert_all_fields(o, a)
     o.close()
 
 
