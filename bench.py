@@ -174,6 +174,13 @@ def max_over_ranks(dist, value: float) -> float:
     return float(t.item())
 
 
+def replica_throughput(dist, world: int, samples_per_rank: int, elapsed_ms: float, steps: int):
+    """(ms per step, Msamples/s) of N replicas that each processed samples_per_rank samples per
+    step: the slowest rank's time, every rank's samples."""
+    ms_per_step = max_over_ranks(dist, elapsed_ms) / steps
+    return ms_per_step, world * samples_per_rank / (ms_per_step * 1e-3) / 1e6
+
+
 def barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -233,9 +240,7 @@ def run_gpu(args):
     launches = job.launches() - launches0
     ktimes = job.kernel_times()
     job.set_profiling(False)
-    elapsed_max = max_over_ranks(dist, elapsed)
-    ms_per_step = elapsed_max / args.steps
-    value = world * n / (ms_per_step * 1e-3) / 1e6
+    ms_per_step, value = replica_throughput(dist, world, n, elapsed, args.steps)
 
     # end-to-end through the C ABI from pinned host buffers: every step pushes the frame's
     # planes from host memory (copied to HBM inside the push) and reads the denoised image back.

@@ -454,7 +454,10 @@ int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, con
  * must not overlap the inputs, and the call is asynchronous on `stream` (a cudaStream_t,
  * NULL for the legacy default stream). One scratch per device: overlapping calls on a
  * device race. The first call on a device looks the scratch up and should precede any
- * stream capture. */
+ * stream capture; the address is kept for the life of the process, so the entry point must
+ * not be called on a device after cudaDeviceReset. The 48 MiB array is part of the library's
+ * module: every context that loads the module reserves it (with lazy loading at first use,
+ * with CUDA_MODULE_LOADING=EAGER at context creation), whether or not this is called. */
 #define RPD_NOALLOC_MAX_PIXELS 4194304 /* 2048 x 2048; 48 MiB of FP32 RGB scratch */
 int rpd_atrous_wavelet_noalloc(const float* raw, const float* normal, const float* albedo,
                                int32_t width, int32_t height, float sigma_c, float sigma_n,

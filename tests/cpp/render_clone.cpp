@@ -2,7 +2,9 @@
 // against include/rpd_statmc.hpp: the four stage functions keep their reference names and
 // signatures, and the per-sample accumulation becomes pushes of synthetic samples.
 //
-//   render_clone W H SPP PASSES   -> prints the mean denoised value and the adaptive total
+//   render_clone W H SPP PASSES [OUT]   -> prints the mean denoised value and the adaptive total;
+//                                        OUT gets each pass's counts (W*H int32 per pass) and
+//                                        the denoised image (W*H*3 float)
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -57,6 +59,8 @@ int main(int argc, char** argv) {
         spp = std::atoi(argv[3]);
     }
     if (argc > 4) config.adaptive_passes = std::atoi(argv[4]);
+    const char* out_path = argc > 5 ? argv[5] : nullptr;
+    std::vector<int32_t> all_counts;
     const int w = config.image_width, h = config.image_height;
     const int64_t np = int64_t(w) * h;
     try {
@@ -82,6 +86,7 @@ int main(int argc, char** argv) {
             rpd::statmc_denoise(config);
             rpd::variance_denoise(config);
             std::vector<int> counts = rpd::compute_adaptive_sample_counts(config);
+            all_counts.insert(all_counts.end(), counts.begin(), counts.end());
             int64_t extra = 0;
             for (int c : counts) extra += c;
             adaptive_total += extra;
@@ -102,6 +107,14 @@ int main(int argc, char** argv) {
         for (float v : den) mean += v;
         mean /= double(den.size());
         std::printf("denoised_mean %.9g adaptive_total %lld\n", mean, (long long)adaptive_total);
+        if (out_path) {
+            std::FILE* fo = std::fopen(out_path, "wb");
+            if (!fo) return 2;
+            const bool ok = std::fwrite(all_counts.data(), sizeof(int32_t), all_counts.size(), fo) == all_counts.size() &&
+                            std::fwrite(den.data(), sizeof(float), den.size(), fo) == den.size();
+            std::fclose(fo);
+            if (!ok) return 2;
+        }
         rpd::set_current_job(nullptr);
     } catch (const rpd::Error& e) {
         std::fprintf(stderr, "rpd error %d: %s\n", e.status, e.what());
