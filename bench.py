@@ -37,7 +37,9 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "rpd-statmc-denoiser_gb300"))
 
 W, H, SPP, SEED = 1920, 1080, 16, 1234
-METRIC = "denoised Msamples/s at 1080p 16spp (plain)"
+# BASELINE's metric: `value` is the plain form's throughput; the line's `served` object holds the
+# served stream's throughput and p50/p99 latency against the plain per-frame drop-in
+METRIC = "denoised Msamples/s at 1080p 16spp, plain vs served; p50/p99 ms @\u22641e-3 relMSE"
 UNIT = "Msamples/s"
 
 
@@ -335,9 +337,49 @@ def run_gpu(args):
     if samples is not dev:
         samples.free()
     dev.free()
+    if args.precision == "fp32" and (W, H, SPP) == (1920, 1080, 16):
+        out["filters"] = filters_leg(R, ctx)
+    if not args.no_served and args.precision == "fp32" and (W, H, SPP) == (1920, 1080, 16):
+        # the served half of the metric (plain vs served; p50/p99 latency)
+        out["served"] = served_summary(R, ctx, args, rank, dist, args.served_requests)
     ctx.close()
     if rank == 0:
         print(json.dumps(out))
+
+
+def filters_leg(R, ctx, w=1920, h=1080, reps=10):
+    """The standalone post-filters on a w x h frame in device memory, through their C ABI
+    calls (each call synchronises; its scratch comes from the stream-ordered pool): a-trous with
+    its 5 default passes and sigmas (denoising/atrous_wavelet.cpp:229) and the joint bilateral
+    with sigma_p 2 (a 13x13 window). Mean host wall time per call after 2 warm-up calls."""
+    rng = np.random.default_rng(5)
+    imgs = [rng.lognormal(-1.0, 0.8, (h, w, 3)).astype(np.float32), rng.uniform(0, 1, (h, w, 3)).astype(np.float32),
+            rng.uniform(0, 1, (h, w, 3)).astype(np.float32)]
+    bufs = [R.DeviceBuffer(ctx, imgs[0].nbytes) for _ in range(6)]
+    try:
+        for b, a in zip(bufs, imgs):
+            b.upload(a)
+        L = R.lib()
+
+        def atrous():
+            R.check(L.rpd_atrous_wavelet(ctx.handle, bufs[0].ptr, bufs[1].ptr, bufs[2].ptr, w, h, 0.3, 0.2, 0.1, 5,
+                                         bufs[3].ptr, R.MEM_DEVICE))
+
+        def joint():
+            R.check(L.rpd_joint_bilateral(ctx.handle, bufs[0].ptr, bufs[1].ptr, bufs[2].ptr, w, h, 0.3, 0.2, 2.0, 0.1,
+                                          bufs[3].ptr, bufs[4].ptr, bufs[5].ptr, R.MEM_DEVICE))
+        out = {"frame": f"{w}x{h}, device memory, host wall time per synchronous call"}
+        for name, fn in (("atrous_5_passes_ms", atrous), ("joint_bilateral_r6_ms", joint)):
+            for _ in range(2):
+                fn()
+            t = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            out[name] = round((time.perf_counter() - t) * 1e3 / reps, 4)
+        return out
+    finally:
+        for b in bufs:
+            b.free()
 
 
 def pinned_host_copy(R, ctx, dev):
@@ -408,7 +450,10 @@ def compact_quality(R, ctx, cfg, dev, dev16):
 
 # DRAM bytes per pixel per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu
 # captures summarised in profiles/, for the kernels whose traffic grows with the pixel count
-NCU_TRAFFIC_PER_PIXEL = {}
+NCU_TRAFFIC_PER_PIXEL = {
+    # k_statmc_tma<5>, one launch at 960x540x16 (--set full): 49.88 MB read + 1.95 MB written
+    "statmc_window": ((49.877504e6 + 1.950208e6) / (960 * 540), "ncu at 960x540x16, per pixel, scaled by the pixels"),
+}
 
 
 def kernel_roofline(kernel, times, steps, cfg, np_, nn, n, peaks, fp32_peak):
@@ -612,22 +657,17 @@ def request_stream(count: int, rate: float, seed: int):
     return out
 
 
-def run_serving(args):
-    """The serving form: a Poisson stream of requests (sizes and spp of the mixed stream, three
-    adaptive passes each, extra samples generated on the device) submitted to rpd_server in
-    real time; the server admits them against a 120 GB HBM budget and overlaps them on the GPU.
-    Against the plain per-frame drop-in (render()'s call sequence from the host, FP32 planes, one
-    request after another) on a bounded prefix of the same stream."""
+def served_stream(R, ctx, args, rank, dist, n_req, storage):
+    """A Poisson stream of n_req requests (sizes and spp of the mixed stream, three adaptive
+    passes each, extra samples generated on the device) submitted to rpd_server in real time;
+    the server admits them against the HBM budget and overlaps them on the GPU. Returns the
+    throughput, latencies and server statistics."""
     import threading
 
-    import rpd_gb300 as R
-
-    world, rank, local, dist = dist_setup()
-    ctx = R.Context(local, 0)
     knobs = serving_knobs(R)
-    n_req = args.steps
+    world = 1 if dist is None else dist.get_world_size()
     stream = request_stream(n_req, args.rate, SEED + 1000 * rank)
-    srv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=args.inflight, storage=args.storage,
+    srv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=args.inflight, storage=storage,
                    allocator_blocks=args.alloc_blocks)
     # warm-up: a few requests of every size (creates the cached jobs, fills the buffer pool)
     for k in range(max(1, args.warmup)):
@@ -637,8 +677,8 @@ def run_serving(args):
     srv.poll(4096)
     st0 = srv.stats()
     barrier(dist)
-    # the arrival process, in real time, from a host thread
-    def submitter(t0):
+
+    def submitter(t0):  # the arrival process, in real time, from a host thread
         for (t, w, h, spp, seed) in stream:
             delay = t0 + t - time.perf_counter()
             if delay > 0.002:
@@ -646,7 +686,8 @@ def run_serving(args):
             while time.perf_counter() < t0 + t:
                 pass
             srv.submit(w, h, spp, seed, tag=seed)
-    with ClockSampler(local) as clocks:
+
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
         t0 = time.perf_counter()
         th = threading.Thread(target=submitter, args=(t0,))
         th.start()
@@ -654,6 +695,7 @@ def run_serving(args):
         srv.drain(3600000)
     done = [c for c in srv.poll(n_req + 16) if c["tag"] != 0]
     st1 = srv.stats()
+    srv.close()
     assert len(done) == n_req and all(c["status"] == 0 for c in done), "serving run incomplete"
     first = min(c["submit_ms"] for c in done)
     last = max(c["done_ms"] for c in done)
@@ -661,15 +703,45 @@ def run_serving(args):
     samples = sum(c["samples"] for c in done)
     lat = np.array([c["done_ms"] - c["submit_ms"] for c in done])
     queue_ms = np.array([c["admit_ms"] - c["submit_ms"] for c in done])
-    value = world * samples / wall_s / 1e6
-    srv.close()
+    return {"value": world * samples / wall_s / 1e6, "samples": samples, "wall_s": wall_s, "stream": stream,
+            "done": done, "stats": st1, "launches": int(st1["launches"] - st0["launches"]),
+            "clocks": clocks.summary(),
+            "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3),
+                           "mean": round(float(lat.mean()), 3), "max": round(float(lat.max()), 3),
+                           "queue_p50": round(float(np.percentile(queue_ms, 50)), 3),
+                           "queue_p99": round(float(np.percentile(queue_ms, 99)), 3)}}
 
-    # quality on the stream's first small requests: the served result against the plain FP32
-    # drop-in on the same request, and both against the plain method at 1024 spp (converged)
+
+def plain_prefix(R, ctx, stream, n_plain, skip_dead=False):
+    """The plain per-frame drop-in on a prefix of the stream, one request after another (jobs
+    cached per size, as a caller of the drop-in would keep them): Msamples/s. skip_dead: without
+    the calls whose results the sequence overwrites unread (what the serving loop leaves out)."""
+    knobs = serving_knobs(R)
+    jobs = {}
+    samples = 0
+    for (_, w, h, spp, seed) in stream[:2]:
+        R.plain_request(ctx, knobs, w, h, spp, seed, skip_dead=skip_dead)  # warm-up
+    t = time.perf_counter()
+    for (_, w, h, spp, seed) in stream[:n_plain]:
+        if (w, h) not in jobs:
+            jobs[(w, h)] = R.Job(ctx, knobs.replace(image_width=w, image_height=h))
+        _, ns = R.plain_request(ctx, knobs, w, h, spp, seed, job=jobs[(w, h)], skip_dead=skip_dead)
+        samples += ns
+    t = time.perf_counter() - t
+    for j in jobs.values():
+        j.close()
+    return {"value": samples / t / 1e6, "requests": n_plain, "samples": samples, "s": round(t, 3)}
+
+
+def served_quality(R, ctx, args, stream, storage):
+    """The served result of the stream's first small requests against the plain FP32 drop-in on
+    the same request, and both against the plain method at 1024 spp (converged)."""
+    knobs = serving_knobs(R)
+
     def relmse(x, ref):
         return float(np.mean((x - ref) ** 2 / (ref * ref + 1e-2)))
     picks = [r for r in stream if r[1] * r[2] <= 640 * 360][:4]
-    qsrv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=4, storage=args.storage)
+    qsrv = R.Server(ctx, knobs, budget_bytes=args.budget_gb << 30, max_inflight=4, storage=storage)
     bufs = []
     for (_, w, h, spp, seed) in picks:
         b = R.PinnedBuffer(w * h * 12)
@@ -688,61 +760,78 @@ def run_serving(args):
         q_served_conv.append(relmse(x, y))
         q_plain_conv.append(relmse(p_, y))
         b.free()
+    return {"requests": [list(r[1:4]) for r in picks], "rel_mse_eps": 1e-2,
+            "vs_plain_fp32": {"mean": float(np.mean(q_plain)), "max": float(np.max(q_plain))},
+            "served_vs_converged": float(np.mean(q_served_conv)),
+            "plain_vs_converged": float(np.mean(q_plain_conv)),
+            "note": "with adaptive passes the compact storage also moves the adaptive counts a little (the "
+                    "systematic residual sampling follows a running sum), so some pixels draw one sample more or "
+                    "less than in the FP32 run; converged = the plain FP32 method at 1024 spp; the error of the "
+                    "compact form against the FP64 oracle is a test (tests/test_gpu_precision.py)"}
 
-    # the plain per-frame drop-in on a bounded prefix of the stream, one request after another
-    # (jobs cached per size, as a caller of the drop-in would keep them)
-    plain_jobs = {}
-    plain_samples = 0
+
+def served_summary(R, ctx, args, rank, dist, n_req, breakdown=True):
+    """The served half of the metric: the FP16-storage stream's Msamples/s and p50/p99 latency
+    against the plain per-frame drop-in on a prefix of the same stream, and how the ratio splits
+    into its parts (each measured): the dead calls the serving loop leaves out (the plain drop-in
+    without them), the overlap of requests on the device (the served stream with FP32 storage),
+    and the compact storage (FP16 against FP32 served)."""
+    fp16 = served_stream(R, ctx, args, rank, dist, n_req, "fp16")
+    stream = fp16["stream"]
     n_plain = min(n_req, args.plain_requests)
-    for (_, w, h, spp, seed) in stream[:2]:
-        R.plain_request(ctx, knobs, w, h, spp, seed)  # warm-up
-    t_plain = time.perf_counter()
-    for (_, w, h, spp, seed) in stream[:n_plain]:
-        if (w, h) not in plain_jobs:
-            plain_jobs[(w, h)] = R.Job(ctx, knobs.replace(image_width=w, image_height=h))
-        _, ns = R.plain_request(ctx, knobs, w, h, spp, seed, job=plain_jobs[(w, h)])
-        plain_samples += ns
-    t_plain = time.perf_counter() - t_plain
-    for j in plain_jobs.values():
-        j.close()
-    plain_value = plain_samples / t_plain / 1e6
+    plain = plain_prefix(R, ctx, stream, n_plain)
     out = {"metric": f"denoised Msamples/s, served stream ({n_req} requests, Poisson {args.rate:g} req/s, "
-                     f"3 adaptive passes, {args.storage} storage)",
-           "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": n_req, "warmup": args.warmup,
-           "ms_per_step": round(wall_s * 1e3 / n_req, 4), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-           "config": {"workload": f"{n_req} requests, Poisson arrivals at {args.rate:g}/s, sizes from {SIZES}, spp "
-                                  f"from {SPPS}, adaptive_passes 3, adaptive_spp 4, base samples 1; samples of every "
-                                  f"pass generated on the device (seed {SEED})",
-                      "step": "one request", "hbm_budget_gb": args.budget_gb, "max_inflight": args.inflight,
-                      "allocator_blocks": args.alloc_blocks,
-                      "storage": args.storage, "samples": samples, "wall_s": round(wall_s, 4),
-                      "l2": "sample planes of every request larger than L2 except the 256x256 ones",
-                      "parallelism": "replicas"},
-           "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3),
-                          "mean": round(float(lat.mean()), 3), "max": round(float(lat.max()), 3),
-                          "queue_p50": round(float(np.percentile(queue_ms, 50)), 3),
-                          "queue_p99": round(float(np.percentile(queue_ms, 99)), 3)},
-           "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
-                   "d2h_bytes_per_step": int(np.mean([c["width"] * c["height"] * 12 for c in done])),
-                   "form": "submit to denoised image in host memory; the per-sample input is generated on the "
-                           "device from each request's seed, so nothing crosses host->device"},
-           "plain": {"value": round(plain_value, 3), "requests": n_plain, "samples": plain_samples,
-                     "s": round(t_plain, 3),
+                     "3 adaptive passes, fp16 storage) vs the plain per-frame drop-in",
+           "value": round(fp16["value"], 3), "unit": UNIT, "requests": n_req, "samples": fp16["samples"],
+           "wall_s": round(fp16["wall_s"], 4), "latency_ms": fp16["latency_ms"],
+           "p50_ms": fp16["latency_ms"]["p50"], "p99_ms": fp16["latency_ms"]["p99"],
+           "plain": {**{k: (round(v, 3) if isinstance(v, float) else v) for k, v in plain.items()},
                      "form": "render()'s call sequence per request from the host, FP32 planes generated on the "
                              "device, adaptive counts read back, one request after another"},
-           "speedup_vs_plain": round(value / plain_value, 3),
-           "quality": {"requests": [list(r[1:4]) for r in picks], "rel_mse_eps": 1e-2,
-                       "vs_plain_fp32": {"mean": float(np.mean(q_plain)), "max": float(np.max(q_plain))},
-                       "served_vs_converged": float(np.mean(q_served_conv)),
-                       "plain_vs_converged": float(np.mean(q_plain_conv)),
-                       "note": "with adaptive passes the compact storage also moves the adaptive counts a "
-                               "little (the systematic residual sampling follows a running sum), so some "
-                               "pixels draw one sample more or less than in the FP32 run; converged = the "
-                               "plain FP32 method at 1024 spp"},
-           "server": {"bytes_peak": st1["bytes_peak"], "bytes_budget": st1["bytes_budget"],
-                      "jobs_cached": st1["jobs_cached"]},
-           "gpu_launches": int(st1["launches"] - st0["launches"]), "clocks": clocks.summary()}
+           "vs_plain": round(fp16["value"] / plain["value"], 3),
+           "gpu_launches": fp16["launches"], "clocks": fp16["clocks"],
+           "server": {"bytes_peak": fp16["stats"]["bytes_peak"], "bytes_budget": fp16["stats"]["bytes_budget"],
+                      "jobs_cached": fp16["stats"]["jobs_cached"], "hbm_budget_gb": args.budget_gb,
+                      "max_inflight": args.inflight}}
+    if breakdown:
+        no_dead = plain_prefix(R, ctx, stream, n_plain, skip_dead=True)
+        fp32 = served_stream(R, ctx, args, rank, dist, n_req, "fp32")
+        out["breakdown"] = {
+            "plain": round(plain["value"], 3),
+            "plain_without_dead_calls": round(no_dead["value"], 3),
+            "served_fp32": round(fp32["value"], 3),
+            "served_fp16": round(fp16["value"], 3),
+            "dead_call_elimination": round(no_dead["value"] / plain["value"], 3),
+            "overlap_and_continuous_batching": round(fp32["value"] / no_dead["value"], 3),
+            "fp16_storage": round(fp16["value"] / fp32["value"], 3),
+            "served_fp32_latency_ms": fp32["latency_ms"],
+            "note": "the factors multiply to vs_plain; each is the ratio of two measured runs of the same stream "
+                    "(the plain legs on its first requests)"}
+    out["quality"] = served_quality(R, ctx, args, stream, "fp16")
+    return out
+
+
+def run_serving(args):
+    """The serving form alone: the served stream of --steps requests and its comparison with
+    the plain per-frame drop-in (served_summary)."""
+    import rpd_gb300 as R
+
+    world, rank, local, dist = dist_setup()
+    ctx = R.Context(local, 0)
+    out = served_summary(R, ctx, args, rank, dist, args.steps, breakdown=not args.no_breakdown)
+    out.update({"n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "ms_per_step": round(out["wall_s"] * 1e3 / args.steps, 4),
+                "config": {"workload": f"{args.steps} requests, Poisson arrivals at {args.rate:g}/s, sizes from "
+                                       f"{SIZES}, spp from {SPPS}, adaptive_passes 3, adaptive_spp 4, base samples "
+                                       f"1; samples of every pass generated on the device (seed {SEED})",
+                           "step": "one request", "l2": "sample planes of every request larger than L2 except the "
+                                                        "256x256 ones", "parallelism": "replicas"},
+                "e2e": {"value": out["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": int(np.mean([w * h * 12 for (_, w, h, _, _) in
+                                                           request_stream(args.steps, args.rate, SEED + 1000 * rank)])),
+                        "form": "submit to denoised image in host memory; the per-sample input is generated on the "
+                                "device from each request's seed, so nothing crosses host->device"}})
     ctx.close()
     if rank == 0:
         print(json.dumps(out))
@@ -817,7 +906,7 @@ def main():
     ap.add_argument("--grid-shape", type=int, default=0, help="random-dimension grid launch shape 1..6 (0: default)")
     ap.add_argument("--precision", choices=["fp32", "fp16"], default="fp32",
                     help="fp16: the precision form (compact per-sample storage, single-precision accumulation)")
-    ap.add_argument("--form", choices=["plain", "batched", "serving", "request"], default="plain",
+    ap.add_argument("--form", choices=["plain", "batched", "serving", "request", "filters"], default="plain",
                     help="batched: uneven frames in one graph-captured launch (fp16 storage, autotuned shapes); "
                          "serving: a Poisson stream of requests through rpd_server (--steps requests)")
     ap.add_argument("--frames", type=int, default=48, help="frames of the batched form")
@@ -831,6 +920,9 @@ def main():
                     help="serving: blocks of each request's parallel adaptive allocation (0: one per SM)")
     ap.add_argument("--plain-requests", type=int, default=200, help="serving: stream prefix run through the plain drop-in")
     ap.add_argument("--passes", type=int, default=1, help="request: adaptive passes of the profiled request")
+    ap.add_argument("--no-served", action="store_true", help="plain form: leave out the served stream")
+    ap.add_argument("--served-requests", type=int, default=2000, help="plain form: requests of the served stream")
+    ap.add_argument("--no-breakdown", action="store_true", help="serving: leave out the ratio's breakdown runs")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # one replica process per GPU, as the driver launches it: rerun this command under
@@ -842,7 +934,7 @@ def main():
         W, H, SPP = args.width, args.height, args.spp
         METRIC = f"denoised Msamples/s at {W}x{H} {SPP}spp (plain)"
     if args.precision == "fp16":
-        METRIC = METRIC.replace("(plain)", "(fp16 storage)")
+        METRIC = METRIC.replace("(plain)", "(fp16 storage)").replace(", plain vs served", " (fp16 storage), plain")
     if args.impl == "reference":
         run_reference(args)
     elif args.form == "batched":
@@ -851,6 +943,12 @@ def main():
         run_serving(args)
     elif args.form == "request":
         run_request(args)
+    elif args.form == "filters":
+        import rpd_gb300 as R
+
+        ctx = R.Context(0, 0)
+        print(json.dumps(filters_leg(R, ctx, W, H, reps=max(1, args.steps))))
+        ctx.close()
     else:
         run_gpu(args)
 

@@ -445,6 +445,88 @@ int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, con
                         float sigma_p, float sigma_a, float* gaussian, float* bilateral,
                         float* joint, rpd_memory where);
 
+/* ---- the tracer side: streaming per-sample records (main.cpp:649-737, 1451-1538) ---------
+ *
+ * The reference's render loops fold each traced sample into the pixel statistics and a
+ * thread-local RPD grid from an OpenMP row loop (accumulate_sample,
+ * accumulate_rpf_sample_to_grid, main.cpp:701-717 and 1509-1519). An emitter replaces those
+ * calls: the loop's threads write each sample's record into page-locked ring buffers, row by
+ * row, and every band of `band_rows` rows is copied to HBM and accumulated on the GPU as soon as
+ * its rows are done, while tracing continues. Rows must be taken in increasing order across the
+ * threads (as a dynamic schedule over rows hands them out); rows inside the ring's window of
+ * `ring_slots` bands may be done in any order. A pass through an emitter accumulates exactly as
+ * one rpd_job_push_samples of the whole image. */
+typedef struct rpd_emitter rpd_emitter;
+/* A ring of ring_slots (>= 2) bands of band_rows rows, each band holding up to
+ * band_rows * width * max_spp samples (page-locked host and device copies of every plane). */
+int rpd_emitter_create(rpd_job* job, int32_t band_rows, int32_t ring_slots, int32_t max_spp, rpd_emitter** out);
+/* Open a pass: spp samples per pixel, or counts[i] (host memory, W*H) for pixel i, e.g. the
+ * counts of rpd_compute_adaptive_sample_counts (render_image_adaptive). */
+int rpd_emitter_begin_pass(rpd_emitter* em, int32_t spp, const int32_t* counts);
+/* Where row y's samples go: the planes of `planes` point at the row's first sample (every plane
+ * of rpd_sample_soa is present; albedo per sample); pixel x of the row owns the samples
+ * [pixel_offsets[x] - pixel_offsets[0], pixel_offsets[x + 1] - pixel_offsets[0]), in the order
+ * the tracer draws them. Waits (bounded) while the row's ring slot still holds an earlier band. */
+int rpd_emitter_row(rpd_emitter* em, int32_t y, rpd_sample_soa* planes, const int64_t** pixel_offsets);
+/* Row y is written. The band's last row sends the band (and every complete band after it). */
+int rpd_emitter_row_done(rpd_emitter* em, int32_t y);
+/* Every row done: waits for the last copies and closes the pass (rpd_job_end_pass). */
+int rpd_emitter_end_pass(rpd_emitter* em);
+void rpd_emitter_destroy(rpd_emitter* em);
+
+/* ---- evaluation metrics (shared/tools/eval_tools.cpp) --------------------------------- */
+
+/* What `eval_tools hdr-metrics <ref> <test>` reports (eval_tools.cpp:215-286, with
+ * compute_extended_metrics 121-213), for interleaved RGB float images. */
+typedef struct rpd_image_metrics {
+    double mae;                 /* mean |ref - test| over pixels and channels */
+    double rmse;                /* sqrt(mean (ref - test)^2) */
+    double psnr;                /* 20 log10(peak / rmse); +inf when rmse is 0 */
+    double peak;                /* max |ref| (1 when that is 0) */
+    double ssim[3];             /* the global per-channel SSIM diagnostic */
+    double ssim_mean;           /* (ssim[0] + ssim[1] + ssim[2]) / 3 */
+    double nrmse;               /* sqrt(sum (ref - test)^2 / max(1e-18, sum ref^2)) */
+    double log_ssim11;          /* mean SSIM over 11x11 windows (clipped at the edges) of
+                                 * log1p(max(0, luminance)), constants from the reference's peak */
+    double log_gradient_nrmse;  /* NRMSE of the forward x and y differences of that log luminance */
+} rpd_image_metrics;
+/* The metrics of `test` against `reference` (w x h, interleaved RGB floats in `where` memory),
+ * computed on the context's GPU in double precision. Scalars agree with the reference's to
+ * about 1e-12 relative (the sums are taken in another order). */
+int rpd_hdr_metrics(rpd_ctx* ctx, const float* reference, const float* test, int32_t width, int32_t height,
+                    rpd_memory where, rpd_image_metrics* out);
+/* The same for a job's denoised image (RPD_FIELD_DENOISED) against `reference`, on the job's
+ * stream without copying the image out: a caller scores each frame where it was denoised. */
+int rpd_job_hdr_metrics(rpd_job* job, const float* reference, rpd_memory where, rpd_image_metrics* out);
+
+/* ---- output writers (core/buffers.h:197-250, shared/image.h) --------------------------- */
+
+/* Tonemapping presets of Image::ToneMapping (shared/image.h:20), in its order. */
+typedef enum rpd_tonemap {
+    RPD_TONEMAP_AGX = 0,         /* AGXDefault */
+    RPD_TONEMAP_AGX_GOLDEN = 1,
+    RPD_TONEMAP_AGX_PUNCHY = 2,
+    RPD_TONEMAP_ACES = 3
+} rpd_tonemap;
+/* Image::save (a Radiance RGBE .hdr file) and Image::save_with_tonemapping (an 8-bit RGB .png)
+ * of an interleaved RGB float image in `where` memory; the pixel encoding runs on the context's
+ * GPU, the file is written from host memory. RGBE has no sign: negative components are written
+ * as 0. */
+int rpd_write_hdr(rpd_ctx* ctx, const float* rgb, int32_t width, int32_t height, rpd_memory where,
+                  const char* path);
+int rpd_write_png(rpd_ctx* ctx, const float* rgb, int32_t width, int32_t height, rpd_memory where,
+                  int tonemap, const char* path);
+/* output_buffers (core/buffers.h:197-250) for a finalized job (rpd_finalize): the files the
+ * reference writes under `prefix` (its directory + name; file names are prefix + suffix), from
+ * the job's device buffers: prefix.png / prefix.hdr (the denoised image when statmc is set,
+ * else the radiance), and with statmc the raw radiance (_raw.png, _raw.hdr), the expanded
+ * sensitivity maps (_sensitivity.hdr, _sensitivity_pixel.hdr ... _sensitivity_rr.hdr),
+ * _sensitivity_confidence, _sensitivity_gradient, _uncertainty, _alpha, _vardenoised,
+ * _adaptive_importance, _sample_fraction; always _albedo, _normal, _depth; with statmc
+ * _var_total, _var_eff, _var_ratio. The per-sample record carries no world position, so the
+ * reference's _worldpos.hdr has no counterpart here. */
+int rpd_job_write_outputs(rpd_job* job, const char* prefix, int tonemap, int statmc);
+
 /* No counterpart in the reference: the a-trous filter above for callers that may not
  * allocate device memory while they run (all HBM reserved up front, no device-wide
  * synchronisation from cudaFree allowed, or an allocator that forbids library-internal

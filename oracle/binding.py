@@ -68,6 +68,7 @@ def port() -> C.CDLL:
         "orc_atrous_wavelet": (C.c_int, [vp, vp, vp, i32, i32, f32, f32, f32, i32, vp, C.c_int]),
         "orc_joint_bilateral": (C.c_int, [vp, vp, vp, i32, i32, f32, f32, f32, f32, vp, vp, vp, C.c_int]),
         "orc_synth_fill": (i64, [C.POINTER(R.SynthParams), i64, i64, i32, vp, vp, C.POINTER(R.SampleSoA), C.c_int]),
+        "orc_hdr_metrics": (C.c_int, [vp, vp, i32, i32, C.POINTER(R.ImageMetrics)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -133,6 +134,123 @@ def fp64_denoise(cfg: R.Config, samples: "R.HostSamples", spp: int, threads: int
         return out
     finally:
         L.orc_job_destroy(h)
+
+
+def fp64_sequence(cfg: R.Config, pushes, threads: int = 0) -> np.ndarray:
+    """render()'s adaptive sequence without its unread calls, in the double-precision
+    restatement: pushes = [(HostSamples, spp, counts or None), ...], the first the base pass and
+    each later one an adaptive pass's extra samples; recompute_sensitivity and statmc_denoise
+    after the last pass. Returns DENOISED (H, W, 3) as float."""
+    L = port64()
+    h = L.orc_job_create(C.byref(cfg))
+    if not h:
+        raise ValueError("invalid config")
+    n = cfg.image_width * cfg.image_height
+    try:
+        L.orc_set_threads(h, threads)
+        L.orc_job_begin_frame(h)
+        for samples, spp, counts in pushes:
+            soa = samples.soa()
+            c, cp = _counts_ptr(counts)
+            assert L.orc_job_push_samples(h, C.byref(soa), 0, n, spp, cp) == 0
+            L.orc_job_end_pass(h)
+        L.orc_recompute_sensitivity(h)
+        L.orc_statmc_denoise(h)
+        out = np.empty((cfg.image_height, cfg.image_width, 3), dtype=np.float32)
+        assert L.orc64_read(h, R.FIELD["DENOISED"], out.ctypes.data) == 0
+        return out
+    finally:
+        L.orc_job_destroy(h)
+
+
+def port_hdr_metrics(ref: np.ndarray, tst: np.ndarray) -> dict:
+    """The restatement of eval_tools hdr-metrics on two (H, W, 3) float images."""
+    h, w, _ = ref.shape
+    a = np.ascontiguousarray(ref, dtype=np.float32)
+    b = np.ascontiguousarray(tst, dtype=np.float32)
+    m = R.ImageMetrics()
+    assert port().orc_hdr_metrics(a.ctypes.data, b.ctypes.data, w, h, C.byref(m)) == 0
+    return m.as_dict()
+
+
+_ref_eval = None
+
+
+def ref_eval() -> C.CDLL:
+    """The reference's shared/tools/eval_tools.cpp (oracle/_ref/libref_eval.so)."""
+    global _ref_eval
+    if _ref_eval is None:
+        L = C.CDLL(str(HERE / "_ref" / "libref_eval.so"))
+        L.ref_extended_metrics.restype = None
+        L.ref_extended_metrics.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.ref_hdr_metrics_text.restype = C.c_int
+        L.ref_hdr_metrics_text.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_int]
+        _ref_eval = L
+    return _ref_eval
+
+
+def ref_hdr_metrics(ref: np.ndarray, tst: np.ndarray) -> dict:
+    """The reference's own metrics: compute_extended_metrics called directly (full double
+    precision) and the printed report of `eval_tools hdr-metrics` parsed (MAE, RMSE, peak and
+    PSNR to 12 and 6 significant digits, SSIM to 4 decimals)."""
+    import re
+
+    h, w, _ = ref.shape
+    a = np.ascontiguousarray(ref, dtype=np.float32)
+    b = np.ascontiguousarray(tst, dtype=np.float32)
+    ext = np.zeros(3)
+    L = ref_eval()
+    L.ref_extended_metrics(a.ctypes.data, b.ctypes.data, w, h, ext.ctypes.data)
+    buf = C.create_string_buffer(4096)
+    assert L.ref_hdr_metrics_text(a.ctypes.data, b.ctypes.data, w, h, buf, 4096) == 0
+    text = buf.value.decode()
+    num = r"([-+0-9.eEinfa]+)"
+    m = re.search(rf"MAE: {num}\s+RMSE: {num}\s+PSNR \(reference peak={num}\): {num} dB", text)
+    s = re.search(rf"R={num} G={num} B={num}\s+mean={num}", text)
+    return {"nrmse": ext[0], "log_ssim11": ext[1], "log_gradient_nrmse": ext[2],
+            "mae": float(m.group(1)), "rmse": float(m.group(2)), "peak": float(m.group(3)), "psnr": float(m.group(4)),
+            "ssim": [float(s.group(k)) for k in (1, 2, 3)], "ssim_mean": float(s.group(4)), "text": text}
+
+
+def ref_outputs(prefix: str, tonemap: int, swap: bool = True) -> dict:
+    """output_buffers of the reference's current frame (after ref_finalize): {file name: HDR
+    floats (h, w, 3) or PNG bytes (h, w, 3) uint8}."""
+    L = ref()
+    L.ref_output_buffers.restype = C.c_int
+    L.ref_output_buffers.argtypes = [C.c_char_p, C.c_int, C.c_int]
+    L.ref_output_names.restype = C.c_int
+    L.ref_output_names.argtypes = [C.c_char_p, C.c_size_t]
+    L.ref_output_image.restype = C.c_int
+    L.ref_output_image.argtypes = [C.c_char_p, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    assert L.ref_output_buffers(prefix.encode(), tonemap, 1 if swap else 0) == 0
+    buf = C.create_string_buffer(1 << 16)
+    assert L.ref_output_names(buf, 1 << 16) >= 0
+    out = {}
+    for name in buf.value.decode().split("\n"):
+        if not name:
+            continue
+        png = name.startswith("png:")
+        key = name[4:] if png else name
+        w, h, comp = C.c_int32(), C.c_int32(), C.c_int32()
+        data = np.empty(1 << 24, dtype=np.uint8)
+        assert L.ref_output_image(key.encode(), 1 if png else 0, data.ctypes.data, data.nbytes, C.byref(w), C.byref(h),
+                                  C.byref(comp)) == 0
+        n = w.value * h.value * comp.value
+        arr = data[:n].copy() if png else data[:4 * n].view(np.float32).copy()
+        out[key] = arr.reshape(h.value, w.value, comp.value)
+    return out
+
+
+def ref_tonemap(rgb: np.ndarray, tonemap: int) -> np.ndarray:
+    """Image::save_with_tonemapping's bytes for (n, 3) float values."""
+    L = ref()
+    L.ref_tonemap.restype = C.c_int
+    L.ref_tonemap.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    a = np.ascontiguousarray(rgb, dtype=np.float32)
+    out = np.empty(a.shape, dtype=np.uint8)
+    assert L.ref_tonemap(a.ctypes.data, len(a), tonemap, out.ctypes.data) == 0
+    return out
 
 
 def have_ref() -> bool:

@@ -560,4 +560,56 @@ int ref_render_cornell(const char* yaml_path, const rpd_config* c, int32_t spp, 
     return 0;
 }
 
+// render()'s last step (main.cpp:1557-1559: the finalized radiance becomes raw_radiance, the
+// denoised image the radiance; with `swap`) and output_buffers (core/buffers.h:197-250) with
+// this prefix and tonemapping preset: every image the reference writes is captured by the stb
+// shim.
+int ref_output_buffers(const char* prefix, int tonemap, int swap) {
+    stb_shim::table().clear();
+    stb_shim::png_table().clear();
+    if (swap) {
+        buffers.raw_radiance = buffers.radiance;
+        buffers.radiance = buffers.denoised;
+    }
+    return output_buffers(buffers, prefix, static_cast<Image::ToneMapping>(tonemap), true) ? 0 : 1;
+}
+
+// Image::save_with_tonemapping (shared/image.h:129-139) of n RGB values as one row; out gets
+// the 3 n bytes it writes.
+int ref_tonemap(const float* rgb, int n, int tonemap, unsigned char* out) {
+    Image img(n, 1);
+    for (int i = 0; i < n; ++i) img[i] = Vec3f(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+    stb_shim::png_table().clear();
+    if (!img.save_with_tonemapping("tonemap.png", static_cast<Image::ToneMapping>(tonemap))) return 1;
+    const auto& png = stb_shim::png_table()["tonemap.png"];
+    std::memcpy(out, png.data.data(), png.data.size());
+    return 0;
+}
+
+// Names of the captured images, '\n'-separated: HDR writes first, then "png:" + each PNG write.
+int ref_output_names(char* buf, size_t cap) {
+    std::string all;
+    for (const auto& kv : stb_shim::table()) all += kv.first + "\n";
+    for (const auto& kv : stb_shim::png_table()) all += "png:" + kv.first + "\n";
+    if (all.size() + 1 > cap) return -1;
+    std::memcpy(buf, all.c_str(), all.size() + 1);
+    return int(all.size());
+}
+
+// One captured image: HDR floats (comp per pixel) or PNG bytes; w, h, comp out.
+int ref_output_image(const char* name, int png, void* dst, size_t cap, int32_t* w, int32_t* h, int32_t* comp) {
+    if (png) {
+        auto it = stb_shim::png_table().find(name);
+        if (it == stb_shim::png_table().end() || it->second.data.size() > cap) return 1;
+        std::memcpy(dst, it->second.data.data(), it->second.data.size());
+        *w = it->second.w, *h = it->second.h, *comp = it->second.comp;
+        return 0;
+    }
+    auto it = stb_shim::table().find(name);
+    if (it == stb_shim::table().end() || it->second.data.size() * sizeof(float) > cap) return 1;
+    std::memcpy(dst, it->second.data.data(), it->second.data.size() * sizeof(float));
+    *w = it->second.w, *h = it->second.h, *comp = it->second.comp;
+    return 0;
+}
+
 }  // extern "C"

@@ -40,3 +40,11 @@ inline float* stbi_loadf(const char* name, int* w, int* h, int* comp, int) {
     return out;
 }
 inline void stbi_image_free(void* p) { std::free(p); }
+// 8-bit loads (the evaluation tool's PNG comparison): the table holds float images only, so
+// every 8-bit load fails as for a missing file.
+inline unsigned char* stbi_load(const char*, int* w, int* h, int* comp, int) {
+    if (w) *w = 0;
+    if (h) *h = 0;
+    if (comp) *comp = 0;
+    return nullptr;
+}

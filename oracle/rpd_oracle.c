@@ -1594,4 +1594,155 @@ int orc_joint_bilateral(const float* raw, const float* normal, const float* albe
     }
     return RPD_OK;
 }
+
+/* compute_extended_metrics (shared/tools/eval_tools.cpp:121-213): NRMSE, the 11x11 box-window
+ * SSIM of log1p luminance from integral images, and the NRMSE of its forward differences, in
+ * double precision and the reference's order. */
+static double orc_box_sum(const double* s, int stride, int x0, int y0, int x1, int y1) {
+    return s[y1 * stride + x1] - s[y0 * stride + x1] - s[y1 * stride + x0] + s[y0 * stride + x0];
+}
+
+static double orc_maxd(double a, double b) { return (a < b) ? b : a; }
+
+static void orc_extended_metrics(const float* ref, const float* tst, int w, int h, rpd_image_metrics* m) {
+    const int pixels = w * h;
+    double* ref_log = (double*)malloc(sizeof(double) * (size_t)pixels);
+    double* tst_log = (double*)malloc(sizeof(double) * (size_t)pixels);
+    double ref_energy = 0.0, error_energy = 0.0, log_peak = 0.0;
+    static const double weights[3] = {0.2126, 0.7152, 0.0722};
+    for (int i = 0; i < pixels; ++i) {
+        double ref_lum = 0.0, tst_lum = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            const double a = ref[3 * i + c];
+            const double b = tst[3 * i + c];
+            ref_energy += a * a;
+            error_energy += (a - b) * (a - b);
+            ref_lum += weights[c] * a;
+            tst_lum += weights[c] * b;
+        }
+        ref_log[i] = log1p(orc_maxd(0.0, ref_lum));
+        tst_log[i] = log1p(orc_maxd(0.0, tst_lum));
+        log_peak = orc_maxd(log_peak, ref_log[i]);
+    }
+    m->nrmse = sqrt(error_energy / orc_maxd(1e-18, ref_energy));
+
+    const int stride = w + 1;
+    const size_t isz = (size_t)stride * (size_t)(h + 1);
+    double* sr = (double*)calloc(isz, sizeof(double));
+    double* st = (double*)calloc(isz, sizeof(double));
+    double* sr2 = (double*)calloc(isz, sizeof(double));
+    double* st2 = (double*)calloc(isz, sizeof(double));
+    double* sx = (double*)calloc(isz, sizeof(double));
+    for (int y = 0; y < h; ++y) {
+        double row_ref = 0.0, row_tst = 0.0, row_ref2 = 0.0, row_tst2 = 0.0, row_cross = 0.0;
+        for (int x = 0; x < w; ++x) {
+            const double a = ref_log[y * w + x];
+            const double b = tst_log[y * w + x];
+            row_ref += a;
+            row_tst += b;
+            row_ref2 += a * a;
+            row_tst2 += b * b;
+            row_cross += a * b;
+            const int out = (y + 1) * stride + x + 1;
+            sr[out] = sr[out - stride] + row_ref;
+            st[out] = st[out - stride] + row_tst;
+            sr2[out] = sr2[out - stride] + row_ref2;
+            st2[out] = st2[out - stride] + row_tst2;
+            sx[out] = sx[out - stride] + row_cross;
+        }
+    }
+    log_peak = orc_maxd(1e-6, log_peak);
+    const double c1 = pow(0.01 * log_peak, 2.0);
+    const double c2 = pow(0.03 * log_peak, 2.0);
+    double ssim_sum = 0.0;
+    for (int y = 0; y < h; ++y) {
+        const int y0 = y - 5 > 0 ? y - 5 : 0;
+        const int y1 = y + 6 < h ? y + 6 : h;
+        for (int x = 0; x < w; ++x) {
+            const int x0 = x - 5 > 0 ? x - 5 : 0;
+            const int x1 = x + 6 < w ? x + 6 : w;
+            const double n = (double)((x1 - x0) * (y1 - y0));
+            const double mean_ref = orc_box_sum(sr, stride, x0, y0, x1, y1) / n;
+            const double mean_tst = orc_box_sum(st, stride, x0, y0, x1, y1) / n;
+            const double var_ref = orc_maxd(0.0, orc_box_sum(sr2, stride, x0, y0, x1, y1) / n - mean_ref * mean_ref);
+            const double var_tst = orc_maxd(0.0, orc_box_sum(st2, stride, x0, y0, x1, y1) / n - mean_tst * mean_tst);
+            const double cov = orc_box_sum(sx, stride, x0, y0, x1, y1) / n - mean_ref * mean_tst;
+            const double num = (2.0 * mean_ref * mean_tst + c1) * (2.0 * cov + c2);
+            const double den = (mean_ref * mean_ref + mean_tst * mean_tst + c1) * (var_ref + var_tst + c2);
+            ssim_sum += (den > 0.0) ? num / den : 1.0;
+        }
+    }
+    m->log_ssim11 = ssim_sum / (double)pixels;
+
+    double gerr = 0.0, gref = 0.0;
+    for (int y = 0; y < h - 1; ++y) {
+        for (int x = 0; x < w - 1; ++x) {
+            const int i = y * w + x;
+            const double rdx = ref_log[i + 1] - ref_log[i];
+            const double rdy = ref_log[i + w] - ref_log[i];
+            const double tdx = tst_log[i + 1] - tst_log[i];
+            const double tdy = tst_log[i + w] - tst_log[i];
+            gerr += (rdx - tdx) * (rdx - tdx) + (rdy - tdy) * (rdy - tdy);
+            gref += rdx * rdx + rdy * rdy;
+        }
+    }
+    m->log_gradient_nrmse = sqrt(gerr / orc_maxd(1e-18, gref));
+    free(ref_log);
+    free(tst_log);
+    free(sr);
+    free(st);
+    free(sr2);
+    free(st2);
+    free(sx);
+}
+
+/* hdr_metrics (shared/tools/eval_tools.cpp:232-286) without the file I/O and the residual image. */
+int orc_hdr_metrics(const float* ref, const float* tst, int32_t w, int32_t h, rpd_image_metrics* out) {
+    if (!ref || !tst || !out || w <= 0 || h <= 0) return RPD_ERR_INVALID_ARGUMENT;
+    const int pixels = w * h;
+    double sum_sq = 0.0, sum_abs = 0.0, peak = 0.0;
+    double mean_ref[3] = {0.0, 0.0, 0.0}, mean_tst[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < pixels; ++i) {
+        for (int c = 0; c < 3; ++c) {
+            const double a = ref[3 * i + c];
+            const double b = tst[3 * i + c];
+            sum_sq += (a - b) * (a - b);
+            sum_abs += fabs(a - b);
+            peak = orc_maxd(peak, fabs(a));
+            mean_ref[c] += a;
+            mean_tst[c] += b;
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        mean_ref[c] /= pixels;
+        mean_tst[c] /= pixels;
+    }
+    if (peak <= 0.0) peak = 1.0;
+    const double C1 = (0.01 * peak) * (0.01 * peak);
+    const double C2 = (0.03 * peak) * (0.03 * peak);
+    for (int c = 0; c < 3; ++c) {
+        double var_ref = 0.0, var_tst = 0.0, cov = 0.0;
+        for (int i = 0; i < pixels; ++i) {
+            const double a = ref[3 * i + c];
+            const double b = tst[3 * i + c];
+            var_ref += (a - mean_ref[c]) * (a - mean_ref[c]);
+            var_tst += (b - mean_tst[c]) * (b - mean_tst[c]);
+            cov += (a - mean_ref[c]) * (b - mean_tst[c]);
+        }
+        var_ref /= pixels;
+        var_tst /= pixels;
+        cov /= pixels;
+        const double num = (2.0 * mean_ref[c] * mean_tst[c] + C1) * (2.0 * cov + C2);
+        const double den = (mean_ref[c] * mean_ref[c] + mean_tst[c] * mean_tst[c] + C1) * (var_ref + var_tst + C2);
+        out->ssim[c] = (den > 0.0) ? num / den : 0.0;
+    }
+    const double mse = sum_sq / (pixels * 3);
+    out->mae = sum_abs / (pixels * 3);
+    out->rmse = sqrt(mse);
+    out->peak = peak;
+    out->psnr = (out->rmse > 0.0) ? 20.0 * log10(peak / out->rmse) : INFINITY;
+    out->ssim_mean = (out->ssim[0] + out->ssim[1] + out->ssim[2]) / 3.0;
+    orc_extended_metrics(ref, tst, w, h, out);
+    return RPD_OK;
+}
 #endif /* ORC_F64 */

@@ -65,6 +65,10 @@ int orc_joint_bilateral(const float* raw, const float* normal, const float* albe
                         float sigma_c, float sigma_n, float sigma_p, float sigma_a,
                         float* gaussian, float* bilateral, float* joint, int threads);
 
+/* eval_tools hdr-metrics (shared/tools/eval_tools.cpp:121-213, 232-286) on interleaved RGB
+ * float images, single-threaded in the reference's order. */
+int orc_hdr_metrics(const float* ref, const float* tst, int32_t w, int32_t h, rpd_image_metrics* out);
+
 /* Synthetic samples (include/rpd_synth.h) for pixels [first, first+count): pixel i gets
  * counts[i] (or spp) samples with ordinals start_n[i] (or 0) onward, written to the
  * planes of `out` (which must all be non-NULL except albedo, env_u; pixel_albedo gets the

@@ -82,8 +82,10 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5]
     for (int c = 0; c < 3; ++c) L.add(p.sqrt_var_stable[c], np);
     L.add(p.win, 6 * np);
     L.add(p.variance_denoised, np);
-    L.add(p.var_ping, np);
-    L.add(p.var_pong, np);
+    // variance_denoise's ping-pong planes: rows padded to a multiple of 4 floats (16 bytes)
+    L.add(p.var_ping, int64_t((g.w + 3) & ~3) * g.h);
+    L.add(p.var_pong, int64_t((g.w + 3) & ~3) * g.h);
+    L.add(p.var_gate, np);
     L.add(p.var_mask, np);
     L.add(p.importance, np);
     L.add(p.importance_tmp, np);
@@ -149,6 +151,7 @@ void rebase_all(PixelPlanes& p, NodePlanes& n, char* base) {
     rebase(p.var_ratio, base);
     rebase(p.variance_denoised, base);
     rebase(p.var_ping, base);
+    rebase(p.var_gate, base);
     rebase(p.var_pong, base);
     rebase(p.var_mask, base);
     rebase(p.importance, base);
@@ -1574,6 +1577,180 @@ int rpd_joint_bilateral(rpd_ctx* ctx, const float* raw, const float* normal, con
     RPD_CUDA(cudaFreeAsync(scratch, st));
     RPD_CUDA(cudaStreamSynchronize(st));
     if (timeouts) return fail(RPD_ERR_TIMEOUT, "a joint-bilateral tile copy did not complete in time");
+    return RPD_OK;
+}
+
+namespace {
+
+// Metrics of `tst` against `ref` on `stream`: scratch from the stream-ordered pool, the result
+// copied to host memory after the stream drains.
+int run_metrics(const rpd::Img3& ref, const rpd::Img3& tst, int w, int h, cudaStream_t st, rpd_image_metrics* out) {
+    void* scratch = nullptr;
+    rpd_image_metrics* d_out = nullptr;
+    RPD_CUDA(cudaMallocAsync(&scratch, metrics_scratch_bytes(w, h), st));
+    RPD_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_out), sizeof(rpd_image_metrics), st));
+    RPD_CUDA(launch_metrics(ref, tst, w, h, scratch, d_out, st));
+    RPD_CUDA(cudaMemcpyAsync(out, d_out, sizeof(rpd_image_metrics), cudaMemcpyDeviceToHost, st));
+    RPD_CUDA(cudaFreeAsync(scratch, st));
+    RPD_CUDA(cudaFreeAsync(d_out, st));
+    RPD_CUDA(cudaStreamSynchronize(st));
+    return RPD_OK;
+}
+
+rpd::Img3 interleaved(const float* base) { return rpd::Img3{{base, base + 1, base + 2}, 3}; }
+
+}  // namespace
+
+int rpd_hdr_metrics(rpd_ctx* ctx, const float* reference, const float* test, int32_t w, int32_t h, rpd_memory where,
+                    rpd_image_metrics* out) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !reference || !test || !out || w <= 0 || h <= 0)
+        return fail(RPD_ERR_INVALID_ARGUMENT, "bad metrics arguments");
+    RPD_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->util_stream;
+    const uint64_t bytes = uint64_t(w) * h * 12;
+    float* d[2] = {nullptr, nullptr};
+    const float* in[2] = {reference, test};
+    if (where == RPD_MEM_HOST) {
+        for (int k = 0; k < 2; ++k) {
+            RPD_CUDA(cudaMallocAsync(&d[k], bytes, st));
+            RPD_CUDA(cudaMemcpyAsync(d[k], in[k], bytes, cudaMemcpyHostToDevice, st));
+            in[k] = d[k];
+        }
+    }
+    const int r = run_metrics(interleaved(in[0]), interleaved(in[1]), w, h, st, out);
+    for (float* p : d)
+        if (p) cudaFreeAsync(p, st);
+    if (r == RPD_OK) RPD_CUDA(cudaStreamSynchronize(st));
+    return r;
+}
+
+int rpd_job_hdr_metrics(rpd_job* job, const float* reference, rpd_memory where, rpd_image_metrics* out) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!reference || !out) return fail(RPD_ERR_INVALID_ARGUMENT, "bad metrics arguments");
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    const uint64_t bytes = uint64_t(j->g.np) * 12;
+    const float* ref = reference;
+    float* d_ref = nullptr;
+    if (where == RPD_MEM_HOST) {
+        RPD_CUDA(cudaMallocAsync(&d_ref, bytes, j->stream));
+        RPD_CUDA(cudaMemcpyAsync(d_ref, reference, bytes, cudaMemcpyHostToDevice, j->stream));
+        ref = d_ref;
+    }
+    const rpd::Img3 den{{j->p.denoised[0], j->p.denoised[1], j->p.denoised[2]}, 1};
+    const int r = run_metrics(interleaved(ref), den, j->g.w, j->g.h, j->stream, out);
+    if (d_ref) cudaFreeAsync(d_ref, j->stream);
+    if (r == RPD_OK) RPD_CUDA(cudaStreamSynchronize(j->stream));
+    return r;
+}
+
+namespace {
+
+// Device and page-locked scratch for writing w x h images, released by the destructor.
+struct WriteScratch {
+    uint8_t* dev = nullptr;
+    uint8_t* host = nullptr;
+    float* plane = nullptr;
+    int* dmax = nullptr;
+    ~WriteScratch() {
+        if (dev) cudaFree(dev);
+        if (host) cudaFreeHost(host);
+        if (plane) cudaFree(plane);
+        if (dmax) cudaFree(dmax);
+    }
+    int init(int64_t np, bool with_plane) {
+        RPD_CUDA(cudaMalloc(&dev, size_t(np) * 4));
+        RPD_CUDA(cudaMallocHost(&host, size_t(np) * 4));
+        if (with_plane) {
+            RPD_CUDA(cudaMalloc(&plane, size_t(np) * sizeof(float)));
+            RPD_CUDA(cudaMalloc(&dmax, sizeof(int)));
+        }
+        return RPD_OK;
+    }
+};
+
+int write_rgb(rpd_ctx* ctx, const float* rgb, int32_t w, int32_t h, rpd_memory where, int tonemap, const char* path) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !rgb || !path || w <= 0 || h <= 0) return fail(RPD_ERR_INVALID_ARGUMENT, "bad image arguments");
+    if (tonemap > RPD_TONEMAP_ACES) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tonemapping preset");
+    RPD_CUDA(cudaSetDevice(c->device));
+    const int64_t np = int64_t(w) * h;
+    WriteScratch ws;
+    int st = ws.init(np, false);
+    if (st != RPD_OK) return st;
+    float* d_rgb = nullptr;
+    const float* src = rgb;
+    if (where == RPD_MEM_HOST) {
+        RPD_CUDA(cudaMalloc(&d_rgb, size_t(np) * 12));
+        RPD_CUDA(cudaMemcpyAsync(d_rgb, rgb, size_t(np) * 12, cudaMemcpyHostToDevice, c->util_stream));
+        src = d_rgb;
+    }
+    st = write_image(rpd::Img3{{src, src + 1, src + 2}, 3}, w, h, tonemap, path, ws.dev, ws.host, c->util_stream);
+    if (d_rgb) cudaFree(d_rgb);
+    return st;
+}
+
+}  // namespace
+
+int rpd_write_hdr(rpd_ctx* ctx, const float* rgb, int32_t w, int32_t h, rpd_memory where, const char* path) {
+    return write_rgb(ctx, rgb, w, h, where, -1, path);
+}
+
+int rpd_write_png(rpd_ctx* ctx, const float* rgb, int32_t w, int32_t h, rpd_memory where, int tonemap, const char* path) {
+    if (tonemap < 0) return fail(RPD_ERR_INVALID_ARGUMENT, "unknown tonemapping preset");
+    return write_rgb(ctx, rgb, w, h, where, tonemap, path);
+}
+
+int rpd_job_write_outputs(rpd_job* job, const char* prefix, int tonemap, int statmc) {
+    Job* j = reinterpret_cast<Job*>(job);
+    CHECK_JOB(j);
+    if (!prefix || tonemap < 0 || tonemap > RPD_TONEMAP_ACES) return fail(RPD_ERR_INVALID_ARGUMENT, "bad output arguments");
+    RPD_CUDA(cudaSetDevice(j->ctx->device));
+    const int w = j->g.w, h = j->g.h;
+    const int64_t np = j->g.np;
+    WriteScratch ws;
+    int st = ws.init(np, true);
+    if (st != RPD_OK) return st;
+    const std::string base(prefix);
+    auto rgb = [](float* const* p) { return rpd::Img3{{p[0], p[1], p[2]}, 1}; };
+    auto grey = [](const float* p) { return rpd::Img3{{p, p, p}, 1}; };
+    auto put = [&](const rpd::Img3& img, const char* suffix, int tm) {
+        return write_image(img, w, h, tm, base + suffix, ws.dev, ws.host, j->stream);
+    };
+    // buffers.radiance after render(): the denoised image with StatMC, else the finalized radiance
+    const rpd::Img3 main = statmc ? rgb(j->p.denoised) : rgb(j->p.radiance);
+    if ((st = put(main, ".png", tonemap)) != RPD_OK) return st;
+    if ((st = put(main, ".hdr", -1)) != RPD_OK) return st;
+    if (statmc) {
+        if ((st = put(rgb(j->p.radiance), "_raw.png", tonemap)) != RPD_OK) return st;
+        if ((st = put(rgb(j->p.radiance), "_raw.hdr", -1)) != RPD_OK) return st;
+        static const int fields[9] = {N_ALL, N_PIXEL, N_BRDF, N_LENS, N_LIGHT, N_LIGHT_UV, N_LIGHT_SELECT, N_ENV, N_RR};
+        static const char* names[9] = {"_sensitivity.hdr", "_sensitivity_pixel.hdr", "_sensitivity_brdf.hdr",
+                                       "_sensitivity_lens.hdr", "_sensitivity_light.hdr", "_sensitivity_light_uv.hdr",
+                                       "_sensitivity_light_select.hdr", "_sensitivity_environment.hdr",
+                                       "_sensitivity_rr.hdr"};
+        for (int k = 0; k < 9; ++k) {
+            RPD_CUDA(launch_expand(*j, j->n.field[fields[k]], ws.plane));
+            if ((st = put(grey(ws.plane), names[k], -1)) != RPD_OK) return st;
+        }
+        const std::pair<const float*, const char*> planes[] = {
+            {j->p.sens_confidence, "_sensitivity_confidence.hdr"}, {j->p.sens_gradient, "_sensitivity_gradient.hdr"},
+            {j->p.uncertainty, "_uncertainty.hdr"}, {j->p.alpha, "_alpha.hdr"},
+            {j->p.variance_denoised, "_vardenoised.hdr"}, {j->p.importance, "_adaptive_importance.hdr"}};
+        for (const auto& pl : planes)
+            if ((st = put(grey(pl.first), pl.second, -1)) != RPD_OK) return st;
+        RPD_CUDA(launch_count_fraction(j->p.sample_count, np, ws.dmax, ws.plane, j->stream));
+        if ((st = put(grey(ws.plane), "_sample_fraction.hdr", -1)) != RPD_OK) return st;
+    }
+    if ((st = put(rgb(j->p.albedo), "_albedo.hdr", -1)) != RPD_OK) return st;
+    if ((st = put(rgb(j->p.normal), "_normal.hdr", -1)) != RPD_OK) return st;
+    if ((st = put(grey(j->p.depth), "_depth.hdr", -1)) != RPD_OK) return st;
+    if (statmc) {
+        if ((st = put(grey(j->p.var_total), "_var_total.hdr", -1)) != RPD_OK) return st;
+        if ((st = put(grey(j->p.var_eff), "_var_eff.hdr", -1)) != RPD_OK) return st;
+        if ((st = put(grey(j->p.var_ratio), "_var_ratio.hdr", -1)) != RPD_OK) return st;
+    }
     return RPD_OK;
 }
 

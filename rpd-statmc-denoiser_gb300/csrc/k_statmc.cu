@@ -29,8 +29,10 @@
 //                          (2^-15 relative by default) of a decision point — q = 25 (reject),
 //                          q = 2 ln 20 (the accepted-neighbour count), the df of the t-table /
 //                          normal-quantile switch, or the 1e-8 df-denominator test — the
-//                          pixel is recomputed wholly in double exactly as the reference
-//                          computes it (rare: no pixel of the 1080p benchmark frame needs it);
+//                          pixel's window is evaluated again with that neighbour's q recomputed
+//                          in double exactly as the reference computes it (out of line: rare on
+//                          uniform sample counts, a few per cent of pixels where adaptive passes
+//                          mix the counts so that df crosses the t-table switch);
 //                        * each block picks a specialised loop from the range of 1/(n-1) over
 //                          its halo: when every pair's df lies below the t-table switch
 //                          (df <= (n_i - 1) + (n_j - 1)) no neighbour needs the switch test, and
@@ -460,7 +462,7 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
     const bool center = dx == 0 && dy == 0;
     exact |= fabsf(q - 25.0f) <= 25.0f * prm.band;
     exact |= !center && fabsf(q - kQAccept) <= kQAccept * prm.band;
-    // a decision inside a guard band sends the whole pixel to the double-precision path
+    // a decision inside a guard band sends the pixel's window to recheck_window
     rechecks += exact ? 1 : 0;
     if (q > 25.0f) return;
     if (!center && q < kQAccept) ++accepted;
@@ -497,6 +499,143 @@ __device__ __forceinline__ void window_rows(const float4* __restrict__ T, int tn
 #pragma unroll
         for (int k = 0; k < 6; ++k) acc[k] += row[k];
     }
+}
+
+// The blend of a pixel from its window's sums (main.cpp:1099-1126) in single precision.
+__device__ __forceinline__ void write_blend(const PixelPlanes& p, int64_t idx, float4 cmi, const float acc[6],
+                                            int accepted) {
+    const float weight_sum = acc[3];
+    const float var_mean_i = cmi.w;
+    float mean_nb[3] = {cmi.x, cmi.y, cmi.z};
+    float var_neighbors = var_mean_i;
+    if (weight_sum > 1e-8f) {
+        const float inv = 1.0f / weight_sum;
+        mean_nb[0] = acc[0] * inv;
+        mean_nb[1] = acc[1] * inv;
+        mean_nb[2] = acc[2] * inv;
+        var_neighbors = acc[5] * inv * inv;
+    }
+    const float effective = weight_sum * weight_sum / fmaxf(1e-8f, acc[4]);
+    const float blend =
+        (accepted >= 2 && weight_sum >= 1.1f) ? fminf(fmaxf(1.0f - rsqrtf(effective), 0.0f), 0.8f) : 0.0f;
+    const float alpha = 1.0f - blend;
+    p.denoised[0][idx] = lerpf(cmi.x, mean_nb[0], blend);
+    p.denoised[1][idx] = lerpf(cmi.y, mean_nb[1], blend);
+    p.denoised[2][idx] = lerpf(cmi.z, mean_nb[2], blend);
+    const float uncertainty = alpha * alpha * var_mean_i + blend * blend * var_neighbors +
+                              2.0f * alpha * blend * (1.0f / fmaxf(weight_sum, 1e-8f)) * var_mean_i;
+    p.alpha[idx] = alpha;
+    p.uncertainty[idx] = uncertainty;
+}
+
+struct WindowSums {
+    float acc[6];  // colour rgb, weight, weight^2, weight^2 * var of the mean
+    int accepted;
+};
+
+// A pixel's window again, for a pixel with a decision inside a guard band: every neighbour in
+// single precision as the fast loop evaluates it, except that a neighbour whose q (or df) lies
+// in a band has its q recomputed in double exactly as the reference computes it
+// (main.cpp:1055-1097) and its rejection, weight and acceptance taken from that. Out of line
+// and rare, so the fast loop keeps its registers.
+__device__ __noinline__ WindowSums recheck_window(const float4* T, int tn, int tw, int r, int ei,
+                                                  const float* spatial, const float2* line, StatmcParams prm,
+                                                  const int32_t* __restrict__ n, int x, int y) {
+    WindowSums out{{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, 0};
+    const int side = 2 * r + 1;
+    const float4 gi = T[W_GATE * tn + ei], ai = T[W_ALB * tn + ei], si = T[W_SM * tn + ei];
+    const float4 vi = T[W_SV * tn + ei], ri = T[W_RPD * tn + ei];
+    float dm = fabsf(gi.w);
+    if (dm < 1e-8f) dm = 1e-8f;
+    const float smi[3] = {si.x, si.y, si.z}, svi[3] = {vi.x, vi.y, vi.z};
+    const float vi0 = vi.x * vi.x * ai.w, vi1 = vi.y * vi.y * ai.w, vi2 = vi.z * vi.z * ai.w;
+    const int n_i = imaxs(1, n[int64_t(y) * prm.w + x]);
+    for (int dy = -r; dy <= r; ++dy) {
+        for (int dx = -r; dx <= r; ++dx) {
+            const int e = ei + dy * tw + dx;
+            const float4 G = T[W_GATE * tn + e];
+            if (dot3(gi.x, gi.y, gi.z, G.x, G.y, G.z) < prm.normal_threshold) continue;
+            const float4 A = T[W_ALB * tn + e];
+            if (!(A.w > 0.0f)) continue;
+            {
+                float m = dm;
+                const float dj = fabsf(G.w);
+                if (m < dj) m = dj;
+                const float num = fabsf(gi.w - G.w);
+                const float tm = prm.depth_threshold * m;
+                const float dl = num - tm;
+                bool far;
+                if (fabsf(dl) <= tm * kDepthBand || !(tm >= 1e-30f)) far = __fdiv_rn(num, m) > prm.depth_threshold;
+                else far = dl > 0.0f;
+                if (far) continue;
+            }
+            const float da0 = ai.x - A.x, da1 = ai.y - A.y, da2 = ai.z - A.z;
+            if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) continue;
+            const float4 S = T[W_SM * tn + e], V = T[W_SV * tn + e], RJ = T[W_RPD * tn + e];
+            const float vs[3] = {vi.x + V.x, vi.y + V.y, vi.z + V.z};
+            const float md[3] = {si.x - S.x, si.y - S.y, si.z - S.z};
+            const float den[3] = {__fmaf_rn(V.x * V.x, A.w, vi0), __fmaf_rn(V.y * V.y, A.w, vi1),
+                                  __fmaf_rn(V.z * V.z, A.w, vi2)};
+            bool exact = fminf(fminf(den[0], den[1]), den[2]) <= 1e-8f * (1.0f + prm.band);
+            float qmax = 0.0f;
+            for (int c = 0; c < 3; ++c) {
+                const float df = __fdividef(vs[c] * vs[c], den[c]);
+                exact |= fabsf(df - prm.df_break) <= prm.df_break * prm.band;
+                const float t = t_crit<0>(df, line, prm);
+                qmax = fmaxf(qmax, __fdividef(md[c] * md[c], vs[c] * (t * t)));
+            }
+            float shared = fmaxf(fmaxf(fminf(ri.x, RJ.x), fminf(ri.y, RJ.y)), fmaxf(fminf(ri.z, RJ.z), fminf(ri.w, RJ.w)));
+            shared = __saturatef(fmaxf(shared, fmaxf(fminf(si.w, S.w), fminf(vi.w, V.w))));
+            const float adjustment = __saturatef(prm.rpd_scale * shared);
+            const float q = __fdividef(qmax, 1.0f + adjustment);
+            const bool center = dx == 0 && dy == 0;
+            exact |= fabsf(q - 25.0f) <= 25.0f * prm.band;
+            exact |= !center && fabsf(q - kQAccept) <= kQAccept * prm.band;
+            float wj;
+            if (exact) {
+                const float smj[3] = {S.x, S.y, S.z}, svj[3] = {V.x, V.y, V.z};
+                const int n_j = imaxs(1, n[int64_t(y + dy) * prm.w + (x + dx)]);
+                const double qx = exact_q(svi, smi, n_i, svj, smj, n_j, prm.alpha, adjustment);
+                if (qx > 25.0) continue;
+                const double sw = 1.0 / (1.0 + double(dx * dx + dy * dy));
+                const double wd = sw * exp(-0.5 * qx);
+                if (!center && wd > 0.05 * sw) ++out.accepted;
+                wj = float(wd);
+            } else {
+                if (q > 25.0f) continue;
+                if (!center && q < kQAccept) ++out.accepted;
+                wj = spatial[(dy + r) * side + dx + r] * __expf(-0.5f * q);
+            }
+            const float4 CM = T[W_CM * tn + e];
+            const float w2 = wj * wj;
+            out.acc[0] = __fmaf_rn(wj, CM.x, out.acc[0]);
+            out.acc[1] = __fmaf_rn(wj, CM.y, out.acc[1]);
+            out.acc[2] = __fmaf_rn(wj, CM.z, out.acc[2]);
+            out.acc[3] += wj;
+            out.acc[4] += w2;
+            out.acc[5] = __fmaf_rn(w2, CM.w, out.acc[5]);
+        }
+    }
+    return out;
+}
+
+// The pixels that leave the fast path: with a decision inside a guard band, the window again
+// (recheck_window); then, when the weight sum lies inside the 1.1 test's band, the whole pixel
+// in double (exact_pixel); else the blend from the sums. One out-of-line call site for both.
+__device__ __noinline__ void finish_slow(const PixelPlanes& p, const StatmcParams& prm, const float4* T, int tn, int tw,
+                                         int r, int ei, const float* spatial, const float2* line, int x, int y,
+                                         int rechecks, WindowSums sums) {
+    const int64_t idx = int64_t(y) * prm.w + x;
+    if (rechecks > 0) {
+        atomicAdd(p.counters + RPD_COUNTER_WINDOW_PAIR_RECHECKS, (unsigned long long)rechecks);
+        sums = recheck_window(T, tn, tw, r, ei, spatial, line, prm, p.n, x, y);
+    }
+    if (sums.accepted >= 2 && fabsf(sums.acc[3] - 1.1f) <= 1.1f * prm.ws_band) {
+        atomicAdd(p.counters + RPD_COUNTER_WINDOW_PIXEL_RECHECKS, 1ull);
+        exact_pixel(p, prm, idx);
+        return;
+    }
+    write_blend(p, idx, T[W_CM * tn + ei], sums.acc, sums.accepted);
 }
 
 // RC > 0: radius RC and kRows block rows fixed at compile time; RC == 0: prm.r and prm.by.
@@ -620,36 +759,14 @@ __global__ void __launch_bounds__(kTileX * kRows, 3)
         window_rows<RC, 0>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, rechecks);
 
     // the blend in single precision from the float sums (relative error ~1e-6, far inside the
-    // plain-form bar); the weight_sum >= 1.1 test keeps its guard band. A pixel with a decision
-    // inside a band is recomputed wholly in double, the reference's operations in its order.
-    const float weight_sum = acc[3];
-    if (rechecks > 0 || (accepted >= 2 && fabsf(weight_sum - 1.1f) <= 1.1f * prm.ws_band)) {
-        if (rechecks > 0) atomicAdd(p.counters + RPD_COUNTER_WINDOW_PAIR_RECHECKS, (unsigned long long)rechecks);
-        atomicAdd(p.counters + RPD_COUNTER_WINDOW_PIXEL_RECHECKS, 1ull);
-        exact_pixel(p, prm, idx);
+    // plain-form bar); a pixel with a decision inside a guard band, or whose weight sum lies
+    // inside the band of the 1.1 test, takes the slow path
+    if (rechecks > 0 || (accepted >= 2 && fabsf(acc[3] - 1.1f) <= 1.1f * prm.ws_band)) {
+        WindowSums sums{{acc[0], acc[1], acc[2], acc[3], acc[4], acc[5]}, accepted};
+        finish_slow(p, prm, T, tn, tw, r, ei, spatial, s_line, x, y, rechecks, sums);
         return;
     }
-    const float var_mean_i = cmi.w;
-    float mean_nb[3] = {cmi.x, cmi.y, cmi.z};
-    float var_neighbors = var_mean_i;
-    if (weight_sum > 1e-8f) {
-        const float inv = 1.0f / weight_sum;
-        mean_nb[0] = acc[0] * inv;
-        mean_nb[1] = acc[1] * inv;
-        mean_nb[2] = acc[2] * inv;
-        var_neighbors = acc[5] * inv * inv;
-    }
-    const float effective = weight_sum * weight_sum / fmaxf(1e-8f, acc[4]);
-    const float blend =
-        (accepted >= 2 && weight_sum >= 1.1f) ? fminf(fmaxf(1.0f - rsqrtf(effective), 0.0f), 0.8f) : 0.0f;
-    const float alpha = 1.0f - blend;
-    p.denoised[0][idx] = lerpf(cmi.x, mean_nb[0], blend);
-    p.denoised[1][idx] = lerpf(cmi.y, mean_nb[1], blend);
-    p.denoised[2][idx] = lerpf(cmi.z, mean_nb[2], blend);
-    const float uncertainty = alpha * alpha * var_mean_i + blend * blend * var_neighbors +
-                              2.0f * alpha * blend * (1.0f / fmaxf(weight_sum, 1e-8f)) * var_mean_i;
-    p.alpha[idx] = alpha;
-    p.uncertainty[idx] = uncertainty;
+    write_blend(p, idx, cmi, acc, accepted);
 }
 
 // Smallest float s with fl(sqrt(s)) > t: the albedo gate sqrt(s) > 0.12 without a sqrt.

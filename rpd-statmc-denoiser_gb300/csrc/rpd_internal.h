@@ -81,8 +81,9 @@ struct PixelPlanes {
     float4* win;
     // variance_denoise (main.cpp:1178-1264)
     float* variance_denoised;
-    float* var_ping;
+    float* var_ping;     // rows of var_pitch(w) floats
     float* var_pong;
+    float4* var_gate;    // variance_denoise's gate records: unit normal, depth
     uint64_t* var_mask;  // variance_denoise: per pixel, the neighbours that pass the geometric gates
     // compute_adaptive_sample_counts (main.cpp:1300-1438)
     float* importance;
@@ -190,6 +191,9 @@ struct Job {
     // halo box of radius win_map_r and win_map_by rows per block (0: not encoded yet)
     alignas(64) unsigned char win_map[128]{};
     int win_map_r = 0, win_map_by = 0;
+    // variance_denoise's tensor maps (gate records, ping, pong) for halo radius var_map_r (0: not encoded)
+    alignas(64) unsigned char var_maps[3][128]{};
+    int var_map_r = 0;
 };
 
 // Brackets the launches of one kernel family with CUDA events when profiling is on.
@@ -350,6 +354,24 @@ cudaError_t launch_joint_bilateral(const float* raw, const float* normal, const 
                                    float sigma_c, float sigma_n, float sigma_p, float sigma_a, float* gaussian,
                                    float* bilateral, float* joint, void* scratch, cudaStream_t stream,
                                    uint64_t* launches);
+
+// eval_tools hdr-metrics on the GPU (k_metrics.cu): the scratch it needs for a w x h image,
+// and the launches; *d_out (device memory) gets the metrics.
+// An RGB image as three channel pointers and a pixel stride: interleaved (p[c] = base + c,
+// step 3) or planar (step 1).
+struct Img3 {
+    const float* p[3];
+    int step;
+    __device__ __forceinline__ double at(int64_t i, int c) const { return double(p[c][i * step]); }
+};
+uint64_t metrics_scratch_bytes(int w, int h);
+// Image products (k_output.cu): encode src on `stream` and write the file (tonemap < 0: Radiance
+// HDR, else a PNG with that preset); dev / host: scratch of 4 w h bytes (host page-locked).
+int write_image(const Img3& src, int w, int h, int tonemap, const std::string& path, uint8_t* dev, uint8_t* host,
+                cudaStream_t stream);
+cudaError_t launch_count_fraction(const int32_t* counts, int64_t np, int* dmax, float* out, cudaStream_t stream);
+cudaError_t launch_metrics(const Img3& ref, const Img3& tst, int w, int h, void* scratch, rpd_image_metrics* d_out,
+                           cudaStream_t stream);
 
 // Pushes without host synchronisation (the serving loop, serve.cu). job_reserve sizes the
 // offsets for every pixel and the per-sample scratch for pushes of up to max_push_samples, so

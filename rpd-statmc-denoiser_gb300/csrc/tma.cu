@@ -41,4 +41,19 @@ cudaError_t encode_record_map(CUtensorMap* map, const void* base, int w, int h, 
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+cudaError_t encode_plane_map(CUtensorMap* map, const float* base, int w, int h, int pitch, int bw, int bh) {
+    if (w < 1 || h < 1 || pitch < w || pitch % 4 || bw < 4 || bw > 256 || bw % 4 || bh < 1 || bh > 256)
+        return cudaErrorInvalidValue;
+    const EncodeTiled fn = encoder();
+    if (!fn) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {cuuint64_t(w), cuuint64_t(h)};
+    const cuuint64_t strides[1] = {cuuint64_t(pitch) * 4};
+    const cuuint32_t box[2] = {cuuint32_t(bw), cuuint32_t(bh)};
+    const cuuint32_t estride[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estride,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 }  // namespace rpd

@@ -62,6 +62,15 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// One tiled tensor copy global -> shared of the 2-D box at (c0, c1), completing on `bar`.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
 // The box of records around pixel (x0, y0) - (r, r): bw x bh pixels of every plane, into
 // shared memory at `dst` (128-byte aligned), with `bar` expecting its bytes. One thread calls it.
 __device__ __forceinline__ void tile_load(float4* dst, const CUtensorMap* map, int x0, int y0, int r, int bw, int bh,
@@ -74,5 +83,9 @@ __device__ __forceinline__ void tile_load(float4* dst, const CUtensorMap* map, i
 // boxes of bw x bh pixels (bw <= 64, bh <= 256). Returns cudaErrorNotSupported when the
 // driver has no tensor-map encoder, cudaErrorInvalidValue when it rejects the layout.
 cudaError_t encode_record_map(CUtensorMap* map, const void* base, int w, int h, int planes, int bw, int bh);
+// Host: the tensor map of one w x h float plane with rows `pitch` floats apart (pitch a multiple
+// of 4, so rows start 16 bytes apart), for boxes of bw x bh floats (bw a multiple of 4, <= 256).
+// Columns from w to the pitch lie outside the tensor: a box reading them gets zeros.
+cudaError_t encode_plane_map(CUtensorMap* map, const float* base, int w, int h, int pitch, int bw, int bh);
 
 }  // namespace rpd

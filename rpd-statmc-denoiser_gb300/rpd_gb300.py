@@ -127,6 +127,18 @@ class SampleSoA16(C.Structure):
     ]
 
 
+class ImageMetrics(C.Structure):
+    """rpd_image_metrics: what `eval_tools hdr-metrics` reports (shared/tools/eval_tools.cpp)."""
+    _fields_ = [("mae", C.c_double), ("rmse", C.c_double), ("psnr", C.c_double), ("peak", C.c_double),
+                ("ssim", C.c_double * 3), ("ssim_mean", C.c_double), ("nrmse", C.c_double),
+                ("log_ssim11", C.c_double), ("log_gradient_nrmse", C.c_double)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "ssim"}
+        d["ssim"] = list(self.ssim)
+        return d
+
+
 class SynthParams(C.Structure):
     """rpd_synth_params (include/rpd_synth.h)."""
     _fields_ = [
@@ -324,6 +336,17 @@ def lib() -> C.CDLL:
         "rpd_server_kernel_times": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
         "rpd_server_destroy": (None, [vp]),
         "rpd_job_counters": (C.c_int, [vp, C.POINTER(C.c_uint64), i32]),
+        "rpd_hdr_metrics": (C.c_int, [vp, vp, vp, i32, i32, C.c_int, C.POINTER(ImageMetrics)]),
+        "rpd_write_hdr": (C.c_int, [vp, vp, i32, i32, C.c_int, C.c_char_p]),
+        "rpd_emitter_create": (C.c_int, [vp, i32, i32, i32, C.POINTER(vp)]),
+        "rpd_emitter_begin_pass": (C.c_int, [vp, i32, vp]),
+        "rpd_emitter_row": (C.c_int, [vp, i32, C.POINTER(SampleSoA), C.POINTER(C.POINTER(C.c_int64))]),
+        "rpd_emitter_row_done": (C.c_int, [vp, i32]),
+        "rpd_emitter_end_pass": (C.c_int, [vp]),
+        "rpd_emitter_destroy": (None, [vp]),
+        "rpd_write_png": (C.c_int, [vp, vp, i32, i32, C.c_int, C.c_int, C.c_char_p]),
+        "rpd_job_write_outputs": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_int]),
+        "rpd_job_hdr_metrics": (C.c_int, [vp, vp, C.c_int, C.POINTER(ImageMetrics)]),
         "rpd_probe_fp32_issue": (C.c_int, [C.c_int, i32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "rpd_last_error": (C.c_char_p, []),
         "rpd_status_string": (C.c_char_p, [C.c_int]),
@@ -354,7 +377,10 @@ def exported_symbols() -> list[str]:
             "rpd_job_mark", "rpd_job_mark_elapsed",
             "rpd_atrous_wavelet", "rpd_joint_bilateral", "rpd_atrous_wavelet_noalloc", "rpd_device_alloc", "rpd_device_free", "rpd_host_alloc",
             "rpd_host_free", "rpd_memcpy", "rpd_synth_fill", "rpd_last_error", "rpd_status_string",
-            "rpd_job_counters", "rpd_probe_fp32_issue"]
+            "rpd_job_counters", "rpd_probe_fp32_issue", "rpd_hdr_metrics", "rpd_job_hdr_metrics",
+            "rpd_write_hdr", "rpd_write_png", "rpd_job_write_outputs", "rpd_emitter_create",
+            "rpd_emitter_begin_pass", "rpd_emitter_row", "rpd_emitter_row_done", "rpd_emitter_end_pass",
+            "rpd_emitter_destroy"]
 
 
 def check(status: int) -> None:
@@ -560,6 +586,15 @@ class Context:
         check(lib().rpd_atrous_wavelet(self.handle, *[a.ctypes.data for a in args], w, h, sigma_c, sigma_n, sigma_a,
                                        iterations, out.ctypes.data, MEM_HOST))
         return out
+
+    def hdr_metrics(self, reference: np.ndarray, test: np.ndarray) -> dict:
+        """rpd_hdr_metrics of two (H, W, 3) float images in host memory."""
+        h, w, _ = reference.shape
+        a = np.ascontiguousarray(reference, dtype=np.float32)
+        b = np.ascontiguousarray(test, dtype=np.float32)
+        m = ImageMetrics()
+        check(lib().rpd_hdr_metrics(self.handle, a.ctypes.data, b.ctypes.data, w, h, MEM_HOST, C.byref(m)))
+        return m.as_dict()
 
     def joint_bilateral(self, raw, normal, albedo, sigma_c, sigma_n, sigma_p, sigma_a):
         h, w, _ = raw.shape
@@ -797,6 +832,13 @@ class Job:
             out[name] = (ms.value, n.value)
         return out
 
+    def hdr_metrics(self, reference: np.ndarray) -> dict:
+        """rpd_job_hdr_metrics: the job's denoised image against a (H, W, 3) host reference."""
+        a = np.ascontiguousarray(reference, dtype=np.float32)
+        m = ImageMetrics()
+        check(lib().rpd_job_hdr_metrics(self.handle, a.ctypes.data, MEM_HOST, C.byref(m)))
+        return m.as_dict()
+
     def counters(self) -> dict[str, int]:
         """The job's device counters (rpd_counter): the StatMC window's double-precision
         rechecks of the last statmc_denoise and the device waits that gave up."""
@@ -874,12 +916,16 @@ SERVED_PLANES = ("radiance", "normal", "depth", "pixel_albedo", "pixel_u", "lens
 
 
 def plain_request(ctx: Context, knobs: Config, width: int, height: int, spp: int, seed: int,
-                  job: "Job | None" = None) -> tuple[np.ndarray, int]:
+                  job: "Job | None" = None, skip_dead: bool = False) -> tuple[np.ndarray, int]:
     """One synthetic request through the plain per-frame drop-in: render()'s call sequence
     (path_tracer/main.cpp:1543-1564) on one job from the host, FP32 planes generated on the
     device with the same ordinals the serving loop draws (first pass 0..spp-1, adaptive pass p
     from p << 16), the adaptive counts read back to the host as compute_adaptive_sample_counts
-    returns them. Returns the denoised image (H, W, 3) and the samples denoised."""
+    returns them. Returns the denoised image (H, W, 3) and the samples denoised.
+
+    skip_dead: leave out the calls whose results nothing reads before they are overwritten —
+    the adaptive passes' statmc_denoise and recompute_sensitivity and the final variance_denoise —
+    as the serving loop does (the denoised image is the same bits)."""
     cfg = knobs.replace(image_width=width, image_height=height)
     n = width * height
     passes = cfg.adaptive_passes if cfg.adaptive_spp > 0 else 0
@@ -898,7 +944,8 @@ def plain_request(ctx: Context, knobs: Config, width: int, height: int, spp: int
         job.end_pass()
         job.recompute_sensitivity()
         for p in range(1, passes + 1):
-            job.statmc_denoise()
+            if not skip_dead:
+                job.statmc_denoise()
             job.variance_denoise()
             counts = job.compute_adaptive_sample_counts()
             samples += int(counts.sum())
@@ -907,10 +954,12 @@ def plain_request(ctx: Context, knobs: Config, width: int, height: int, spp: int
             ctx.synth_fill(params, 0, n, 0, dev, counts=counts_dev, start_n=start_dev)
             job.push(dev, 0, n, 0, counts=counts_dev)
             job.end_pass()
-            job.recompute_sensitivity()
+            if not skip_dead:
+                job.recompute_sensitivity()
         job.recompute_sensitivity()
         job.statmc_denoise()
-        job.variance_denoise()
+        if not skip_dead:
+            job.variance_denoise()
         job.finalize()
         return job.read("DENOISED"), samples
     finally:
@@ -919,6 +968,55 @@ def plain_request(ctx: Context, knobs: Config, width: int, height: int, spp: int
         start_dev.free()
         if own:
             job.close()
+
+
+class Emitter:
+    """rpd_emitter: a tracer's per-sample records streamed to a job band by band."""
+
+    PLANES = {"radiance": 3, "normal": 3, "albedo": 3, "pixel_u": 2, "lens_u": 2, "brdf_u": 2, "light_u": 2,
+              "env_u": 2}
+
+    def __init__(self, job: "Job", band_rows: int, ring_slots: int, max_spp: int):
+        self.job = job
+        self.handle = C.c_void_p()
+        check(lib().rpd_emitter_create(job.handle, band_rows, ring_slots, max_spp, C.byref(self.handle)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().rpd_emitter_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def begin_pass(self, spp: int = 0, counts: np.ndarray | None = None) -> None:
+        self._counts = None if counts is None else np.ascontiguousarray(counts, dtype=np.int32)
+        check(lib().rpd_emitter_begin_pass(self.handle, spp, None if self._counts is None else self._counts.ctypes.data))
+
+    def write_row(self, y: int, samples: "HostSamples") -> None:
+        """Row y's samples (all pixels of the row, pixel-major) copied into the ring."""
+        soa = SampleSoA()
+        offs = C.POINTER(C.c_int64)()
+        check(lib().rpd_emitter_row(self.handle, y, C.byref(soa), C.byref(offs)))
+        n = samples.n_samples
+        planes = dict(samples.planes)
+        if "albedo" not in planes and "pixel_albedo" in planes:
+            # a pixel's albedo for each of its samples (the record carries albedo per sample)
+            w = samples.n_pixels
+            counts = np.diff(np.array([offs[x] - offs[0] for x in range(w + 1)], dtype=np.int64))
+            planes["albedo"] = np.stack([np.repeat(planes["pixel_albedo"][c], counts) for c in range(3)])
+        for name, comps in self.PLANES.items():
+            src = planes.get(name)
+            dst = getattr(soa, name)
+            for c in range(comps):
+                if src is None:
+                    C.memset(dst[c], 0, 4 * n)
+                else:
+                    C.memmove(dst[c], np.ascontiguousarray(src[c], dtype=np.float32).ctypes.data, 4 * n)
+        for name in ("depth", "flags", "category"):
+            src = np.ascontiguousarray(samples.planes[name])
+            C.memmove(getattr(soa, name), src.ctypes.data, src.nbytes)
+        check(lib().rpd_emitter_row_done(self.handle, y))
+
+    def end_pass(self) -> None:
+        check(lib().rpd_emitter_end_pass(self.handle))
 
 
 def probe_fp32_issue(device: int = 0, repeats: int = 5) -> dict:

@@ -1,12 +1,19 @@
 // A clone of the reference's render() StatMC sequence (path_tracer/main.cpp:1543-1564) written
 // against include/rpd_statmc.hpp: the four stage functions keep their reference names and
-// signatures, and the per-sample accumulation becomes pushes of synthetic samples.
+// signatures, and the render loops (render_image_statmc, 649-737; render_image_adaptive,
+// 1451-1538) trace on host threads — here the seeded synthetic generator stands in for
+// mis_path_trace — and hand each sample's record to an emitter, which streams the rows to the
+// GPU band by band while the threads go on; the adaptive passes trace the counts the GPU
+// computed.
 //
 //   render_clone W H SPP PASSES [OUT]   -> prints the mean denoised value and the adaptive total;
 //                                        OUT gets each pass's counts (W*H int32 per pass) and
 //                                        the denoised image (W*H*3 float)
+#include <atomic>
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <thread>
 #include <vector>
 
 #include "rpd_statmc.hpp"
@@ -27,28 +34,33 @@ struct RenderConfig {
     bool debug_statmc_outputs = false;
 };
 
-struct HostPlanes {
-    std::vector<float> f[18];
-    std::vector<uint8_t> flags, category;
-    rpd_sample_soa soa{};
-    HostPlanes(int64_t n_samples, int64_t n_pixels) {
-        for (auto& v : f) v.resize(size_t(n_samples));
-        f[17].resize(size_t(n_pixels) * 3);
-        flags.resize(size_t(n_samples));
-        category.resize(size_t(n_samples));
-        int k = 0;
-        for (int c = 0; c < 3; ++c) soa.radiance[c] = f[k++].data();
-        for (int c = 0; c < 3; ++c) soa.normal[c] = f[k++].data();
-        soa.depth = f[k++].data();
-        for (int c = 0; c < 2; ++c) soa.pixel_u[c] = f[k++].data();
-        for (int c = 0; c < 2; ++c) soa.lens_u[c] = f[k++].data();
-        for (int c = 0; c < 2; ++c) soa.brdf_u[c] = f[k++].data();
-        for (int c = 0; c < 2; ++c) soa.light_u[c] = f[k++].data();
-        for (int c = 0; c < 3; ++c) soa.pixel_albedo[c] = f[17].data() + size_t(c) * size_t(n_pixels);
-        soa.flags = flags.data();
-        soa.category = category.data();
-    }
-};
+// The render loop of one pass: `threads` host threads take rows in increasing order (OpenMP's
+// dynamic schedule over rows, main.cpp:678-681 and 1488-1490) and trace each row's samples into
+// the emitter's row planes; counts: the adaptive pass's per-pixel counts, or null for spp each.
+void trace_pass(rpd_ctx* ctx, rpd_emitter* em, const rpd_synth_params& prm, int w, int h, int spp,
+                const int32_t* counts, const int32_t* start_n, int threads) {
+    rpd::check(rpd_emitter_begin_pass(em, spp, counts));
+    std::atomic<int> next_row{0};
+    std::atomic<int> status{RPD_OK};
+    auto worker = [&]() {
+        for (int y = next_row++; y < h && status == RPD_OK; y = next_row++) {
+            rpd_sample_soa row{};
+            const int64_t* offsets = nullptr;
+            int st = rpd_emitter_row(em, y, &row, &offsets);
+            const int64_t p0 = int64_t(y) * w;
+            if (st == RPD_OK)
+                st = rpd_synth_fill(ctx, &prm, p0, w, spp, counts ? counts + p0 : nullptr, start_n ? start_n + p0 : nullptr,
+                                    &row, RPD_MEM_HOST);
+            if (st == RPD_OK) st = rpd_emitter_row_done(em, y);
+            if (st != RPD_OK) status = st;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    rpd::check(status.load());
+    rpd::check(rpd_emitter_end_pass(em));
+}
 
 int main(int argc, char** argv) {
     RenderConfig config;
@@ -71,14 +83,11 @@ int main(int argc, char** argv) {
         rpd_synth_params prm;
         rpd_synth_defaults(&prm, w, h, 1234);
 
-        // render_image_statmc (main.cpp:649-737): the first pass
+        // render_image_statmc (main.cpp:649-737): the first pass, traced on 4 host threads
+        rpd_emitter* em = nullptr;
+        rpd::check(rpd_emitter_create(job.get(), 8, 3, std::max(spp, 8 * config.adaptive_spp), &em));
         job.begin_frame();
-        {
-            HostPlanes s(np * spp, np);
-            rpd::check(rpd_synth_fill(ctx.get(), &prm, 0, np, spp, nullptr, nullptr, &s.soa, RPD_MEM_HOST));
-            job.push(s.soa, 0, np, spp);
-        }
-        job.end_pass();
+        trace_pass(ctx.get(), em, prm, w, h, spp, nullptr, nullptr, 4);
         rpd::recompute_sensitivity(config);
         std::vector<int32_t> n_so_far(size_t(np), spp);
         int64_t adaptive_total = 0;
@@ -87,17 +96,13 @@ int main(int argc, char** argv) {
             rpd::variance_denoise(config);
             std::vector<int> counts = rpd::compute_adaptive_sample_counts(config);
             all_counts.insert(all_counts.end(), counts.begin(), counts.end());
-            int64_t extra = 0;
-            for (int c : counts) extra += c;
-            adaptive_total += extra;
-            HostPlanes s(extra, np);  // render_image_adaptive (main.cpp:1451-1538)
-            rpd::check(rpd_synth_fill(ctx.get(), &prm, 0, np, 0, counts.data(), n_so_far.data(), &s.soa,
-                                      RPD_MEM_HOST));
-            job.push(s.soa, 0, np, 0, counts.data());
-            job.end_pass();
+            for (int c : counts) adaptive_total += c;
+            // render_image_adaptive (main.cpp:1451-1538): the extra samples the GPU asked for
+            trace_pass(ctx.get(), em, prm, w, h, 0, counts.data(), n_so_far.data(), 4);
             for (int64_t p = 0; p < np; ++p) n_so_far[size_t(p)] += counts[size_t(p)];
             rpd::recompute_sensitivity(config);
         }
+        rpd_emitter_destroy(em);
         rpd::recompute_sensitivity(config);
         rpd::statmc_denoise(config);
         rpd::variance_denoise(config);

@@ -13,6 +13,8 @@ oracle/binding.py:
     the replayed adaptive sequence is the one render() performs;
   * `ref_atrous` / `ref_joint_bilateral`: denoising/atrous_wavelet.cpp and
     joint_bilateral.cpp filter() on in-memory images;
+  * `ref_hdr_metrics`: shared/tools/eval_tools.cpp (its hdr-metrics command and
+    compute_extended_metrics) on in-memory images;
   * `ref_parse_yaml`: core/config.h parse_render_config, for the validation messages.
 
 Fixtures (numpy .npz, compressed; `meta` is a JSON string):
@@ -27,6 +29,10 @@ Fixtures (numpy .npz, compressed; `meta` is a JSON string):
                               `meta.synth`; a SHA-256 of each plane pins the generator)
   synth_32x24_adaptive.npz    the adaptive sequence with synthetic extra samples
   filters_37x53.npz           filter inputs and the reference filter outputs
+  outputs_48x48.npz           every image output_buffers writes for the 48x48 cornell frame
+                              (HDR floats, tonemapped PNG bytes) and the tonemapping curves
+  eval_metrics.npz            image pairs and the reference's eval_tools hdr-metrics of each
+                              (compute_extended_metrics in full precision, the printed report)
   config_messages.json        (field, value, message) of the reference's validation
 
     REF_ROOT=<reference checkout> python tests/golden/make_golden.py
@@ -233,6 +239,58 @@ def filters() -> None:
          dict(raw=raw, normal=normal, albedo=albedo, atrous=a, gaussian=g, bilateral=b, joint=j))
 
 
+def outputs() -> None:
+    """output_buffers of the 48x48 cornell frame (agx preset) as the reference writes it, and its
+    tonemapping curves (every preset) on a spread of HDR values."""
+    w = h = 48
+    spp = 4
+    cfg = B.ref_parse_yaml(str(YAML)).replace(image_width=w, image_height=h, adaptive_passes=0,
+                                               adaptive_spp=4, adaptive_base_samples=1, **CORNELL_KNOBS)
+    s = B.trace_cornell(str(YAML), w, h, spp, cfg.seed)
+    job = B.RefJob(cfg, threads=1)
+    B.run_pipeline(job, s, spp)
+    job.compute_adaptive_sample_counts()  # fills adaptive_importance
+    job.finalize()
+    files = B.ref_outputs("out", 0)
+    job.close()
+    arrays = {}
+    for name, arr in files.items():
+        arrays["f_" + name.replace(".", "__")] = arr
+    put_samples(arrays, "s_", s)
+    rng = np.random.default_rng(21)
+    vals = np.concatenate([rng.lognormal(-1.5, 2.0, (3000, 3)), rng.uniform(0, 1, (800, 3)),
+                           np.array([[0, 0, 0], [1e-9, 0, 0], [1e4, 1e4, 1e4], [1, 1, 1], [0.5, 0.25, 0.125]])]
+                          ).astype(np.float32)
+    arrays["tonemap_in"] = vals
+    for t in range(4):
+        arrays[f"tonemap_{t}"] = B.ref_tonemap(vals, t)
+    save("outputs_48x48.npz", {"config": B.config_dict(cfg), "spp": spp, "planes": list(s.planes), "prefix": "out",
+                               "files": sorted(files)}, arrays)
+
+
+def metrics() -> None:
+    """eval_tools hdr-metrics of image pairs: the reference's compute_extended_metrics (full
+    precision) and its printed report, with the images."""
+    rng = np.random.default_rng(9)
+    pairs = {}
+    ref = rng.lognormal(-1.0, 0.8, size=(29, 37, 3)).astype(np.float32)
+    pairs["noisy"] = (ref, (ref * rng.lognormal(0.0, 0.1, ref.shape)).astype(np.float32))
+    ramp = np.add.outer(np.arange(16), np.arange(16)).astype(np.float32)[..., None] + 1.0
+    ramp = np.repeat(ramp / 32.0, 3, axis=2).astype(np.float32)
+    changed = ramp.copy()
+    changed[8, 8, 0] += 0.25  # the reference's self-test pair (eval_tools.cpp:317-338)
+    pairs["selftest"] = (ramp, changed)
+    pairs["identical"] = (ramp, ramp.copy())
+    dark = rng.uniform(-0.05, 0.2, size=(23, 41, 3)).astype(np.float32)  # negative luminance clamps to 0
+    pairs["dark"] = (dark, (dark + rng.normal(0, 0.02, dark.shape)).astype(np.float32))
+    arrays, meta = {}, {}
+    for name, (a, b) in pairs.items():
+        arrays[f"{name}_ref"], arrays[f"{name}_tst"] = a, b
+        r = B.ref_hdr_metrics(a, b)
+        meta[name] = {k: v for k, v in r.items() if k != "text"}
+    save("eval_metrics.npz", {"metrics": meta}, arrays)
+
+
 # (field, invalid value) pairs for the stage knobs core/config.h:116-195 validates
 INVALID = [
     ("image_width", 0), ("image_height", -3), ("rpf_tile_size", 0), ("color_window_radius", 0),
@@ -275,4 +333,6 @@ if __name__ == "__main__":
     synth_single()
     synth_adaptive()
     filters()
+    metrics()
+    outputs()
     config_messages()

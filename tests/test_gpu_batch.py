@@ -58,3 +58,40 @@ def test_batch_rejects_duplicate_job(gpu_ctx):
     batch.close()
     job.close()
     dev.free()
+
+
+def test_batched_frames_against_the_fp64_oracle(gpu_ctx):
+    """Each frame of a batch (compact storage, autotuned shapes, one graph) against the
+    double-precision restatement of the same frame (oracle/rpd_oracle64.c on the FP32 samples):
+    relMSE = mean((x - r)^2 / (r^2 + 1e-2)) <= 1e-3, the precision form's bar."""
+    from conftest import B
+
+    frames = [(256, 256, 16), (160, 90, 4), (96, 64, 32)]
+    jobs, planes, refs = [], [], []
+    batch = R.Batch(gpu_ctx)
+    try:
+        for i, (w, h, spp) in enumerate(frames):
+            cfg = small_config(w, h)
+            p = R.synth_params(w, h, 500 + i)
+            host = B.synth_fill(p, 0, w * h, spp, threads=8)
+            refs.append(B.fp64_denoise(cfg, host, spp, threads=8).astype(np.float64))
+            dev = R.DeviceSamples.from_host(gpu_ctx, host)
+            dev16 = R.DeviceSamples16.encode(gpu_ctx, dev)
+            dev.free()
+            job = R.Job(gpu_ctx, cfg)
+            job.autotune(dev16, spp)
+            jobs.append(job)
+            planes.append(dev16)
+            batch.add(job, dev16, spp)
+        batch.run()
+        batch.sync()
+        for job, r in zip(jobs, refs):
+            x = job.read("DENOISED").astype(np.float64)
+            err = float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+            assert err <= 1e-3, err
+    finally:
+        batch.close()
+        for j in jobs:
+            j.close()
+        for p in planes:
+            p.free()

@@ -136,3 +136,54 @@ def test_forms_against_the_fp64_oracle(gpu_ctx, w, h, spp):
         b.close()
         dev.free()
         dev16.free()
+
+
+@pytest.mark.parametrize("w,h,spp", [(256, 256, 16), (640, 360, 4)])
+def test_served_sequence_against_the_fp64_oracle(gpu_ctx, w, h, spp):
+    """The serving workload's request (3 adaptive passes of 4 extra samples per pixel on
+    average, floor 1) in compact storage, as the serving loop runs it — base pass, then per
+    adaptive pass variance_denoise, the adaptive counts and the extra samples drawn for them
+    (ordinals from p << 16), then recompute_sensitivity and statmc_denoise — against the
+    double-precision restatement fed the same samples: relMSE <= 1e-3 (epsilon 1e-2)."""
+    from conftest import B
+
+    cfg = small_config(w, h, adaptive_passes=3, adaptive_spp=4, adaptive_base_samples=1,
+                       color_normal_threshold=0.6, color_depth_threshold=0.2, color_compat_alpha=0.01,
+                       color_sigma_max=4.0, var_normal_threshold=0.6, var_compat_sigma=3.0, var_shrinkage_k=0.7,
+                       adaptive_sigma_max=4.0)
+    n = w * h
+    p = R.synth_params(w, h, 777)
+    job = R.Job(gpu_ctx, cfg)
+    bufs = []
+    pushes = []
+    try:
+        dev = R.DeviceSamples(gpu_ctx, n * spp, n)
+        bufs.append(dev)
+        gpu_ctx.synth_fill(p, 0, n, spp, dev)
+        dev16 = R.DeviceSamples16.encode(gpu_ctx, dev)
+        bufs.append(dev16)
+        job.begin_frame()
+        job.push(dev16, 0, n, spp)
+        job.end_pass()
+        pushes.append((B.synth_fill(p, 0, n, spp, threads=8), spp, None))
+        for k in range(1, cfg.adaptive_passes + 1):
+            job.variance_denoise()
+            counts = job.compute_adaptive_sample_counts()
+            start = np.full(n, k << 16, dtype=np.int32)
+            ex = R.DeviceSamples(gpu_ctx, int(counts.sum()), n)
+            bufs.append(ex)
+            gpu_ctx.synth_fill(p, 0, n, 0, ex, counts=counts, start_n=start)
+            ex16 = R.DeviceSamples16.encode(gpu_ctx, ex)
+            bufs.append(ex16)
+            job.push(ex16, 0, n, 0, counts=counts)
+            job.end_pass()
+            pushes.append((B.synth_fill(p, 0, n, 0, counts=counts, start_n=start, threads=8), 0, counts))
+        job.recompute_sensitivity()
+        job.statmc_denoise()
+        ref = B.fp64_sequence(cfg, pushes, threads=8)
+        err = rel_mse(job.read("DENOISED"), ref)
+        assert err <= REL_MSE_BAR, err
+    finally:
+        job.close()
+        for b in bufs:
+            b.free()

@@ -250,3 +250,50 @@ def test_fp64_restatement_stays_close_to_the_float_one():
     assert np.all(np.isfinite(d64))
     assert float(np.mean((d32 - d64) ** 2 / (d64 ** 2 + 1e-2))) <= 1e-9
 
+
+
+# ---- evaluation metrics (shared/tools/eval_tools.cpp) -------------------------------------
+
+PRINTED = {"mae": 1e-10, "rmse": 1e-10, "peak": 1e-10, "psnr": 1e-5}  # %.12g and %.6g in the report
+
+
+def assert_metrics_match(got: dict, want: dict, extended_exact: bool) -> None:
+    for k in ("nrmse", "log_ssim11", "log_gradient_nrmse"):
+        if extended_exact:
+            assert got[k] == want[k], (k, got[k], want[k])
+        else:
+            assert got[k] == pytest.approx(want[k], rel=1e-9, abs=1e-12), k
+    for k, rel in PRINTED.items():
+        if np.isinf(want[k]):
+            assert np.isinf(got[k]), k
+        else:
+            assert got[k] == pytest.approx(want[k], rel=rel, abs=1e-12), k
+    for c in range(3):
+        assert abs(got["ssim"][c] - want["ssim"][c]) <= 5e-5  # printed with 4 decimals
+    assert abs(got["ssim_mean"] - want["ssim_mean"]) <= 5e-5
+
+
+def test_port_metrics_golden():
+    meta, a = load_golden("eval_metrics.npz")
+    for name, want in meta["metrics"].items():
+        got = B.port_hdr_metrics(a[f"{name}_ref"], a[f"{name}_tst"])
+        assert_metrics_match(got, want, extended_exact=True)
+
+
+def test_port_metrics_self_test_properties():
+    """eval_tools self-test (eval_tools.cpp:317-338): identical images give NRMSE 0,
+    LogSSIM11 1 and LogGradNRMSE 0; one changed value moves all three."""
+    meta, a = load_golden("eval_metrics.npz")
+    same = B.port_hdr_metrics(a["identical_ref"], a["identical_tst"])
+    assert same["nrmse"] <= 1e-12 and abs(same["log_ssim11"] - 1.0) <= 1e-12 and same["log_gradient_nrmse"] <= 1e-12
+    diff = B.port_hdr_metrics(a["selftest_ref"], a["selftest_tst"])
+    assert diff["nrmse"] > 0.0 and diff["log_ssim11"] < 1.0 and diff["log_gradient_nrmse"] > 0.0
+
+
+@needs_ref
+def test_port_metrics_match_live_reference():
+    rng = np.random.default_rng(41)
+    for (h, w) in [(17, 13), (64, 96), (5, 300)]:
+        a = rng.lognormal(-0.5, 1.0, (h, w, 3)).astype(np.float32)
+        b = (a + rng.normal(0, 0.05, a.shape)).astype(np.float32)
+        assert_metrics_match(B.port_hdr_metrics(a, b), B.ref_hdr_metrics(a, b), extended_exact=True)
