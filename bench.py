@@ -854,11 +854,16 @@ def run_request(args):
         srv.close()
         assert len(done) == 1 and done[0]["status"] == 0, done
         samples = done[0]["samples"]
+        counters = None
     else:
-        _, samples = R.plain_request(ctx, knobs, args.width, args.height, args.spp, SEED)
+        job = R.Job(ctx, knobs.replace(image_width=args.width, image_height=args.height))
+        _, samples = R.plain_request(ctx, knobs, args.width, args.height, args.spp, SEED, job=job)
+        counters = job.counters()  # the last statmc_denoise's slow-pass pixels and rechecks
+        job.close()
     ctx.close()
     print(json.dumps({"form": "request", "served": bool(args.served), "width": args.width, "height": args.height,
-                      "spp": args.spp, "adaptive_passes": args.passes, "samples": samples}))
+                      "spp": args.spp, "adaptive_passes": args.passes, "samples": samples,
+                      "window_counters": counters}))
 
 
 def run_reference(args):

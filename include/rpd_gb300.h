@@ -418,6 +418,9 @@ typedef enum rpd_counter {
                                             * (weight sum within the 1.1 test's band; last statmc_denoise) */
     RPD_COUNTER_DEVICE_WAIT_TIMEOUTS,      /* bounded device-side waits that gave up (since job creation);
                                             * rpd_job_sync returns RPD_ERR_TIMEOUT while it is non-zero */
+    RPD_COUNTER_WINDOW_SLOW_PIXELS,        /* pixels the fast loop handed to the slow pass: a decision
+                                            * inside a guard band, or the weight sum inside the 1.1
+                                            * test's band (last statmc_denoise) */
     RPD_COUNTER_COUNT_ = 8
 } rpd_counter;
 /* Waits for the job's stream and copies min(n, RPD_COUNTER_COUNT_) counters to out. */

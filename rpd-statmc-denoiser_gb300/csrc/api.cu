@@ -94,6 +94,7 @@ uint64_t plan(const Geometry& g, PixelPlanes& p, NodePlanes& n, float* (*cls)[5]
     L.add(p.counts, np);
     L.add(p.active_a, np);
     L.add(p.active_b, np);
+    L.add(p.slow, np);
     L.add(p.alloc_state, np);
     L.add(p.alloc_work, int64_t(allocator_work_bytes(np)));
     L.add(p.counters, RPD_COUNTER_COUNT_);
@@ -161,6 +162,7 @@ void rebase_all(PixelPlanes& p, NodePlanes& n, char* base) {
     rebase(p.counts, base);
     rebase(p.active_a, base);
     rebase(p.active_b, base);
+    rebase(p.slow, base);
     rebase(p.alloc_state, base);
     rebase(p.alloc_work, base);
     rebase(p.counters, base);
@@ -1046,8 +1048,10 @@ int rpd_statmc_denoise(rpd_job* job) {
     if (st != RPD_OK) return st;
     st = ensure_cache(*j);
     if (st != RPD_OK) return st;
-    // the window's recheck counters describe the last call
+    // the window's recheck counters and its slow-pixel list describe the last call
     RPD_CUDA(cudaMemsetAsync(j->p.counters + RPD_COUNTER_WINDOW_PAIR_RECHECKS, 0, 2 * sizeof(unsigned long long),
+                             j->stream));
+    RPD_CUDA(cudaMemsetAsync(j->p.counters + RPD_COUNTER_WINDOW_SLOW_PIXELS, 0, sizeof(unsigned long long),
                              j->stream));
     RPD_CUDA(launch_statmc(*j));
     return RPD_OK;

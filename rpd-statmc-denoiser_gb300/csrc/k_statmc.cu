@@ -29,18 +29,21 @@
 //                          (2^-15 relative by default) of a decision point — q = 25 (reject),
 //                          q = 2 ln 20 (the accepted-neighbour count), the df of the t-table /
 //                          normal-quantile switch, or the 1e-8 df-denominator test — the
-//                          pixel's window is evaluated again with that neighbour's q recomputed
-//                          in double exactly as the reference computes it (out of line: rare on
-//                          uniform sample counts, a few per cent of pixels where adaptive passes
-//                          mix the counts so that df crosses the t-table switch);
+//                          pixel goes on a list for k_statmc_slow (rare on uniform sample
+//                          counts, a few per cent of pixels where adaptive passes mix the
+//                          counts so that df crosses the t-table switch);
 //                        * each block picks a specialised loop from the range of 1/(n-1) over
 //                          its halo: when every pair's df lies below the t-table switch
 //                          (df <= (n_i - 1) + (n_j - 1)) no neighbour needs the switch test, and
 //                          when every df lies above it (df >= min(n_i, n_j) - 1 >= 31) the t
 //                          critical value is the normal quantile and df is not formed at all.
 //                      Weights are summed in float per window row and across rows. The blend's
-//                      weight_sum >= 1.1 test has its own guard band; a pixel inside it is
-//                      recomputed wholly in double.
+//                      weight_sum >= 1.1 test has its own guard band; a pixel inside it goes
+//                      on the list too.
+//   k_statmc_slow      the listed pixels, one warp each: the window again with every banded
+//                      neighbour's q recomputed in double exactly as the reference computes
+//                      it, then the whole pixel in double if its weight sum is still inside
+//                      the 1.1 test's band.
 //   k_statmc_window    the whole window in double, the reference's operations in its order
 //                      (the exact mode, and the path for radii whose halo tile would not fit in
 //                      shared memory).
@@ -462,7 +465,7 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
     const bool center = dx == 0 && dy == 0;
     exact |= fabsf(q - 25.0f) <= 25.0f * prm.band;
     exact |= !center && fabsf(q - kQAccept) <= kQAccept * prm.band;
-    // a decision inside a guard band sends the pixel's window to recheck_window
+    // a decision inside a guard band hands the pixel to the slow pass (k_statmc_slow)
     rechecks += exact ? 1 : 0;
     if (q > 25.0f) return;
     if (!center && q < kQAccept) ++accepted;
@@ -528,34 +531,52 @@ __device__ __forceinline__ void write_blend(const PixelPlanes& p, int64_t idx, f
     p.uncertainty[idx] = uncertainty;
 }
 
-struct WindowSums {
-    float acc[6];  // colour rgb, weight, weight^2, weight^2 * var of the mean
-    int accepted;
-};
+// ---- slow pass -----------------------------------------------------------------------------
 
-// A pixel's window again, for a pixel with a decision inside a guard band: every neighbour in
-// single precision as the fast loop evaluates it, except that a neighbour whose q (or df) lies
-// in a band has its q recomputed in double exactly as the reference computes it
-// (main.cpp:1055-1097) and its rejection, weight and acceptance taken from that. Out of line
-// and rare, so the fast loop keeps its registers.
-__device__ __noinline__ WindowSums recheck_window(const float4* T, int tn, int tw, int r, int ei,
-                                                  const float* spatial, const float2* line, StatmcParams prm,
-                                                  const int32_t* __restrict__ n, int x, int y) {
-    WindowSums out{{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, 0};
-    const int side = 2 * r + 1;
-    const float4 gi = T[W_GATE * tn + ei], ai = T[W_ALB * tn + ei], si = T[W_SM * tn + ei];
-    const float4 vi = T[W_SV * tn + ei], ri = T[W_RPD * tn + ei];
-    float dm = fabsf(gi.w);
-    if (dm < 1e-8f) dm = 1e-8f;
-    const float smi[3] = {si.x, si.y, si.z}, svi[3] = {vi.x, vi.y, vi.z};
-    const float vi0 = vi.x * vi.x * ai.w, vi1 = vi.y * vi.y * ai.w, vi2 = vi.z * vi.z * ai.w;
-    const int n_i = imaxs(1, n[int64_t(y) * prm.w + x]);
-    for (int dy = -r; dy <= r; ++dy) {
-        for (int dx = -r; dx <= r; ++dx) {
-            const int e = ei + dy * tw + dx;
-            const float4 G = T[W_GATE * tn + e];
+// The pixels the fast loop hands over (a decision inside a guard band, or the weight sum inside
+// the band of the 1.1 test), one warp per pixel, the window's neighbours split over the lanes
+// and read from the packed records in HBM. Every neighbour is evaluated in single precision as
+// the fast loop evaluates it, except that a neighbour whose q (or df) lies in a band has its q
+// recomputed in double exactly as the reference computes it (main.cpp:1055-1097) and its
+// rejection, weight and acceptance taken from that; a pixel whose summed weight lies inside
+// the 1.1 test's band is then recomputed wholly in double (exact_pixel). Run as its own
+// launch, the rare pixel costs one warp's share of a short pass instead of holding the 31
+// other lanes of its warp in the fast loop.
+constexpr int kSlowThreads = 256;
+constexpr int kSlowBlocks = 152 * 8;  // eight blocks on each of GB300's 152 SMs
+
+__global__ void __launch_bounds__(kSlowThreads) k_statmc_slow(PixelPlanes p, StatmcParams prm, LineTable lt) {
+    __shared__ float2 s_line[64];
+    if (threadIdx.x < 64) s_line[threadIdx.x] = lt.v[threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t np = int64_t(prm.w) * prm.h;
+    unsigned long long count = p.counters[RPD_COUNTER_WINDOW_SLOW_PIXELS];
+    if (count > (unsigned long long)np) count = (unsigned long long)np;
+    const int r = prm.r, side = 2 * r + 1, visits = side * side;
+    const float4* win = p.win;
+    const unsigned long long warps = (unsigned long long)gridDim.x * (kSlowThreads / 32);
+    for (unsigned long long k = (unsigned long long)blockIdx.x * (kSlowThreads / 32) + threadIdx.x / 32; k < count;
+         k += warps) {
+        const int64_t idx = p.slow[k];
+        const int y = int(idx / prm.w), x = int(idx % prm.w);
+        const float4 gi = win[W_GATE * np + idx], ai = win[W_ALB * np + idx], si = win[W_SM * np + idx];
+        const float4 vi = win[W_SV * np + idx], ri = win[W_RPD * np + idx];
+        float dm = fabsf(gi.w);
+        if (dm < 1e-8f) dm = 1e-8f;
+        const float smi[3] = {si.x, si.y, si.z}, svi[3] = {vi.x, vi.y, vi.z};
+        const float vi0 = vi.x * vi.x * ai.w, vi1 = vi.y * vi.y * ai.w, vi2 = vi.z * vi.z * ai.w;
+        const int n_i = imaxs(1, p.n[idx]);
+        float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        int accepted = 0, pairs = 0;
+        for (int v = lane; v < visits; v += 32) {
+            const int dx = v % side - r, dy = v / side - r;
+            const int xx = x + dx, yy = y + dy;
+            if (xx < 0 || xx >= prm.w || yy < 0 || yy >= prm.h) continue;  // the zero record: no neighbour
+            const int64_t jn = int64_t(yy) * prm.w + xx;
+            const float4 G = win[W_GATE * np + jn];
             if (dot3(gi.x, gi.y, gi.z, G.x, G.y, G.z) < prm.normal_threshold) continue;
-            const float4 A = T[W_ALB * tn + e];
+            const float4 A = win[W_ALB * np + jn];
             if (!(A.w > 0.0f)) continue;
             {
                 float m = dm;
@@ -571,7 +592,7 @@ __device__ __noinline__ WindowSums recheck_window(const float4* T, int tn, int t
             }
             const float da0 = ai.x - A.x, da1 = ai.y - A.y, da2 = ai.z - A.z;
             if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) continue;
-            const float4 S = T[W_SM * tn + e], V = T[W_SV * tn + e], RJ = T[W_RPD * tn + e];
+            const float4 S = win[W_SM * np + jn], V = win[W_SV * np + jn], RJ = win[W_RPD * np + jn];
             const float vs[3] = {vi.x + V.x, vi.y + V.y, vi.z + V.z};
             const float md[3] = {si.x - S.x, si.y - S.y, si.z - S.z};
             const float den[3] = {__fmaf_rn(V.x * V.x, A.w, vi0), __fmaf_rn(V.y * V.y, A.w, vi1),
@@ -581,7 +602,7 @@ __device__ __noinline__ WindowSums recheck_window(const float4* T, int tn, int t
             for (int c = 0; c < 3; ++c) {
                 const float df = __fdividef(vs[c] * vs[c], den[c]);
                 exact |= fabsf(df - prm.df_break) <= prm.df_break * prm.band;
-                const float t = t_crit<0>(df, line, prm);
+                const float t = t_crit<0>(df, s_line, prm);
                 qmax = fmaxf(qmax, __fdividef(md[c] * md[c], vs[c] * (t * t)));
             }
             float shared = fmaxf(fmaxf(fminf(ri.x, RJ.x), fminf(ri.y, RJ.y)), fmaxf(fminf(ri.z, RJ.z), fminf(ri.w, RJ.w)));
@@ -593,49 +614,47 @@ __device__ __noinline__ WindowSums recheck_window(const float4* T, int tn, int t
             exact |= !center && fabsf(q - kQAccept) <= kQAccept * prm.band;
             float wj;
             if (exact) {
+                ++pairs;
                 const float smj[3] = {S.x, S.y, S.z}, svj[3] = {V.x, V.y, V.z};
-                const int n_j = imaxs(1, n[int64_t(y + dy) * prm.w + (x + dx)]);
-                const double qx = exact_q(svi, smi, n_i, svj, smj, n_j, prm.alpha, adjustment);
+                const double qx = exact_q(svi, smi, n_i, svj, smj, imaxs(1, p.n[jn]), prm.alpha, adjustment);
                 if (qx > 25.0) continue;
                 const double sw = 1.0 / (1.0 + double(dx * dx + dy * dy));
                 const double wd = sw * exp(-0.5 * qx);
-                if (!center && wd > 0.05 * sw) ++out.accepted;
+                if (!center && wd > 0.05 * sw) ++accepted;
                 wj = float(wd);
             } else {
                 if (q > 25.0f) continue;
-                if (!center && q < kQAccept) ++out.accepted;
-                wj = spatial[(dy + r) * side + dx + r] * __expf(-0.5f * q);
+                if (!center && q < kQAccept) ++accepted;
+                wj = __frcp_rn(1.0f + float(dx * dx + dy * dy)) * __expf(-0.5f * q);
             }
-            const float4 CM = T[W_CM * tn + e];
+            const float4 CM = win[W_CM * np + jn];
             const float w2 = wj * wj;
-            out.acc[0] = __fmaf_rn(wj, CM.x, out.acc[0]);
-            out.acc[1] = __fmaf_rn(wj, CM.y, out.acc[1]);
-            out.acc[2] = __fmaf_rn(wj, CM.z, out.acc[2]);
-            out.acc[3] += wj;
-            out.acc[4] += w2;
-            out.acc[5] = __fmaf_rn(w2, CM.w, out.acc[5]);
+            acc[0] = __fmaf_rn(wj, CM.x, acc[0]);
+            acc[1] = __fmaf_rn(wj, CM.y, acc[1]);
+            acc[2] = __fmaf_rn(wj, CM.z, acc[2]);
+            acc[3] += wj;
+            acc[4] += w2;
+            acc[5] = __fmaf_rn(w2, CM.w, acc[5]);
         }
+        // the lanes' sums in a fixed butterfly order: the same bits on every run
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+            accepted += __shfl_xor_sync(0xffffffffu, accepted, o);
+            pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+        }
+        if (lane == 0) {
+            if (pairs > 0) atomicAdd(p.counters + RPD_COUNTER_WINDOW_PAIR_RECHECKS, (unsigned long long)pairs);
+            if (accepted >= 2 && fabsf(acc[3] - 1.1f) <= 1.1f * prm.ws_band) {
+                atomicAdd(p.counters + RPD_COUNTER_WINDOW_PIXEL_RECHECKS, 1ull);
+                exact_pixel(p, prm, idx);
+            } else {
+                write_blend(p, idx, win[W_CM * np + idx], acc, accepted);
+            }
+        }
+        __syncwarp();
     }
-    return out;
-}
-
-// The pixels that leave the fast path: with a decision inside a guard band, the window again
-// (recheck_window); then, when the weight sum lies inside the 1.1 test's band, the whole pixel
-// in double (exact_pixel); else the blend from the sums. One out-of-line call site for both.
-__device__ __noinline__ void finish_slow(const PixelPlanes& p, const StatmcParams& prm, const float4* T, int tn, int tw,
-                                         int r, int ei, const float* spatial, const float2* line, int x, int y,
-                                         int rechecks, WindowSums sums) {
-    const int64_t idx = int64_t(y) * prm.w + x;
-    if (rechecks > 0) {
-        atomicAdd(p.counters + RPD_COUNTER_WINDOW_PAIR_RECHECKS, (unsigned long long)rechecks);
-        sums = recheck_window(T, tn, tw, r, ei, spatial, line, prm, p.n, x, y);
-    }
-    if (sums.accepted >= 2 && fabsf(sums.acc[3] - 1.1f) <= 1.1f * prm.ws_band) {
-        atomicAdd(p.counters + RPD_COUNTER_WINDOW_PIXEL_RECHECKS, 1ull);
-        exact_pixel(p, prm, idx);
-        return;
-    }
-    write_blend(p, idx, T[W_CM * tn + ei], sums.acc, sums.accepted);
 }
 
 // RC > 0: radius RC and kRows block rows fixed at compile time; RC == 0: prm.r and prm.by.
@@ -760,10 +779,11 @@ __global__ void __launch_bounds__(kTileX * kRows, 3)
 
     // the blend in single precision from the float sums (relative error ~1e-6, far inside the
     // plain-form bar); a pixel with a decision inside a guard band, or whose weight sum lies
-    // inside the band of the 1.1 test, takes the slow path
+    // inside the band of the 1.1 test, goes on the slow pass's list (each pixel at most once,
+    // so the list never outgrows its W*H entries)
     if (rechecks > 0 || (accepted >= 2 && fabsf(acc[3] - 1.1f) <= 1.1f * prm.ws_band)) {
-        WindowSums sums{{acc[0], acc[1], acc[2], acc[3], acc[4], acc[5]}, accepted};
-        finish_slow(p, prm, T, tn, tw, r, ei, spatial, s_line, x, y, rechecks, sums);
+        const unsigned long long k = atomicAdd(p.counters + RPD_COUNTER_WINDOW_SLOW_PIXELS, 1ull);
+        p.slow[k] = int32_t(idx);
         return;
     }
     write_blend(p, idx, cmi, acc, accepted);
@@ -894,6 +914,7 @@ cudaError_t launch_statmc(Job& j) {
         e = cudaGetLastError();
     } else {
         const LineTable lt = line_table(prm.table, prm.z);
+        bool tiled = true;
         const size_t limit = size_t(200) * 1024;
         const bool fixed = (r == 3 || r == 5 || r == 7) && (j.statmc_by == 0 || j.statmc_by == kRows) &&
                            tile_bytes(r, kRows) <= limit;
@@ -911,10 +932,17 @@ cudaError_t launch_statmc(Job& j) {
             if (by == 0) {
                 k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
                 e = cudaGetLastError();
+                tiled = false;
             } else {
                 prm.by = by;
                 e = launch_tma<0>(j, prm, lt, by);
             }
+        }
+        if (tiled && e == cudaSuccess) {
+            const int64_t blocks = std::min<int64_t>(kSlowBlocks, (np + kSlowThreads / 32 - 1) / (kSlowThreads / 32));
+            k_statmc_slow<<<unsigned(blocks), kSlowThreads, 0, j.stream>>>(j.p, prm, lt);
+            e = cudaGetLastError();
+            j.launches += 1;
         }
     }
     j.launches += 3;

@@ -93,6 +93,7 @@ struct PixelPlanes {
     int32_t* counts;
     int32_t* active_a;
     int32_t* active_b;
+    int32_t* slow;       // pixels the StatMC window's fast loop handed to its slow pass
     // scratch of the parallel allocation (k_allocate.cu)
     uint8_t* alloc_state;
     unsigned char* alloc_work;

@@ -841,11 +841,12 @@ class Job:
 
     def counters(self) -> dict[str, int]:
         """The job's device counters (rpd_counter): the StatMC window's double-precision
-        rechecks of the last statmc_denoise and the device waits that gave up."""
+        rechecks and slow-pass pixels of the last statmc_denoise, and the device waits that
+        gave up."""
         out = (C.c_uint64 * 8)()
         check(lib().rpd_job_counters(self.handle, out, 8))
         return {"window_pair_rechecks": int(out[0]), "window_pixel_rechecks": int(out[1]),
-                "device_wait_timeouts": int(out[2])}
+                "device_wait_timeouts": int(out[2]), "window_slow_pixels": int(out[3])}
 
 
 class Server:

@@ -1,10 +1,10 @@
 """The fast StatMC window's guard bands and its per-block loops.
 
-The window evaluates each neighbour's Welch compatibility in single precision and sends a
-pixel to the double-precision path (the reference's operations in its order) when one of its
-decisions — q against 25 and against 2 ln 20, df against the t-table switch, the df
-denominator against 1e-8 — lies within the guard band (the neighbour's q is then recomputed in
-double), or its weight sum lies within the band of the 1.1 test (the whole pixel in double). On
+The window evaluates each neighbour's Welch compatibility in single precision and hands a
+pixel to its slow pass (one warp per pixel) when one of its decisions — q against 25 and
+against 2 ln 20, df against the t-table switch, the df denominator against 1e-8 — lies within
+the guard band (the neighbour's q is then recomputed in double, the reference's operations in
+its order), or its weight sum lies within the band of the 1.1 test (the whole pixel in double). On
 the synthetic frames the default band (2^-15) is rarely entered, so these cases widen it
 (RPD_TUNE_WINDOW_GUARD down to 2^0, where most decisions are recomputed) and check that the
 result stays within the plain-form bar of the oracle for every width, and that the rechecks
@@ -49,9 +49,11 @@ def test_guard_band_width(gpu_ctx, w, h, spp, radius, alpha, nan_rate, guard):
     counters = g.counters()
     check_pipeline(g, o, exact_grid=False)
     assert counters["device_wait_timeouts"] == 0
+    assert counters["window_slow_pixels"] <= w * h, counters
     if guard == 0:
         # a band as wide as the decision points themselves: most neighbour decisions were
-        # recomputed in double
+        # recomputed in double, on most pixels
         assert counters["window_pair_rechecks"] > (w * h) // 4, counters
+        assert counters["window_slow_pixels"] > (w * h) // 4, counters
     g.close()
     o.close()
