@@ -233,6 +233,10 @@ struct StatmcParams {
     float df_break;             // 30.5 with a table, 30 with the quantile
     float band;                 // relative guard band of the q and df decisions
     float ws_band;              // relative guard band of the weight_sum >= 1.1 test
+    float den_lim;              // 1e-8 (1 + band): the df denominator's band edge
+    float df_lim;               // df_break * band
+    float q25_lim;              // 25 * band
+    float qacc_lim;             // 2 ln 20 * band
     float rp_below;             // a block whose smallest 1/(n-1) is at least this has every df below df_break
     float rp_above;             // a block whose largest 1/(n-1) is at most this has every df at or above 31
     int by;                     // block rows of the generic-radius tiled kernel
@@ -371,6 +375,16 @@ struct LineTable {
     float2 v[64];
 };
 
+// e^x as 2^(x log2 e) with the PTX base-2 exponential (ex2.approx, relative error about 2^-22):
+// the weights exp(-q/2) carry no decision (the decisions are taken on q), so the stage's 1e-4
+// bar is far away. x = -q/2 is formed as q * (-log2(e) / 2) in one multiplication.
+constexpr float kNegHalfLog2e = -0.72134752044448170368f;
+__device__ __forceinline__ float exp_neg_half(float q) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(q * kNegHalfLog2e));
+    return r;
+}
+
 // The centre pixel's record, held in registers through its window.
 struct Pix {
     float n0, n1, n2;        // unit normal
@@ -382,34 +396,43 @@ struct Pix {
     float r0, r1, r2, r3, r4, r5;  // RPD components
 };
 
-// t critical value of a neighbour's df. MODE 1: the block's df all lie below the table /
-// quantile switch, so the switch is not tested.
+// t critical value of a neighbour's df. MODE 0-2: an alpha with a t table (0.05, 0.01): the
+// line of the half-step table, t = v.y * df + v.x; lines 61-63 hold the normal quantile, so the
+// table also covers df at or above the switch. MODE 3: any other alpha, the normal quantile
+// scaled by sqrt(df / (df - 1)) below df = 30 (main.cpp:214-225).
 template <int MODE>
 __device__ __forceinline__ float t_crit(float df, const float2* __restrict__ line, const StatmcParams& prm) {
-    if (prm.table < 2) {
-        const float dfc = fminf(df, 31.75f);
-        const float fl = __fadd_rd(dfc + dfc, 12582912.0f);  // 1.5 * 2^23: floor(2 df) in the low bits
+    if constexpr (MODE != 3) {
+        // MODE 1: every df is at most (n_i - 1) + (n_j - 1) <= 30, inside the table already
+        const float dfc = MODE == 1 ? df : fminf(df, 31.75f);
+        // 2 dfc is exact, so one rounding down of 2 dfc + 1.5 * 2^23 leaves floor(2 dfc) in the low bits
+        const float fl = __fmaf_rd(dfc, 2.0f, 12582912.0f);
         const float2 l = line[__float_as_int(fl) - 0x4B400000];
         return __fmaf_rn(l.y, dfc, l.x);
+    } else {
+        const float dfc = fmaxf(df, 1.0f);
+        if (dfc < 30.0f) {
+            const float x = __fdividef(dfc, fmaxf(1.0f, dfc - 1.0f));
+            return prm.z * (x * rsqrtf(x));
+        }
+        return prm.z;
     }
-    const float dfc = fmaxf(df, 1.0f);
-    if (MODE == 1 || dfc < 30.0f) {
-        const float x = __fdividef(dfc, fmaxf(1.0f, dfc - 1.0f));
-        return prm.z * (x * rsqrtf(x));
-    }
-    return prm.z;
 }
 
 // One neighbour of the window: gates, Welch q, relaxation, weight, accumulation. MODE 0: any
-// df; 1: every df of the block below the switch; 2: every df at or above 31 (t = z).
+// df (t table); 1: every df of the block below the switch (t table); 2: every df at or above
+// 31 (t = z); 3: any df, normal-quantile alpha.
+// Straight-line: the gates are folded into one predicate (each written as the negation of the
+// reference's `continue` test, so a NaN passes a gate as it does there) and only the
+// accumulation is conditional, so a warp whose lanes leave at different gates runs one path.
 template <int MODE>
 __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int e, float sw, int dx, int dy,
                                       const StatmcParams& prm, const Pix& P, const float2* __restrict__ line,
-                                      float row[6], int& accepted, int& rechecks) {
+                                      float row[6], int& accepted, bool& slow) {
     const float4 G = T[W_GATE * tn + e];
-    if (dot3(P.n0, P.n1, P.n2, G.x, G.y, G.z) < prm.normal_threshold) return;
     const float4 A = T[W_ALB * tn + e];
-    if (!(A.w > 0.0f)) return;  // outside the image or no primary hit
+    bool ok = !(dot3(P.n0, P.n1, P.n2, G.x, G.y, G.z) < prm.normal_threshold);
+    ok = ok && A.w > 0.0f;  // outside the image or no primary hit
     {
         // relative_depth_delta(d_i, d_j) > threshold: fl(|d_i - d_j| / m) against the threshold,
         // decided by the product threshold * m away from it and by the IEEE quotient near it
@@ -422,10 +445,10 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
         bool far;
         if (fabsf(dl) <= tm * kDepthBand || !(tm >= 1e-30f)) far = __fdiv_rn(num, m) > prm.depth_threshold;
         else far = dl > 0.0f;
-        if (far) return;
+        ok = ok && !far;
     }
     const float da0 = P.a0 - A.x, da1 = P.a1 - A.y, da2 = P.a2 - A.z;
-    if (dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold) return;
+    ok = ok && !(dot3(da0, da1, da2, da0, da1, da2) >= prm.albedo_sq_threshold);
 
     const float4 S = T[W_SM * tn + e], V = T[W_SV * tn + e];
     bool exact = false;
@@ -440,15 +463,15 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
         const float den0 = __fmaf_rn(V.x * V.x, rpj, P.v0);
         const float den1 = __fmaf_rn(V.y * V.y, rpj, P.v1);
         const float den2 = __fmaf_rn(V.z * V.z, rpj, P.v2);
-        exact |= fminf(fminf(den0, den1), den2) <= 1e-8f * (1.0f + prm.band);
+        // MODE 1 blocks have every denominator above the band (their smallest term is)
+        if constexpr (MODE != 1) exact |= fminf(fminf(den0, den1), den2) <= prm.den_lim;
         const float df0 = __fdividef(vs0 * vs0, den0);
         const float df1 = __fdividef(vs1 * vs1, den1);
         const float df2 = __fdividef(vs2 * vs2, den2);
-        if constexpr (MODE == 0) {
-            const float lim = prm.df_break * prm.band;
-            exact |= fabsf(df0 - prm.df_break) <= lim;
-            exact |= fabsf(df1 - prm.df_break) <= lim;
-            exact |= fabsf(df2 - prm.df_break) <= lim;
+        if constexpr (MODE == 0 || MODE == 3) {
+            exact |= fabsf(df0 - prm.df_break) <= prm.df_lim;
+            exact |= fabsf(df1 - prm.df_break) <= prm.df_lim;
+            exact |= fabsf(df2 - prm.df_break) <= prm.df_lim;
         }
         const float t0 = t_crit<MODE>(df0, line, prm);
         const float t1 = t_crit<MODE>(df1, line, prm);
@@ -463,28 +486,29 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
     const float adjustment = __saturatef(prm.rpd_scale * shared);
     const float q = __fdividef(qmax, 1.0f + adjustment);
     const bool center = dx == 0 && dy == 0;
-    exact |= fabsf(q - 25.0f) <= 25.0f * prm.band;
-    exact |= !center && fabsf(q - kQAccept) <= kQAccept * prm.band;
+    exact |= fabsf(q - 25.0f) <= prm.q25_lim;
+    exact |= !center && fabsf(q - kQAccept) <= prm.qacc_lim;
     // a decision inside a guard band hands the pixel to the slow pass (k_statmc_slow)
-    rechecks += exact ? 1 : 0;
-    if (q > 25.0f) return;
-    if (!center && q < kQAccept) ++accepted;
-    const float wj = sw * __expf(-0.5f * q);
-    const float4 CM = T[W_CM * tn + e];
-    const float w2 = wj * wj;
-    row[0] = __fmaf_rn(wj, CM.x, row[0]);
-    row[1] = __fmaf_rn(wj, CM.y, row[1]);
-    row[2] = __fmaf_rn(wj, CM.z, row[2]);
-    row[3] += wj;
-    row[4] += w2;
-    row[5] = __fmaf_rn(w2, CM.w, row[5]);
+    slow = slow || (ok && exact);
+    if (ok && !(q > 25.0f)) {
+        if (!center && q < kQAccept) ++accepted;
+        const float wj = sw * exp_neg_half(q);
+        const float4 CM = T[W_CM * tn + e];
+        const float w2 = wj * wj;
+        row[0] = __fmaf_rn(wj, CM.x, row[0]);
+        row[1] = __fmaf_rn(wj, CM.y, row[1]);
+        row[2] = __fmaf_rn(wj, CM.z, row[2]);
+        row[3] += wj;
+        row[4] += w2;
+        row[5] = __fmaf_rn(w2, CM.w, row[5]);
+    }
 }
 
 template <int RC, int MODE>
 __device__ __forceinline__ void window_rows(const float4* __restrict__ T, int tn, int tw, int r,
                                             const float* __restrict__ spatial, const float2* __restrict__ line,
                                             const StatmcParams& prm, const Pix& P, int ei, float acc[6],
-                                            int& accepted, int& rechecks) {
+                                            int& accepted, bool& slow) {
     const int side = 2 * r + 1;
     for (int dy = -r; dy <= r; ++dy) {
         float row[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -493,11 +517,11 @@ __device__ __forceinline__ void window_rows(const float4* __restrict__ T, int tn
         if constexpr (RC > 0) {
 #pragma unroll
             for (int dx = -RC; dx <= RC; ++dx)
-                visit<MODE>(T, tn, erow + dx, srow[dx], dx, dy, prm, P, line, row, accepted, rechecks);
+                visit<MODE>(T, tn, erow + dx, srow[dx], dx, dy, prm, P, line, row, accepted, slow);
         } else {
 #pragma unroll 1
             for (int dx = -r; dx <= r; ++dx)
-                visit<MODE>(T, tn, erow + dx, srow[dx], dx, dy, prm, P, line, row, accepted, rechecks);
+                visit<MODE>(T, tn, erow + dx, srow[dx], dx, dy, prm, P, line, row, accepted, slow);
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) acc[k] += row[k];
@@ -543,16 +567,17 @@ __device__ __forceinline__ void write_blend(const PixelPlanes& p, int64_t idx, f
 // launch, the rare pixel costs one warp's share of a short pass instead of holding the 31
 // other lanes of its warp in the fast loop.
 constexpr int kSlowThreads = 256;
-constexpr int kSlowBlocks = 152 * 8;  // eight blocks on each of GB300's 152 SMs
+constexpr int kSlowBlocks = 152 * 2;  // two blocks on each of GB300's 152 SMs
 
 __global__ void __launch_bounds__(kSlowThreads) k_statmc_slow(PixelPlanes p, StatmcParams prm, LineTable lt) {
     __shared__ float2 s_line[64];
+    const int64_t np = int64_t(prm.w) * prm.h;
+    unsigned long long count = p.counters[RPD_COUNTER_WINDOW_SLOW_PIXELS];
+    if (count == 0) return;  // the usual case on uniform sample counts: the whole block leaves
+    if (count > (unsigned long long)np) count = (unsigned long long)np;
     if (threadIdx.x < 64) s_line[threadIdx.x] = lt.v[threadIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int64_t np = int64_t(prm.w) * prm.h;
-    unsigned long long count = p.counters[RPD_COUNTER_WINDOW_SLOW_PIXELS];
-    if (count > (unsigned long long)np) count = (unsigned long long)np;
     const int r = prm.r, side = 2 * r + 1, visits = side * side;
     const float4* win = p.win;
     const unsigned long long warps = (unsigned long long)gridDim.x * (kSlowThreads / 32);
@@ -597,12 +622,12 @@ __global__ void __launch_bounds__(kSlowThreads) k_statmc_slow(PixelPlanes p, Sta
             const float md[3] = {si.x - S.x, si.y - S.y, si.z - S.z};
             const float den[3] = {__fmaf_rn(V.x * V.x, A.w, vi0), __fmaf_rn(V.y * V.y, A.w, vi1),
                                   __fmaf_rn(V.z * V.z, A.w, vi2)};
-            bool exact = fminf(fminf(den[0], den[1]), den[2]) <= 1e-8f * (1.0f + prm.band);
+            bool exact = fminf(fminf(den[0], den[1]), den[2]) <= prm.den_lim;
             float qmax = 0.0f;
             for (int c = 0; c < 3; ++c) {
                 const float df = __fdividef(vs[c] * vs[c], den[c]);
-                exact |= fabsf(df - prm.df_break) <= prm.df_break * prm.band;
-                const float t = t_crit<0>(df, s_line, prm);
+                exact |= fabsf(df - prm.df_break) <= prm.df_lim;
+                const float t = prm.table < 2 ? t_crit<0>(df, s_line, prm) : t_crit<3>(df, s_line, prm);
                 qmax = fmaxf(qmax, __fdividef(md[c] * md[c], vs[c] * (t * t)));
             }
             float shared = fmaxf(fmaxf(fminf(ri.x, RJ.x), fminf(ri.y, RJ.y)), fmaxf(fminf(ri.z, RJ.z), fminf(ri.w, RJ.w)));
@@ -610,8 +635,8 @@ __global__ void __launch_bounds__(kSlowThreads) k_statmc_slow(PixelPlanes p, Sta
             const float adjustment = __saturatef(prm.rpd_scale * shared);
             const float q = __fdividef(qmax, 1.0f + adjustment);
             const bool center = dx == 0 && dy == 0;
-            exact |= fabsf(q - 25.0f) <= 25.0f * prm.band;
-            exact |= !center && fabsf(q - kQAccept) <= kQAccept * prm.band;
+            exact |= fabsf(q - 25.0f) <= prm.q25_lim;
+            exact |= !center && fabsf(q - kQAccept) <= prm.qacc_lim;
             float wj;
             if (exact) {
                 ++pairs;
@@ -625,7 +650,7 @@ __global__ void __launch_bounds__(kSlowThreads) k_statmc_slow(PixelPlanes p, Sta
             } else {
                 if (q > 25.0f) continue;
                 if (!center && q < kQAccept) ++accepted;
-                wj = __frcp_rn(1.0f + float(dx * dx + dy * dy)) * __expf(-0.5f * q);
+                wj = __frcp_rn(1.0f + float(dx * dx + dy * dy)) * exp_neg_half(q);
             }
             const float4 CM = win[W_CM * np + jn];
             const float w2 = wj * wj;
@@ -664,7 +689,7 @@ __global__ void __launch_bounds__(kTileX * kRows, 3)
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long bar;
     __shared__ float2 s_line[64];
-    __shared__ unsigned s_rpmin, s_rpmax;
+    __shared__ unsigned s_rpmin, s_rpmax, s_dmin;
     __shared__ int s_fail;
     const int r = RC > 0 ? RC : prm.r;
     const int by = RC > 0 ? kRows : prm.by;
@@ -682,6 +707,7 @@ __global__ void __launch_bounds__(kTileX * kRows, 3)
         mbar_init(bar_a, 1);
         s_rpmin = 0x7f800000u;  // +inf
         s_rpmax = 0u;
+        s_dmin = 0x7f800000u;
         s_fail = 0;
     }
     __syncthreads();
@@ -705,26 +731,35 @@ __global__ void __launch_bounds__(kTileX * kRows, 3)
         return;
     }
 
-    // the halo's range of 1/max(n-1, 1) selects the block's loop
-    float lmin = __uint_as_float(0x7f800000u), lmax = 0.0f;
+    // the halo's range of 1/max(n-1, 1) selects the block's loop; so does the smallest term
+    // fl(fl(sv^2) * rp) of a df denominator: every denominator fl(sv_j^2 * rp_j + v_i) is at
+    // least its neighbour's term, so above the band when the smallest term is
+    float lmin = __uint_as_float(0x7f800000u), lmax = 0.0f, dmin = __uint_as_float(0x7f800000u);
     for (int e = tid; e < tn; e += nthreads) {
         const float rp = T[W_ALB * tn + e].w;
         if (rp > 0.0f) {
+            const float4 v = T[W_SV * tn + e];
             lmin = fminf(lmin, rp);
             lmax = fmaxf(lmax, rp);
+            dmin = fminf(dmin, fminf(fminf((v.x * v.x) * rp, (v.y * v.y) * rp), (v.z * v.z) * rp));
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
         lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        dmin = fminf(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
     }
     if ((tid & 31) == 0) {
         atomicMin(&s_rpmin, __float_as_uint(lmin));  // non-negative floats order as their bits
         atomicMax(&s_rpmax, __float_as_uint(lmax));
+        atomicMin(&s_dmin, __float_as_uint(dmin));
     }
     __syncthreads();
-    const int mode = __uint_as_float(s_rpmax) <= prm.rp_above ? 2 : __uint_as_float(s_rpmin) >= prm.rp_below ? 1 : 0;
+    const int mode = __uint_as_float(s_rpmax) <= prm.rp_above                                     ? 2
+                     : prm.table == 2                                                              ? 3
+                     : __uint_as_float(s_rpmin) >= prm.rp_below && __uint_as_float(s_dmin) > prm.den_lim ? 1
+                                                                                                   : 0;
 
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
     if (x >= prm.w || y >= prm.h) return;
@@ -769,19 +804,22 @@ __global__ void __launch_bounds__(kTileX * kRows, 3)
         P.r5 = v.w;
     }
     float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    int accepted = 0, rechecks = 0;
+    int accepted = 0;
+    bool slow = false;
     if (mode == 2)
-        window_rows<RC, 2>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, rechecks);
+        window_rows<RC, 2>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, slow);
     else if (mode == 1)
-        window_rows<RC, 1>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, rechecks);
+        window_rows<RC, 1>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, slow);
+    else if (mode == 3)
+        window_rows<RC, 3>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, slow);
     else
-        window_rows<RC, 0>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, rechecks);
+        window_rows<RC, 0>(T, tn, tw, r, spatial, s_line, prm, P, ei, acc, accepted, slow);
 
     // the blend in single precision from the float sums (relative error ~1e-6, far inside the
     // plain-form bar); a pixel with a decision inside a guard band, or whose weight sum lies
     // inside the band of the 1.1 test, goes on the slow pass's list (each pixel at most once,
     // so the list never outgrows its W*H entries)
-    if (rechecks > 0 || (accepted >= 2 && fabsf(acc[3] - 1.1f) <= 1.1f * prm.ws_band)) {
+    if (slow || (accepted >= 2 && fabsf(acc[3] - 1.1f) <= 1.1f * prm.ws_band)) {
         const unsigned long long k = atomicAdd(p.counters + RPD_COUNTER_WINDOW_SLOW_PIXELS, 1ull);
         p.slow[k] = int32_t(idx);
         return;
@@ -903,6 +941,10 @@ cudaError_t launch_statmc(Job& j) {
     prm.df_break = prm.table < 2 ? 30.5f : 30.0f;
     prm.band = std::ldexp(1.0f, -j.window_guard);
     prm.ws_band = std::ldexp(1.0f, -j.window_guard - 1);
+    prm.den_lim = 1e-8f * (1.0f + prm.band);
+    prm.df_lim = prm.df_break * prm.band;
+    prm.q25_lim = 25.0f * prm.band;
+    prm.qacc_lim = kQAccept * prm.band;
     // df <= (n_i - 1) + (n_j - 1) < 30.5 (table) / 30 (quantile) when every n - 1 <= 15 / 14;
     // df >= min(n_i, n_j) - 1 >= 31 when every n - 1 >= 31
     prm.rp_below = prm.table < 2 ? 1.0f / 15.0f : 1.0f / 14.0f;
