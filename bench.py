@@ -705,6 +705,7 @@ def served_stream(R, ctx, args, rank, dist, n_req, storage):
     queue_ms = np.array([c["admit_ms"] - c["submit_ms"] for c in done])
     return {"value": world * samples / wall_s / 1e6, "samples": samples, "wall_s": wall_s, "stream": stream,
             "done": done, "stats": st1, "launches": int(st1["launches"] - st0["launches"]),
+            "jobs": {k: int(st1[k] - st0[k]) for k in ("jobs_created", "jobs_destroyed", "scratch_grown")},
             "clocks": clocks.summary(),
             "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3),
                            "mean": round(float(lat.mean()), 3), "max": round(float(lat.max()), 3),
@@ -792,7 +793,7 @@ def served_summary(R, ctx, args, rank, dist, n_req, breakdown=True):
            "gpu_launches": fp16["launches"], "clocks": fp16["clocks"],
            "server": {"bytes_peak": fp16["stats"]["bytes_peak"], "bytes_budget": fp16["stats"]["bytes_budget"],
                       "jobs_cached": fp16["stats"]["jobs_cached"], "hbm_budget_gb": args.budget_gb,
-                      "max_inflight": args.inflight}}
+                      "max_inflight": args.inflight, "during_stream": fp16["jobs"]}}
     if breakdown:
         no_dead = plain_prefix(R, ctx, stream, n_plain, skip_dead=True)
         fp32 = served_stream(R, ctx, args, rank, dist, n_req, "fp32")

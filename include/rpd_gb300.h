@@ -660,6 +660,9 @@ typedef struct rpd_server_stats {
     int64_t jobs_cached;
     double now_ms;               /* server clock */
     int64_t launches;            /* kernels enqueued for requests so far */
+    int64_t jobs_created;        /* jobs (per-size arenas) created so far */
+    int64_t jobs_destroyed;      /* cached jobs destroyed to make room for other sizes */
+    int64_t scratch_grown;       /* cached jobs whose push scratch had to grow on reuse */
 } rpd_server_stats;
 
 void rpd_server_config_defaults(rpd_server_config* cfg);

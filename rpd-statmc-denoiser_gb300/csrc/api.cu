@@ -216,11 +216,37 @@ bool device_ok(int device, std::string* why) {
     return true;
 }
 
-int grow_device(Job& j, void** buf, uint64_t* cap, uint64_t need) {
-    if (*cap >= need) return RPD_OK;
-    if (*buf) {
+// A job buffer: from the job's pool in stream order when it has one, else cudaMalloc.
+cudaError_t job_alloc(Job& j, void** p, uint64_t bytes) {
+    if (j.pool) return cudaMallocFromPoolAsync(p, bytes, j.pool, j.stream);
+    return cudaMalloc(p, bytes);
+}
+
+// Frees a job buffer: after the job stream's earlier work (a pool buffer, without synchronising
+// anything), or with cudaFree once that work is done.
+void job_free(Job& j, void* p) {
+    if (!p) return;
+    if (j.pool) {
+        cudaFreeAsync(p, j.stream);
+    } else {
         cudaStreamSynchronize(j.stream);
-        cudaFree(*buf);
+        cudaFree(p);
+    }
+}
+
+// stream_only: the buffer is used on the job's stream alone, so a pool job may replace it in
+// stream order; a buffer that other streams use (the host-push staging) is always replaced
+// after the job's work has finished.
+int grow_device(Job& j, void** buf, uint64_t* cap, uint64_t need, bool stream_only = false) {
+    if (*cap >= need) return RPD_OK;
+    const bool ordered = stream_only && j.pool;
+    if (*buf) {
+        if (ordered) {
+            cudaFreeAsync(*buf, j.stream);
+        } else {
+            cudaStreamSynchronize(j.stream);
+            cudaFree(*buf);
+        }
         j.ctx->in_use -= *cap;
         *buf = nullptr;
         *cap = 0;
@@ -228,7 +254,7 @@ int grow_device(Job& j, void** buf, uint64_t* cap, uint64_t need) {
     const uint64_t want = need + need / 8;
     if (j.ctx->in_use.load() + want > j.ctx->budget)
         return fail(RPD_ERR_OVER_BUDGET, "staging buffer of " + std::to_string(want) + " bytes exceeds the HBM budget");
-    cudaError_t e = cudaMalloc(buf, want);
+    cudaError_t e = ordered ? cudaMallocFromPoolAsync(buf, want, j.pool, j.stream) : cudaMalloc(buf, want);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMalloc staging: ") + cudaGetErrorString(e));
@@ -243,14 +269,13 @@ int ensure_offsets(Job& j, int64_t count) {
     const int64_t need = count + 1 + 2 * ((count + 1023) / 1024) + 4;
     if (j.offsets_cap >= need) return RPD_OK;
     if (j.offsets) {
-        cudaStreamSynchronize(j.stream);
-        cudaFree(j.offsets);
+        job_free(j, j.offsets);
         j.ctx->in_use -= uint64_t(j.offsets_cap) * 8;
         j.offsets = nullptr;
         j.offsets_cap = 0;
     }
     const int64_t want = need + need / 8 + 64;
-    cudaError_t e = cudaMalloc(&j.offsets, uint64_t(want) * 8);
+    cudaError_t e = job_alloc(j, reinterpret_cast<void**>(&j.offsets), uint64_t(want) * 8);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMalloc offsets: ") + cudaGetErrorString(e));
@@ -437,6 +462,18 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!c || !cfg || !out) return fail(RPD_ERR_INVALID_ARGUMENT, "null argument");
     *out = nullptr;
+    Job* j = nullptr;
+    const int st = job_create(c, cfg, nullptr, &j);
+    if (st == RPD_OK) *out = reinterpret_cast<rpd_job*>(j);
+    return st;
+}
+
+}  // extern "C"
+
+namespace rpd {
+
+int job_create(Ctx* c, const rpd_config* cfg, cudaMemPool_t pool, Job** out) {
+    *out = nullptr;
     char msg[256];
     if (rpd_config_validate(cfg, msg, sizeof(msg)) != RPD_OK) return fail(RPD_ERR_INVALID_CONFIG, msg);
     RPD_CUDA(cudaSetDevice(c->device));
@@ -445,21 +482,31 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
     j->ctx = c;
     j->cfg = *cfg;
     j->g = make_geometry(*cfg);
+    j->pool = pool;
     j->arena_bytes = plan(j->g, j->p, j->n, j->cls, &j->pat4, &j->pat2);
+    // the streams first: a pool job's arena is allocated in the order of its stream
+    cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete j;
+        return cuda_fail(e, "job stream");
+    }
     {
         std::lock_guard<std::mutex> lock(c->mu);
         if (c->in_use.load() + j->arena_bytes > c->budget) {
             const uint64_t need = j->arena_bytes;
+            cudaStreamDestroy(j->stream);
             delete j;
             return fail(RPD_ERR_OVER_BUDGET, "job needs " + std::to_string(need) + " bytes of HBM; " +
                                                  std::to_string(c->budget - std::min(c->budget, c->in_use.load())) +
                                                  " left in the budget");
         }
-        cudaError_t e = cudaMalloc(&j->arena, j->arena_bytes);
+        e = job_alloc(*j, &j->arena, j->arena_bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
+            j->arena = nullptr;
+            cudaStreamDestroy(j->stream);
             delete j;
-            return fail(RPD_ERR_OUT_OF_MEMORY, std::string("cudaMalloc job arena: ") + cudaGetErrorString(e));
+            return fail(RPD_ERR_OUT_OF_MEMORY, std::string("job arena: ") + cudaGetErrorString(e));
         }
         c->in_use += j->arena_bytes;
     }
@@ -468,8 +515,7 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
         for (int f = 0; f < 5; ++f) rebase(j->cls[c][f], static_cast<char*>(j->arena));
     rebase(j->pat4, static_cast<char*>(j->arena));
     rebase(j->pat2, static_cast<char*>(j->arena));
-    cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&j->copy_stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithFlags(&j->copy_stream, cudaStreamNonBlocking);
     for (int b = 0; b < Job::kMaxBands && e == cudaSuccess; ++b)
         e = cudaEventCreateWithFlags(&j->band_copied[b], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->staging_free, cudaEventDisableTiming);
@@ -485,9 +531,13 @@ int rpd_job_create(rpd_ctx* ctx, const rpd_config* cfg, rpd_job** out) {
         rpd_job_destroy(reinterpret_cast<rpd_job*>(j));
         return cuda_fail(e, "job set-up");
     }
-    *out = reinterpret_cast<rpd_job*>(j);
+    *out = j;
     return RPD_OK;
 }
+
+}  // namespace rpd
+
+extern "C" {
 
 void rpd_job_destroy(rpd_job* job) {
     Job* j = reinterpret_cast<Job*>(job);
@@ -495,8 +545,9 @@ void rpd_job_destroy(rpd_job* job) {
     cudaSetDevice(j->ctx->device);
     if (j->stream) cudaStreamSynchronize(j->stream);
     if (j->copy_stream) cudaStreamSynchronize(j->copy_stream);
+    // a pool job's buffers go back to the pool in stream order (the streams are idle here)
     if (j->arena) {
-        cudaFree(j->arena);
+        job_free(*j, j->arena);
         j->ctx->in_use -= j->arena_bytes;
     }
     if (j->staging) {
@@ -504,11 +555,11 @@ void rpd_job_destroy(rpd_job* job) {
         j->ctx->in_use -= j->staging_bytes;
     }
     if (j->offsets) {
-        cudaFree(j->offsets);
+        job_free(*j, j->offsets);
         j->ctx->in_use -= uint64_t(j->offsets_cap) * 8;
     }
     if (j->lum) {
-        cudaFree(j->lum);
+        job_free(*j, j->lum);
         j->ctx->in_use -= j->lum_cap;
     }
     if (j->scalars) cudaFreeHost(j->scalars);
@@ -975,7 +1026,7 @@ static int push_tail(Job* j, DeviceSamples& d, int64_t first, int64_t count, int
         const int64_t ns64 = ((std::max<int64_t>(nsamp, 1) + 63) / 64) * 64;
         const bool with_col = counts != nullptr && j->g.w <= 65535;
         void* lum = j->lum;
-        st = grow_device(*j, &lum, &j->lum_cap, uint64_t(ns64) * (with_col ? 10 : 8) + 256);
+        st = grow_device(*j, &lum, &j->lum_cap, uint64_t(ns64) * (with_col ? 10 : 8) + 256, true);
         if (st != RPD_OK) return st;
         j->lum = static_cast<float*>(lum);
         gp.key = reinterpret_cast<uint32_t*>(j->lum + ns64);
@@ -1768,7 +1819,7 @@ int job_reserve(Job& j, int64_t max_push_samples) {
     if (j.cfg.rpf_shrinkage_scale > 0.0f && !j.exact_grid) {
         void* lum = j.lum;
         const int64_t ns64 = ((std::max<int64_t>(max_push_samples, 1) + 63) / 64) * 64;
-        st = grow_device(j, &lum, &j.lum_cap, uint64_t(ns64) * 10 + 256);
+        st = grow_device(j, &lum, &j.lum_cap, uint64_t(ns64) * 10 + 256, true);
         j.lum = static_cast<float*>(lum);
     }
     return st;

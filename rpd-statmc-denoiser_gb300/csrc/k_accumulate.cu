@@ -778,7 +778,14 @@ __global__ void k_merge_grid(double* grid, double* pass_grid, int64_t n) {
     } else {
         v = pass_grid[i];
     }
-    grid[i] = FRESH ? 0.0 + v : grid[i] + v;
+    if (FRESH) {
+        // 0 + v without a double-precision add (GB300 runs those at a small fraction of its
+        // single-precision rate): the same value, with -0 turned into +0
+        const long long b = __double_as_longlong(v);
+        grid[i] = __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+    } else {
+        grid[i] = grid[i] + v;
+    }
     pass_grid[i] = 0.0;
 }
 

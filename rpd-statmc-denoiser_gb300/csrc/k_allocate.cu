@@ -1289,7 +1289,7 @@ __device__ void phase_decide_round(const CoopArgs& a, double R0, int Rs0, int fb
 
 }  // namespace
 
-__global__ void __launch_bounds__(kAT, 1) k_allocate_coop(CoopArgs a) {
+__global__ void __launch_bounds__(kAT, 2) k_allocate_coop(CoopArgs a) {
     __shared__ Shared sh;
     AllocScalars* sc = a.sc;
     const int G = gridDim.x;

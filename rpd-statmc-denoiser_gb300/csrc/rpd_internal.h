@@ -136,6 +136,10 @@ struct Job {
     rpd_config cfg{};
     Geometry g{};
     cudaStream_t stream = nullptr;
+    // set (jobs of the serving loop): the arena, the offsets and the push scratch come from this
+    // memory pool in the order of the job's stream, so creating, growing and destroying them
+    // never synchronises the device (cudaFree does), which would drain every other request
+    cudaMemPool_t pool = nullptr;
     void* arena = nullptr;       // one allocation holding every plane
     uint64_t arena_bytes = 0;
     PixelPlanes p{};
@@ -379,6 +383,9 @@ cudaError_t launch_metrics(const Img3& ref, const Img3& tst, int w, int h, void*
 // that later pushes allocate nothing; push_device_async takes device planes and, with device
 // counts, a bound on the push's sample total instead of reading the total back.
 int job_reserve(Job& j, int64_t max_push_samples);
+// rpd_job_create with the job's device memory from `pool` (nullptr: cudaMalloc, as
+// rpd_job_create does); rpd_job_destroy releases either kind.
+int job_create(Ctx* c, const rpd_config* cfg, cudaMemPool_t pool, Job** out);
 // offsets_ready: j.offsets already holds the push's offsets (a scan of the same counts).
 int push_device_async(Job& j, const DeviceSamples& d, int64_t first, int64_t count, int32_t spp, const int32_t* counts,
                       int64_t total_bound, bool offsets_ready = false);

@@ -270,6 +270,7 @@ struct Server {
     uint64_t next_id = 1;
     int64_t submitted = 0, completed = 0, rejected = 0;
     uint64_t launches = 0;              // kernels enqueued for requests
+    int64_t jobs_created = 0, jobs_destroyed = 0, scratch_grown = 0;
     double kernel_ms[RPD_KERNEL_COUNT_] = {};  // profile: per kernel family over finished requests
     uint64_t kernel_n[RPD_KERNEL_COUNT_] = {};
     uint64_t reserved = 0, peak = 0;    // request buffers + cached jobs
@@ -329,6 +330,7 @@ bool make_room(Server& s, uint64_t need, std::pair<int, int> keep) {
         if (victim == s.idle_jobs.end()) victim = s.idle_jobs.begin();
         if (victim == s.idle_jobs.end()) return false;
         rpd_job_destroy(reinterpret_cast<rpd_job*>(victim->second.job));
+        ++s.jobs_destroyed;
         s.reserved -= victim->second.bytes;
         s.idle_jobs.erase(victim);
     }
@@ -511,7 +513,9 @@ int acquire_job(Server& s, Request& r, Job** out) {
         Job* j = it->second.job;
         uint64_t bytes = it->second.bytes;
         s.idle_jobs.erase(it);
+        const uint64_t caps = j->lum_cap + j->offsets_cap;
         const int st = job_reserve(*j, need_span);
+        if (j->lum_cap + j->offsets_cap != caps) ++s.scratch_grown;
         if (st != RPD_OK) {
             rpd_job_destroy(reinterpret_cast<rpd_job*>(j));
             s.reserved -= bytes;
@@ -523,10 +527,13 @@ int acquire_job(Server& s, Request& r, Job** out) {
         *out = j;
         return RPD_OK;
     }
-    rpd_job* h = nullptr;
-    int st = rpd_job_create(reinterpret_cast<rpd_ctx*>(s.ctx), &c, &h);
+    // the job's memory from the server's pool, in the order of its stream: creating, growing and
+    // destroying cached jobs then never synchronises the device while other requests run
+    Job* j = nullptr;
+    int st = job_create(s.ctx, &c, s.pool, &j);
     if (st != RPD_OK) return st;
-    Job* j = reinterpret_cast<Job*>(h);
+    rpd_job* h = reinterpret_cast<rpd_job*>(j);
+    ++s.jobs_created;
     if (s.cfg.profile) rpd_job_set_profiling(h, 1);
     if (s.cfg.allocator_blocks >= 2) rpd_job_set_tuning(h, RPD_TUNE_ALLOCATOR, s.cfg.allocator_blocks);
     st = job_reserve(*j, need_span);
@@ -630,10 +637,13 @@ void worker_loop(Server* sp) {
             const uint64_t out_bytes = uint64_t(r->req.width) * r->req.height * 12;
             int st = RPD_OK;
             if (!r->req.denoised_out && sl.staging_bytes < out_bytes) {
+                // at least doubled, so a slot's staging is replaced a few times at most (freeing
+                // page-locked memory may wait for the device)
+                const uint64_t grow = std::max<uint64_t>(out_bytes, 2 * sl.staging_bytes);
                 if (sl.staging) cudaFreeHost(sl.staging);
                 sl.staging = nullptr;
                 sl.staging_bytes = 0;
-                if (cudaMallocHost(&sl.staging, out_bytes) == cudaSuccess) sl.staging_bytes = out_bytes;
+                if (cudaMallocHost(&sl.staging, grow) == cudaSuccess) sl.staging_bytes = grow;
                 else st = cuda_fail(cudaErrorMemoryAllocation, "pinned result buffer");
             }
             if (st == RPD_OK) st = acquire_job(s, *r, &r->job);
@@ -857,6 +867,9 @@ int rpd_server_get_stats(rpd_server* srv, rpd_server_stats* out) {
     out->jobs_cached = int64_t(s->idle_jobs.size() + s->busy_jobs.size());
     out->now_ms = s->now_ms();
     out->launches = int64_t(s->launches);
+    out->jobs_created = s->jobs_created;
+    out->jobs_destroyed = s->jobs_destroyed;
+    out->scratch_grown = s->scratch_grown;
     return RPD_OK;
 }
 

@@ -173,7 +173,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("rejected", C.c_int64), ("queued", C.c_int64),
                 ("inflight", C.c_int64), ("bytes_reserved", C.c_uint64), ("bytes_peak", C.c_uint64),
                 ("bytes_budget", C.c_uint64), ("jobs_cached", C.c_int64), ("now_ms", C.c_double),
-                ("launches", C.c_int64)]
+                ("launches", C.c_int64), ("jobs_created", C.c_int64), ("jobs_destroyed", C.c_int64),
+                ("scratch_grown", C.c_int64)]
 
 
 STORAGE = {"fp32": 0, "fp16": 1}
