@@ -375,6 +375,15 @@ struct LineTable {
     float2 v[64];
 };
 
+// a / b as a times the PTX approximate reciprocal of b (rcp.approx: at most 1 ulp from 1/b over
+// the full range, subnormal b flushed); every decision taken on a quotient has a guard band
+// thousands of ulps wide.
+__device__ __forceinline__ float div_approx(float a, float b) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+    return a * r;
+}
+
 // e^x as 2^(x log2 e) with the PTX base-2 exponential (ex2.approx, relative error about 2^-22):
 // the weights exp(-q/2) carry no decision (the decisions are taken on q), so the stage's 1e-4
 // bar is far away. x = -q/2 is formed as q * (-log2(e) / 2) in one multiplication.
@@ -412,7 +421,7 @@ __device__ __forceinline__ float t_crit(float df, const float2* __restrict__ lin
     } else {
         const float dfc = fmaxf(df, 1.0f);
         if (dfc < 30.0f) {
-            const float x = __fdividef(dfc, fmaxf(1.0f, dfc - 1.0f));
+            const float x = div_approx(dfc, fmaxf(1.0f, dfc - 1.0f));
             return prm.z * (x * rsqrtf(x));
         }
         return prm.z;
@@ -456,7 +465,7 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
     const float md0 = P.sm0 - S.x, md1 = P.sm1 - S.y, md2 = P.sm2 - S.z;
     float qmax;
     if constexpr (MODE == 2) {
-        qmax = fmaxf(fmaxf(__fdividef(md0 * md0, vs0), __fdividef(md1 * md1, vs1)), __fdividef(md2 * md2, vs2)) *
+        qmax = fmaxf(fmaxf(div_approx(md0 * md0, vs0), div_approx(md1 * md1, vs1)), div_approx(md2 * md2, vs2)) *
                prm.inv_z2;
     } else {
         const float rpj = A.w;
@@ -465,9 +474,9 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
         const float den2 = __fmaf_rn(V.z * V.z, rpj, P.v2);
         // MODE 1 blocks have every denominator above the band (their smallest term is)
         if constexpr (MODE != 1) exact |= fminf(fminf(den0, den1), den2) <= prm.den_lim;
-        const float df0 = __fdividef(vs0 * vs0, den0);
-        const float df1 = __fdividef(vs1 * vs1, den1);
-        const float df2 = __fdividef(vs2 * vs2, den2);
+        const float df0 = div_approx(vs0 * vs0, den0);
+        const float df1 = div_approx(vs1 * vs1, den1);
+        const float df2 = div_approx(vs2 * vs2, den2);
         if constexpr (MODE == 0 || MODE == 3) {
             exact |= fabsf(df0 - prm.df_break) <= prm.df_lim;
             exact |= fabsf(df1 - prm.df_break) <= prm.df_lim;
@@ -476,15 +485,15 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
         const float t0 = t_crit<MODE>(df0, line, prm);
         const float t1 = t_crit<MODE>(df1, line, prm);
         const float t2 = t_crit<MODE>(df2, line, prm);
-        qmax = fmaxf(fmaxf(__fdividef(md0 * md0, vs0 * (t0 * t0)), __fdividef(md1 * md1, vs1 * (t1 * t1))),
-                     __fdividef(md2 * md2, vs2 * (t2 * t2)));
+        qmax = fmaxf(fmaxf(div_approx(md0 * md0, vs0 * (t0 * t0)), div_approx(md1 * md1, vs1 * (t1 * t1))),
+                     div_approx(md2 * md2, vs2 * (t2 * t2)));
     }
     // rpf::shared_reliability + relax_compatibility (core/stats.h:56-78)
     const float4 RJ = T[W_RPD * tn + e];
     float shared = fmaxf(fmaxf(fminf(P.r0, RJ.x), fminf(P.r1, RJ.y)), fmaxf(fminf(P.r2, RJ.z), fminf(P.r3, RJ.w)));
     shared = __saturatef(fmaxf(shared, fmaxf(fminf(P.r4, S.w), fminf(P.r5, V.w))));
     const float adjustment = __saturatef(prm.rpd_scale * shared);
-    const float q = __fdividef(qmax, 1.0f + adjustment);
+    const float q = div_approx(qmax, 1.0f + adjustment);
     const bool center = dx == 0 && dy == 0;
     exact |= fabsf(q - 25.0f) <= prm.q25_lim;
     exact |= !center && fabsf(q - kQAccept) <= prm.qacc_lim;
@@ -625,15 +634,15 @@ __global__ void __launch_bounds__(kSlowThreads) k_statmc_slow(PixelPlanes p, Sta
             bool exact = fminf(fminf(den[0], den[1]), den[2]) <= prm.den_lim;
             float qmax = 0.0f;
             for (int c = 0; c < 3; ++c) {
-                const float df = __fdividef(vs[c] * vs[c], den[c]);
+                const float df = div_approx(vs[c] * vs[c], den[c]);
                 exact |= fabsf(df - prm.df_break) <= prm.df_lim;
                 const float t = prm.table < 2 ? t_crit<0>(df, s_line, prm) : t_crit<3>(df, s_line, prm);
-                qmax = fmaxf(qmax, __fdividef(md[c] * md[c], vs[c] * (t * t)));
+                qmax = fmaxf(qmax, div_approx(md[c] * md[c], vs[c] * (t * t)));
             }
             float shared = fmaxf(fmaxf(fminf(ri.x, RJ.x), fminf(ri.y, RJ.y)), fmaxf(fminf(ri.z, RJ.z), fminf(ri.w, RJ.w)));
             shared = __saturatef(fmaxf(shared, fmaxf(fminf(si.w, S.w), fminf(vi.w, V.w))));
             const float adjustment = __saturatef(prm.rpd_scale * shared);
-            const float q = __fdividef(qmax, 1.0f + adjustment);
+            const float q = div_approx(qmax, 1.0f + adjustment);
             const bool center = dx == 0 && dy == 0;
             exact |= fabsf(q - 25.0f) <= prm.q25_lim;
             exact |= !center && fabsf(q - kQAccept) <= prm.qacc_lim;
