@@ -318,6 +318,14 @@ __device__ __forceinline__ void acc_store_empty(const GridPrep& gp, int64_t idx)
     gp.pat2[idx] = make_float2(0.0f, __uint_as_float(uint32_t(kPixUniform) << 8));
 }
 
+__device__ __forceinline__ void acc_zero(PixelAcc& a) {
+    a.mean = a.m2 = 0.0f;
+    a.n = 0;
+    for (int c = 0; c < 3; ++c) a.cm[c] = a.sm[c] = a.sq[c] = a.rad[c] = a.nor[c] = a.alb[c] = 0.0f;
+    a.dep = 0.0f;
+    a.hits = a.nsamples = 0;
+}
+
 __device__ __forceinline__ void acc_load(PixelAcc& a, const PixelPlanes& p, int64_t idx) {
     a.mean = p.mean[idx];
     a.m2 = p.square_diff[idx];
@@ -385,7 +393,8 @@ __device__ __forceinline__ void acc_store(const PixelAcc& a, const PixelPlanes& 
 // bytes) per load. MINB: resident blocks per SM the register allocation must allow.
 template <bool VEC4, bool COMPACT, bool WIDE, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, DeviceSamples s, const int64_t* offsets,
-                                                           int32_t spp, int64_t first, int64_t count, GridPrep gp) {
+                                                           int32_t spp, int64_t first, int64_t count, GridPrep gp,
+                                                           int fresh) {
     const int64_t local = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (local >= count) return;
     const int64_t idx = first + local;
@@ -409,7 +418,9 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
         if (prep) acc_store_empty(gp, idx);
         return;
     }
-    acc_load(a, p, idx);
+    // fresh: the frame's first push over every pixel, whose statistics the frame start zeroed
+    if (fresh) acc_zero(a);
+    else acc_load(a, p, idx);
     const bool per_sample_albedo = !COMPACT && s.albedo[0] != nullptr;
     float palb[3] = {0.0f, 0.0f, 0.0f};
     if (COMPACT) {
@@ -868,6 +879,10 @@ const int64_t* offsets_count_max(const Job& j, int64_t count) {
 cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t first, int64_t count,
                                      const GridPrep& gp, int32_t spp) {
     KernelScope ks(j, RPD_KERNEL_ACCUMULATE_PIXELS);
+    // the frame's first push over every pixel starts from the zeros the frame start wrote
+    // instead of reading them
+    const int fresh = (j.acc_zero && first == 0 && count == j.g.np) ? 1 : 0;
+    j.acc_zero = false;
     auto aligned = [](const void* ptr, uintptr_t a) { return (reinterpret_cast<uintptr_t>(ptr) & (a - 1)) == 0; };
     bool vec4 = spp > 0 && spp % 4 == 0 && aligned(s.flags, 16) && (!s.category || aligned(s.category, 16));
     if (s.compact) {
@@ -905,20 +920,20 @@ cudaError_t launch_accumulate_pixels(Job& j, const DeviceSamples& s, int64_t fir
                    (!h.brdf_u[0] || aligned(h.brdf_u[c], 16)) && (!h.light_u[0] || aligned(h.light_u[c], 16)) &&
                    (!h.env_u[0] || aligned(h.env_u[c], 16));
         if (wide)
-            k_accumulate_pixels<true, true, true, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<true, true, true, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp, fresh);
         else if (vec4 && many)
-            k_accumulate_pixels<true, true, false, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<true, true, false, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp, fresh);
         else if (vec4)
-            k_accumulate_pixels<true, true, false, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<true, true, false, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp, fresh);
         else
-            k_accumulate_pixels<false, true, false, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<false, true, false, 4><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp, fresh);
     } else {
         if (vec4 && many)
-            k_accumulate_pixels<true, false, false, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<true, false, false, 1><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp, fresh);
         else if (vec4)
-            k_accumulate_pixels<true, false, false, 3><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<true, false, false, 3><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp, fresh);
         else
-            k_accumulate_pixels<false, false, false, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp);
+            k_accumulate_pixels<false, false, false, 5><<<blocks, 128, 0, j.stream>>>(j.p, s, j.offsets, 0, first, count, gp, fresh);
     }
     j.launches += 1;
     return cudaGetLastError();

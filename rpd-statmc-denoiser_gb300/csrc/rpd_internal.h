@@ -175,6 +175,7 @@ struct Job {
     bool smooth_fp64 = false;       // RPD_TUNE_SMOOTHING = 1: the importance smoothing in double-precision instructions
     int allocator_blocks = 0;       // RPD_TUNE_ALLOCATOR >= 2: blocks of the parallel allocation
     bool pass_open = false;
+    bool acc_zero = false;      // the per-pixel statistics are the frame start's zeros (no push yet)
     bool host_async = false;  // the current host push returns before its copies complete
     bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)
     bool features_valid = false;
