@@ -393,6 +393,12 @@ __device__ __forceinline__ float exp_neg_half(float q) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(q * kNegHalfLog2e));
     return r;
 }
+// sw * e^(-q/2) as one base-2 exponential, with l2sw = log2(sw)
+__device__ __forceinline__ float weight_of(float q, float l2sw) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__fmaf_rn(q, kNegHalfLog2e, l2sw)));
+    return r;
+}
 
 // The centre pixel's record, held in registers through its window.
 struct Pix {
@@ -435,7 +441,7 @@ __device__ __forceinline__ float t_crit(float df, const float2* __restrict__ lin
 // reference's `continue` test, so a NaN passes a gate as it does there) and only the
 // accumulation is conditional, so a warp whose lanes leave at different gates runs one path.
 template <int MODE>
-__device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int e, float sw, int dx, int dy,
+__device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int e, float l2sw, int dx, int dy,
                                       const StatmcParams& prm, const Pix& P, const float2* __restrict__ line,
                                       float row[6], int& accepted, bool& slow) {
     const float4 G = T[W_GATE * tn + e];
@@ -452,7 +458,8 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
         const float tm = prm.depth_threshold * m;
         const float dl = num - tm;
         bool far;
-        if (fabsf(dl) <= tm * kDepthBand || !(tm >= 1e-30f)) far = __fdiv_rn(num, m) > prm.depth_threshold;
+        // tm >= 1e-30 here: thresholds below 1e-21 take the exact window (m >= 1e-8)
+        if (fabsf(dl) <= tm * kDepthBand) far = __fdiv_rn(num, m) > prm.depth_threshold;
         else far = dl > 0.0f;
         ok = ok && !far;
     }
@@ -501,7 +508,7 @@ __device__ __forceinline__ void visit(const float4* __restrict__ T, int tn, int 
     slow = slow || (ok && exact);
     if (ok && !(q > 25.0f)) {
         if (!center && q < kQAccept) ++accepted;
-        const float wj = sw * exp_neg_half(q);
+        const float wj = weight_of(q, l2sw);
         const float4 CM = T[W_CM * tn + e];
         const float w2 = wj * wj;
         row[0] = __fmaf_rn(wj, CM.x, row[0]);
@@ -726,7 +733,8 @@ __global__ void __launch_bounds__(kTileX * kRows, 3)
     if (tid < 64) s_line[tid] = lt.v[tid];
     for (int e = tid; e < side * side; e += nthreads) {
         const int dx = e % side - r, dy = e / side - r;
-        spatial[e] = __frcp_rn(1.0f + float(dx * dx + dy * dy));  // 1 / (1 + d^2), main.cpp:1094
+        // log2 of 1 / (1 + d^2) (main.cpp:1094): the weight is then one base-2 exponential
+        spatial[e] = log2f(__frcp_rn(1.0f + float(dx * dx + dy * dy)));
     }
     if (!mbar_wait_bounded(bar_a, 0)) s_fail = 1;
     __syncthreads();
@@ -960,7 +968,9 @@ cudaError_t launch_statmc(Job& j) {
     prm.rp_above = 1.0f / 31.0f;
     cudaError_t e = cudaSuccess;
     const int r = prm.r;
-    if (j.exact_window || r > 16) {
+    // the fast window decides the depth gate through threshold * m, which for m >= 1e-8 stays a
+    // normal float away from 0 only when the threshold is at least about 1e-21
+    if (j.exact_window || r > 16 || !(prm.depth_threshold >= 1e-21f)) {
         k_statmc_window<<<grid_for(np, 128), 128, 0, j.stream>>>(j.p, prm);
         e = cudaGetLastError();
     } else {
