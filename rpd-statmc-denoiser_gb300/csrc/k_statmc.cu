@@ -29,9 +29,9 @@
 //                          (2^-15 relative by default) of a decision point — q = 25 (reject),
 //                          q = 2 ln 20 (the accepted-neighbour count), the df of the t-table /
 //                          normal-quantile switch, or the 1e-8 df-denominator test — the
-//                          pixel goes on a list for k_statmc_slow (rare on uniform sample
-//                          counts, a few per cent of pixels where adaptive passes mix the
-//                          counts so that df crosses the t-table switch);
+//                          pixel goes on a list for k_statmc_slow (none on the uniform 16-spp
+//                          frame; about 0.1 % of the pixels after three adaptive passes, where
+//                          mixed counts put some df near the t-table switch);
 //                        * each block picks a specialised loop from the range of 1/(n-1) over
 //                          its halo: when every pair's df lies below the t-table switch
 //                          (df <= (n_i - 1) + (n_j - 1)) no neighbour needs the switch test, and
@@ -46,7 +46,7 @@
 //                      the 1.1 test's band.
 //   k_statmc_window    the whole window in double, the reference's operations in its order
 //                      (the exact mode, and the path for radii whose halo tile would not fit in
-//                      shared memory).
+//                      shared memory and for depth thresholds below 1e-21).
 
 #include <algorithm>
 #include <cmath>
