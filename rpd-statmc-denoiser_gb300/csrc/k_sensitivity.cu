@@ -19,12 +19,75 @@ namespace rpd {
 
 namespace {
 
+// ---- the per-bin sums of compute_sensitivity in double-float ---------------------------------
+// GB300 executes double precision at a small fraction of its single-precision rate, and the
+// sixteen bins' quotients and squares are most of this pass's double work. With the grid in
+// its double-float mode (itself within 1e-9 of the reference's double sums) the bin loop runs on
+// pairs of floats (about 2^-44 relative), the scalars around it stay in double.
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }  // k in [-126, 127]
+// |a| >= |b|
+__device__ __forceinline__ F2 f2_fast(float a, float b) {
+    const float s = a + b;
+    return F2{s, b - (s - a)};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float e = ((a.h - (s - bb)) + (b.h - bb)) + (a.l + b.l);
+    return f2_fast(s, e);
+}
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    const float p = a.h * b.h;
+    const float e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.h, -p)));
+    return f2_fast(p, e);
+}
+// a / b: a quotient from the float reciprocal, corrected once by the double-float remainder
+__device__ __forceinline__ F2 f2_div(F2 a, F2 b) {
+    float rb;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rb) : "f"(b.h));
+    const float q1 = a.h * rb;
+    const F2 bq = f2_mul(b, F2{q1, 0.0f});
+    const F2 r = f2_add(a, F2{-bq.h, -bq.l});
+    return f2_fast(q1, r.h * rb);
+}
+// d as hi + lo, hi = RN_float(d), lo = RN_float(d - hi), in integer operations; false when
+// |d| lies outside [2^-60, 2^61) (the double loop then takes the dependency)
+__device__ __forceinline__ bool f2_split(double d, F2& out) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
+    if ((b << 1) == 0ull) {
+        out = F2{0.0f, 0.0f};
+        return true;
+    }
+    const int e = int((b >> 52) & 0x7ffull) - 1023;
+    if (e < -60 || e > 60) return false;
+    const unsigned sign = unsigned(b >> 63);
+    const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);  // 53-bit significand
+    unsigned long long mh = m >> 29;                                     // its top 24 bits
+    long long rem = static_cast<long long>(m & ((1ull << 29) - 1ull));   // the rest, units of 2^(e-52)
+    if (rem > (1ll << 28) || (rem == (1ll << 28) && (mh & 1ull))) {      // round to nearest, ties to even
+        ++mh;
+        rem -= 1ll << 29;
+    }
+    int eh = e;
+    if (mh == (1ull << 24)) {
+        mh >>= 1;
+        ++eh;
+    }
+    out.h = __int_as_float(int((sign << 31) | (unsigned(eh + 127) << 23) | unsigned(mh & 0x7fffffull)));
+    out.l = __ll2float_rn(sign ? -rem : rem) * pow2f(e - 52);
+    return true;
+}
+
 __device__ __forceinline__ double sample_mass(const double* d) {
     return d[33] > 0.0 ? d[32] * d[32] / d[33] : 0.0;
 }
 
-// BinnedDependency::compute_sensitivity (core/stats.h:115-137)
-__device__ float compute_sensitivity(const double* d, int bins) {
+// BinnedDependency::compute_sensitivity (core/stats.h:115-137). df_bins: the between-bin sum in
+// double-float (the grid's fast mode), else in double as the reference sums it.
+__device__ float compute_sensitivity(const double* d, int bins, bool df_bins) {
     const double kEps = 1e-18;
     const double effective_n = sample_mass(d);
     if (effective_n <= 2.0) return 0.0f;
@@ -33,11 +96,35 @@ __device__ float compute_sensitivity(const double* d, int bins) {
     if (total <= kEps) return 0.0f;
     int active = 0;
     double between = 0.0;
-    for (int b = 0; b < bins; ++b) {
-        if (d[b] <= kEps) continue;
-        ++active;
-        const double delta = d[16 + b] / d[b] - mean;
-        between += d[b] * delta * delta;
+    F2 mf;
+    if (df_bins && f2_split(mean, mf)) {
+        const F2 nmean{-mf.h, -mf.l};
+        F2 acc{0.0f, 0.0f};
+        bool ok = true;
+        for (int b = 0; b < bins && ok; ++b) {
+            if (d[b] <= kEps) continue;
+            ++active;
+            F2 w, sy;
+            ok = f2_split(d[b], w) && f2_split(d[16 + b], sy);
+            const F2 delta = f2_add(f2_div(sy, w), nmean);
+            acc = f2_add(acc, f2_mul(w, f2_mul(delta, delta)));
+        }
+        if (ok) {
+            between = double(acc.h) + double(acc.l);
+        } else {
+            active = 0;
+            df_bins = false;  // a value outside the split's range: the double loop below
+        }
+    } else {
+        df_bins = false;
+    }
+    if (!df_bins) {
+        for (int b = 0; b < bins; ++b) {
+            if (d[b] <= kEps) continue;
+            ++active;
+            const double delta = d[16 + b] / d[b] - mean;
+            between += d[b] * delta * delta;
+        }
     }
     if (active < 2 || effective_n <= double(active)) return 0.0f;
     const double eta2 = dclamps(between / total, 0.0, 1.0);
@@ -90,14 +177,14 @@ __device__ void local_avg3(float* const* v, int w, int h, int cx, int cy, float 
 // One thread per (node, task): tasks 0 .. R_FIELDS-1 are the dependencies' sensitivity and
 // confidence, task R_FIELDS the node's features (blockIdx.y). The tasks are independent, so the
 // double-precision chains of a node run side by side instead of one after another.
-__global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0) {
+__global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0, int df_bins) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= g.nn) return;
     const int f = int(blockIdx.y);
     if (f < R_FIELDS) {
         const int d = c_raw_dep[f];
         const double* dep = n.grid + idx * kDeps * kDepStride + d * kDepStride;
-        n.raw[f][idx] = compute_sensitivity(dep, d == D_RR ? 2 : 16);
+        n.raw[f][idx] = compute_sensitivity(dep, d == D_RR ? 2 : 16, df_bins != 0);
         const double mass = sample_mass(dep);
         n.conf[f][idx] = float(mass / (mass + double(n0)));
         return;
@@ -261,8 +348,8 @@ __global__ void k_expand(Geometry g, const float* tiles, float* out) {
 cudaError_t launch_sensitivity(Job& j) {
     {
         KernelScope ks(j, RPD_KERNEL_NODE_STATS);
-        k_node_stats<<<dim3(grid_for(j.g.nn, 128), R_FIELDS + 1), 128, 0, j.stream>>>(j.g, j.n, j.p,
-                                                                                    j.cfg.rpf_confidence_samples);
+        k_node_stats<<<dim3(grid_for(j.g.nn, 128), R_FIELDS + 1), 128, 0, j.stream>>>(
+            j.g, j.n, j.p, j.cfg.rpf_confidence_samples, j.exact_grid ? 0 : 1);
     }
     {
         KernelScope ks(j, RPD_KERNEL_NODE_COMBINE);
