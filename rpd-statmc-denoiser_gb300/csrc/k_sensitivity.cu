@@ -85,9 +85,8 @@ __device__ __forceinline__ double sample_mass(const double* d) {
     return d[33] > 0.0 ? d[32] * d[32] / d[33] : 0.0;
 }
 
-// BinnedDependency::compute_sensitivity (core/stats.h:115-137). df_bins: the between-bin sum in
-// double-float (the grid's fast mode), else in double as the reference sums it.
-__device__ float compute_sensitivity(const double* d, int bins, bool df_bins) {
+// BinnedDependency::compute_sensitivity (core/stats.h:115-137), in double as the reference sums it.
+__device__ float compute_sensitivity(const double* d, int bins) {
     const double kEps = 1e-18;
     const double effective_n = sample_mass(d);
     if (effective_n <= 2.0) return 0.0f;
@@ -96,40 +95,62 @@ __device__ float compute_sensitivity(const double* d, int bins, bool df_bins) {
     if (total <= kEps) return 0.0f;
     int active = 0;
     double between = 0.0;
-    F2 mf;
-    if (df_bins && f2_split(mean, mf)) {
-        const F2 nmean{-mf.h, -mf.l};
-        F2 acc{0.0f, 0.0f};
-        bool ok = true;
-        for (int b = 0; b < bins && ok; ++b) {
-            if (d[b] <= kEps) continue;
-            ++active;
-            F2 w, sy;
-            ok = f2_split(d[b], w) && f2_split(d[16 + b], sy);
-            const F2 delta = f2_add(f2_div(sy, w), nmean);
-            acc = f2_add(acc, f2_mul(w, f2_mul(delta, delta)));
-        }
-        if (ok) {
-            between = double(acc.h) + double(acc.l);
-        } else {
-            active = 0;
-            df_bins = false;  // a value outside the split's range: the double loop below
-        }
-    } else {
-        df_bins = false;
-    }
-    if (!df_bins) {
-        for (int b = 0; b < bins; ++b) {
-            if (d[b] <= kEps) continue;
-            ++active;
-            const double delta = d[16 + b] / d[b] - mean;
-            between += d[b] * delta * delta;
-        }
+    for (int b = 0; b < bins; ++b) {
+        if (d[b] <= kEps) continue;
+        ++active;
+        const double delta = d[16 + b] / d[b] - mean;
+        between += d[b] * delta * delta;
     }
     if (active < 2 || effective_n <= double(active)) return 0.0f;
     const double eta2 = dclamps(between / total, 0.0, 1.0);
     const double adjusted = dmaxs(0.0, 1.0 - (1.0 - eta2) * (effective_n - 1.0) / (effective_n - active));
     return float(sqrt(adjusted));
+}
+
+__device__ __forceinline__ bool f2_le(F2 a, float c) { return a.h < c || (a.h == c && a.l <= 0.0f); }
+__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, F2{-b.h, -b.l}); }
+__device__ __forceinline__ double f2_double(F2 a) { return double(a.h) + double(a.l); }
+
+// compute_sensitivity and the node's confidence, sample_mass / (sample_mass + n0), with every
+// quotient, product and the square root in double-float (about 2^-44 relative; the results are
+// floats). False when a grid value lies outside the split's range: the caller then takes the
+// double path. Decisions follow the reference's tests in its order.
+__device__ bool sensitivity_df(const double* d, int bins, float n0, float& sens, float& conf) {
+    const double kEps = 1e-18;
+    F2 w, w2, ys, y2;
+    if (!(f2_split(d[32], w) && f2_split(d[33], w2) && f2_split(d[34], ys) && f2_split(d[35], y2))) return false;
+    const F2 en = d[33] > 0.0 ? f2_div(f2_mul(w, w), w2) : F2{0.0f, 0.0f};  // sample_mass
+    const F2 c = f2_div(en, f2_add(en, F2{n0, 0.0f}));
+    conf = c.h + c.l;
+    sens = 0.0f;
+    if (f2_le(en, 2.0f)) return true;
+    const F2 mean = f2_div(ys, w);
+    const F2 total = f2_sub(y2, f2_mul(w, f2_mul(mean, mean)));
+    if (f2_double(total) <= kEps) return true;
+    const F2 nmean{-mean.h, -mean.l};
+    F2 between{0.0f, 0.0f};
+    int active = 0;
+    for (int b = 0; b < bins; ++b) {
+        if (d[b] <= kEps) continue;
+        ++active;
+        F2 wb, sb;
+        if (!(f2_split(d[b], wb) && f2_split(d[16 + b], sb))) return false;
+        const F2 delta = f2_add(f2_div(sb, wb), nmean);
+        between = f2_add(between, f2_mul(wb, f2_mul(delta, delta)));
+    }
+    if (active < 2 || f2_le(en, float(active))) return true;
+    F2 eta2 = f2_div(between, total);
+    if (eta2.h < 0.0f) eta2 = F2{0.0f, 0.0f};
+    if (eta2.h > 1.0f || (eta2.h == 1.0f && eta2.l > 0.0f)) eta2 = F2{1.0f, 0.0f};
+    const F2 one{1.0f, 0.0f};
+    const F2 fa = f2_div(f2_sub(en, one), f2_sub(en, F2{float(active), 0.0f}));
+    const F2 adj = f2_sub(one, f2_mul(f2_sub(one, eta2), fa));
+    if (!(adj.h > 0.0f)) return true;  // max(0, adjusted)
+    // sqrt(hi + lo) from the float root of hi and one correction
+    const float s0 = sqrtf(adj.h);
+    const float r = __fmaf_rn(-s0, s0, adj.h) + adj.l;
+    sens = __fmaf_rn(r, 0.5f / s0, s0);
+    return true;
 }
 
 __constant__ int c_raw_dep[R_FIELDS] = {D_PIXEL, D_BRDF, D_LENS, D_LIGHT_UV, D_LIGHT_SELECT, D_ENV, D_RR,
@@ -184,9 +205,14 @@ __global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0, 
     if (f < R_FIELDS) {
         const int d = c_raw_dep[f];
         const double* dep = n.grid + idx * kDeps * kDepStride + d * kDepStride;
-        n.raw[f][idx] = compute_sensitivity(dep, d == D_RR ? 2 : 16, df_bins != 0);
-        const double mass = sample_mass(dep);
-        n.conf[f][idx] = float(mass / (mass + double(n0)));
+        float sens, conf;
+        if (!(df_bins && sensitivity_df(dep, d == D_RR ? 2 : 16, n0, sens, conf))) {
+            sens = compute_sensitivity(dep, d == D_RR ? 2 : 16);
+            const double mass = sample_mass(dep);
+            conf = float(mass / (mass + double(n0)));
+        }
+        n.raw[f][idx] = sens;
+        n.conf[f][idx] = conf;
         return;
     }
     const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
