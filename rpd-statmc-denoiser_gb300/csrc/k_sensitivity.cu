@@ -233,15 +233,20 @@ __global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0, 
     for (int c = 0; c < 3; ++c) n.n_albedo[c][idx] = na3[c];
 }
 
-__global__ void k_node_combine(Geometry g, NodePlanes n) {
-    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= g.nn) return;
-    const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
+// The prior smoothing's weighted sums (main.cpp:817-851) in double-float (df) or in double as the
+// reference sums them; the prior is their quotient rounded to float either way.
+template <bool DF>
+__device__ __forceinline__ void prior_sums(const Geometry& g, const NodePlanes& n, int ix, int iy, int64_t idx,
+                                           float prior[R_FIELDS]) {
     const float ni0 = n.n_normal[0][idx], ni1 = n.n_normal[1][idx], ni2 = n.n_normal[2][idx];
     const float di = n.n_depth[idx];
     const float ai0 = n.n_albedo[0][idx], ai1 = n.n_albedo[1][idx], ai2 = n.n_albedo[2][idx];
     double accum[R_FIELDS], wsum[R_FIELDS];
-    for (int f = 0; f < R_FIELDS; ++f) accum[f] = wsum[f] = 0.0;
+    F2 acc2[R_FIELDS], ws2[R_FIELDS];
+    for (int f = 0; f < R_FIELDS; ++f) {
+        if (DF) acc2[f] = ws2[f] = F2{0.0f, 0.0f};
+        else accum[f] = wsum[f] = 0.0;
+    }
     for (int dy = -1; dy <= 1; ++dy) {
         const int sy = iy + dy;
         if (sy < 0 || sy >= g.nodes_y) continue;
@@ -256,19 +261,47 @@ __global__ void k_node_combine(Geometry g, NodePlanes n) {
             const float depth_w = expf(-4.0f * relative_depth_delta(di, n.n_depth[sidx]));
             const float albedo_w = expf(-2.5f * norm3(ai0 - n.n_albedo[0][sidx], ai1 - n.n_albedo[1][sidx],
                                                       ai2 - n.n_albedo[2][sidx]));
-            const double base = double(spatial_w) * double(normal_w) * double(depth_w) * double(albedo_w);
-            for (int f = 0; f < R_FIELDS; ++f) {
-                const double w_neighbor = base * double(fmaxs(0.05f, n.conf[f][sidx]));
-                accum[f] += w_neighbor * double(n.raw[f][sidx]);
-                wsum[f] += w_neighbor;
+            if (DF) {
+                // the product of the four float weights, exact in its first step
+                const float p = spatial_w * normal_w;
+                const F2 b2 = f2_mul(f2_mul(F2{p, __fmaf_rn(spatial_w, normal_w, -p)}, F2{depth_w, 0.0f}),
+                                     F2{albedo_w, 0.0f});
+                for (int f = 0; f < R_FIELDS; ++f) {
+                    const F2 wn = f2_mul(b2, F2{fmaxs(0.05f, n.conf[f][sidx]), 0.0f});
+                    acc2[f] = f2_add(acc2[f], f2_mul(wn, F2{n.raw[f][sidx], 0.0f}));
+                    ws2[f] = f2_add(ws2[f], wn);
+                }
+            } else {
+                const double base = double(spatial_w) * double(normal_w) * double(depth_w) * double(albedo_w);
+                for (int f = 0; f < R_FIELDS; ++f) {
+                    const double w_neighbor = base * double(fmaxs(0.05f, n.conf[f][sidx]));
+                    accum[f] += w_neighbor * double(n.raw[f][sidx]);
+                    wsum[f] += w_neighbor;
+                }
             }
         }
     }
+    for (int f = 0; f < R_FIELDS; ++f) {
+        if (DF) {
+            const bool some = ws2[f].h > 1e-8f || (ws2[f].h == 1e-8f && ws2[f].l > 0.0f);
+            const F2 q = some ? f2_div(acc2[f], ws2[f]) : F2{0.0f, 0.0f};
+            prior[f] = some ? q.h + q.l : n.raw[f][idx];
+        } else {
+            prior[f] = (wsum[f] > double(1e-8f)) ? float(accum[f] / wsum[f]) : n.raw[f][idx];
+        }
+    }
+}
+
+__global__ void k_node_combine(Geometry g, NodePlanes n, int df) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= g.nn) return;
+    const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
     float prior[R_FIELDS], raw[R_FIELDS], conf[R_FIELDS];
+    if (df) prior_sums<true>(g, n, ix, iy, idx, prior);
+    else prior_sums<false>(g, n, ix, iy, idx, prior);
     for (int f = 0; f < R_FIELDS; ++f) {
         raw[f] = n.raw[f][idx];
         conf[f] = n.conf[f][idx];
-        prior[f] = (wsum[f] > double(1e-8f)) ? float(accum[f] / wsum[f]) : raw[f];
         n.prior[f][idx] = prior[f];
     }
     float fin[7];
@@ -379,7 +412,7 @@ cudaError_t launch_sensitivity(Job& j) {
     }
     {
         KernelScope ks(j, RPD_KERNEL_NODE_COMBINE);
-        k_node_combine<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n);
+        k_node_combine<<<grid_for(j.g.nn, 128), 128, 0, j.stream>>>(j.g, j.n, j.exact_grid ? 0 : 1);
     }
     {
         KernelScope ks(j, RPD_KERNEL_SENS_PIXELS);

@@ -190,30 +190,18 @@ __global__ void __launch_bounds__(kSvTx * kSvTy) k_sqrt_var_stable(PixelPlanes p
         const double* t1 = tile[c][0];
         const double* th = tile[c][1];
         const double* tt = tile[c][2];
-        double a;
-        if (c == 0) {
-            XD x = xd_of_double(tt[e - tw - 1]);
-            x = xd_add(x, xd_of_double(th[e - tw]));
-            x = xd_add(x, xd_of_double(tt[e - tw + 1]));
-            x = xd_add(x, xd_of_double(th[e - 1]));
-            x = xd_add(x, xd_of_double(t1[e]));
-            x = xd_add(x, xd_of_double(th[e + 1]));
-            x = xd_add(x, xd_of_double(tt[e + tw - 1]));
-            x = xd_add(x, xd_of_double(th[e + tw]));
-            x = xd_add(x, xd_of_double(tt[e + tw + 1]));
-            a = xd_to_double(x);
-        } else {
-            a = 0.0;
-            a += tt[e - tw - 1];
-            a += th[e - tw];
-            a += tt[e - tw + 1];
-            a += th[e - 1];
-            a += t1[e];
-            a += th[e + 1];
-            a += tt[e + tw - 1];
-            a += th[e + tw];
-            a += tt[e + tw + 1];
-        }
+        // the reference's nine double additions in its order, each rounded as the double-precision
+        // add rounds it, in integer arithmetic (GB300's double-precision pipe is the scarce one)
+        XD x = xd_of_double(tt[e - tw - 1]);
+        x = xd_add(x, xd_of_double(th[e - tw]));
+        x = xd_add(x, xd_of_double(tt[e - tw + 1]));
+        x = xd_add(x, xd_of_double(th[e - 1]));
+        x = xd_add(x, xd_of_double(t1[e]));
+        x = xd_add(x, xd_of_double(th[e + 1]));
+        x = xd_add(x, xd_of_double(tt[e + tw - 1]));
+        x = xd_add(x, xd_of_double(th[e + tw]));
+        x = xd_add(x, xd_of_double(tt[e + tw + 1]));
+        const double a = xd_to_double(x);
         const XD ax = xd_of_double(a);
         float q;
         if (!quotient_to_float(ax.m, ax.e, wsum.m, wsum.e, q)) q = float(a / weight_sum);
