@@ -195,6 +195,30 @@ __device__ void local_avg3(float* const* v, int w, int h, int cx, int cy, float 
     out[2] = float(a2 / weight_sum);
 }
 
+// local_avg3 / local_avg1 in double-float (the grid's fast mode): C planes, the weights
+// 1 / (1 + d^2) as pairs of floats, the quotient by their sum rounded to float.
+template <int C>
+__device__ void local_avg_df(const float* const* v, int w, int h, int cx, int cy, float* out) {
+    // 1, 1/2 and the double 1/3 as hi + lo
+    const F2 wts[3] = {F2{1.0f, 0.0f}, F2{0.5f, 0.0f}, F2{0.333333343f, -9.934107758624577e-09f}};
+    F2 acc[C], ws{0.0f, 0.0f};
+    for (int c = 0; c < C; ++c) acc[c] = F2{0.0f, 0.0f};
+    for (int dy = -1; dy <= 1; ++dy) {
+        const int y = iclamps(cy + dy, 0, h - 1);
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int x = iclamps(cx + dx, 0, w - 1);
+            const F2 wt = wts[dx * dx + dy * dy];
+            const int64_t i = int64_t(y) * w + x;
+            for (int c = 0; c < C; ++c) acc[c] = f2_add(acc[c], f2_mul(wt, F2{v[c][i], 0.0f}));
+            ws = f2_add(ws, wt);
+        }
+    }
+    for (int c = 0; c < C; ++c) {
+        const F2 q = f2_div(acc[c], ws);
+        out[c] = q.h + q.l;
+    }
+}
+
 // One thread per (node, task): tasks 0 .. R_FIELDS-1 are the dependencies' sensitivity and
 // confidence, task R_FIELDS the node's features (blockIdx.y). The tasks are independent, so the
 // double-precision chains of a node run side by side instead of one after another.
@@ -218,8 +242,16 @@ __global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0, 
     const int ix = int(idx % g.nodes_x), iy = int(idx / g.nodes_x);
     const int px = iclamps(ix * g.step, 0, g.w - 1);
     const int py = iclamps(iy * g.step, 0, g.h - 1);
-    float nn3[3], na3[3];
-    local_avg3(p.f_normal, g.w, g.h, px, py, nn3);
+    float nn3[3], na3[3], nd1;
+    if (df_bins) {
+        local_avg_df<3>(p.f_normal, g.w, g.h, px, py, nn3);
+        local_avg_df<1>(&p.f_depth, g.w, g.h, px, py, &nd1);
+        local_avg_df<3>(p.f_albedo, g.w, g.h, px, py, na3);
+    } else {
+        local_avg3(p.f_normal, g.w, g.h, px, py, nn3);
+        nd1 = local_avg1(p.f_depth, g.w, g.h, px, py);
+        local_avg3(p.f_albedo, g.w, g.h, px, py, na3);
+    }
     const float z = dot3(nn3[0], nn3[1], nn3[2], nn3[0], nn3[1], nn3[2]);
     if (z > 1e-8f) {
         const float sn = sqrtf(z);
@@ -228,8 +260,7 @@ __global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0, 
         nn3[2] = nn3[2] / sn;
     }
     for (int c = 0; c < 3; ++c) n.n_normal[c][idx] = nn3[c];
-    n.n_depth[idx] = local_avg1(p.f_depth, g.w, g.h, px, py);
-    local_avg3(p.f_albedo, g.w, g.h, px, py, na3);
+    n.n_depth[idx] = nd1;
     for (int c = 0; c < 3; ++c) n.n_albedo[c][idx] = na3[c];
 }
 
