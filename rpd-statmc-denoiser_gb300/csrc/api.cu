@@ -1251,6 +1251,7 @@ static int job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memo
         RPD_CUDA(cudaStreamSynchronize(j->stream));
         return RPD_OK;
     }
+    if (f == RPD_FIELD_GRID && j->grid_pairs) src = nullptr;  // pairs: widened on the way out
     if (src) {
         RPD_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, j->stream));
         if (sync) RPD_CUDA(cudaStreamSynchronize(j->stream));
@@ -1260,7 +1261,9 @@ static int job_read(rpd_job* job, rpd_field f, void* dst, size_t bytes, rpd_memo
     int st = grow_device(*j, &j->staging, &j->staging_bytes, need);
     if (st != RPD_OK) return st;
     float* tmp = static_cast<float*>(j->staging);
-    if (rgb) {
+    if (f == RPD_FIELD_GRID) {
+        RPD_CUDA(launch_grid_to_double(*j, reinterpret_cast<double*>(tmp)));
+    } else if (rgb) {
         k_pack3<<<grid_for(np, 256), 256, 0, j->stream>>>(rgb[0], rgb[1], rgb[2], tmp, np);
         j->launches += 1;
         RPD_CUDA(cudaGetLastError());

@@ -776,28 +776,62 @@ __device__ __forceinline__ double widen(float f) {
                                                        (uint64_t(b & 0x7fffffu) << 29)));
 }
 
-// grid += pass (the first pass of a frame: grid = 0 + pass), then clear the pass grid. The
-// fast path's pass grid holds double-float pairs (hi, lo) in the bytes of each double.
-template <bool DF, bool FRESH>
+// grid += pass (the first pass of a frame: grid = 0 + pass), then clear the pass grid. The pass
+// grid holds double-float pairs (hi, lo) in the bytes of each double in the fast grid mode, doubles
+// in the exact one. The frame grid takes the first merged pass's form: in the fast mode it stays
+// pairs, each merge a double-float addition (about 2^-44 relative, within the grid's 1e-9 of the
+// reference) with no double-precision instruction, which GB300 issues at 2 per SM per clock; a
+// frame whose passes mix the modes ends in doubles.
+enum MergeMode {
+    kMergePairsFresh,     // pairs -> the frame's pairs
+    kMergePairsPairs,     // frame pairs + pass pairs
+    kMergeDoubleFresh,    // doubles -> the frame's doubles
+    kMergeDoubleDouble,   // frame doubles + pass doubles
+    kMergePairsIntoDouble,  // frame doubles + pass pairs
+    kMergeDoubleIntoPairs   // frame pairs + pass doubles -> frame doubles
+};
+__device__ __forceinline__ float2 pair_add(float2 a, float2 b) {
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = ((a.x - (s - bb)) + (b.x - bb)) + (a.y + b.y);
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+
+template <int MODE>
 __global__ void k_merge_grid(double* grid, double* pass_grid, int64_t n) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double v;
-    if (DF) {
-        const float2 p = reinterpret_cast<const float2*>(pass_grid)[i];
-        v = widen(p.x) + widen(p.y);
+    float2* gp = reinterpret_cast<float2*>(grid);
+    const float2* pp = reinterpret_cast<const float2*>(pass_grid);
+    if (MODE == kMergePairsFresh) {
+        gp[i] = pp[i];
+    } else if (MODE == kMergePairsPairs) {
+        gp[i] = pair_add(gp[i], pp[i]);
     } else {
-        v = pass_grid[i];
-    }
-    if (FRESH) {
-        // 0 + v without a double-precision add (GB300 runs those at a small fraction of its
-        // single-precision rate): the same value, with -0 turned into +0
-        const long long b = __double_as_longlong(v);
-        grid[i] = __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
-    } else {
-        grid[i] = grid[i] + v;
+        double v;
+        if (MODE == kMergePairsIntoDouble) v = widen(pp[i].x) + widen(pp[i].y);
+        else v = pass_grid[i];
+        if (MODE == kMergeDoubleFresh) {
+            // 0 + v without a double-precision add: the same value, with -0 turned into +0
+            const long long b = __double_as_longlong(v);
+            grid[i] = __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+        } else if (MODE == kMergeDoubleIntoPairs) {
+            const float2 g = gp[i];
+            grid[i] = (widen(g.x) + widen(g.y)) + v;
+        } else {
+            grid[i] = grid[i] + v;
+        }
     }
     pass_grid[i] = 0.0;
+}
+
+// The frame grid as doubles (for reads): pairs widened and added.
+__global__ void k_grid_pairs_to_double(const float2* pairs, double* out, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 g = pairs[i];
+    out[i] = widen(g.x) + widen(g.y);
 }
 
 __global__ void k_feature_cache(PixelPlanes p, int64_t np) {
@@ -950,12 +984,32 @@ cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first
 cudaError_t launch_merge_grid(Job& j) {
     KernelScope ks(j, RPD_KERNEL_MERGE);
     const int64_t n = j.g.nn * kDeps * kDepStride;
-    const bool df = !j.exact_grid;
-    if (df && j.grid_fresh) k_merge_grid<true, true><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
-    else if (df) k_merge_grid<true, false><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
-    else if (j.grid_fresh) k_merge_grid<false, true><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
-    else k_merge_grid<false, false><<<grid_for(n, 256), 256, 0, j.stream>>>(j.n.grid, j.n.pass_grid, n);
+    const bool pass_pairs = !j.exact_grid;  // the pass grid's form (k_grid_ordered writes doubles)
+    const unsigned blocks = grid_for(n, 256);
+    double* g = j.n.grid;
+    double* pg = j.n.pass_grid;
+    if (j.grid_fresh) {
+        if (pass_pairs) k_merge_grid<kMergePairsFresh><<<blocks, 256, 0, j.stream>>>(g, pg, n);
+        else k_merge_grid<kMergeDoubleFresh><<<blocks, 256, 0, j.stream>>>(g, pg, n);
+        j.grid_pairs = pass_pairs;
+    } else if (pass_pairs && j.grid_pairs) {
+        k_merge_grid<kMergePairsPairs><<<blocks, 256, 0, j.stream>>>(g, pg, n);
+    } else if (!pass_pairs && !j.grid_pairs) {
+        k_merge_grid<kMergeDoubleDouble><<<blocks, 256, 0, j.stream>>>(g, pg, n);
+    } else if (pass_pairs) {
+        k_merge_grid<kMergePairsIntoDouble><<<blocks, 256, 0, j.stream>>>(g, pg, n);
+    } else {
+        k_merge_grid<kMergeDoubleIntoPairs><<<blocks, 256, 0, j.stream>>>(g, pg, n);
+        j.grid_pairs = false;
+    }
     j.grid_fresh = false;
+    j.launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_to_double(Job& j, double* out) {
+    const int64_t n = j.g.nn * kDeps * kDepStride;
+    k_grid_pairs_to_double<<<grid_for(n, 256), 256, 0, j.stream>>>(reinterpret_cast<const float2*>(j.n.grid), out, n);
     j.launches += 1;
     return cudaGetLastError();
 }

@@ -113,13 +113,32 @@ __device__ __forceinline__ double f2_double(F2 a) { return double(a.h) + double(
 
 // compute_sensitivity and the node's confidence, sample_mass / (sample_mass + n0), with every
 // quotient, product and the square root in double-float (about 2^-44 relative; the results are
-// floats). False when a grid value lies outside the split's range: the caller then takes the
-// double path. Decisions follow the reference's tests in its order.
+// floats). GRID_DF: the frame grid holds double-float pairs (the grid's fast mode merges them so);
+// else its doubles are split into pairs, and false comes back when one lies outside the split's
+// range (the caller then takes the double path). Decisions follow the reference's tests in its
+// order.
+template <bool GRID_DF>
 __device__ bool sensitivity_df(const double* d, int bins, float n0, float& sens, float& conf) {
     const double kEps = 1e-18;
+    const float2* dp = reinterpret_cast<const float2*>(d);
+    auto get = [&](int k, F2& out) -> bool {
+        if (GRID_DF) {
+            const float2 v = dp[k];
+            out = F2{v.x, v.y};
+            return true;
+        }
+        return f2_split(d[k], out);
+    };
+    // value > kEps (or > 0) as the double test decides it: on the pairs, against kEps as a pair
+    const F2 eps2{1.0e-18f, float(1e-18 - double(1.0e-18f))};
+    auto above = [&](int k, F2 v, double t) {
+        if (!GRID_DF) return d[k] > t;
+        const F2 tt = t > 0.0 ? eps2 : F2{0.0f, 0.0f};
+        return v.h > tt.h || (v.h == tt.h && v.l > tt.l);
+    };
     F2 w, w2, ys, y2;
-    if (!(f2_split(d[32], w) && f2_split(d[33], w2) && f2_split(d[34], ys) && f2_split(d[35], y2))) return false;
-    const F2 en = d[33] > 0.0 ? f2_div(f2_mul(w, w), w2) : F2{0.0f, 0.0f};  // sample_mass
+    if (!(get(32, w) && get(33, w2) && get(34, ys) && get(35, y2))) return false;
+    const F2 en = above(33, w2, 0.0) ? f2_div(f2_mul(w, w), w2) : F2{0.0f, 0.0f};  // sample_mass
     const F2 c = f2_div(en, f2_add(en, F2{n0, 0.0f}));
     conf = c.h + c.l;
     sens = 0.0f;
@@ -131,10 +150,11 @@ __device__ bool sensitivity_df(const double* d, int bins, float n0, float& sens,
     F2 between{0.0f, 0.0f};
     int active = 0;
     for (int b = 0; b < bins; ++b) {
-        if (d[b] <= kEps) continue;
-        ++active;
         F2 wb, sb;
-        if (!(f2_split(d[b], wb) && f2_split(d[16 + b], sb))) return false;
+        if (!get(b, wb)) return false;
+        if (!above(b, wb, kEps)) continue;
+        ++active;
+        if (!get(16 + b, sb)) return false;
         const F2 delta = f2_add(f2_div(sb, wb), nmean);
         between = f2_add(between, f2_mul(wb, f2_mul(delta, delta)));
     }
@@ -222,6 +242,8 @@ __device__ void local_avg_df(const float* const* v, int w, int h, int cx, int cy
 // One thread per (node, task): tasks 0 .. R_FIELDS-1 are the dependencies' sensitivity and
 // confidence, task R_FIELDS the node's features (blockIdx.y). The tasks are independent, so the
 // double-precision chains of a node run side by side instead of one after another.
+// df_bins: 0 the reference's double arithmetic (exact grid), 1 double-float on the split doubles
+// of the grid, 2 double-float on a grid that holds double-float pairs
 __global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0, int df_bins) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= g.nn) return;
@@ -230,7 +252,10 @@ __global__ void k_node_stats(Geometry g, NodePlanes n, PixelPlanes p, float n0, 
         const int d = c_raw_dep[f];
         const double* dep = n.grid + idx * kDeps * kDepStride + d * kDepStride;
         float sens, conf;
-        if (!(df_bins && sensitivity_df(dep, d == D_RR ? 2 : 16, n0, sens, conf))) {
+        const bool done = df_bins == 2   ? sensitivity_df<true>(dep, d == D_RR ? 2 : 16, n0, sens, conf)
+                          : df_bins == 1 ? sensitivity_df<false>(dep, d == D_RR ? 2 : 16, n0, sens, conf)
+                                         : false;
+        if (!done) {
             sens = compute_sensitivity(dep, d == D_RR ? 2 : 16);
             const double mass = sample_mass(dep);
             conf = float(mass / (mass + double(n0)));
@@ -439,7 +464,7 @@ cudaError_t launch_sensitivity(Job& j) {
     {
         KernelScope ks(j, RPD_KERNEL_NODE_STATS);
         k_node_stats<<<dim3(grid_for(j.g.nn, 128), R_FIELDS + 1), 128, 0, j.stream>>>(
-            j.g, j.n, j.p, j.cfg.rpf_confidence_samples, j.exact_grid ? 0 : 1);
+            j.g, j.n, j.p, j.cfg.rpf_confidence_samples, j.grid_pairs ? 2 : j.exact_grid ? 0 : 1);
     }
     {
         KernelScope ks(j, RPD_KERNEL_NODE_COMBINE);

@@ -178,6 +178,7 @@ struct Job {
     bool acc_zero = false;      // the per-pixel statistics are the frame start's zeros (no push yet)
     bool host_async = false;  // the current host push returns before its copies complete
     bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)
+    bool grid_pairs = false;     // the frame grid holds double-float pairs (fast grid mode), not doubles
     bool features_valid = false;
     bool cache_valid = false;
     bool have_samples = false;
@@ -327,6 +328,8 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
                              int32_t spp, int32_t max_count, int64_t total_samples,
                              const int64_t* d_max_count = nullptr);
 cudaError_t launch_merge_grid(Job& j);
+// The frame grid as doubles into out (nn * kDeps * kDepStride entries) when it holds pairs.
+cudaError_t launch_grid_to_double(Job& j, double* out);
 cudaError_t launch_feature_cache(Job& j);
 cudaError_t launch_sensitivity(Job& j);
 cudaError_t launch_sensitivity_zero(Job& j);
