@@ -427,7 +427,6 @@ int rpd_ctx_create(int device, uint64_t budget, rpd_ctx** out) {
     c->device = device;
     c->budget = budget ? budget : uint64_t(free_b);
     cudaError_t e = cudaStreamCreateWithFlags(&c->util_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->alloc_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         if (c->util_stream) cudaStreamDestroy(c->util_stream);
         delete c;
@@ -442,7 +441,6 @@ void rpd_ctx_destroy(rpd_ctx* ctx) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->util_stream) cudaStreamDestroy(c->util_stream);
-    if (c->alloc_stream) cudaStreamDestroy(c->alloc_stream);
     delete c;
 }
 
@@ -519,8 +517,6 @@ int job_create(Ctx* c, const rpd_config* cfg, cudaMemPool_t pool, Job** out) {
     for (int b = 0; b < Job::kMaxBands && e == cudaSuccess; ++b)
         e = cudaEventCreateWithFlags(&j->band_copied[b], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->staging_free, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->alloc_ready, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->alloc_done, cudaEventDisableTiming);
     for (int s = 0; s < RPD_STAGE_COUNT_ && e == cudaSuccess; ++s) {
         e = cudaEventCreate(&j->ev_start[s]);
         if (e == cudaSuccess) e = cudaEventCreate(&j->ev_stop[s]);
@@ -577,8 +573,6 @@ void rpd_job_destroy(rpd_job* job) {
     for (int b = 0; b < Job::kMaxBands; ++b)
         if (j->band_copied[b]) cudaEventDestroy(j->band_copied[b]);
     if (j->staging_free) cudaEventDestroy(j->staging_free);
-    if (j->alloc_ready) cudaEventDestroy(j->alloc_ready);
-    if (j->alloc_done) cudaEventDestroy(j->alloc_done);
     if (j->copy_stream) cudaStreamDestroy(j->copy_stream);
     if (j->stream) cudaStreamDestroy(j->stream);
     delete j;

@@ -1582,10 +1582,11 @@ cudaError_t launch_allocate_parallel(Job& j, const float* importance, int extra_
     ChunkRec* rec = reinterpret_cast<ChunkRec*>(work + kScalarBytes);
     double* pool = reinterpret_cast<double*>(work + kScalarBytes + ((uint64_t(nch) * sizeof(ChunkRec) + 255) & ~uint64_t(255)));
     *fallback_flag = &sc->fallback;
-    cudaStream_t as = j.ctx->alloc_stream;
-    cudaError_t e = cudaEventRecord(j.alloc_ready, j.stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(as, j.alloc_ready, 0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sc, 0, sizeof(AllocScalars), as);
+    // on the job's own stream: a cooperative launch starts only when all of its blocks are
+    // resident, so the allocations of jobs running side by side never wait on each other's
+    // blocks (each block is built for half an SM's registers, so two share an SM)
+    cudaStream_t as = j.stream;
+    cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(AllocScalars), as);
     if (e != cudaSuccess) return e;
     int dev = 0;
     e = cudaGetDevice(&dev);
@@ -1638,8 +1639,6 @@ cudaError_t launch_allocate_parallel(Job& j, const float* importance, int extra_
                                         as);
         j.launches += 1;
     }
-    if (e == cudaSuccess) e = cudaEventRecord(j.alloc_done, as);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(j.stream, j.alloc_done, 0);
     return e;
 }
 

@@ -125,9 +125,6 @@ struct Ctx {
     std::atomic<uint64_t> in_use{0};
     std::mutex mu;
     cudaStream_t util_stream = nullptr;
-    // every job's parallel allocation runs on this stream, one at a time: two cooperative
-    // launches that each hold part of the GPU must not wait on each other's blocks
-    cudaStream_t alloc_stream = nullptr;
     std::unordered_map<void*, uint64_t> user_allocs;  // rpd_device_alloc bookkeeping
 };
 
@@ -156,8 +153,6 @@ struct Job {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t band_copied[kMaxBands]{};
     cudaEvent_t staging_free = nullptr;
-    cudaEvent_t alloc_ready = nullptr;  // the job's stream reached the allocation
-    cudaEvent_t alloc_done = nullptr;   // the allocation stream finished it
     int64_t band_bytes = int64_t(768) << 20;  // target size of a band (RPD_TUNE_HOST_BAND_MB)
     float* lum = nullptr;        // per-sample luminance of the current push (fast grid pass)
     uint64_t lum_cap = 0;
