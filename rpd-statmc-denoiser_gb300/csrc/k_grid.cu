@@ -623,6 +623,7 @@ __global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pas
 // update has no branches). The block combines row groups and lanes in a fixed order at the
 // end: deterministic, no atomics.
 constexpr int kRandDims = 6;
+constexpr int kAllDims = 0x3f, kNoEnvDims = 0x37;  // dimension masks (bit d: dimension d)
 constexpr int kRandSlots = 5 * 16 + 2;  // brdf, lens, light_uv, environment, light_select; rr has 2 bins
 // d: 0 brdf, 1 lens, 2 light_uv, 3 environment, 4 light_select, 5 rr (grid group d + 1)
 __host__ __device__ constexpr int rand_slot0(int d) { return d * 16; }
@@ -697,9 +698,10 @@ struct WalkCtx {
 };
 
 // One sample: add w (weights) and w*y (sums) to the bin of every dimension of set SET the
-// sample carries. Absent dimensions (and w <= 1e-8, which BinnedDependency::add skips,
+// sample carries; dimensions outside the mask DIMS are never valid in the push's keys (their
+// sample planes are absent) and are skipped. Absent dimensions (and w <= 1e-8, which BinnedDependency::add skips,
 // core/stats.h:103) go to the trash slot with the same arithmetic.
-template <int WB, int DS, int SET>
+template <int WB, int DS, int SET, int DIMS>
 __device__ __forceinline__ void rand_update(const WalkCtx<WB, DS>& c, uint32_t key, float w, uint32_t iw,
                                             float y) {
     constexpr bool INT_W = WB != 8;
@@ -712,7 +714,7 @@ __device__ __forceinline__ void rand_update(const WalkCtx<WB, DS>& c, uint32_t k
     float2 wd[kRandDims], sy[kRandDims];
 #pragma unroll
     for (int d = 0; d < kRandDims; ++d) {
-        if (dim_set<DS>(d) != SET) continue;
+        if (dim_set<DS>(d) != SET || !((DIMS >> d) & 1)) continue;
         const bool on = wok && (key & key_valid_bit(d + 1)) != 0;
         const int bin = int((key >> rand_shift(d)) & rand_mask(d));
         slot[d] = (on ? dim_slot0<DS>(d) + bin : L::kTrash) * 32 + c.lane;
@@ -721,14 +723,14 @@ __device__ __forceinline__ void rand_update(const WalkCtx<WB, DS>& c, uint32_t k
     // update, store all
 #pragma unroll
     for (int d = 0; d < kRandDims; ++d) {
-        if (dim_set<DS>(d) != SET) continue;
+        if (dim_set<DS>(d) != SET || !((DIMS >> d) & 1)) continue;
         if (INT_W) wi[d] = c.wint[slot[d]];
         else wd[d] = c.wdf[slot[d]];
         sy[d] = c.sums[slot[d]];
     }
 #pragma unroll
     for (int d = 0; d < kRandDims; ++d) {
-        if (dim_set<DS>(d) != SET) continue;
+        if (dim_set<DS>(d) != SET || !((DIMS >> d) & 1)) continue;
         if (INT_W) wi[d] += iw;
         else df_add(wd[d].x, wd[d].y, w);
         df_add(sy[d].x, sy[d].y, wy);
@@ -736,7 +738,7 @@ __device__ __forceinline__ void rand_update(const WalkCtx<WB, DS>& c, uint32_t k
     }
 #pragma unroll
     for (int d = 0; d < kRandDims; ++d) {
-        if (dim_set<DS>(d) != SET) continue;
+        if (dim_set<DS>(d) != SET || !((DIMS >> d) & 1)) continue;
         if (INT_W) c.wint[slot[d]] = wi[d];
         else c.wdf[slot[d]] = wd[d];
         c.sums[slot[d]] = sy[d];
@@ -749,7 +751,7 @@ constexpr int kWalkScalar = 0, kWalkPixelQuads = 1, kWalkColumnQuads = 2;
 
 // The flat walk of one row-segment chunk (total samples, or total quads in the quad modes) for
 // dimension set SET.
-template <int WB, int DS, int SET, int MODE>
+template <int WB, int DS, int SET, int MODE, int DIMS>
 __device__ __forceinline__ void rand_walk(const WalkCtx<WB, DS>& c, const RandParams& rp, const GridPrep& gp,
                                           const int64_t* offsets, int total) {
     constexpr bool INT_W = WB != 8;
@@ -815,10 +817,10 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<WB, DS>& c, const RandPa
                         if (k >= ks && k < ke && unsigned(ci) < unsigned(rp.cols)) w[i] = c.xf[ci] * ay;
                     }
                 }
-                rand_update<WB, DS, SET>(c, ck[u].x, w[0], INT_W ? uint32_t(w[0] * c.wscale) : 0u, cy[u].x);
-                rand_update<WB, DS, SET>(c, ck[u].y, w[1], INT_W ? uint32_t(w[1] * c.wscale) : 0u, cy[u].y);
-                rand_update<WB, DS, SET>(c, ck[u].z, w[2], INT_W ? uint32_t(w[2] * c.wscale) : 0u, cy[u].z);
-                rand_update<WB, DS, SET>(c, ck[u].w, w[3], INT_W ? uint32_t(w[3] * c.wscale) : 0u, cy[u].w);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].x, w[0], INT_W ? uint32_t(w[0] * c.wscale) : 0u, cy[u].x);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].y, w[1], INT_W ? uint32_t(w[1] * c.wscale) : 0u, cy[u].y);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].z, w[2], INT_W ? uint32_t(w[2] * c.wscale) : 0u, cy[u].z);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].w, w[3], INT_W ? uint32_t(w[3] * c.wscale) : 0u, cy[u].w);
             }
         }
     } else if (MODE == kWalkPixelQuads) {
@@ -862,10 +864,10 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<WB, DS>& c, const RandPa
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const uint32_t iw = INT_W ? uint32_t(cw[u] * c.wscale) : 0u;
-                rand_update<WB, DS, SET>(c, ck[u].x, cw[u], iw, cy[u].x);
-                rand_update<WB, DS, SET>(c, ck[u].y, cw[u], iw, cy[u].y);
-                rand_update<WB, DS, SET>(c, ck[u].z, cw[u], iw, cy[u].z);
-                rand_update<WB, DS, SET>(c, ck[u].w, cw[u], iw, cy[u].w);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].x, cw[u], iw, cy[u].x);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].y, cw[u], iw, cy[u].y);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].z, cw[u], iw, cy[u].z);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u].w, cw[u], iw, cy[u].w);
             }
         }
     } else {
@@ -925,12 +927,12 @@ __device__ __forceinline__ void rand_walk(const WalkCtx<WB, DS>& c, const RandPa
             }
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                rand_update<WB, DS, SET>(c, ck[u], cw[u], INT_W ? uint32_t(cw[u] * c.wscale) : 0u, cy[u]);
+                rand_update<WB, DS, SET, DIMS>(c, ck[u], cw[u], INT_W ? uint32_t(cw[u] * c.wscale) : 0u, cy[u]);
         }
     }
 }
 
-template <int WB, int RW, int DS, int MODE>
+template <int WB, int RW, int DS, int MODE, int DIMS>
 __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, float2* pass_grid,
                                                               const int64_t* offsets, GridPrep gp) {
     constexpr bool INT_W = WB != 8;
@@ -1027,9 +1029,9 @@ __global__ void __launch_bounds__(RW * DS * 32) k_grid_random(RandParams rp, flo
         if (lane == 0) rt->base[0] = 0;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
-        if (dset == 0) rand_walk<WB, DS, 0, MODE>(c, rp, gp, offsets, total);
-        if (DS > 1 && dset == 1) rand_walk<WB, DS, 1, MODE>(c, rp, gp, offsets, total);
-        if (DS > 2 && dset == 2) rand_walk<WB, DS, 2, MODE>(c, rp, gp, offsets, total);
+        if (dset == 0) rand_walk<WB, DS, 0, MODE, DIMS>(c, rp, gp, offsets, total);
+        if (DS > 1 && dset == 1) rand_walk<WB, DS, 1, MODE, DIMS>(c, rp, gp, offsets, total);
+        if (DS > 2 && dset == 2) rand_walk<WB, DS, 2, MODE, DIMS>(c, rp, gp, offsets, total);
         __syncwarp();
     }
     __syncthreads();
@@ -1118,16 +1120,16 @@ uint32_t spp_magic_for(int spp, int max_k) {
     return uint32_t(m);
 }
 
-template <int WB, int RW, int DS, int MODE>
+template <int WB, int RW, int DS, int MODE, int DIMS>
 cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) {
     constexpr int NW = RW * DS;
     const size_t smem = size_t(NW) * RandLayout<WB, DS>::kWarpBytes + size_t(NW) * sizeof(RowTable) +
                         size_t(rp.cols) * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(k_grid_random<WB, RW, DS, MODE>,
+    cudaError_t e = cudaFuncSetAttribute(k_grid_random<WB, RW, DS, MODE, DIMS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     const unsigned nblocks = unsigned(rp.gp.count_nodes);
-    k_grid_random<WB, RW, DS, MODE><<<nblocks, NW * 32, smem, j.stream>>>(
+    k_grid_random<WB, RW, DS, MODE, DIMS><<<nblocks, NW * 32, smem, j.stream>>>(
         rp, reinterpret_cast<float2*>(j.n.pass_grid), j.offsets, gp);
     j.launches += 1;
     return cudaGetLastError();
@@ -1136,21 +1138,21 @@ cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) 
 // Pixel quads need samples per pixel a multiple of 4 (and a power of two, for the shift) with
 // 16-byte aligned key and luminance planes; column quads need the per-sample columns (per-pixel
 // counts) with 16-byte aligned key and luminance planes and an 8-byte aligned column plane.
-template <int WB, int RW, int DS>
+template <int WB, int RW, int DS, int DIMS = kAllDims>
 cudaError_t launch_random(Job& j, const RandParams& rp, const GridPrep& gp) {
     const bool aligned = (reinterpret_cast<uintptr_t>(gp.key) & 15u) == 0 && (reinterpret_cast<uintptr_t>(gp.lum) & 15u) == 0;
-    if (rp.spp_shift >= 2 && aligned) return launch_random_vec<WB, RW, DS, kWalkPixelQuads>(j, rp, gp);
+    if (rp.spp_shift >= 2 && aligned) return launch_random_vec<WB, RW, DS, kWalkPixelQuads, DIMS>(j, rp, gp);
     if (gp.col && aligned && (reinterpret_cast<uintptr_t>(gp.col) & 7u) == 0)
-        return launch_random_vec<WB, RW, DS, kWalkColumnQuads>(j, rp, gp);
-    return launch_random_vec<WB, RW, DS, kWalkScalar>(j, rp, gp);
+        return launch_random_vec<WB, RW, DS, kWalkColumnQuads, DIMS>(j, rp, gp);
+    return launch_random_vec<WB, RW, DS, kWalkScalar, DIMS>(j, rp, gp);
 }
 
 // WB: bytes of a lane-private bin weight (8 double-float, 4 or 2 exact integers); the 2-byte
 // form is built for the default shape only (the caller checks that the lane sums fit)
 template <int WB>
-cudaError_t launch_random_shape(Job& j, const RandParams& rp, const GridPrep& gp, int shape) {
+cudaError_t launch_random_shape(Job& j, const RandParams& rp, const GridPrep& gp, int shape, bool env) {
     if constexpr (WB == 2) {
-        return launch_random<2, 1, 1>(j, rp, gp);
+        return env ? launch_random<2, 1, 1>(j, rp, gp) : launch_random<2, 1, 1, kNoEnvDims>(j, rp, gp);
     } else {
         switch (shape) {
         case 1: return launch_random<WB, 2, 1>(j, rp, gp);
@@ -1220,6 +1222,9 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
     }
     KernelScope ks(j, RPD_KERNEL_GRID_RANDOM);
     RandParams rp{gpar, 0u, -1, 2 * step + 3, nullptr, 0, 0};
+    // the statistics pass clears a dimension's valid bit when the push has no plane for it: without
+    // environment planes (a closed scene) the form without the environment dimension runs
+    const bool env = s.compact ? s.c16.env_u[0] != nullptr : s.env_u[0] != nullptr;
     if (spp > 0) {
         if ((spp & (spp - 1)) == 0) {
             int sh = 0;
@@ -1242,9 +1247,9 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
     if (int_w && default_shape) {
         if (spp > 0) {
             if ((double(sup + 3) * double(sup + 3) * double(spp) / 32.0 + 8.0) * units < 65536.0)
-                return launch_random_shape<2>(j, rp, gp, j.grid_shape);
+                return launch_random_shape<2>(j, rp, gp, j.grid_shape, env);
         } else if (max_count != INT32_MAX) {
-            if (counts_fit(double(std::max(max_count, 1)))) return launch_random_shape<2>(j, rp, gp, j.grid_shape);
+            if (counts_fit(double(std::max(max_count, 1)))) return launch_random_shape<2>(j, rp, gp, j.grid_shape, env);
         } else if (d_max_count) {
             // the largest count is known on the device only: launch both forms, each block of the
             // one that does not apply returns at once
@@ -1255,14 +1260,14 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
                 r16.max_count = d_max_count;
                 r16.max_limit = lim;
                 r16.max_mode = 1;
-                if ((e = launch_random_shape<2>(j, r16, gp, j.grid_shape)) != cudaSuccess) return e;
+                if ((e = launch_random_shape<2>(j, r16, gp, j.grid_shape, env)) != cudaSuccess) return e;
                 RandParams r32 = r16;
                 r32.max_mode = 2;
-                return launch_random_shape<4>(j, r32, gp, j.grid_shape);
+                return launch_random_shape<4>(j, r32, gp, j.grid_shape, env);
             }
         }
     }
-    return int_w ? launch_random_shape<4>(j, rp, gp, j.grid_shape) : launch_random_shape<8>(j, rp, gp, j.grid_shape);
+    return int_w ? launch_random_shape<4>(j, rp, gp, j.grid_shape, env) : launch_random_shape<8>(j, rp, gp, j.grid_shape, env);
 }
 
 }  // namespace rpd
