@@ -669,6 +669,7 @@ int rpd_job_begin_frame(rpd_job* job) {
     if (j->pass_open)
         RPD_CUDA(cudaMemsetAsync(j->n.pass_grid, 0, size_t(j->g.nn) * kDeps * kDepStride * sizeof(double), j->stream));
     j->grid_fresh = true;
+    j->pass_direct = j->pass_indirect = false;
     j->acc_zero = true;
     j->pass_open = false;
     j->features_valid = false;

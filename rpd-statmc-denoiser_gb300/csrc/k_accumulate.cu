@@ -977,11 +977,16 @@ cudaError_t launch_accumulate_grid(Job& j, const DeviceSamples& s, int64_t first
     KernelScope ks(j, RPD_KERNEL_GRID);
     const int64_t threads = j.g.nn * kDeps;
     k_grid_ordered<<<grid_for(threads, 128), 128, 0, j.stream>>>(j.g, j.n.pass_grid, s, j.offsets, 0, first, count);
+    j.pass_indirect = true;
     j.launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_merge_grid(Job& j) {
+    // pushes that added straight into the frame grid leave nothing in the pass grid
+    const bool any = j.pass_indirect;
+    j.pass_direct = j.pass_indirect = false;
+    if (!any) return cudaSuccess;
     KernelScope ks(j, RPD_KERNEL_MERGE);
     const int64_t n = j.g.nn * kDeps * kDepStride;
     const bool pass_pairs = !j.exact_grid;  // the pass grid's form (k_grid_ordered writes doubles)

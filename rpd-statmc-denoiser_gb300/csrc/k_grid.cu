@@ -660,6 +660,7 @@ struct RandParams {
     const int64_t* max_count;
     int64_t max_limit;
     int max_mode;
+    float2* target;  // the grid the pass adds to (the pass grid or, in pairs, the frame grid)
 };
 
 template <int WB, int DS>
@@ -1129,8 +1130,7 @@ cudaError_t launch_random_vec(Job& j, const RandParams& rp, const GridPrep& gp) 
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     const unsigned nblocks = unsigned(rp.gp.count_nodes);
-    k_grid_random<WB, RW, DS, MODE, DIMS><<<nblocks, NW * 32, smem, j.stream>>>(
-        rp, reinterpret_cast<float2*>(j.n.pass_grid), j.offsets, gp);
+    k_grid_random<WB, RW, DS, MODE, DIMS><<<nblocks, NW * 32, smem, j.stream>>>(rp, rp.target, j.offsets, gp);
     j.launches += 1;
     return cudaGetLastError();
 }
@@ -1167,8 +1167,33 @@ cudaError_t launch_random_shape(Job& j, const RandParams& rp, const GridPrep& gp
 
 }  // namespace
 
+// Where a fast-mode push adds its bins. The reference adds each pass's grid to the frame grid at the
+// end of the pass; with the frame grid in double-float pairs (or still empty) the push adds its
+// pairs straight into it instead (the pairs' sums differ from pass-then-merge only in the rounding
+// of the low words), and the end of the pass has nothing to merge. Otherwise the pass grid
+// collects the pass as in the reference.
+static cudaError_t grid_target(Job& j, float2** out) {
+    const int64_t n = j.g.nn * kDeps * kDepStride;
+    if (j.cfg.rpf_shrinkage_scale > 0.0f && (j.grid_fresh || j.grid_pairs)) {
+        if (j.grid_fresh) {
+            const cudaError_t e = cudaMemsetAsync(j.n.grid, 0, size_t(n) * sizeof(double), j.stream);
+            if (e != cudaSuccess) return e;
+            j.grid_fresh = false;
+            j.grid_pairs = true;
+        }
+        j.pass_direct = true;
+        *out = reinterpret_cast<float2*>(j.n.grid);
+    } else {
+        j.pass_indirect = true;
+        *out = reinterpret_cast<float2*>(j.n.pass_grid);
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int64_t count, const GridPrep& gp,
                              int32_t spp, int32_t max_count, int64_t total_samples, const int64_t* d_max_count) {
+    float2* target = nullptr;
+    if (const cudaError_t e0 = grid_target(j, &target); e0 != cudaSuccess) return e0;
     const int step = j.g.step;
     const bool pow2 = (step & (step - 1)) == 0;
     GridParams gpar{j.g, first, count, 0, 0, 0, pow2 ? 1 : 0, 1.0f / float(step), spp, spp > 0 ? 1.0f / float(spp) : 0.0f};
@@ -1200,28 +1225,28 @@ cudaError_t launch_grid_fast(Job& j, const DeviceSamples& s, int64_t first, int6
             if (int_w) {
                 e = cudaFuncSetAttribute(k_grid_screen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
                 if (e != cudaSuccess) return e;
-                k_grid_screen<true><<<nblocks, 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+                k_grid_screen<true><<<nblocks, 32, smem, j.stream>>>(gpar, target, s, j.offsets, gp);
             } else {
                 e = cudaFuncSetAttribute(k_grid_screen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
                 if (e != cudaSuccess) return e;
-                k_grid_screen<false><<<nblocks, 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+                k_grid_screen<false><<<nblocks, 32, smem, j.stream>>>(gpar, target, s, j.offsets, gp);
             }
         } else if (int_w) {
             const size_t smem = size_t(kGroups) * LaneBins<true>::kSlots * 32 * sizeof(float);
             e = cudaFuncSetAttribute(k_grid_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if (e != cudaSuccess) return e;
-            k_grid_fast<true><<<nblocks, kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+            k_grid_fast<true><<<nblocks, kGroups * 32, smem, j.stream>>>(gpar, target, s, j.offsets, gp);
         } else {
             const size_t smem = size_t(kGroups) * LaneBins<false>::kSlots * 32 * sizeof(float);
             e = cudaFuncSetAttribute(k_grid_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
             if (e != cudaSuccess) return e;
-            k_grid_fast<false><<<nblocks, kGroups * 32, smem, j.stream>>>(gpar, reinterpret_cast<float2*>(j.n.pass_grid), s, j.offsets, gp);
+            k_grid_fast<false><<<nblocks, kGroups * 32, smem, j.stream>>>(gpar, target, s, j.offsets, gp);
         }
         j.launches += 1;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     KernelScope ks(j, RPD_KERNEL_GRID_RANDOM);
-    RandParams rp{gpar, 0u, -1, 2 * step + 3, nullptr, 0, 0};
+    RandParams rp{gpar, 0u, -1, 2 * step + 3, nullptr, 0, 0, target};
     // the statistics pass clears a dimension's valid bit when the push has no plane for it: without
     // environment planes (a closed scene) the form without the environment dimension runs
     const bool env = s.compact ? s.c16.env_u[0] != nullptr : s.env_u[0] != nullptr;

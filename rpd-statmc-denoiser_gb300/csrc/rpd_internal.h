@@ -174,6 +174,10 @@ struct Job {
     bool host_async = false;  // the current host push returns before its copies complete
     bool grid_fresh = true;      // the frame grid has no merged pass yet (the next merge assigns)
     bool grid_pairs = false;     // the frame grid holds double-float pairs (fast grid mode), not doubles
+    // the open pass's fast-mode pushes added straight into the frame grid (pairs), so the end of
+    // the pass merges nothing of theirs; pass_indirect: some push of the pass wrote the pass grid
+    bool pass_direct = false;
+    bool pass_indirect = false;
     bool features_valid = false;
     bool cache_valid = false;
     bool have_samples = false;
