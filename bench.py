@@ -923,7 +923,7 @@ def main():
     ap.add_argument("--storage", choices=["fp16", "fp32"], default="fp16", help="serving: sample storage")
     ap.add_argument("--served", action="store_true", help="request form: through rpd_server instead of the plain drop-in")
     ap.add_argument("--alloc-blocks", type=int, default=0,
-                    help="serving: blocks of each request's parallel adaptive allocation (0: one per SM)")
+                    help="serving: blocks of each request's parallel adaptive allocation (0: half the SMs)")
     ap.add_argument("--plain-requests", type=int, default=200, help="serving: stream prefix run through the plain drop-in")
     ap.add_argument("--passes", type=int, default=1, help="request: adaptive passes of the profiled request")
     ap.add_argument("--no-served", action="store_true", help="plain form: leave out the served stream")

@@ -630,9 +630,10 @@ typedef struct rpd_server_config {
     int32_t max_inflight;        /* requests on the GPU at once, 1..256 */
     int32_t storage;             /* rpd_storage of the sample buffers */
     int32_t profile;             /* nonzero: time every kernel family of every request (CUDA events) */
-    int32_t allocator_blocks;    /* blocks of each request's parallel adaptive allocation: 0 one per SM,
-                                  * N >= 2 at most N (RPD_TUNE_ALLOCATOR); fewer leave SMs to the
-                                  * other requests' kernels while an allocation walks its chain */
+    int32_t allocator_blocks;    /* blocks of each request's parallel adaptive allocation: 0 one on
+                                  * half the SMs, N >= 2 at most N (RPD_TUNE_ALLOCATOR); fewer leave
+                                  * SMs to the other requests' kernels while an allocation walks its
+                                  * chain */
 } rpd_server_config;
 
 typedef struct rpd_request {
