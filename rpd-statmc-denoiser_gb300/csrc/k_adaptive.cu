@@ -61,9 +61,11 @@ __device__ float smooth_pixel_fp64(const PixelPlanes& p, int w, int h, int radiu
     return (weight_sum > double(1e-8f)) ? float(accum / weight_sum) : in[idx];
 }
 
-// The same pixel with the products and the two sums in integer instructions (XD, each operation
-// rounded as the double-precision one rounds it): the same bits as smooth_pixel_fp64 without its
-// double-precision operations (GB300 issues those at 2 per SM per clock). R > 0 fixes
+// The same pixel with the products in integer instructions (XD) and the two sums as double
+// additions of the products' bits: the same bits as smooth_pixel_fp64 with three of its five
+// double-precision operations per neighbour, and none of its conversions, left out (the two sums
+// in integer instructions as well measured slower: 0.53 -> 0.61 ms per 1920x1080 adaptive
+// step, the integer additions cost more issue than the double pipe's wait). R > 0 fixes
 // the radius at compile time (R = 0: `radius`). Returns false for inputs outside the integer
 // form (negative, subnormal or non-finite weights or importances).
 template <int R>
@@ -72,7 +74,7 @@ __device__ bool smooth_pixel_int(const PixelPlanes& p, int w, int h, int radius,
     const int rad = R > 0 ? R : radius;
     const float ni0 = p.f_normal[0][idx], ni1 = p.f_normal[1][idx], ni2 = p.f_normal[2][idx];
     const float di = p.f_depth[idx];
-    XD accum{0ull, 0}, weight_sum{0ull, 0};  // the reference's sums from 0.0
+    double accum = 0.0, weight_sum = 0.0;
     bool ok = true;
 #pragma unroll
     for (int dy = -rad; dy <= rad; ++dy) {
@@ -107,22 +109,25 @@ __device__ bool smooth_pixel_int(const PixelPlanes& p, int w, int h, int radius,
             // rounded
             const XD wn = sm == 0x800000u ? xd_exact48(uint64_t(nm) * dm, ne + de + se + 23)
                                           : xd_mul24(uint64_t(sm) * nm, dm, se + ne + de);
-            if (iok) accum = xd_add(accum, xd_mul24(wn.m, im, wn.e + ie));
+            if (iok) accum += xd_to_double(xd_mul24(wn.m, im, wn.e + ie));
             else if (imp != 0.0f) ok = false;
-            weight_sum = xd_add(weight_sum, wn);
+            weight_sum += xd_to_double(wn);
         }
     }
     if (!ok) return false;
-    if (!(xd_to_double(weight_sum) > double(1e-8f))) {
+    if (!(weight_sum > double(1e-8f))) {
         out = in[idx];
         return true;
     }
-    if (accum.m == 0ull) {
+    if (accum == 0.0) {
         out = 0.0f;
         return true;
     }
-    if (!quotient_to_float(accum.m, accum.e, weight_sum.m, weight_sum.e, out))
-        out = float(xd_to_double(accum) / xd_to_double(weight_sum));
+    const long long ab = __double_as_longlong(accum), wb = __double_as_longlong(weight_sum);
+    const uint64_t am = (uint64_t(ab) & ((1ull << 52) - 1ull)) | (1ull << 52);
+    const uint64_t wm = (uint64_t(wb) & ((1ull << 52) - 1ull)) | (1ull << 52);
+    const int ae = int((ab >> 52) & 0x7ff) - 1075, we = int((wb >> 52) & 0x7ff) - 1075;
+    if (!quotient_to_float(am, ae, wm, we, out)) out = float(accum / weight_sum);
     return true;
 }
 
