@@ -187,6 +187,11 @@ __device__ void reduce_totals(Totals t, float2* out4) {
     for (int q = 0; q < 4; ++q) out4[q] = make_float2(v[2 * q], v[2 * q + 1]);
 }
 
+// v[q] for a lane-dependent q in 0-3, without indexing the registers
+__device__ __forceinline__ float2 pick4(const float2* v, int q) {
+    return q == 0 ? v[0] : q == 1 ? v[1] : q == 2 ? v[2] : v[3];
+}
+
 // As reduce_totals, adding the result to the pass-grid entries acc[32..35].
 __device__ void reduce_totals_into(Totals t, float2* acc) {
     float2 r[4];
@@ -511,6 +516,10 @@ __global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pas
     __syncwarp();
     float2 tp[4];
     reduce_totals(TP, tp);
+    // lane k of 0-7 adds total k & 3 of P0's pixels (the sums are lane 0's)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) tp[k] = make_float2(__shfl_sync(0xffffffffu, tp[k].x, 0), __shfl_sync(0xffffffffu, tp[k].y, 0));
+    const float2 tpq = pick4(tp, lane & 3);
     const float2 va = binsA.reduce_value();
     LaneBins<INT_W>& binsB = binsA;  // bins A are folded into va: reuse their storage
 
@@ -581,33 +590,54 @@ __global__ void __launch_bounds__(32) k_grid_screen(GridParams gpar, float2* pas
             df_add(bh, bl, va.x);
             bl += va.y;
         }
-        if (bh != 0.0f || bl != 0.0f) df_accum(base + dep_s * kDepStride + lane, bh, bl);
-        // no listed pixel: this class's totals are all zeros on every lane (nothing to reduce)
-        float2 t4[4] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f),
-                        make_float2(0.0f, 0.0f)};
-        if (nlist > 0) reduce_totals(ts, t4);
-        if (lane == 0) {
-            for (int k = 0; k < 4; ++k) {
-                float h = t4[k].x, l = t4[k].y;
-                if (p0screen) {
-                    df_add(h, l, tp[k].x);
-                    l += tp[k].y;
+        // the class's totals, one entry per lane: lanes 0-3 the screen dependency's (32-35),
+        // lanes 4-7 the random dimension's (classes 1-6); with no listed pixel the list's part is
+        // zero on every lane (nothing to reduce)
+        float th = 0.0f, tl = 0.0f;
+        float2* te = nullptr;
+        {
+            float2 t4s[4] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f),
+                             make_float2(0.0f, 0.0f)};
+            float2 t4x[4] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f),
+                             make_float2(0.0f, 0.0f)};
+            if (nlist > 0) {
+                reduce_totals(ts, t4s);
+                if (cl > 0) reduce_totals(tx, t4x);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {  // the sums are lane 0's
+                    t4s[k] = make_float2(__shfl_sync(0xffffffffu, t4s[k].x, 0), __shfl_sync(0xffffffffu, t4s[k].y, 0));
+                    t4x[k] = make_float2(__shfl_sync(0xffffffffu, t4x[k].x, 0), __shfl_sync(0xffffffffu, t4x[k].y, 0));
                 }
-                if (h != 0.0f || l != 0.0f) df_accum(base + dep_s * kDepStride + 32 + k, h, l);
+            }
+            if (lane < 4 || (lane < 8 && cl > 0)) {
+                const bool scr = lane < 4;
+                const float2 ps = pick4(t4s, lane & 3), px = pick4(t4x, lane & 3);
+                const float2 t = scr ? ps : px;
+                th = t.x;
+                tl = t.y;
+                if (scr ? p0screen : inP0) {
+                    df_add(th, tl, tpq.x);
+                    tl += tpq.y;
+                }
+                te = base + (scr ? dep_s : dep_x) * kDepStride + 32 + (lane & 3);
             }
         }
-        if (cl > 0) {
-            if (nlist > 0) reduce_totals(tx, t4);
-            if (lane == 0) {
-                for (int k = 0; k < 4; ++k) {
-                    float h = t4[k].x, l = t4[k].y;
-                    if (inP0) {
-                        df_add(h, l, tp[k].x);
-                        l += tp[k].y;
-                    }
-                    if (h != 0.0f || l != 0.0f) df_accum(base + dep_x * kDepStride + 32 + k, h, l);
-                }
-            }
+        // both read-modify-writes of the lane with their loads issued first
+        const bool bw = bh != 0.0f || bl != 0.0f;
+        const bool tw = te != nullptr && (th != 0.0f || tl != 0.0f);
+        float2* be = base + dep_s * kDepStride + lane;
+        float2 bv = make_float2(0.0f, 0.0f), tv = make_float2(0.0f, 0.0f);
+        if (bw) bv = *be;
+        if (tw) tv = *te;
+        if (bw) {
+            df_add(bv.x, bv.y, bh);
+            bv.y += bl;
+            *be = bv;
+        }
+        if (tw) {
+            df_add(tv.x, tv.y, th);
+            tv.y += tl;
+            *te = tv;
         }
     }
 }
