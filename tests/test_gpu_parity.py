@@ -343,3 +343,40 @@ def test_banded_host_push_equals_device_push(gpu_ctx, counts_mode):
     a.close()
     b.close()
     dev.free()
+
+
+@pytest.mark.parametrize("modes", [(False, True, False), (True, False, False), (False, False, True)],
+                         ids=["fast-exact-fast", "exact-fast-fast", "fast-fast-exact"])
+def test_grid_modes_across_passes(gpu_ctx, modes):
+    """Three passes of one frame whose grid mode changes between passes, the first pushed in two
+    row bands: in the double-float mode the pushes add their pairs straight into the frame grid
+    (or into the pass grid when an exact pass has left the frame grid in doubles), the exact mode
+    adds into the pass grid and merges. The frame grid stays within 1e-9 of the oracle's, and the
+    node fields within their bar."""
+    w, h, spp = 40, 36, 4
+    cfg = small_config(w, h, rpf_tile_size=8)
+    p = R.synth_params(w, h, 23, miss_regions=3)
+    passes = [B.synth_fill(p, 0, w * h, spp, start_n=np.full(w * h, q << 16, dtype=np.int32)) for q in range(3)]
+    offsets = np.arange(w * h + 1, dtype=np.int64) * spp
+    g = R.Job(gpu_ctx, cfg)
+    o = B.OracleJob(cfg, threads=1)
+    for job in (g, o):
+        job.begin_frame()
+        for q, s in enumerate(passes):
+            if job is g:
+                g.set_exact(grid=modes[q], window=False)
+            if q == 0:
+                mid = (h // 2) * w
+                job.push(s.slice_pixels(offsets, 0, mid), 0, mid, spp)
+                job.push(s.slice_pixels(offsets, mid, w * h), mid, w * h - mid, spp)
+            else:
+                job.push(s, 0, w * h, spp)
+            job.end_pass()
+        job.recompute_sensitivity()
+    assert_grid_close(g.read("GRID"), o.read("GRID"))
+    for f in NODE_FIELDS:
+        assert np.max(np.abs(g.read(f) - o.read(f))) <= 1e-5, f
+    for f in ["STATS_MEAN", "STATS_SQUARE_DIFF", "STATS_N"]:
+        assert_bitwise(g.read(f), o.read(f), f)
+    g.close()
+    o.close()
