@@ -210,7 +210,7 @@ typedef enum rpd_kernel {
     RPD_KERNEL_ACCUMULATE_PIXELS,   /* Welford statistics + features */
     RPD_KERNEL_GRID,                /* RPD grid: totals and screen bins */
     RPD_KERNEL_GRID_RANDOM,         /* RPD grid: random-dimension bins */
-    RPD_KERNEL_MERGE,               /* pass grid merge */
+    RPD_KERNEL_MERGE,               /* pass grid merge (the exact grid mode's passes) */
     RPD_KERNEL_FEATURES,            /* feature cache */
     RPD_KERNEL_NODE_STATS,          /* per-node sensitivities, confidences, features */
     RPD_KERNEL_NODE_COMBINE,        /* prior smoothing + combine */
@@ -344,7 +344,9 @@ int rpd_encode_samples16(rpd_ctx* ctx, const rpd_sample_soa* in, int64_t n_sampl
                          const rpd_sample_soa16* out);
 
 /* End of a render pass: merge_rpf_grids_into (main.cpp:378-388, 730, 1531) and cache
- * invalidation (main.cpp:1533). */
+ * invalidation (main.cpp:1533). In the exact grid mode the pass grid is added to the frame grid
+ * here; in the default double-float mode the pushes add straight into the frame grid (the
+ * frame's first push clears it), so a GRID read already reflects the pushes of an open pass. */
 int rpd_job_end_pass(rpd_job* job);
 
 /* The four stage entry points (main.cpp:741, 957, 1166, 1273). */
