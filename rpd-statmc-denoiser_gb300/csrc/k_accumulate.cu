@@ -167,7 +167,10 @@ struct PixelAcc {
     uint8_t pat;
     bool have_pat, dev;
     float pc, p1h, p1l, p2h, p2l;
-    float cc[kClasses], s1h[kClasses], s1l[kClasses], s2h[kClasses], s2l[kClasses];
+    // the per-class sums [class][count, s1 hi, s1 lo, s2 hi, s2 lo] of a deviant pixel, in the
+    // thread's local memory (written only once the pixel deviates, which is rare): held in
+    // registers they would cost 35 registers through the whole sample loop
+    float* cs;
     uint8_t pflags;
 };
 
@@ -268,14 +271,22 @@ __device__ __forceinline__ void process_sample(PixelAcc& a, const SampleIn& in, 
         df_add(a.p2h, a.p2l, y2);
         a.p2l += y2e;
     } else {
-        a.dev = true;
-        #pragma unroll
+        if (!a.dev) {
+            a.dev = true;
+            for (int q = 0; q < kClasses * 5; ++q) a.cs[q] = 0.0f;
+        }
         for (int c = 0; c < kClasses; ++c) {
             if (!(cls_bits & class_bit(c))) continue;
-            a.cc[c] += 1.0f;
-            df_add(a.s1h[c], a.s1l[c], lum);
-            df_add(a.s2h[c], a.s2l[c], y2);
-            a.s2l[c] += y2e;
+            float* e = a.cs + 5 * c;
+            float h1 = e[1], l1 = e[2], h2 = e[3], l2 = e[4];
+            df_add(h1, l1, lum);
+            df_add(h2, l2, y2);
+            l2 += y2e;
+            e[0] += 1.0f;
+            e[1] = h1;
+            e[2] = l1;
+            e[3] = h2;
+            e[4] = l2;
         }
     }
     if (fm & RPD_SAMPLE_PIXEL_VALID) {
@@ -308,8 +319,7 @@ __device__ __forceinline__ void acc_init(PixelAcc& a) {
     a.have_pat = false;
     a.dev = false;
     a.pat = 0;
-    a.pc = a.p1h = a.p1l = a.p2h = a.p2l = 0.0f;
-    for (int c = 0; c < kClasses; ++c) a.cc[c] = a.s1h[c] = a.s1l[c] = a.s2h[c] = a.s2l[c] = 0.0f;
+    a.pc = a.p1h = a.p1l = a.p2h = a.p2l = 0.0f;  // the class sums are cleared when the pixel deviates
 }
 
 // The grid-pass sums of a pixel without samples in the push.
@@ -369,7 +379,8 @@ __device__ __forceinline__ void acc_store(const PixelAcc& a, const PixelPlanes& 
         if (a.dev) {
             // full per-class sums: the deviating samples plus the pattern's
             for (int c = 0; c < kClasses; ++c) {
-                float h1 = a.s1h[c], l1 = a.s1l[c], h2 = a.s2h[c], l2 = a.s2l[c], cnt = a.cc[c];
+                const float* e = a.cs + 5 * c;
+                float h1 = e[1], l1 = e[2], h2 = e[3], l2 = e[4], cnt = e[0];
                 if (a.have_pat && (a.pat & class_bit(c))) {
                     cnt += a.pc;
                     df_add(h1, l1, a.p1h);
@@ -413,6 +424,10 @@ __global__ void __launch_bounds__(128, MINB) k_accumulate_pixels(PixelPlanes p, 
                                                  (has_eu ? 0 : RPD_SAMPLE_ENV_VALID)));
     const float fx = float(idx % gp.width), fy = float(idx / gp.width);
     PixelAcc a;
+    // the class sums' local array, addressed through an offset the compiler cannot fold, so that
+    // it stays in local memory instead of registers
+    float cls_local[kClasses * 5];
+    a.cs = cls_local + (uint32_t(gp.width) >> 31);  // the width is positive: offset 0
     acc_init(a);
     if (k0 == k1) {
         if (prep) acc_store_empty(gp, idx);
