@@ -37,8 +37,8 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "rpd-statmc-denoiser_gb300"))
 
 W, H, SPP, SEED = 1920, 1080, 16, 1234
-# BASELINE's metric: `value` is the plain form's throughput; the line's `served` object holds the
-# served stream's throughput and p50/p99 latency against the plain per-frame drop-in
+# The headline metric: `value` is the plain form's throughput; the line's `served` object holds
+# the served stream's throughput and p50/p99 latency against the plain per-frame drop-in
 METRIC = "denoised Msamples/s at 1080p 16spp, plain vs served; p50/p99 ms @\u22641e-3 relMSE"
 UNIT = "Msamples/s"
 
